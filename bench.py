@@ -1,0 +1,353 @@
+"""Benchmark of the GB300 GeoClaw patch update (cell-updates/s, FP64).
+
+Workload (the plain GPU drop-in microbenchmark): one uniform level of
+4096 patches of 32 x 32 cells (64 x 64 patches, 2048 x 2048 = 4,194,304
+cells, dx = 1 m) over a seeded diamond-square DEM (Hurst 0.8, 30 m relief)
+with a 5 m deep, 40 m wide carved channel; dam-break start (surface 10 m
+above the bed for x < 600 m, dry beyond); Manning n = 0.035; dry tolerance
+1e-3 m; FP64. A step is one level step: the fused patch update of every
+patch (b4step2, step2, CFL, src2) followed by the same-level ghost copy.
+
+value  - cell-updates/s with the level resident in HBM (inputs 170 MB, larger
+         than the 129 MB L2, so no flush between steps).
+e2e    - the same through the C ABI with host buffers: gf_level_step_host
+         copies q in (pinned, Fortran layout), steps, copies q out.
+roofline - HBM roofline of the patch kernel (56 algorithmic bytes per
+         interior cell-update) against the measured copy bandwidth, plus the
+         FP64 issue roofline it is actually bound by.
+cpu_baseline - the CPU oracle (Fortran-faithful C restatement, OpenMP over
+         patches) on a bounded sample of the same level.
+
+--impl reference times the reference CPU path (the oracle port; the
+reference's Fortran cannot be built on this image) on all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s"
+BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
+M = 32
+NPX = NPY = 64
+DX = 1.0
+DT = 0.03  # CFL ~ 0.4-0.6 on this state
+SEED = 2024
+MTHBC = (1, 1, 1, 1)  # zero-order extrapolation, as the reference dam_break example
+
+
+def workload():
+    from geoflood_gb300 import synth
+
+    q, aux, py, px = synth.uniform_dam_break_level(NPX, NPY, M, DX, seed=SEED, x_dam=600.0)
+    return q, aux, py, px
+
+
+def config(extra=None):
+    c = {"workload": "uniform dam-break level, 4096 patches of 32x32 (2048x2048 cells), "
+                     "fractal DEM Hurst 0.8 relief 30 m + 5x40 m channel, FP64",
+         "patches": NPX * NPY, "mx": M, "mbc": 2, "cells": NPX * NPY * M * M,
+         "dx_m": DX, "dt_s": DT, "l2": "inputs (170 MB) larger than L2; no flush"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", os.environ.get("GF_BENCH_GPU_INDEX", "0"), "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(q, aux, seconds=12.0, rows=8, threads=0):
+    """Time the CPU oracle on whole patch rows of the level (same wet fraction
+    as the full level); repeats one step until `seconds` have elapsed."""
+    import oracle
+
+    n = rows * NPX
+    start_row = NPY // 2 - rows // 2
+    sl = slice(start_row * NPX, start_row * NPX + n)
+    qs = np.ascontiguousarray(q[sl])
+    aus = np.ascontiguousarray(aux[sl])
+    from geoflood_gb300 import Phys
+
+    phys = Phys()
+    oracle.load()
+    cells = 0
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        work = qs.copy()
+        oracle.level_update(work, aus, DX, DX, 0.0, DT, phys, nthreads=threads)
+        cells += n * M * M
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return cells / el, cores, f"{reps} step(s) of {rows} patch rows ({n} patches, {n * M * M} cells)"
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU patch update (oracle port) on all host threads."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    q, aux, _, _ = workload()
+    import oracle
+
+    from geoflood_gb300 import Phys
+
+    oracle.load()
+    rows = 4
+    n = rows * NPX
+    sl = slice((NPY // 2) * NPX, (NPY // 2) * NPX + n)
+    qs = np.ascontiguousarray(q[sl])
+    aus = np.ascontiguousarray(aux[sl])
+    phys = Phys()
+    for _ in range(args.warmup):
+        w = qs.copy()
+        oracle.level_update(w, aus, DX, DX, 0.0, DT, phys, nthreads=0)
+    times = []
+    for _ in range(args.steps):
+        w = qs.copy()
+        t0 = time.perf_counter()
+        oracle.level_update(w, aus, DX, DX, 0.0, DT, phys, nthreads=0)
+        times.append(time.perf_counter() - t0)
+    cells = n * M * M
+    v = cells * len(times) / sum(times)
+    cores = os.cpu_count() or 1
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": config({"sample": f"{rows} patch rows ({n} patches, {cells} cells) per step"}),
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": f"{rows} patch rows ({n} patches) per step; reference "
+                                       "Fortran not buildable (no Fortran compiler/ForestClaw)"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    q, aux, py, px = workload()
+    ncell = NPX * NPY * M * M
+    ctx = gf.Context(local, gf.Phys())
+    lev = gf.Level(ctx, q.shape[0], M, 1)
+    lev.set_geometry(DX, DX)
+    lev.upload(q, aux)
+    nbr, xl, yl = synth.brick_layout(py, px, M, DX)
+    lev.set_layout(nbr, xl, yl)
+    lev.set_bc(MTHBC)
+    lev.ghost_fill(0.0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    launches_per_step = 2  # patch update + ghost fill
+    clock = [0.0]
+
+    def step():
+        lev.step_async(clock[0], DT)
+        clock[0] += DT
+        lev.ghost_fill_async(clock[0])
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    lev.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+    maxcfl = lev.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # kernel-only timing of the patch update (no ghost fill) for the roofline
+    with torch.cuda.stream(stream):
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        nk = max(3, min(args.steps, 10))
+        for _ in range(nk):
+            lev.step_async(0.0, DT)
+        k1.record(stream)
+    lev.sync()
+    kernel_ms = k0.elapsed_time(k1) / nk
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # e2e through the C ABI with host buffers (pinned, Fortran layout); the
+    # host array carries the filled ghost cells, as ForestClaw's storage does
+    qh = torch.empty(q.size, dtype=torch.float64, pin_memory=True).numpy().reshape(q.shape)
+    lev.upload(q, aux)
+    lev.ghost_fill(0.0)
+    qh[...] = lev.download()
+    for _ in range(2):
+        lev.step_host(qh, 0.0, DT)
+    ne = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        h0 = torch.cuda.Event(enable_timing=True)
+        h1 = torch.cuda.Event(enable_timing=True)
+        h0.record(stream)
+        for _ in range(ne):
+            lev.step_host(qh, 0.0, DT)
+        h1.record(stream)
+    torch.cuda.synchronize()
+    e2e_wall = (time.perf_counter() - t0) / ne
+    e2e_ms = max(h0.elapsed_time(h1) / ne, 1e3 * e2e_wall)
+    qbytes = q.size * 8
+
+    hbm_peak, peak_kind = load_peaks()
+    algo = BYTES_PER_CELL_UPDATE * ncell
+    achieved = algo / (kernel_ms * 1e-3) / 1e9
+    fp64 = fp64_peak_gops()
+    result = {
+        "metric": METRIC, "value": world * ncell / (ms * 1e-3), "unit": METRIC,
+        "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                          "step": "patch update + ghost fill (same-level copy, extrapolation BC)",
+                          "max_cfl_last_step": maxcfl}),
+        "e2e": {"value": world * ncell / (e2e_ms * 1e-3), "unit": METRIC,
+                "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes + 16},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel_ms": kernel_ms,
+                     "note": "FP64-issue bound, not HBM bound: see fp64"},
+        "fp64": fp64,
+        "clocks": clk,
+    }
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
+            result["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
+                                      "sample": sample}
+        print(json.dumps(result))
+    lev.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def fp64_peak_gops():
+    """Measured FP64 FMA issue rate of this GPU (gf_measure_fp64_peak), if exported."""
+    try:
+        from geoflood_gb300 import _lib
+
+        lib = _lib.load()
+        if not hasattr(lib, "gf_measure_fp64_peak"):
+            return None
+        import ctypes as C
+
+        v = C.c_double()
+        rc = lib.gf_measure_fp64_peak(0, C.byref(v))
+        return {"dfma_gops": v.value} if rc == 0 else None
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,116 @@
+"""ctypes binding of ``libgeoflood_gb300.so`` (the C ABI in include/geoflood_gb300.h).
+
+The library is the only compute path: if it is missing this module raises
+instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libgeoflood_gb300.so"
+
+GF_OK = 0
+GF_MAX_MANNING = 4
+GF_MAX_PHYS = 1024
+
+STATUS_NAMES = {
+    0: "GF_OK", -1: "GF_ERR_ARG", -2: "GF_ERR_CUDA", -3: "GF_ERR_NOMEM",
+    -4: "GF_ERR_DEVICE", -5: "GF_ERR_STATE", -6: "GF_ERR_UNSUPPORTED",
+}
+
+
+class gf_phys(C.Structure):
+    _fields_ = [
+        ("grav", C.c_double),
+        ("dry_tolerance", C.c_double),
+        ("sea_level", C.c_double),
+        ("friction_depth", C.c_double),
+        ("manning_coefficient", C.c_double * GF_MAX_MANNING),
+        ("manning_break", C.c_double * GF_MAX_MANNING),
+        ("num_manning", C.c_int),
+        ("friction_forcing", C.c_int),
+        ("variable_friction", C.c_int),
+        ("friction_index", C.c_int),
+        ("order", C.c_int),
+        ("transverse", C.c_int),
+        ("mthlim", C.c_int * 3),
+        ("src_term", C.c_int),
+        ("maxcfl_cap", C.c_double),
+    ]
+
+
+_dp = C.POINTER(C.c_double)
+_vp = C.c_void_p
+
+# (name, restype, argtypes) for every exported entry point.
+SIGNATURES = [
+    ("gf_phys_default", None, [C.POINTER(gf_phys)]),
+    ("gf_ctx_create", C.c_int, [C.c_int, C.POINTER(_vp)]),
+    ("gf_ctx_destroy", None, [_vp]),
+    ("gf_ctx_last_error", C.c_char_p, [_vp]),
+    ("gf_ctx_set_phys", C.c_int, [_vp, C.c_int, C.POINTER(gf_phys)]),
+    ("gf_patch_update", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                  C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]),
+    ("gf_patch_update_batch", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        _dp, _dp, C.c_double, C.c_double, C.POINTER(_dp),
+                                        C.POINTER(_dp), _dp, _dp]),
+    ("gf_level_create", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
+    ("gf_level_destroy", None, [_vp]),
+    ("gf_level_set_geometry", C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_int)]),
+    ("gf_level_upload", C.c_int, [_vp, _dp, _dp]),
+    ("gf_level_download", C.c_int, [_vp, _dp]),
+    ("gf_level_download_aux", C.c_int, [_vp, _dp]),
+    ("gf_level_step", C.c_int, [_vp, C.c_double, C.c_double, _dp]),
+    ("gf_level_step_host", C.c_int, [_vp, _dp, C.c_double, C.c_double, _dp]),
+    ("gf_level_step_async", C.c_int, [_vp, C.c_double, C.c_double]),
+    ("gf_level_sync", C.c_int, [_vp, _dp]),
+    ("gf_ctx_stream", C.c_int, [_vp, C.POINTER(_vp)]),
+    ("gf_ctx_set_fp_contract", C.c_int, [_vp, C.c_int]),
+    ("gf_level_patch_cfl", C.c_int, [_vp, _dp]),
+    ("gf_level_set_layout", C.c_int, [_vp, C.POINTER(C.c_int), _dp, _dp]),
+    ("gf_level_set_bc", C.c_int, [_vp, C.POINTER(C.c_int)]),
+    ("gf_level_set_hydrograph", C.c_int, [_vp, C.c_int, _dp, _dp, C.POINTER(C.c_int), C.c_double,
+                                          C.c_double, C.c_double]),
+    ("gf_level_ghost_fill", C.c_int, [_vp, C.c_double]),
+    ("gf_level_ghost_fill_async", C.c_int, [_vp, C.c_double]),
+    ("gf_level_device_planes", C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
+]
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the CUDA library; raise if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH.name} is not built; run geoflood_gb300.build.build() "
+            "(the CUDA library is the only compute path)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def dptr(a: np.ndarray | None):
+    """Pointer to a C-contiguous float64 array (or NULL)."""
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], "need contiguous float64"
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_int))

@@ -1,0 +1,704 @@
+/*
+ * C ABI of the GB300 patch update: contexts, physics sets, the plain
+ * per-patch drop-in, the batched drop-in and device-resident levels.
+ *
+ * Nothing here computes the solution on the host: every update runs in the
+ * sm_103a kernels of gf_kernels.cu. Errors are returned as gf_status codes
+ * with a message kept on the context.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gf_internal.h"
+
+namespace {
+
+struct DevStatus {
+    unsigned long long gmax; /* order-preserving bits of the max CFL */
+    int err;                 /* non-zero: a bounded wait expired     */
+    int pad;
+};
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t want)
+    {
+        if (want <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+template <typename T>
+struct HostBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t want)
+    {
+        if (want <= n) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+inline bool valid_m(int m) { return m == 8 || m == 16 || m == 32; }
+inline long cells_of(int mx, int my) { return (long)(mx + 2 * GF_MBC) * (my + 2 * GF_MBC); }
+
+} // namespace
+
+struct gf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    gf_phys* d_phys = nullptr;
+    std::vector<gf_phys> h_phys;
+    std::vector<unsigned char> phys_set;
+    DevStatus* d_status = nullptr;
+    DevStatus* h_status = nullptr; /* pinned */
+    double* d_gdt = nullptr;
+    double* h_gdt = nullptr; /* pinned */
+    std::string last_error;
+    bool exact = false; /* run the contraction-free build */
+    /* scratch for the host-buffer drop-in paths */
+    DevBuf<double> q_aos, q_soa, aux_aos, aux_soa, cfl;
+    DevBuf<gf_patch_work> work;
+    HostBuf<double> h_stage, h_cfl;
+    HostBuf<gf_patch_work> h_work;
+};
+
+struct gf_level {
+    gf_ctx* ctx = nullptr;
+    int npatch = 0, mx = 0, my = 0, maux = 0;
+    long S = 0;
+    double* d_q = nullptr;
+    double* d_aux = nullptr;
+    double* d_stage = nullptr;
+    double* d_cfl = nullptr;
+    gf_patch_work* d_work = nullptr;
+    DevStatus* d_status = nullptr;
+    std::vector<double> dx, dy;
+    std::vector<int> phys;
+    bool work_dirty = true;
+    bool aux_loaded = false;
+    /* ghost fill */
+    int* d_nbr = nullptr;
+    gf_patch_geom* d_geom = nullptr;
+    int* d_phys_of = nullptr;
+    std::vector<double> xlower, ylower;
+    bool layout_set = false;
+    bool geom_dirty = true;
+    gf_bc_spec bc{};
+    std::vector<double> hy_time, hy_hu;
+};
+
+namespace {
+
+int fail(gf_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->last_error = msg;
+    return code;
+}
+
+int cuda_fail(gf_ctx* c, cudaError_t e, const char* what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(c, e == cudaErrorMemoryAllocation ? GF_ERR_NOMEM : GF_ERR_CUDA, m);
+}
+
+#define GF_CK(ctx, call)                                   \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+int check_phys_slot(gf_ctx* c, int slot)
+{
+    if (slot < 0 || slot >= GF_MAX_PHYS) return fail(c, GF_ERR_ARG, "physics slot out of range");
+    if (!c->phys_set[slot]) return fail(c, GF_ERR_STATE, "physics slot not set");
+    return GF_OK;
+}
+
+/* Enqueue one batch on the context stream: clear the status, launch. */
+int enqueue_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int maux, double dt,
+                  double* d_cfl, DevStatus* d_status)
+{
+    GF_CK(c, cudaMemsetAsync(d_status, 0, sizeof(DevStatus), c->stream));
+    if (c->exact)
+        GF_CK(c, gf::launch_patch_update_exact(m, d_work, nwork, c->d_phys, dt, nullptr, maux,
+                                               d_cfl, &d_status->gmax, &d_status->err, c->stream));
+    else
+        GF_CK(c, gf::launch_patch_update(m, d_work, nwork, c->d_phys, dt, nullptr, maux, d_cfl,
+                                         &d_status->gmax, &d_status->err, c->stream));
+    return GF_OK;
+}
+
+/* Fetch a batch status (waits for the stream). */
+int finish_batch(gf_ctx* c, DevStatus* d_status, double* maxcfl)
+{
+    GF_CK(c, cudaMemcpyAsync(c->h_status, d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                             c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    if (c->h_status->err) return fail(c, GF_ERR_DEVICE, "patch kernel: bounded wait expired");
+    double v;
+    std::memcpy(&v, &c->h_status->gmax, sizeof v);
+    if (maxcfl) *maxcfl = v;
+    return GF_OK;
+}
+
+int run_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int maux, double dt,
+              double* d_cfl, DevStatus* d_status, double* maxcfl)
+{
+    int rc = enqueue_batch(c, m, d_work, nwork, maux, dt, d_cfl, d_status);
+    if (rc) return rc;
+    return finish_batch(c, d_status, maxcfl);
+}
+
+int check_shape(gf_ctx* c, int mx, int my, int mbc, int meqn, int maux)
+{
+    if (mx != my || !valid_m(mx)) return fail(c, GF_ERR_UNSUPPORTED, "patch size must be mx = my in {8,16,32}");
+    if (mbc != GF_MBC) return fail(c, GF_ERR_UNSUPPORTED, "mbc must be 2");
+    if (meqn != GF_MEQN) return fail(c, GF_ERR_UNSUPPORTED, "meqn must be 3");
+    if (maux < 1) return fail(c, GF_ERR_ARG, "maux must be >= 1 (aux(1) = bathymetry)");
+    return GF_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+void gf_phys_default(gf_phys* p)
+{
+    std::memset(p, 0, sizeof(*p));
+    p->grav = 9.81;
+    p->dry_tolerance = 1.0e-3;
+    p->sea_level = 0.0;
+    p->friction_depth = 1.0e6;
+    p->manning_coefficient[0] = 0.035;
+    p->manning_break[0] = 1.0e10;
+    p->num_manning = 1;
+    p->friction_forcing = 1;
+    p->variable_friction = 0;
+    p->friction_index = 0;
+    p->order = 2;
+    p->transverse = 2;
+    p->mthlim[0] = p->mthlim[1] = p->mthlim[2] = 4;
+    p->src_term = 1;
+    p->maxcfl_cap = 100.0;
+}
+
+int gf_ctx_create(int device, gf_ctx** out)
+{
+    if (!out) return GF_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GF_ERR_CUDA;
+    if (device < 0 || device >= ndev) return GF_ERR_ARG;
+    gf_ctx* c = new gf_ctx();
+    c->device = device;
+    c->h_phys.resize(GF_MAX_PHYS);
+    c->phys_set.assign(GF_MAX_PHYS, 0);
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_phys, sizeof(gf_phys) * GF_MAX_PHYS);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_gdt, sizeof(double) * 64);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_gdt, sizeof(double) * 64);
+    if (e != cudaSuccess) {
+        gf_ctx_destroy(c);
+        return e == cudaErrorMemoryAllocation ? GF_ERR_NOMEM : GF_ERR_CUDA;
+    }
+    *out = c;
+    return GF_OK;
+}
+
+void gf_ctx_destroy(gf_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->q_aos.release();
+    c->q_soa.release();
+    c->aux_aos.release();
+    c->aux_soa.release();
+    c->cfl.release();
+    c->work.release();
+    c->h_stage.release();
+    c->h_cfl.release();
+    c->h_work.release();
+    if (c->d_phys) cudaFree(c->d_phys);
+    if (c->d_status) cudaFree(c->d_status);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->d_gdt) cudaFree(c->d_gdt);
+    if (c->h_gdt) cudaFreeHost(c->h_gdt);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* gf_ctx_last_error(const gf_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+int gf_ctx_set_phys(gf_ctx* c, int slot, const gf_phys* p)
+{
+    if (!c || !p) return GF_ERR_ARG;
+    if (slot < 0 || slot >= GF_MAX_PHYS) return fail(c, GF_ERR_ARG, "physics slot out of range");
+    if (p->num_manning < 0 || p->num_manning > GF_MAX_MANNING)
+        return fail(c, GF_ERR_ARG, "num_manning out of range");
+    if (p->order != 1 && p->order != 2) return fail(c, GF_ERR_ARG, "order must be 1 or 2");
+    if (p->transverse < 0 || p->transverse > 2) return fail(c, GF_ERR_ARG, "transverse must be 0..2");
+    if (!(p->grav > 0.0) || !(p->dry_tolerance >= 0.0)) return fail(c, GF_ERR_ARG, "bad grav / dry_tolerance");
+    GF_CK(c, cudaSetDevice(c->device));
+    c->h_phys[slot] = *p;
+    c->phys_set[slot] = 1;
+    GF_CK(c, cudaMemcpyAsync(c->d_phys + slot, &c->h_phys[slot], sizeof(gf_phys),
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_patch_update(gf_ctx* c, int mx, int my, int mbc, int meqn, int maux, double dx, double dy,
+                    double t, double dt, double* q, const double* aux, double* cfl)
+{
+    double* qs[1] = {q};
+    const double* as[1] = {aux};
+    double dxs[1] = {dx}, dys[1] = {dy};
+    double maxcfl = 0.0;
+    int rc = gf_patch_update_batch(c, 1, mx, my, mbc, meqn, maux, dxs, dys, t, dt, qs, as, nullptr,
+                                   &maxcfl);
+    if (rc == GF_OK && cfl) *cfl = maxcfl;
+    return rc;
+}
+
+int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int meqn, int maux,
+                          const double* dx, const double* dy, double t, double dt, double* const* q,
+                          const double* const* aux, double* cfl, double* maxcfl)
+{
+    (void)t;
+    if (!c) return GF_ERR_ARG;
+    int rc = check_shape(c, mx, my, mbc, meqn, maux);
+    if (rc) return rc;
+    if (npatch < 0 || (npatch > 0 && (!dx || !dy || !q || !aux)))
+        return fail(c, GF_ERR_ARG, "null argument");
+    if ((rc = check_phys_slot(c, 0))) return rc;
+    if (npatch == 0) {
+        if (maxcfl) *maxcfl = 0.0;
+        return GF_OK;
+    }
+    GF_CK(c, cudaSetDevice(c->device));
+    const long S = cells_of(mx, my);
+    const size_t qn = (size_t)npatch * 3 * S, an = (size_t)npatch * maux * S;
+    GF_CK(c, c->q_aos.reserve(qn));
+    GF_CK(c, c->q_soa.reserve(qn));
+    GF_CK(c, c->aux_aos.reserve(an));
+    GF_CK(c, c->aux_soa.reserve(an));
+    GF_CK(c, c->cfl.reserve(npatch));
+    GF_CK(c, c->work.reserve(npatch));
+    GF_CK(c, c->h_stage.reserve(qn + an));
+    GF_CK(c, c->h_work.reserve(npatch));
+    GF_CK(c, c->h_cfl.reserve(npatch));
+
+    /* Gather the patches into one pinned block, one copy in each direction. */
+    double* hq = c->h_stage.p;
+    double* ha = c->h_stage.p + qn;
+    for (int k = 0; k < npatch; ++k) {
+        if (!q[k] || !aux[k]) return fail(c, GF_ERR_ARG, "null patch pointer");
+        std::memcpy(hq + (size_t)k * 3 * S, q[k], sizeof(double) * 3 * S);
+        std::memcpy(ha + (size_t)k * maux * S, aux[k], sizeof(double) * maux * S);
+        gf_patch_work w;
+        w.q = c->q_soa.p + (size_t)k * 3 * S;
+        w.aux = c->aux_soa.p + (size_t)k * maux * S;
+        w.dx = dx[k];
+        w.dy = dy[k];
+        w.phys = 0;
+        w.group = 0;
+        c->h_work.p[k] = w;
+    }
+    GF_CK(c, cudaMemcpyAsync(c->q_aos.p, hq, sizeof(double) * qn, cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaMemcpyAsync(c->aux_aos.p, ha, sizeof(double) * an, cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaMemcpyAsync(c->work.p, c->h_work.p, sizeof(gf_patch_work) * npatch,
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_aos_to_soa(c->q_aos.p, c->q_soa.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
+    GF_CK(c, gf::launch_aos_to_soa(c->aux_aos.p, c->aux_soa.p, npatch, (int)S, maux, maux * S,
+                                   maux * S, c->stream));
+    double mc = 0.0;
+    rc = run_batch(c, mx, c->work.p, npatch, maux, dt, c->cfl.p, c->d_status, &mc);
+    if (rc) return rc;
+    GF_CK(c, gf::launch_soa_to_aos(c->q_soa.p, c->q_aos.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
+    GF_CK(c, cudaMemcpyAsync(hq, c->q_aos.p, sizeof(double) * qn, cudaMemcpyDeviceToHost, c->stream));
+    if (cfl)
+        GF_CK(c, cudaMemcpyAsync(c->h_cfl.p, c->cfl.p, sizeof(double) * npatch,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < npatch; ++k) std::memcpy(q[k], hq + (size_t)k * 3 * S, sizeof(double) * 3 * S);
+    if (cfl) std::memcpy(cfl, c->h_cfl.p, sizeof(double) * npatch);
+    if (maxcfl) *maxcfl = mc;
+    return GF_OK;
+}
+
+/* ------------------------------------------------------------- levels */
+
+int gf_level_create(gf_ctx* c, int npatch, int mx, int my, int maux, gf_level** out)
+{
+    if (!c || !out) return GF_ERR_ARG;
+    *out = nullptr;
+    int rc = check_shape(c, mx, my, GF_MBC, GF_MEQN, maux);
+    if (rc) return rc;
+    if (npatch <= 0) return fail(c, GF_ERR_ARG, "npatch must be positive");
+    GF_CK(c, cudaSetDevice(c->device));
+    gf_level* L = new gf_level();
+    L->ctx = c;
+    L->npatch = npatch;
+    L->mx = mx;
+    L->my = my;
+    L->maux = maux;
+    L->S = cells_of(mx, my);
+    L->dx.assign(npatch, 1.0);
+    L->dy.assign(npatch, 1.0);
+    L->phys.assign(npatch, 0);
+    L->xlower.assign(npatch, 0.0);
+    L->ylower.assign(npatch, 0.0);
+    for (int s = 0; s < 4; ++s) L->bc.mthbc[s] = 1;
+    const size_t qn = (size_t)npatch * 3 * L->S, an = (size_t)npatch * maux * L->S;
+    cudaError_t e = cudaMalloc(&L->d_q, qn * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_aux, an * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_stage, std::max(qn, an) * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_cfl, npatch * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_work, npatch * sizeof(gf_patch_work));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_status, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_nbr, (size_t)npatch * 8 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_geom, (size_t)npatch * sizeof(gf_patch_geom));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_phys_of, (size_t)npatch * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(L->d_aux, 0, an * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(L->d_q, 0, qn * sizeof(double));
+    if (e != cudaSuccess) {
+        gf_level_destroy(L);
+        return cuda_fail(c, e, "gf_level_create");
+    }
+    *out = L;
+    return GF_OK;
+}
+
+void gf_level_destroy(gf_level* L)
+{
+    if (!L) return;
+    cudaSetDevice(L->ctx->device);
+    cudaStreamSynchronize(L->ctx->stream);
+    if (L->d_q) cudaFree(L->d_q);
+    if (L->d_aux) cudaFree(L->d_aux);
+    if (L->d_stage) cudaFree(L->d_stage);
+    if (L->d_cfl) cudaFree(L->d_cfl);
+    if (L->d_work) cudaFree(L->d_work);
+    if (L->d_status) cudaFree(L->d_status);
+    if (L->d_nbr) cudaFree(L->d_nbr);
+    if (L->d_geom) cudaFree(L->d_geom);
+    if (L->d_phys_of) cudaFree(L->d_phys_of);
+    delete L;
+}
+
+int gf_level_set_geometry(gf_level* L, const double* dx, const double* dy, const int* phys)
+{
+    if (!L || !dx || !dy) return GF_ERR_ARG;
+    for (int k = 0; k < L->npatch; ++k) {
+        if (!(dx[k] > 0.0) || !(dy[k] > 0.0)) return fail(L->ctx, GF_ERR_ARG, "dx, dy must be positive");
+        if (phys && (phys[k] < 0 || phys[k] >= GF_MAX_PHYS)) return fail(L->ctx, GF_ERR_ARG, "bad physics slot");
+    }
+    std::copy(dx, dx + L->npatch, L->dx.begin());
+    std::copy(dy, dy + L->npatch, L->dy.begin());
+    if (phys) std::copy(phys, phys + L->npatch, L->phys.begin());
+    else std::fill(L->phys.begin(), L->phys.end(), 0);
+    L->work_dirty = true;
+    L->geom_dirty = true;
+    return GF_OK;
+}
+
+int gf_level_set_layout(gf_level* L, const int* nbr, const double* xlower, const double* ylower)
+{
+    if (!L || !nbr) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    for (long k = 0; k < 8L * L->npatch; ++k)
+        if (nbr[k] < -1 || nbr[k] >= L->npatch) return fail(c, GF_ERR_ARG, "neighbour index out of range");
+    for (int k = 0; k < L->npatch; ++k)
+        for (int s = 0; s < 8; ++s)
+            if (nbr[8 * k + s] == k) return fail(c, GF_ERR_ARG, "a patch cannot neighbour itself");
+    GF_CK(c, cudaSetDevice(c->device));
+    if (xlower) std::copy(xlower, xlower + L->npatch, L->xlower.begin());
+    if (ylower) std::copy(ylower, ylower + L->npatch, L->ylower.begin());
+    GF_CK(c, cudaMemcpyAsync(L->d_nbr, nbr, (size_t)L->npatch * 8 * sizeof(int),
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    L->layout_set = true;
+    L->geom_dirty = true;
+    return GF_OK;
+}
+
+int gf_level_set_bc(gf_level* L, const int* mthbc)
+{
+    if (!L || !mthbc) return GF_ERR_ARG;
+    for (int s = 0; s < 4; ++s) {
+        if (mthbc[s] < 0 || mthbc[s] > 3) return fail(L->ctx, GF_ERR_ARG, "mthbc must be 0..3");
+        if (mthbc[s] == 0 && !L->bc.hydro_side[s])
+            return fail(L->ctx, GF_ERR_ARG,
+                        "mthbc = 0 needs a hydrograph on that side (the reference stops here)");
+        L->bc.mthbc[s] = mthbc[s];
+    }
+    return GF_OK;
+}
+
+int gf_level_set_hydrograph(gf_level* L, int n, const double* time, const double* hu,
+                            const int* side, double width, double x0, double y0)
+{
+    if (!L || n < 0 || (n > 0 && (!time || !hu || !side))) return GF_ERR_ARG;
+    for (int i = 1; i < n; ++i)
+        if (!(time[i] >= time[i - 1])) return fail(L->ctx, GF_ERR_ARG, "hydrograph times must increase");
+    L->hy_time.assign(time, time + n);
+    L->hy_hu.assign(hu, hu + n);
+    for (int s = 0; s < 4; ++s) L->bc.hydro_side[s] = n > 0 ? (side[s] != 0) : 0;
+    L->bc.width = width;
+    L->bc.x0 = x0;
+    L->bc.y0 = y0;
+    return GF_OK;
+}
+
+/* interpolation (hydrograph/hydrograh_module.f90:176-221), discharge type */
+static double hydro_interp(const gf_level* L, double t)
+{
+    const std::vector<double>& tm = L->hy_time;
+    const std::vector<double>& hu = L->hy_hu;
+    const size_t n = tm.size();
+    if (n == 0) return 0.0;
+    if (t < tm[0]) return hu[0];
+    if (t > tm[n - 1]) return hu[n - 1];
+    for (size_t i = 0; i + 1 < n; ++i)
+        if (t >= tm[i] && t <= tm[i + 1])
+            return hu[i] + (hu[i + 1] - hu[i]) / (tm[i + 1] - tm[i]) * (t - tm[i]);
+    return 0.0;
+}
+
+int gf_level_ghost_fill_async(gf_level* L, double t)
+{
+    if (!L) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    if (!L->layout_set) return fail(c, GF_ERR_STATE, "level layout (neighbour table) not set");
+    GF_CK(c, cudaSetDevice(c->device));
+    if (L->geom_dirty) {
+        std::vector<gf_patch_geom> g(L->npatch);
+        for (int k = 0; k < L->npatch; ++k) g[k] = {L->xlower[k], L->ylower[k], L->dx[k], L->dy[k]};
+        GF_CK(c, cudaMemcpyAsync(L->d_geom, g.data(), g.size() * sizeof(gf_patch_geom),
+                                 cudaMemcpyHostToDevice, c->stream));
+        GF_CK(c, cudaMemcpyAsync(L->d_phys_of, L->phys.data(), L->phys.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, c->stream));
+        GF_CK(c, cudaStreamSynchronize(c->stream));
+        L->geom_dirty = false;
+    }
+    gf_bc_spec bc = L->bc;
+    bc.q0hu = hydro_interp(L, t);
+    GF_CK(c, gf::launch_ghost_fill(L->mx, L->d_q, L->d_aux, L->maux, L->npatch, L->d_nbr, L->d_geom,
+                                   bc, c->d_phys, L->d_phys_of, c->stream));
+    return GF_OK;
+}
+
+int gf_level_ghost_fill(gf_level* L, double t)
+{
+    int rc = gf_level_ghost_fill_async(L, t);
+    if (rc) return rc;
+    GF_CK(L->ctx, cudaStreamSynchronize(L->ctx->stream));
+    return GF_OK;
+}
+
+static int level_upload_q_async(gf_level* L, const double* q)
+{
+    gf_ctx* c = L->ctx;
+    const size_t qn = (size_t)L->npatch * 3 * L->S;
+    GF_CK(c, cudaMemcpyAsync(L->d_stage, q, qn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_aos_to_soa(L->d_stage, L->d_q, L->npatch, (int)L->S, 3, 3 * L->S, 3 * L->S,
+                                   c->stream));
+    return GF_OK;
+}
+
+static int level_download_q_async(gf_level* L, double* q)
+{
+    gf_ctx* c = L->ctx;
+    const size_t qn = (size_t)L->npatch * 3 * L->S;
+    GF_CK(c, gf::launch_soa_to_aos(L->d_q, L->d_stage, L->npatch, (int)L->S, 3, 3 * L->S, 3 * L->S,
+                                   c->stream));
+    GF_CK(c, cudaMemcpyAsync(q, L->d_stage, qn * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return GF_OK;
+}
+
+int gf_level_upload(gf_level* L, const double* q, const double* aux)
+{
+    if (!L || !q) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    if (aux) {
+        const size_t an = (size_t)L->npatch * L->maux * L->S;
+        GF_CK(c, cudaMemcpyAsync(L->d_stage, aux, an * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        GF_CK(c, gf::launch_aos_to_soa(L->d_stage, L->d_aux, L->npatch, (int)L->S, L->maux,
+                                       L->maux * L->S, L->maux * L->S, c->stream));
+        L->aux_loaded = true;
+    }
+    int rc = level_upload_q_async(L, q);
+    if (rc) return rc;
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_level_download(gf_level* L, double* q)
+{
+    if (!L || !q) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    int rc = level_download_q_async(L, q);
+    if (rc) return rc;
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_level_download_aux(gf_level* L, double* aux)
+{
+    if (!L || !aux) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    const size_t an = (size_t)L->npatch * L->maux * L->S;
+    GF_CK(c, gf::launch_soa_to_aos(L->d_aux, L->d_stage, L->npatch, (int)L->S, L->maux,
+                                   L->maux * L->S, L->maux * L->S, c->stream));
+    GF_CK(c, cudaMemcpyAsync(aux, L->d_stage, an * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+static int level_prepare(gf_level* L)
+{
+    gf_ctx* c = L->ctx;
+    if (!L->aux_loaded) return fail(c, GF_ERR_STATE, "level aux (bathymetry) not uploaded");
+    for (int k = 0; k < L->npatch; ++k) {
+        int rc = check_phys_slot(c, L->phys[k]);
+        if (rc) return rc;
+    }
+    if (!L->work_dirty) return GF_OK;
+    std::vector<gf_patch_work> w(L->npatch);
+    for (int k = 0; k < L->npatch; ++k) {
+        w[k].q = L->d_q + (size_t)k * 3 * L->S;
+        w[k].aux = L->d_aux + (size_t)k * L->maux * L->S;
+        w[k].dx = L->dx[k];
+        w[k].dy = L->dy[k];
+        w[k].phys = L->phys[k];
+        w[k].group = 0;
+    }
+    GF_CK(c, cudaMemcpyAsync(L->d_work, w.data(), w.size() * sizeof(gf_patch_work),
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    L->work_dirty = false;
+    return GF_OK;
+}
+
+int gf_level_step(gf_level* L, double t, double dt, double* maxcfl)
+{
+    (void)t;
+    if (!L) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    int rc = level_prepare(L);
+    if (rc) return rc;
+    return run_batch(c, L->mx, L->d_work, L->npatch, L->maux, dt, L->d_cfl, L->d_status, maxcfl);
+}
+
+int gf_level_ghost_fill_async(gf_level* L, double t);
+
+int gf_level_step_host(gf_level* L, double* q, double t, double dt, double* maxcfl)
+{
+    if (!L || !q) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    int rc = level_prepare(L);
+    if (rc) return rc;
+    if ((rc = level_upload_q_async(L, q))) return rc;
+    double mc = 0.0;
+    if ((rc = enqueue_batch(c, L->mx, L->d_work, L->npatch, L->maux, dt, L->d_cfl, L->d_status)))
+        return rc;
+    if (L->layout_set && (rc = gf_level_ghost_fill_async(L, t + dt))) return rc;
+    if ((rc = finish_batch(c, L->d_status, &mc))) return rc;
+    if ((rc = level_download_q_async(L, q))) return rc;
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    if (maxcfl) *maxcfl = mc;
+    return GF_OK;
+}
+
+int gf_level_step_async(gf_level* L, double t, double dt)
+{
+    (void)t;
+    if (!L) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    int rc = level_prepare(L);
+    if (rc) return rc;
+    return enqueue_batch(c, L->mx, L->d_work, L->npatch, L->maux, dt, L->d_cfl, L->d_status);
+}
+
+int gf_level_sync(gf_level* L, double* maxcfl)
+{
+    if (!L) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    return finish_batch(c, L->d_status, maxcfl);
+}
+
+int gf_ctx_set_fp_contract(gf_ctx* c, int allow)
+{
+    if (!c) return GF_ERR_ARG;
+    c->exact = (allow == 0);
+    return GF_OK;
+}
+
+int gf_ctx_stream(gf_ctx* c, void** stream)
+{
+    if (!c || !stream) return GF_ERR_ARG;
+    *stream = (void*)c->stream;
+    return GF_OK;
+}
+
+int gf_level_patch_cfl(gf_level* L, double* cfl)
+{
+    if (!L || !cfl) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    GF_CK(c, cudaSetDevice(c->device));
+    GF_CK(c, cudaMemcpyAsync(cfl, L->d_cfl, L->npatch * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_level_device_planes(gf_level* L, double** q, double** aux)
+{
+    if (!L) return GF_ERR_ARG;
+    if (q) *q = L->d_q;
+    if (aux) *aux = L->d_aux;
+    return GF_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,32 @@
+/* Internal declarations shared by the kernels and the C-ABI layer. */
+#ifndef GF_INTERNAL_H
+#define GF_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "gf_types.h"
+
+namespace gf {
+
+cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, const gf_phys* phys,
+                                double dt, const double* gdt, int maux, double* cfl,
+                                unsigned long long* gmax, int* err, cudaStream_t st);
+size_t patch_update_smem_bytes(int m);
+cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwork,
+                                      const gf_phys* phys, double dt, const double* gdt, int maux,
+                                      double* cfl, unsigned long long* gmax, int* err,
+                                      cudaStream_t st);
+
+cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int ncell, int nf,
+                              long src_stride, long dst_stride, cudaStream_t st);
+cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int ncell, int nf,
+                              long src_stride, long dst_stride, cudaStream_t st);
+
+cudaError_t launch_ghost_fill(int m, double* q, double* aux, int maux, int npatch, const int* nbr,
+                              const gf_patch_geom* geom, const gf_bc_spec& bc,
+                              const gf_phys* phys, const int* phys_of, cudaStream_t st);
+
+} // namespace gf
+
+#endif

@@ -1,0 +1,50 @@
+/*
+ * The patch update compiled with floating-point contraction off
+ * (-fmad=false, set by the build for this file) and with the reference's
+ * four flux accumulators fm, fp, gm, gp summed in its order. Every FP64
+ * operation then rounds as the Fortran expression is written, so the result
+ * matches the restated Fortran bit for bit apart from the libm/CUDA pow()
+ * in the friction term. Used to prove parity; the production path is the
+ * contracted build in gf_kernels.cu.
+ */
+#include <cuda_runtime.h>
+
+#define GF_KNS gf_exact
+#include "gf_internal.h"
+#include "gf_patch_update.cuh"
+
+namespace gf {
+
+template <int M, int NT, int RB>
+static cudaError_t launch_exact(const gf_patch_work* work, int nwork, const gf_phys* phys,
+                                double dt, const double* gdt, int maux, double* cfl,
+                                unsigned long long* gmax, int* err, cudaStream_t st)
+{
+    using L = gf_exact::Smem<M, RB, true>;
+    auto kern = gf_exact::patch_update_kernel<M, NT, RB, 1, true>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)L::BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    if (nwork <= 0) return cudaSuccess;
+    kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwork,
+                                      const gf_phys* phys, double dt, const double* gdt, int maux,
+                                      double* cfl, unsigned long long* gmax, int* err,
+                                      cudaStream_t st)
+{
+    switch (m) {
+    case 32: return launch_exact<32, 256, 4>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
+    case 16: return launch_exact<16, 128, 6>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
+    case 8: return launch_exact<8, 64, 5>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+} // namespace gf

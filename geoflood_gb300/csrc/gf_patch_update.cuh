@@ -1,0 +1,556 @@
+/*
+ * Fused GeoClaw patch update for sm_103a: b4step2 + step2 + CFL + src2 on a
+ * batch of patches, one CTA per patch.
+ *
+ * Reference behaviour (paths relative to the GeoFlood source tree):
+ *   geoclaw_update              src/fc2d_geoclaw/fc2d_geoclaw.cpp:352-387
+ *   b4step2                     fortran_source/geoclaw_b4step2_fort.f90:183-186
+ *   step2 sweeps                fortran_source/geoclaw_step2_fort.f90:80-250
+ *   flux2 (f-wave form)         fortran_source/geoclaw_flux2fw_fort.f:113-267
+ *   limiter / philim            fortran_source/geoclaw_limiter_fort.f:34-58, philim.f
+ *   flux-difference update      fortran_source/geoclaw_step2_wrap_fort.f:95-115
+ *   src2 (Manning friction)     fortran_source/geoclaw_src2_fort.f90:41-71
+ *
+ * The kernel computes exactly the faces the interior update depends on:
+ * normal solves on faces 0..m+2 of slices 0..m+1, limiting / transverse
+ * splitting on faces 1..m+1 (the Fortran's own ranges), and writes the
+ * interior cells only. Ghost cells are refilled by the ghost-fill step
+ * before they are read again, so their post-step values are not part of
+ * the state.
+ *
+ * Accumulation: the per-face outputs of a band of slices go to shared
+ * memory; each interior cell then gathers its six contributing faces in
+ * slice order into two flux-difference accumulators
+ *   DX = fm(i+1,j) - fp(i,j),  DY = gm(i,j+1) - gp(i,j)
+ * so every cell is written by one thread per band, in a fixed order: the
+ * result is deterministic and independent of launch shape.
+ */
+#ifndef GF_PATCH_UPDATE_CUH
+#define GF_PATCH_UPDATE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gf_riemann.cuh"
+#include "gf_types.h"
+
+#ifndef GF_KNS
+#define GF_KNS gf
+#endif
+
+namespace GF_KNS {
+
+/* ---- bulk-async (TMA) copy + mbarrier helpers (inline PTX, sm_90+) ---- */
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+/* Bounded wait on phase `parity`; returns false if the limit ran out. */
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_iter)
+{
+    for (uint32_t it = 0; it < max_iter; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+/* Order-preserving key of a non-negative double (for atomicMax). */
+__device__ __forceinline__ unsigned long long dkey(double v)
+{
+    return static_cast<unsigned long long>(__double_as_longlong(v));
+}
+
+template <int M>
+struct Geo {
+    static constexpr int N = M + 2 * GF_MBC; /* cells per row incl. halo */
+    static constexpr int S = N * N;          /* cells per plane          */
+    static constexpr int FA = M + 3;         /* normal-solve faces/slice */
+    static constexpr int FB = M + 1;         /* limited faces / slice    */
+    static constexpr int NSLICE = M + 2;     /* slices 0..m+1            */
+};
+
+/* Shared-memory layout (doubles unless noted). NACC flux accumulators of
+ * 3 components per interior cell: 2 (DX, DY) in the fast form, 4 (fm, fp,
+ * gm, gp) in the exact form. */
+template <int M, int RB, bool EXACT = false>
+struct Smem {
+    static constexpr int NACC = EXACT ? 4 : 2;
+    using G = Geo<M>;
+    static constexpr int W_STRIDE = 12; /* s[3] + fw[3][3]                   */
+    static constexpr int O_STRIDE = 18; /* faddm faddp A B C D, 3 comps each */
+    static constexpr int OFF_H = 0;
+    static constexpr int OFF_HU = OFF_H + G::S;
+    static constexpr int OFF_HV = OFF_HU + G::S;
+    static constexpr int OFF_B = OFF_HV + G::S;
+    static constexpr int OFF_U = OFF_B + G::S;
+    static constexpr int OFF_V = OFF_U + G::S;
+    static constexpr int OFF_C = OFF_V + G::S;
+    static constexpr int OFF_ACC = OFF_C + G::S;           /* NACC x [3][M*M] */
+    static constexpr int OFF_W = OFF_ACC + NACC * 3 * M * M;
+    static constexpr int OFF_O = OFF_W + RB * G::FA * W_STRIDE;
+    static constexpr int OFF_RED = OFF_O + RB * G::FB * O_STRIDE; /* 2*32 doubles */
+    static constexpr int OFF_BAR = OFF_RED + 64;                    /* 1 x u64     */
+    static constexpr int OFF_WET = OFF_BAR + 2;                     /* S bytes     */
+    static constexpr size_t BYTES = (size_t)OFF_WET * 8 + ((G::S + 15) / 16) * 16;
+};
+
+/* Load the cell view for a face sweep in direction DIR (0 = x, 1 = y). */
+template <int DIR>
+__device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned char* wet, int k,
+                                             int offH, int offHU, int offHV, int offB, int offU,
+                                             int offV, int offC)
+{
+    gf_cell c;
+    c.h = sm[offH + k];
+    c.b = sm[offB + k];
+    c.c = sm[offC + k];
+    c.wet = wet[k] != 0;
+    if (DIR == 0) {
+        c.hun = sm[offHU + k]; c.hut = sm[offHV + k];
+        c.un = sm[offU + k];   c.ut = sm[offV + k];
+    } else {
+        c.hun = sm[offHV + k]; c.hut = sm[offHU + k];
+        c.un = sm[offV + k];   c.ut = sm[offU + k];
+    }
+    return c;
+}
+
+/* One sweep direction over all slices, banded. Accumulates into the DX/DY
+ * shared accumulators; returns this thread's max |s| over normal faces. */
+template <int M, int NT, int RB, int DIR, bool EXACT>
+__device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, const gf_phys& P,
+                                        double dtdn, double c16g, double crit, double crit2)
+{
+    using G = Geo<M>;
+    using L = Smem<M, RB, EXACT>;
+    constexpr int N = G::N;
+    double* W = sm + L::OFF_W;
+    double* O = sm + L::OFF_O;
+    /* Normal accumulator N (DX for x-sweeps) and transverse T (DY). */
+    double* ACCN = sm + L::OFF_ACC + (DIR == 0 ? 0 : 3 * M * M);
+    double* ACCT = sm + L::OFF_ACC + (DIR == 0 ? 3 * M * M : 0);
+    const double g = P.grav, drytol = P.dry_tolerance;
+    const double half_dtdn = 0.5 * dtdn;
+    /* local component l -> global component (h, hu, hv) */
+    constexpr int G1 = (DIR == 0) ? 1 : 2; /* normal momentum     */
+    constexpr int G2 = (DIR == 0) ? 2 : 1; /* transverse momentum */
+    double smax = 0.0;
+
+    /* cell (n, t) in sweep coordinates -> shared-plane offset */
+    auto cidx = [](int n, int t) -> int {
+        return DIR == 0 ? (t + 1) * N + (n + 1) : (n + 1) * N + (t + 1);
+    };
+    /* interior cell (n, t) -> accumulator offset */
+    auto aidx = [](int n, int t) -> int {
+        return DIR == 0 ? (n - 1) + M * (t - 1) : (t - 1) + M * (n - 1);
+    };
+
+    /* Exact form: accumulators fm(i+1,j), fp(i,j), gm(i,j+1), gp(i,j) of the
+     * reference, in sweep coordinates N_M, N_P (normal) and T_M, T_P
+     * (transverse), each summed in the reference's order (slices in
+     * increasing order, x sweeps before y sweeps). */
+    constexpr int MM = M * M;
+    double* NM = sm + L::OFF_ACC + (DIR == 0 ? 0 : 6 * MM);
+    double* NP = NM + 3 * MM;
+    double* TM = sm + L::OFF_ACC + (DIR == 0 ? 6 * MM : 0);
+    double* TP = TM + 3 * MM;
+
+    auto gather = [&](int t0, int t1) {
+        /* slices t0..t1 feed cells n in [1, M], t in [t0-1, t1+1] (interior) */
+        const int ta = max(1, t0 - 1), tb = min(M, t1 + 1);
+        const int cnt = (tb - ta + 1) * M;
+        for (int e = threadIdx.x; e < cnt; e += NT) {
+            const int t = ta + e / M;
+            const int n = 1 + e % M;
+            const int a = aidx(n, t);
+            if (EXACT) {
+                if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
+                    const double* fr = O + ((t - 1 - t0) * G::FB + n) * L::O_STRIDE;
+                    const double* fl = O + ((t - 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) TP[a + c * MM] += (0.0 - fr[9 + c]) - fl[15 + c];
+                }
+                if (t >= t0 && t <= t1) {
+                    const double* fr = O + ((t - t0) * G::FB + n) * L::O_STRIDE;
+                    const double* fl = O + ((t - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        NM[a + c * MM] += fr[c];
+                        NP[a + c * MM] += fl[3 + c];
+                        TM[a + c * MM] += (0.0 - fr[9 + c]) - fl[15 + c];
+                        TP[a + c * MM] += (0.0 - fr[6 + c]) - fl[12 + c];
+                    }
+                }
+                if (t + 1 >= t0 && t + 1 <= t1) { /* slice above: down-going parts */
+                    const double* fr = O + ((t + 1 - t0) * G::FB + n) * L::O_STRIDE;
+                    const double* fl = O + ((t + 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) TM[a + c * MM] += (0.0 - fr[6 + c]) - fl[12 + c];
+                }
+            } else {
+                double dn0 = 0.0, dn1 = 0.0, dn2 = 0.0, dt0 = 0.0, dt1 = 0.0, dt2 = 0.0;
+                if (t >= t0 && t <= t1) {
+                    const double* fr = O + ((t - t0) * G::FB + n) * L::O_STRIDE;       /* face n+1 */
+                    const double* fl = O + ((t - t0) * G::FB + (n - 1)) * L::O_STRIDE; /* face n   */
+                    dn0 = fr[0] - fl[3]; dn1 = fr[1] - fl[4]; dn2 = fr[2] - fl[5];
+                    dt0 = (fr[6] - fr[9]) + (fl[12] - fl[15]);
+                    dt1 = (fr[7] - fr[10]) + (fl[13] - fl[16]);
+                    dt2 = (fr[8] - fr[11]) + (fl[14] - fl[17]);
+                }
+                if (t + 1 >= t0 && t + 1 <= t1) { /* slice above: down-going parts */
+                    const double* fr = O + ((t + 1 - t0) * G::FB + n) * L::O_STRIDE;
+                    const double* fl = O + ((t + 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    dt0 += -fr[6] - fl[12]; dt1 += -fr[7] - fl[13]; dt2 += -fr[8] - fl[14];
+                }
+                if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
+                    const double* fr = O + ((t - 1 - t0) * G::FB + n) * L::O_STRIDE;
+                    const double* fl = O + ((t - 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    dt0 += fr[9] + fl[15]; dt1 += fr[10] + fl[16]; dt2 += fr[11] + fl[17];
+                }
+                ACCN[a] += dn0; ACCN[a + MM] += dn1; ACCN[a + 2 * MM] += dn2;
+                ACCT[a] += dt0; ACCT[a + MM] += dt1; ACCT[a + 2 * MM] += dt2;
+            }
+        }
+    };
+
+    int prev_t0 = -1, prev_t1 = -1;
+    for (int t0 = 0; t0 < G::NSLICE; t0 += RB) {
+        const int t1 = min(t0 + RB, G::NSLICE) - 1; /* last slice of band */
+        const int nrow = t1 - t0 + 1;
+
+        /* ---- stage A: normal Riemann solves, faces 0..M+2 ---- */
+        for (int f = threadIdx.x; f < nrow * G::FA; f += NT) {
+            const int t = t0 + f / G::FA;
+            const int n = f % G::FA;
+            const int kl = cidx(n - 1, t), kr = cidx(n, t);
+            double* w = W + f * L::W_STRIDE;
+            if (!wet[kl] && !wet[kr]) {
+#pragma unroll
+                for (int q = 0; q < L::W_STRIDE; ++q) w[q] = 0.0;
+                continue;
+            }
+            const gf_cell cl = load_cell<DIR>(sm, wet, kl, L::OFF_H, L::OFF_HU, L::OFF_HV,
+                                              L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
+            const gf_cell cr = load_cell<DIR>(sm, wet, kr, L::OFF_H, L::OFF_HU, L::OFF_HV,
+                                              L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
+            double s[3], fw[3][3];
+            gf_rpn2_face(cl, cr, g, drytol, c16g, crit, crit2, s, fw);
+#pragma unroll
+            for (int mw = 0; mw < 3; ++mw) {
+                w[mw] = s[mw];
+                w[3 + 3 * mw + 0] = fw[mw][0];
+                w[3 + 3 * mw + 1] = fw[mw][1];
+                w[3 + 3 * mw + 2] = fw[mw][2];
+                smax = fmax(smax, fabs(s[mw]));
+            }
+        }
+        if (prev_t0 >= 0) gather(prev_t0, prev_t1);
+        __syncthreads();
+
+        /* ---- stage B: limiter, 2nd-order terms, transverse split ---- */
+        for (int f = threadIdx.x; f < nrow * G::FB; f += NT) {
+            const int t = t0 + f / G::FB;
+            const int n = 1 + f % G::FB;
+            const int kl = cidx(n - 1, t), kr = cidx(n, t);
+            double* o = O + f * L::O_STRIDE;
+            if (!wet[kl] && !wet[kr]) {
+#pragma unroll
+                for (int q = 0; q < L::O_STRIDE; ++q) o[q] = 0.0;
+                continue;
+            }
+            const double* wc = W + ((t - t0) * G::FA + n) * L::W_STRIDE;
+            double s[3], fw[3][3];
+#pragma unroll
+            for (int mw = 0; mw < 3; ++mw) {
+                s[mw] = wc[mw];
+                fw[mw][0] = wc[3 + 3 * mw]; fw[mw][1] = wc[4 + 3 * mw]; fw[mw][2] = wc[5 + 3 * mw];
+            }
+            /* fluctuations from the unlimited f-waves (rpn2_geoclaw.f:359-376) */
+            double amdq[3] = {0.0, 0.0, 0.0}, apdq[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+            for (int mw = 0; mw < 3; ++mw) {
+                if (s[mw] < 0.0) {
+                    amdq[0] += fw[mw][0]; amdq[1] += fw[mw][1]; amdq[2] += fw[mw][2];
+                } else if (s[mw] > 0.0) {
+                    apdq[0] += fw[mw][0]; apdq[1] += fw[mw][1]; apdq[2] += fw[mw][2];
+                } else {
+                    amdq[0] += 0.5 * fw[mw][0]; amdq[1] += 0.5 * fw[mw][1]; amdq[2] += 0.5 * fw[mw][2];
+                    apdq[0] += 0.5 * fw[mw][0]; apdq[1] += 0.5 * fw[mw][1]; apdq[2] += 0.5 * fw[mw][2];
+                }
+            }
+            double faddm[3] = {amdq[0], amdq[1], amdq[2]};
+            double faddp[3] = {-apdq[0], -apdq[1], -apdq[2]};
+            if (P.order != 1) {
+                const double* wl = wc - L::W_STRIDE; /* face n-1 */
+                const double* wr = wc + L::W_STRIDE; /* face n+1 */
+                double cq[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+                for (int mw = 0; mw < 3; ++mw) {
+                    const double* fa = fw[mw];
+                    double lim = 1.0;
+                    if (P.mthlim[mw] != 0) {
+                        /* dot products in the global (h, hu, hv) order */
+                        const double a0 = fa[0], a1 = (DIR == 0) ? fa[1] : fa[2],
+                                     a2 = (DIR == 0) ? fa[2] : fa[1];
+                        const double* ql = wl + 3 + 3 * mw;
+                        const double* qr = wr + 3 + 3 * mw;
+                        const double l0 = ql[0], l1 = (DIR == 0) ? ql[1] : ql[2],
+                                     l2 = (DIR == 0) ? ql[2] : ql[1];
+                        const double r0 = qr[0], r1 = (DIR == 0) ? qr[1] : qr[2],
+                                     r2 = (DIR == 0) ? qr[2] : qr[1];
+                        const double wnorm2 = a0 * a0 + a1 * a1 + a2 * a2;
+                        if (wnorm2 != 0.0) {
+                            const double dotl = l0 * a0 + l1 * a1 + l2 * a2;
+                            const double dotr = a0 * r0 + a1 * r1 + a2 * r2;
+                            lim = gf_philim(wnorm2, s[mw] > 0.0 ? dotl : dotr, P.mthlim[mw]);
+                        }
+                    }
+                    const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
+                    cq[0] += fac * (lim * fa[0]);
+                    cq[1] += fac * (lim * fa[1]);
+                    cq[2] += fac * (lim * fa[2]);
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    faddm[c] += 0.5 * cq[c];
+                    faddp[c] += 0.5 * cq[c];
+                }
+                if (P.transverse == 2) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        amdq[c] += cq[c];
+                        apdq[c] -= cq[c];
+                    }
+                }
+            }
+            double A[3] = {0, 0, 0}, B[3] = {0, 0, 0}, C[3] = {0, 0, 0}, D[3] = {0, 0, 0};
+            if (P.transverse != 0) {
+                double bm[3], bp[3];
+                if (wet[kl]) { /* rpt2 imp=1: left-going part into cell n-1 */
+                    const gf_cell cl = load_cell<DIR>(sm, wet, kl, L::OFF_H, L::OFF_HU, L::OFF_HV,
+                                                      L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
+                    gf_rpt2_face(cl, sm[L::OFF_B + cidx(n - 1, t - 1)],
+                                 sm[L::OFF_B + cidx(n - 1, t + 1)], drytol, amdq, bm, bp);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { A[c] = half_dtdn * bm[c]; B[c] = half_dtdn * bp[c]; }
+                }
+                if (wet[kr]) { /* rpt2 imp=2: right-going part into cell n */
+                    const gf_cell cr = load_cell<DIR>(sm, wet, kr, L::OFF_H, L::OFF_HU, L::OFF_HV,
+                                                      L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
+                    gf_rpt2_face(cr, sm[L::OFF_B + cidx(n, t - 1)], sm[L::OFF_B + cidx(n, t + 1)],
+                                 drytol, apdq, bm, bp);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { C[c] = half_dtdn * bm[c]; D[c] = half_dtdn * bp[c]; }
+                }
+            }
+            /* write in global component order (h, hu, hv) */
+            o[0] = faddm[0]; o[G1] = faddm[1]; o[G2] = faddm[2];
+            o[3] = faddp[0]; o[3 + G1] = faddp[1]; o[3 + G2] = faddp[2];
+            o[6] = A[0]; o[6 + G1] = A[1]; o[6 + G2] = A[2];
+            o[9] = B[0]; o[9 + G1] = B[1]; o[9 + G2] = B[2];
+            o[12] = C[0]; o[12 + G1] = C[1]; o[12 + G2] = C[2];
+            o[15] = D[0]; o[15 + G1] = D[1]; o[15 + G2] = D[2];
+        }
+        __syncthreads();
+        prev_t0 = t0;
+        prev_t1 = t1;
+    }
+    gather(prev_t0, prev_t1);
+    __syncthreads();
+    return smax;
+}
+
+/* Manning friction source term on one interior cell (geoclaw_src2_fort.f90:41-71). */
+__device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double bathy, double nvar,
+                                          double& h, double& hu, double& hv)
+{
+    if (!P.friction_forcing) return;
+    if (h < 1.0e-30) {
+        hu = 0.0;
+        hv = 0.0;
+    } else if (h <= P.friction_depth) {
+        double coeff = 0.0;
+        if (!P.variable_friction) {
+            for (int nman = P.num_manning; nman >= 1; --nman)
+                if (bathy < P.manning_break[nman - 1]) coeff = P.manning_coefficient[nman - 1];
+        } else {
+            coeff = nvar;
+        }
+        const double gamma =
+            sqrt(hu * hu + hv * hv) * P.grav * (coeff * coeff) / pow(h, 7.0 / 3.0);
+        const double dgamma = 1.0 + dt * gamma;
+        hu = hu / dgamma;
+        hv = hv / dgamma;
+    }
+}
+
+/* The fused kernel. One CTA per work item. */
+template <int M, int NT, int RB, int MINB, bool EXACT>
+__global__ void __launch_bounds__(NT, MINB)
+    patch_update_kernel(const gf_patch_work* __restrict__ work, int nwork,
+                        const gf_phys* __restrict__ phys_table, double dt_uniform,
+                        const double* __restrict__ group_dt, int maux,
+                        double* __restrict__ cfl_out, unsigned long long* __restrict__ group_max,
+                        int* __restrict__ err)
+{
+    using G = Geo<M>;
+    using L = Smem<M, RB, EXACT>;
+    constexpr int N = G::N;
+    constexpr int S = G::S;
+    extern __shared__ __align__(128) double sm[];
+    unsigned char* wet = reinterpret_cast<unsigned char*>(sm + L::OFF_WET);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::OFF_BAR);
+    double* red = sm + L::OFF_RED;
+
+    const int wi = blockIdx.x;
+    if (wi >= nwork) return;
+    const gf_patch_work wk = work[wi];
+    const gf_phys P = phys_table[wk.phys];
+    const double g = P.grav, drytol = P.dry_tolerance;
+    const double dt = group_dt ? group_dt[wk.group] : dt_uniform;
+
+    /* ---- stage the patch (h, hu, hv planes and b) with bulk copies ---- */
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(bar, (uint32_t)(4 * S * sizeof(double)));
+        bulk_g2s(sm + L::OFF_H, wk.q, (uint32_t)(3 * S * sizeof(double)), bar);
+        bulk_g2s(sm + L::OFF_B, wk.aux, (uint32_t)(S * sizeof(double)), bar);
+    }
+    if (!mbar_wait(bar, 0, 1u << 22)) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        mbar_wait(bar, 0, 1u << 22); /* let any copy in flight land */
+        return;
+    }
+
+    /* ---- b4step2 on all cells + per-cell quotients ---- */
+    int any_wet = 0;
+    for (int k = threadIdx.x; k < S; k += NT) {
+        double h = sm[L::OFF_H + k];
+        if (h < drytol) {
+            h = fmax(h, 0.0);
+            sm[L::OFF_H + k] = h;
+            sm[L::OFF_HU + k] = 0.0;
+            sm[L::OFF_HV + k] = 0.0;
+        }
+        const bool w = h > drytol;
+        wet[k] = w ? 1 : 0;
+        any_wet |= w;
+        if (w) {
+            sm[L::OFF_U + k] = sm[L::OFF_HU + k] / h;
+            sm[L::OFF_V + k] = sm[L::OFF_HV + k] / h;
+            sm[L::OFF_C + k] = sqrt(g * h);
+        } else {
+            sm[L::OFF_U + k] = 0.0;
+            sm[L::OFF_V + k] = 0.0;
+            sm[L::OFF_C + k] = 0.0;
+        }
+    }
+    for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
+    any_wet = __syncthreads_or(any_wet);
+
+    const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
+    double smax_x = 0.0, smax_y = 0.0;
+    if (any_wet) {
+        const double c16g = 1.0 / (16.0 * g);
+        const double crit = fmax(drytol * g, 1e-6);
+        const double crit2 = sqrt(crit);
+        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, P, dtdx, c16g, crit, crit2);
+        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, P, dtdy, c16g, crit, crit2);
+    }
+
+    /* ---- flux-difference update, src2, write interior ---- */
+    double* gq = wk.q;
+    const double* gaux = wk.aux;
+    const int fidx = P.friction_index - 1;
+    for (int e = threadIdx.x; e < M * M; e += NT) {
+        const int i = 1 + e % M, j = 1 + e / M;
+        const int k = (j + 1) * N + (i + 1);
+        double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
+        if (EXACT) {
+            /* q - dtdx*(fm(i+1,j) - fp(i,j)) - dtdy*(gm(i,j+1) - gp(i,j)) */
+            const double* FM = sm + L::OFF_ACC;
+            const double* FP = FM + 3 * M * M;
+            const double* GM = FP + 3 * M * M;
+            const double* GP = GM + 3 * M * M;
+            h = h - dtdx * (FM[e] - FP[e]) - dtdy * (GM[e] - GP[e]);
+            hu = hu - dtdx * (FM[e + M * M] - FP[e + M * M]) - dtdy * (GM[e + M * M] - GP[e + M * M]);
+            hv = hv - dtdx * (FM[e + 2 * M * M] - FP[e + 2 * M * M]) -
+                 dtdy * (GM[e + 2 * M * M] - GP[e + 2 * M * M]);
+        } else {
+            const double* DX = sm + L::OFF_ACC;
+            const double* DY = sm + L::OFF_ACC + 3 * M * M;
+            h = h - dtdx * DX[e] - dtdy * DY[e];
+            hu = hu - dtdx * DX[e + M * M] - dtdy * DY[e + M * M];
+            hv = hv - dtdx * DX[e + 2 * M * M] - dtdy * DY[e + 2 * M * M];
+        }
+        if (P.src_term > 0) {
+            const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
+                                    ? gaux[(size_t)fidx * S + k]
+                                    : 0.0;
+            src2_cell(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
+        }
+        gq[k] = h;
+        gq[S + k] = hu;
+        gq[2 * S + k] = hv;
+    }
+
+    /* ---- CFL: warp-shuffle max, then across warps ---- */
+    double cx = smax_x, cy = smax_y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
+        cy = fmax(cy, __shfl_xor_sync(0xffffffffu, cy, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[warp] = cx;
+        red[32 + warp] = cy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = 0.0, my = 0.0;
+        for (int w2 = 0; w2 < NT / 32; ++w2) {
+            mx = fmax(mx, red[w2]);
+            my = fmax(my, red[32 + w2]);
+        }
+        double cfl = fmax(dtdx * mx, dtdy * my);
+        if (cfl > P.maxcfl_cap) cfl = 0.0;
+        if (cfl_out) cfl_out[wi] = cfl;
+        if (group_max) atomicMax(group_max + wk.group, dkey(cfl));
+    }
+}
+
+} // namespace GF_KNS
+
+#endif

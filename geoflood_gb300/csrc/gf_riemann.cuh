@@ -1,0 +1,294 @@
+/*
+ * Face-level shallow-water Riemann solvers, FP64, device side.
+ *
+ * Restates the reference's GeoClaw solvers for one face at a time:
+ *   - normal solve: rpn2_geoclaw.f:84-330 with riemann_aug_JCP
+ *     (geoclaw_riemann_utils.f:2-311, maxiter = 1) and riemanntype
+ *     (geoclaw_riemann_utils.f:566-677);
+ *   - transverse split: rpt2_geoclaw.f:61-187.
+ *
+ * Inputs per cell come pre-digested from shared memory (gf_cell): the
+ * quotients hu/h, hv/h and sqrt(g h) are computed once per cell instead of
+ * once per face side. Each is the same IEEE operation the Fortran performs,
+ * so the values are identical. Cramer's rule in riemann_aug_JCP is written
+ * out for the fixed eigenvector pattern r(:,2) = (0,0,1), r(1,:) = 1, which
+ * removes multiplications by exact 0 and 1 only.
+ *
+ * Component order inside these routines is LOCAL: 0 = depth, 1 = momentum
+ * normal to the face, 2 = momentum along the face.
+ */
+#ifndef GF_RIEMANN_CUH
+#define GF_RIEMANN_CUH
+
+#include "gf_types.h"
+
+struct gf_cell {
+    double h;    /* depth after b4step2                         */
+    double hun;  /* momentum normal to the face                 */
+    double hut;  /* momentum along the face                     */
+    double un;   /* hun/h if wet else 0                         */
+    double ut;   /* hut/h if wet else 0                         */
+    double c;    /* sqrt(g h) if wet else 0                     */
+    double b;    /* bathymetry                                  */
+    bool wet;    /* h > dry_tolerance                           */
+};
+
+/* riemanntype (geoclaw_riemann_utils.f:566-677), maxiter = 1.
+ * cL = sqrt(g hL), cR = sqrt(g hR) are supplied by the caller (they equal
+ * the Fortran's sqrt(g*hL), sqrt(g*hR) bit for bit). Returns hm, s1m, s2m. */
+__device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
+                                               double uR, double cL, double cR,
+                                               double g, double drytol,
+                                               double c16g, double& hm,
+                                               double& s1m, double& s2m)
+{
+    const double h_min = fmin(hR, hL);
+    const double h_max = fmax(hR, hL);
+    const double delu = uR - uL;
+    if (h_min <= drytol) {
+        hm = 0.0;
+        s1m = uR + uL - 2.0 * cR + 2.0 * cL;
+        s2m = s1m;
+        return;
+    }
+    /* sqrt is monotone, so sqrt(g*h_min) = min(cL, cR). */
+    const double c_min = fmin(cR, cL);
+    const double c_max = fmax(cR, cL);
+    const double F_min = delu + 2.0 * (c_min - c_max);
+    const double F_max =
+        delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
+    if (F_min > 0.0) { /* 2-rarefactions */
+        const double t = fmax(0.0, -delu + 2.0 * (cL + cR));
+        hm = c16g * (t * t);
+        const double cm = sqrt(g * hm);
+        s1m = uL + 2.0 * cL - 3.0 * cm;
+        s2m = uR - 2.0 * cR + 3.0 * cm;
+    } else if (F_max <= 0.0) { /* 2 shocks, one Newton step on sqrt(h) */
+        const double h0 = h_max;
+        const double rL = 1.0 / hL, rR = 1.0 / hR;
+        const double r0 = 1.0 / h0; /* equals rL or rR */
+        const double gL = sqrt(0.5 * g * (r0 + rL));
+        const double gR = sqrt(0.5 * g * (r0 + rR));
+        const double F0 = delu + (h0 - hL) * gL + (h0 - hR) * gR;
+        const double dfdh = gL - g * (h0 - hL) / (4.0 * (h0 * h0) * gL) + gR -
+                            g * (h0 - hR) / (4.0 * (h0 * h0) * gR);
+        const double sh0 = sqrt(h0);
+        const double slope = 2.0 * sh0 * dfdh;
+        const double t = sh0 - F0 / slope;
+        hm = t * t;
+        const double rm = 1.0 / hm;
+        const double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (rm + rL));
+        const double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (rm + rR));
+        const double cm = sqrt(g * hm);
+        s1m = u1m - cm;
+        s2m = u2m + cm;
+    } else { /* one shock, one rarefaction, one secant step.
+                The first F0 has (h0 - h_min) = 0, so F0 = F_min exactly. */
+        const double F0 = F_min;
+        const double slope = (F_max - F0) / (h_max - h_min);
+        hm = h_min - F0 / slope;
+        const double cm = sqrt(g * hm);
+        if (hL > hR) {
+            s1m = uL + 2.0 * cL - 3.0 * cm;
+            s2m = uL + 2.0 * cL - cm;
+        } else {
+            s2m = uR - 2.0 * cR + 3.0 * cm;
+            s1m = uR - 2.0 * cR + cm;
+        }
+    }
+}
+
+/* Normal Riemann problem at one face: rpn2_geoclaw.f:110-315 + aug_JCP.
+ * Outputs speeds s[3] and f-waves fw[mw][m] (LOCAL component order). */
+__device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& Rc,
+                                             double g, double drytol,
+                                             double c16g, double crit,
+                                             double crit2, double s[3],
+                                             double fw[3][3])
+{
+    /* Riemann problem variables (rpn2_geoclaw.f:136-171). */
+    double hL, huL, hvL, uL, vL, phiL, cL;
+    double hR, huR, hvR, uR, vR, phiR, cR;
+    double bL = Lc.b, bR = Rc.b;
+    if (Rc.wet) {
+        hR = Rc.h; huR = Rc.hun; hvR = Rc.hut; uR = Rc.un; vR = Rc.ut; cR = Rc.c;
+        phiR = 0.5 * g * (hR * hR) + (huR * huR) / hR;
+    } else {
+        hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0; phiR = 0.0; cR = 0.0;
+    }
+    if (Lc.wet) {
+        hL = Lc.h; huL = Lc.hun; hvL = Lc.hut; uL = Lc.un; vL = Lc.ut; cL = Lc.c;
+        phiL = 0.5 * g * (hL * hL) + (huL * huL) / hL;
+    } else {
+        hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0; phiL = 0.0; cL = 0.0;
+    }
+    (void)hvL; (void)hvR;
+
+    /* Wet/dry interface: wall or overtopping (rpn2_geoclaw.f:185-242). */
+    double wall0 = 1.0, wall1 = 1.0, wall2 = 1.0;
+    if (!Rc.wet) {
+        double hstar, s1x, s2x;
+        gf_riemanntype(hL, hL, uL, -uL, cL, cL, g, drytol, c16g, hstar, s1x, s2x);
+        const double hstartest = fmax(hL, hstar);
+        if (hstartest + bL < bR) {
+            wall1 = 0.0; wall2 = 0.0;
+            hR = hL; huR = -huL; bR = bL; phiR = phiL; uR = -uL; vR = vL; cR = cL;
+        } else if (hL + bL < bR) {
+            bR = hL + bL;
+        }
+    } else if (!Lc.wet) {
+        double hstar, s1x, s2x;
+        gf_riemanntype(hR, hR, -uR, uR, cR, cR, g, drytol, c16g, hstar, s1x, s2x);
+        const double hstartest = fmax(hR, hstar);
+        if (hstartest + bR < bL) {
+            wall0 = 0.0; wall1 = 0.0;
+            hL = hR; huL = -huR; bL = bR; phiL = phiR; uL = -uR; vL = vR; cL = cR;
+        } else if (hR + bR < bL) {
+            bL = hR + bR;
+        }
+    }
+
+    /* Einfeldt / Roe speeds (rpn2_geoclaw.f:257-266). */
+    const double sL = uL - cL;
+    const double sR = uR + cR;
+    const double uhat = (cL * uL + cR * uR) / (cR + cL);
+    const double chat = sqrt(g * 0.5 * (hR + hL));
+    double sE1 = fmin(sL, uhat - chat);
+    double sE2 = fmax(sR, uhat + chat);
+
+    /* ---- riemann_aug_JCP (geoclaw_riemann_utils.f:57-306) ---- */
+    const double delh = hR - hL;
+    const double delhu = huR - huL;
+    const double delphi = phiR - phiL;
+    const double delb = bR - bL;
+
+    double hm, s1m, s2m;
+    gf_riemanntype(hL, hR, uL, uR, cL, cR, g, drytol, c16g, hm, s1m, s2m);
+    (void)hm;
+
+    const double l1 = fmin(sE1, s2m);
+    const double l3 = fmax(sE2, s1m);
+    sE1 = l1;
+    sE2 = l3;
+    const double hstarHLL = fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
+    const double l2 = 0.5 * (l1 + l3);
+
+    /* steady-state wave, first (only) iteration: hLstar = hL etc. */
+    const double hbar = fmax(0.5 * (hL + hR), 0.0);
+    const double s1s2bar = 0.25 * ((uL + uR) * (uL + uR)) - g * hbar;
+    const double s1s2tilde = fmax(0.0, uL * uR) - g * hbar;
+    bool sonic;
+    if (fabs(s1s2bar) <= crit) sonic = true;
+    else if (s1s2bar * s1s2tilde <= crit * crit) sonic = true;
+    else if (s1s2bar * sE1 * sE2 <= crit * crit) sonic = true;
+    else if (fmin(fabs(sE1), fabs(sE2)) < crit2) sonic = true;
+    else if (sE1 < crit2 && s1m > -crit2) sonic = true;
+    else if (sE2 > -crit2 && s2m < crit2) sonic = true;
+    else if ((uL + cL) * (uR + cR) < 0.0) sonic = true;
+    else if ((uL - cL) * (uR - cR) < 0.0) sonic = true;
+    else sonic = false;
+
+    double deldelh = sonic ? -delb : delb * g * hbar / s1s2bar;
+    if (sE1 < -crit && sE2 > crit) {
+        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+    } else if (sE1 >= crit) {
+        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = fmax(deldelh, -hL);
+    } else if (sE2 <= -crit) {
+        deldelh = fmin(deldelh, hR);
+        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+    }
+    double deldelphi = sonic ? -g * hbar * delb : -delb * g * hbar * s1s2tilde / s1s2bar;
+    deldelphi = fmin(deldelphi, g * fmax(-hL * delb, -hR * delb));
+    deldelphi = fmax(deldelphi, g * fmin(-hL * delb, -hR * delb));
+
+    const double d1 = delh - deldelh;
+    const double d2 = delhu;
+    const double d3 = delphi - deldelphi;
+
+    /* Cramer's rule with r(:,1) = (1,l1,l1^2), r(:,2) = (0,0,1),
+     * r(:,3) = (1,l3,l3^2): determinant = l1 - l3. */
+    const double A2 = l1 * l1, C2 = l3 * l3;
+    const double det = l1 - l3;
+    const double beta1 = (d2 - d1 * l3) / det;
+    const double beta2 = ((d2 * C2 - l3 * d3) - d1 * (l1 * C2 - l3 * A2) + (l1 * d3 - d2 * A2)) / det;
+    const double beta3 = (d1 * l1 - d2) / det;
+
+    /* f-waves (geoclaw_riemann_utils.f:289-306). */
+    double f11 = beta1 * l1, f21 = beta1 * A2, f31 = beta1 * l1 * vL;
+    double f13 = beta3 * l3, f23 = beta3 * C2, f33 = beta3 * l3 * vR;
+    const double corr = hR * uR * vR - hL * uL * vL - f31 - f33;
+    if (huL + f11 <= 0.0) f31 = f31 + corr;
+    else f33 = f33 + corr;
+
+    /* Wall masking (rpn2_geoclaw.f:303-309). */
+    s[0] = l1 * wall0; s[1] = l2 * wall1; s[2] = l3 * wall2;
+    fw[0][0] = f11 * wall0; fw[0][1] = f21 * wall0; fw[0][2] = f31 * wall0;
+    fw[1][0] = 0.0 * wall1; fw[1][1] = beta2 * wall1; fw[1][2] = 0.0 * wall1;
+    fw[2][0] = f13 * wall2; fw[2][1] = f23 * wall2; fw[2][2] = f33 * wall2;
+}
+
+/* Transverse split of one fluctuation (rpt2_geoclaw.f:63-182), one face.
+ * cell: the cell the fluctuation enters; topo_lo / topo_hi: bathymetry of
+ * the transverse neighbours below / above it. asdq in LOCAL order (0 = h,
+ * 1 = momentum normal to the face, 2 = momentum along the face; "along the
+ * face" is the transverse sweep direction). Accumulates into bm / bp. */
+__device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
+                                             double topo_hi, double tol,
+                                             const double asdq[3], double bm[3],
+                                             double bp[3])
+{
+    bm[0] = bm[1] = bm[2] = 0.0;
+    bp[0] = bp[1] = bp[2] = 0.0;
+    if (cl.h <= tol) return;
+    const double eta = cl.h + cl.b;
+    if (eta < fmin(topo_lo, topo_hi)) return;
+    const double u = cl.un;  /* q(mu)/h */
+    const double v = cl.ut;  /* q(mv)/h */
+    const double s1 = v - cl.c;
+    const double s2 = v;
+    const double s3 = v + cl.c;
+    const double delf1 = asdq[0], delf2 = asdq[1], delf3 = asdq[2];
+    const double den = s3 - s1;
+    const double beta1 = (s3 * delf1 - delf3) / den;
+    const double beta2 = -u * delf1 + delf2;
+    const double beta3 = (delf3 - s1 * delf1) / den;
+    /* r(:,1) = (1, u, s1); r(:,2) = (0, 1, 0); r(:,3) = (1, u, s3) */
+    if (s1 < 0.0 && eta >= topo_lo) {
+        const double a = s1 * beta1;
+        bm[0] += a; bm[1] += a * u; bm[2] += a * s1;
+    } else if (s1 > 0.0 && eta >= topo_hi) {
+        const double a = s1 * beta1;
+        bp[0] += a; bp[1] += a * u; bp[2] += a * s1;
+    }
+    if (s2 < 0.0 && eta >= topo_lo) {
+        bm[1] += s2 * beta2;
+    } else if (s2 > 0.0 && eta >= topo_hi) {
+        bp[1] += s2 * beta2;
+    }
+    if (s3 < 0.0 && eta >= topo_lo) {
+        const double a = s3 * beta3;
+        bm[0] += a; bm[1] += a * u; bm[2] += a * s3;
+    } else if (s3 > 0.0 && eta >= topo_hi) {
+        const double a = s3 * beta3;
+        bp[0] += a; bp[1] += a * u; bp[2] += a * s3;
+    }
+}
+
+/* philim (philim.f:4-65): limiter value for wave strengths a (= |w|^2) and
+ * b (= projection of the upwind wave). */
+__device__ __forceinline__ double gf_philim(double a, double b, int meth)
+{
+    if (a == 0.0) return 0.0;
+    const double r = b / a;
+    switch (meth) {
+    case 2: return fmax(fmax(0.0, fmin(1.0, 2.0 * r)), fmin(2.0, r));
+    case 3: return (r + fabs(r)) / (1.0 + fabs(r));
+    case 4: { const double c = (1.0 + r) * 0.5; return fmax(0.0, fmin(fmin(c, 2.0), 2.0 * r)); }
+    case 5: return r;
+    default: return fmax(0.0, fmin(1.0, r));
+    }
+}
+
+#endif

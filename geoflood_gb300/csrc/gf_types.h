@@ -1,0 +1,43 @@
+/*
+ * Shared host/device types for the GB300 patch-update path.
+ *
+ * Device layout of a level batch (structure of arrays, per patch contiguous):
+ *   q   : [patch][field h|hu|hv][j = 0..my+3][i = 0..mx+3]   (mbc = 2 halo)
+ *   aux : [patch][field][j][i], field 0 = bathymetry b
+ * Each patch block starts on a 16-byte boundary so it can be staged into
+ * shared memory with one bulk-async (TMA) copy per field group.
+ */
+#ifndef GF_TYPES_H
+#define GF_TYPES_H
+
+#include <stdint.h>
+
+#include "geoflood_gb300.h"
+
+#define GF_MBC 2
+#define GF_MEQN 3
+
+/* One unit of work for the patch-update kernel: a patch of any forest. */
+typedef struct gf_patch_work {
+    double* q;          /* device: 3 planes of (mx+4)*(my+4) doubles   */
+    const double* aux;  /* device: maux planes of (mx+4)*(my+4) doubles */
+    double dx, dy;
+    int phys;           /* index into the gf_phys table                */
+    int group;          /* time-step group: dt slot and CFL max slot   */
+} gf_patch_work;
+
+/* Position and spacing of one patch (lower-left corner of cell (1,1)). */
+typedef struct gf_patch_geom {
+    double xlower, ylower, dx, dy;
+} gf_patch_geom;
+
+/* Physical boundary rules of a level and the hydrograph inflow state for
+ * the current time (q0hu = interpolated discharge per unit width). */
+typedef struct gf_bc_spec {
+    int mthbc[4];      /* left, right, bottom, top: 0 inflow, 1 extrap, 2 periodic, 3 wall */
+    int hydro_side[4]; /* side uses the hydrograph (rule 0)                                */
+    double width, x0, y0;
+    double q0hu;
+} gf_bc_spec;
+
+#endif

@@ -1,0 +1,201 @@
+"""Seeded synthetic flood inputs: DEMs, initial states and patch tilings.
+
+No public dataset is used; these generators produce inputs with the shapes,
+sizes and value ranges of the workloads the patch update is measured on:
+
+* ``bump_ramp_dem``   - b = 0.001 x + 8 seeded Gaussian bumps (amplitude
+  U[0.5, 3] m, sigma U[20, 80] m): the dam-break workload on a ramp.
+* ``fractal_dem``     - diamond-square fractal DEM (Hurst exponent, relief)
+  with an optional straight carved channel.
+* ``dam_break_state`` - water surface 10 m above b for x < x_dam, dry beyond.
+* ``tile_level``      - cut a global cell array (with a 2-cell halo) into
+  patches with ghost cells, in the Fortran layout the hooks use.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+MBC = 2
+
+
+def rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def diamond_square(levels: int, hurst: float, seed: int) -> np.ndarray:
+    """(2^levels + 1)^2 lattice of a diamond-square fractal with displacement
+    scale 2^(-hurst) per level, normalised to zero mean and unit deviation."""
+    n = 2 ** levels
+    g = rng(seed)
+    a = np.zeros((n + 1, n + 1))
+    a[::n, ::n] = g.standard_normal((2, 2))
+    step, scale = n, 1.0
+    while step > 1:
+        half = step // 2
+        scale *= 0.5 ** hurst
+        # diamond step: centres of the squares
+        c = 0.25 * (a[0:n:step, 0:n:step] + a[step::step, 0:n:step]
+                    + a[0:n:step, step::step] + a[step::step, step::step])
+        a[half::step, half::step] = c + scale * g.standard_normal(c.shape)
+        # square step: edge midpoints (their neighbours are corners and centres)
+        for rr, cc in ((np.arange(0, n + 1, step), np.arange(half, n, step)),
+                       (np.arange(half, n, step), np.arange(0, n + 1, step))):
+            R, Cc = np.meshgrid(rr, cc, indexing="ij")
+            acc = np.zeros(R.shape)
+            cnt = np.zeros(R.shape)
+            for dr, dc in ((-half, 0), (half, 0), (0, -half), (0, half)):
+                r2, c2 = R + dr, Cc + dc
+                ok = (r2 >= 0) & (r2 <= n) & (c2 >= 0) & (c2 <= n)
+                acc += np.where(ok, a[np.clip(r2, 0, n), np.clip(c2, 0, n)], 0.0)
+                cnt += ok
+            a[R, Cc] = acc / cnt + scale * g.standard_normal(acc.shape)
+        step = half
+    a -= a.mean()
+    sd = a.std()
+    return a / sd if sd > 0 else a
+
+
+def fractal_dem(nx: int, ny: int, dx: float, hurst: float, relief: float, seed: int,
+                channel_depth: float = 0.0, channel_width: float = 0.0,
+                x0: float = 0.0, y0: float = 0.0) -> np.ndarray:
+    """Cell-centred bathymetry (ny, nx): a diamond-square surface scaled to
+    `relief` metres peak to peak, plus a straight channel along x at the
+    domain centre `channel_depth` deep and `channel_width` wide."""
+    n = max(nx, ny)
+    lv = int(np.ceil(np.log2(max(n, 2))))
+    lat = diamond_square(lv, hurst, seed)
+    cell = 0.25 * (lat[:-1, :-1] + lat[1:, :-1] + lat[:-1, 1:] + lat[1:, 1:])
+    b = cell[:ny, :nx]
+    b = (b - b.min()) / max(b.max() - b.min(), 1e-300) * relief
+    if channel_depth > 0.0 and channel_width > 0.0:
+        y = y0 + (np.arange(ny) + 0.5) * dx
+        yc = y0 + 0.5 * ny * dx
+        inside = np.abs(y - yc) <= 0.5 * channel_width
+        b = b - channel_depth * inside[:, None]
+    return np.ascontiguousarray(b)
+
+
+def bump_ramp_dem(nx: int, ny: int, dx: float, dy: float, seed: int, nbump: int = 8,
+                  x0: float = 0.0, y0: float = 0.0) -> np.ndarray:
+    """b = 0.001 x + sum of nbump Gaussian bumps (amplitude U[0.5,3] m,
+    sigma U[20,80] m, centres uniform over the domain)."""
+    g = rng(seed)
+    x = x0 + (np.arange(nx) + 0.5) * dx
+    y = y0 + (np.arange(ny) + 0.5) * dy
+    X, Y = np.meshgrid(x, y)
+    lx, ly = nx * dx, ny * dy
+    b = 0.001 * X
+    for _ in range(nbump):
+        amp = g.uniform(0.5, 3.0)
+        sig = g.uniform(20.0, 80.0)
+        cx, cy = x0 + g.uniform(0, lx), y0 + g.uniform(0, ly)
+        b = b + amp * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * sig * sig))
+    return np.ascontiguousarray(b)
+
+
+def dam_break_state(b: np.ndarray, dx: float, x_dam: float = 600.0, depth: float = 10.0,
+                    x0: float = 0.0) -> np.ndarray:
+    """q (ny, nx, 3): surface `depth` metres above b for x < x_dam, dry beyond."""
+    ny, nx = b.shape
+    x = x0 + (np.arange(nx) + 0.5) * dx
+    h = np.where(x[None, :] < x_dam, depth, 0.0) * np.ones_like(b)
+    q = np.zeros((ny, nx, 3))
+    q[..., 0] = h
+    return q
+
+
+def pad_extrap(a: np.ndarray, mbc: int = MBC) -> np.ndarray:
+    """Add a halo by zero-order extrapolation (the mthbc = 1 rule)."""
+    pad = [(mbc, mbc), (mbc, mbc)] + [(0, 0)] * (a.ndim - 2)
+    return np.pad(a, pad, mode="edge")
+
+
+def pad_wall(q: np.ndarray, mbc: int = MBC) -> np.ndarray:
+    """Halo for q by the solid-wall rule (mthbc = 3): mirror, negate the
+    normal momentum (geoflood_bc2_fort.f90:118-131 and the y analogue)."""
+    out = np.pad(q, [(mbc, mbc), (mbc, mbc), (0, 0)], mode="symmetric")
+    ny, nx = q.shape[:2]
+    out[:, :mbc, 1] *= -1
+    out[:, nx + mbc:, 1] *= -1
+    out[:mbc, :, 2] *= -1
+    out[ny + mbc:, :, 2] *= -1
+    return out
+
+
+def tile_level(field: np.ndarray, m: int, mbc: int = MBC) -> np.ndarray:
+    """Cut a haloed global array (NY+2mbc, NX+2mbc, nf) into patches of m x m
+    interior cells, each with its mbc-wide ghost ring taken from the global
+    array. Returns (npatch, m+2mbc, m+2mbc, nf), patches row-major in (py, px)."""
+    NY, NX = field.shape[0] - 2 * mbc, field.shape[1] - 2 * mbc
+    assert NX % m == 0 and NY % m == 0
+    py, px = NY // m, NX // m
+    n4 = m + 2 * mbc
+    out = np.empty((py * px, n4, n4, field.shape[2]))
+    k = 0
+    for j in range(py):
+        for i in range(px):
+            out[k] = field[j * m:j * m + n4, i * m:i * m + n4]
+            k += 1
+    return out
+
+
+def untile_level(patches: np.ndarray, py: int, px: int, mbc: int = MBC) -> np.ndarray:
+    """Inverse of tile_level for the interiors: (py*m, px*m, nf)."""
+    n4 = patches.shape[1]
+    m = n4 - 2 * mbc
+    out = np.empty((py * m, px * m, patches.shape[3]))
+    k = 0
+    for j in range(py):
+        for i in range(px):
+            out[j * m:(j + 1) * m, i * m:(i + 1) * m] = patches[k, mbc:mbc + m, mbc:mbc + m]
+            k += 1
+    return out
+
+
+def uniform_dam_break_level(npx: int, npy: int, m: int, dx: float, seed: int,
+                            dem: str = "fractal", x_dam: float = 600.0,
+                            depth: float = 10.0):
+    """A single uniform level of npx x npy patches of m x m cells for the
+    dam-break workload. Returns (q_patches, aux_patches, py, px)."""
+    nx, ny = npx * m, npy * m
+    if dem == "fractal":
+        b = fractal_dem(nx, ny, dx, hurst=0.8, relief=30.0, seed=seed,
+                        channel_depth=5.0, channel_width=40.0)
+    else:
+        b = bump_ramp_dem(nx, ny, dx, dx, seed)
+    q = dam_break_state(b, dx, x_dam=x_dam, depth=depth)
+    qh = pad_extrap(q)
+    bh = pad_extrap(b[..., None])
+    return tile_level(qh, m), tile_level(bh, m), npy, npx
+
+
+def brick_layout(py: int, px: int, m: int, dx: float, dy: float | None = None,
+                 x0: float = 0.0, y0: float = 0.0, periodic_x: bool = False,
+                 periodic_y: bool = False):
+    """Neighbour table (npatch, 8) and patch origins of a uniform py x px grid
+    of m x m patches (row-major, as tile_level orders them). Entries: faces
+    left, right, bottom, top, corners ll, lr, ul, ur; -1 = physical side."""
+    dy = dx if dy is None else dy
+    n = py * px
+    nbr = -np.ones((n, 8), np.int32)
+    xl = np.zeros(n)
+    yl = np.zeros(n)
+
+    def idx(j, i):
+        if periodic_x:
+            i %= px
+        if periodic_y:
+            j %= py
+        if 0 <= i < px and 0 <= j < py:
+            return j * px + i
+        return -1
+
+    for j in range(py):
+        for i in range(px):
+            k = j * px + i
+            nbr[k] = [idx(j, i - 1), idx(j, i + 1), idx(j - 1, i), idx(j + 1, i),
+                      idx(j - 1, i - 1), idx(j - 1, i + 1), idx(j + 1, i - 1), idx(j + 1, i + 1)]
+            xl[k] = x0 + i * m * dx
+            yl[k] = y0 + j * m * dy
+    nbr[nbr == np.arange(n)[:, None]] = -1  # a 1-wide periodic grid has no true neighbour
+    return nbr, xl, yl

@@ -1,0 +1,191 @@
+/*
+ * geoflood_gb300 -- C ABI of the GB300 (sm_103a) GeoClaw patch update.
+ *
+ * This is the drop-in boundary for the reference's patch-update hot path.
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the GeoFlood source tree). All functions return GF_OK (0) or a
+ * negative gf_status; none throws or exits. A context is single-threaded;
+ * contexts are independent. Host arrays use the reference's Fortran layout
+ *   q(meqn, 1-mbc:mx+mbc, 1-mbc:my+mbc), aux(maux, 1-mbc:mx+mbc, 1-mbc:my+mbc)
+ * (equation index fastest), with meqn = 3 (h, hu, hv), mbc = 2 and aux(1)
+ * the bathymetry. Patch sizes mx = my in {8, 16, 32}. Arithmetic is FP64.
+ */
+#ifndef GEOFLOOD_GB300_H
+#define GEOFLOOD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum gf_status {
+    GF_OK = 0,
+    GF_ERR_ARG = -1,      /* invalid argument (size, layout, null pointer) */
+    GF_ERR_CUDA = -2,     /* a CUDA runtime call failed                    */
+    GF_ERR_NOMEM = -3,    /* device or pinned allocation failed            */
+    GF_ERR_DEVICE = -4,   /* a kernel reported a bounded wait that expired */
+    GF_ERR_STATE = -5,    /* call out of order (e.g. no physics set)       */
+    GF_ERR_UNSUPPORTED = -6
+};
+
+#define GF_MAX_MANNING 4
+#define GF_MAX_PHYS 1024
+
+/* Physics and method parameters of one scenario.
+ * Replaces geoclaw_module (geolib_source/geoclaw_module.f90:30-48, set_geo
+ * :57-161), friction_module (geolib_source/friction_module.f90:62-190) and the
+ * [geoclaw] options order/mthlim/src_term (fc2d_geoclaw_options.c:44-91). */
+typedef struct gf_phys {
+    double grav;
+    double dry_tolerance;
+    double sea_level;
+    double friction_depth;
+    double manning_coefficient[GF_MAX_MANNING];
+    double manning_break[GF_MAX_MANNING];
+    int num_manning;
+    int friction_forcing;
+    int variable_friction; /* 1: Manning n per cell from aux(friction_index) */
+    int friction_index;    /* 1-based aux field                              */
+    int order;             /* method(2): 1 or 2                              */
+    int transverse;        /* method(3): 0, 1 or 2                           */
+    int mthlim[3];         /* philim.f limiter per wave family (1..5, 0 off)  */
+    int src_term;          /* call src2 after step2                          */
+    double maxcfl_cap;     /* fc2d_geoclaw.h:40 MAXCFL_CAP (100): a larger
+                              patch CFL is returned as 0                     */
+} gf_phys;
+
+/* Defaults of the reference examples: g = 9.81, dry tolerance 1e-3,
+ * Manning 0.035 below a break of 1e10, MC limiter, order 2, transverse 2. */
+void gf_phys_default(gf_phys* p);
+
+/* --------------------------------------------------------------- context */
+typedef struct gf_ctx gf_ctx;
+
+/* Create a context on CUDA device `device` (the reference's
+ * fc2d_cudaclaw_initialize_GPUs, src/fc2d_cpu_cuda/cuda_source/
+ * cudaclaw_initialize.cu:37-74, without the MPI rank mapping). */
+int gf_ctx_create(int device, gf_ctx** out);
+void gf_ctx_destroy(gf_ctx* ctx);
+/* Text of the last error on this context ("" if none). */
+const char* gf_ctx_last_error(const gf_ctx* ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for event timing and
+ * ordering with other work. */
+int gf_ctx_stream(gf_ctx* ctx, void** stream);
+
+/* Floating-point contraction of the patch kernel. allow = 1 (default) runs
+ * the production build, which fuses multiply-adds; allow = 0 runs a build
+ * compiled without contraction that also sums the fluxes in the reference's
+ * order, so each FP64 operation rounds as the Fortran expression is written
+ * (fortran_source/geoclaw_step2_wrap_fort.f:97-115 for the final sum). */
+int gf_ctx_set_fp_contract(gf_ctx* ctx, int allow);
+
+/* Store physics set `slot` (0 <= slot < GF_MAX_PHYS). Replaces the
+ * module set-up fc2d_geoclaw_module_setup (fc2d_geoclaw.cpp, calling
+ * fortran_source/geoclaw_set_modules_fort.f90:1-63) and, for the GPU build,
+ * setprob_cuda (src/fc2d_cpu_cuda/riemann_source/variables.cu:72-113). */
+int gf_ctx_set_phys(gf_ctx* ctx, int slot, const gf_phys* phys);
+
+/* ---------------------------------------------- plain per-patch drop-in */
+/* One patch, host arrays in the Fortran layout: b4step2, step2, CFL cap and
+ * src2 with physics slot 0, exactly the work of the single_step_update hook
+ * geoclaw_update (src/fc2d_geoclaw/fc2d_geoclaw.cpp:352-387). Interior cells
+ * of q are updated in place; ghost cells are left as they were on entry
+ * (ghost filling rewrites them before the next step). *cfl receives the
+ * patch CFL number (0 if above maxcfl_cap). */
+int gf_patch_update(gf_ctx* ctx, int mx, int my, int mbc, int meqn, int maux,
+                    double dx, double dy, double t, double dt, double* q,
+                    const double* aux, double* cfl);
+
+/* A buffer of patches with host arrays, one launch: the batched GPU hook
+ * cudaclaw_update + cudaclaw_step2_batch (src/fc2d_cpu_cuda/fc2d_cpucuda.cpp:
+ * 410-495, src/fc2d_cpu_cuda/cuda_source/cudaclaw_step2.cu:57-324).
+ * q[k], aux[k] point at patch k's arrays; dx[k], dy[k] its spacing.
+ * cfl (nullable) receives per-patch CFL; *maxcfl the maximum. */
+int gf_patch_update_batch(gf_ctx* ctx, int npatch, int mx, int my, int mbc,
+                          int meqn, int maux, const double* dx,
+                          const double* dy, double t, double dt,
+                          double* const* q, const double* const* aux,
+                          double* cfl, double* maxcfl);
+
+/* ------------------------------------------- device-resident level batch */
+typedef struct gf_level gf_level;
+
+/* A batch of npatch patches of size mx x my kept in HBM as planes
+ * [patch][h|hu|hv][j][i] and [patch][aux field][j][i]. Replaces the per-patch
+ * device buffers of cudaclaw_allocate_fluxes / fc2d_cudaclaw_allocate_buffers
+ * (src/fc2d_cpu_cuda/cuda_source/cudaclaw_allocate.cu:21-138). */
+int gf_level_create(gf_ctx* ctx, int npatch, int mx, int my, int maux,
+                    gf_level** out);
+void gf_level_destroy(gf_level* lev);
+
+/* Per-patch cell sizes and physics slots (phys may be NULL: slot 0). */
+int gf_level_set_geometry(gf_level* lev, const double* dx, const double* dy,
+                          const int* phys);
+
+/* Ghost-fill layout: nbr[8*k + s] is the same-level neighbour of patch k
+ * across face s (0 left, 1 right, 2 bottom, 3 top) or corner 4 + c
+ * (c = 0 lower-left, 1 lower-right, 2 upper-left, 3 upper-right), or -1 on
+ * a physical boundary; xlower/ylower (nullable) position each patch.
+ * Periodic sides are expressed by wrapping the neighbour table. */
+int gf_level_set_layout(gf_level* lev, const int* nbr, const double* xlower,
+                        const double* ylower);
+
+/* Physical boundary rule per side (left, right, bottom, top): 0 hydrograph
+ * inflow, 1 zero-order extrapolation, 2 periodic, 3 solid wall -- the
+ * [geoclaw] mthbc option (fc2d_geoclaw_options.c:44-91). Default 1 1 1 1. */
+int gf_level_set_bc(gf_level* lev, const int* mthbc);
+
+/* Discharge hydrograph (time, hu per unit width; n rows) applied by rule 0
+ * on the flagged sides (side[4]: left, right, bottom, top) inside the
+ * channel |y - y0| <= width/2 (x for bottom/top): the data read by
+ * read_hydrograph_data (hydrograph/hydrograh_module.f90:36-152). */
+int gf_level_set_hydrograph(gf_level* lev, int n, const double* time,
+                            const double* hu, const int* side, double width,
+                            double x0, double y0);
+
+/* Fill every ghost cell of the level at time t: same-level face and corner
+ * copies (fc2d_geoclaw_fort_copy_face/_corner, fclaw2d_source/
+ * fc2d_geoclaw_copy_fort.f:11-107) then physical boundaries
+ * (fc2d_geoclaw_bc2, fortran_source/geoflood_bc2_fort.f90:7-409). */
+int gf_level_ghost_fill(gf_level* lev, double t);
+int gf_level_ghost_fill_async(gf_level* lev, double t);
+
+/* Copy npatch Fortran-layout blocks (contiguous, patch k at
+ * q + k*meqn*(mx+4)*(my+4)) to the device; aux may be NULL to keep the
+ * resident bathymetry. */
+int gf_level_upload(gf_level* lev, const double* q, const double* aux);
+int gf_level_download(gf_level* lev, double* q);
+int gf_level_download_aux(gf_level* lev, double* aux);
+
+/* One level step on device-resident state (no host copies of q): the work
+ * ForestClaw's level step does through single_step_update for every patch,
+ * plus the CFL reduction (fc2d_geoclaw_run.c:305-312 within one process).
+ * *maxcfl receives the maximum patch CFL. */
+int gf_level_step(gf_level* lev, double t, double dt, double* maxcfl);
+
+/* The same step end to end from host buffers: upload q (Fortran layout),
+ * step, fill ghost cells at t + dt if a layout is set, download q. aux stays
+ * resident. */
+int gf_level_step_host(gf_level* lev, double* q, double t, double dt,
+                       double* maxcfl);
+
+/* Asynchronous form of gf_level_step: enqueue the step on the context
+ * stream and return; gf_level_sync waits and reports the max CFL of the
+ * last enqueued step. */
+int gf_level_step_async(gf_level* lev, double t, double dt);
+int gf_level_sync(gf_level* lev, double* maxcfl);
+
+/* Per-patch CFL numbers of the last step (npatch doubles). */
+int gf_level_patch_cfl(gf_level* lev, double* cfl);
+
+/* Device pointers of the resident planes (for graph capture / tooling). */
+int gf_level_device_planes(gf_level* lev, double** q, double** aux);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,208 @@
+"""CPU oracle for the GeoClaw patch update -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``liboracle.so`` built from ``geoclaw_oracle.c`` (a plain-C restatement
+of the reference's Fortran patch update). Only the tests, the smoke check and
+the CPU-baseline leg of bench.py use it, as the checker / the timed CPU
+reference; the shipped library never does.
+
+Parity status: the reference's own Fortran cannot be compiled here and its
+tests hold no golden vectors for this path. The Riemann-solver core is pinned
+against the reference's CUDA device functions compiled for the host
+(``oracle/_ref``, built by ``build_ref.sh`` where the reference tree is
+present; the generated vectors live in ``tests/golden/``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+MBC = 2
+
+
+class orc_params(C.Structure):
+    _fields_ = [
+        ("grav", C.c_double), ("dry_tolerance", C.c_double), ("sea_level", C.c_double),
+        ("friction_depth", C.c_double), ("friction_forcing", C.c_int),
+        ("num_manning", C.c_int), ("manning_coefficient", C.c_double * 4),
+        ("manning_break", C.c_double * 4), ("variable_friction", C.c_int),
+        ("friction_index", C.c_int), ("order", C.c_int), ("transverse", C.c_int),
+        ("mthlim", C.c_int * 3), ("src_term", C.c_int), ("maxcfl_cap", C.c_double),
+    ]
+
+
+def build(force: bool = False) -> Path:
+    srcs = [HERE / "geoclaw_oracle.c", HERE / "geoclaw_oracle_ghost.c"]
+    deps = srcs + [HERE / "geoclaw_oracle.h"]
+    if not force and LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
+        return LIB
+    tmp = LIB.with_suffix(f".so.{os.getpid()}")
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+           "-std=c99", "-Wall", "-o", str(tmp), *map(str, srcs), "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_dp = C.POINTER(C.c_double)
+_lib = None
+
+
+class orc_hydro(C.Structure):
+    _fields_ = [("use", C.c_int), ("side", C.c_int * 4), ("width", C.c_double),
+                ("x0", C.c_double), ("y0", C.c_double), ("n", C.c_int),
+                ("time", _dp), ("hu", _dp)]
+
+
+def hydro(time=None, hu=None, side=(0, 0, 0, 0), width=0.0, x0=0.0, y0=0.0):
+    """orc_hydro for a discharge hydrograph (keeps the arrays alive on the struct)."""
+    h = orc_hydro()
+    if time is None:
+        h.use = 0
+        h.n = 0
+        return h
+    tm = np.ascontiguousarray(time, dtype=np.float64)
+    hv = np.ascontiguousarray(hu, dtype=np.float64)
+    h.use = 1
+    for k in range(4):
+        h.side[k] = int(side[k])
+    h.width, h.x0, h.y0 = width, x0, y0
+    h.n = len(tm)
+    h.time = tm.ctypes.data_as(_dp)
+    h.hu = hv.ctypes.data_as(_dp)
+    h._keep = (tm, hv)
+    return h
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        P = C.POINTER(orc_params)
+        lib.orc_default_params.argtypes = [P]
+        lib.orc_patch_update.restype = C.c_double
+        lib.orc_patch_update.argtypes = [P, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int,
+                                         C.c_double, C.c_double, C.c_double, C.c_double]
+        lib.orc_level_update.restype = C.c_double
+        lib.orc_level_update.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_long,
+                                         _dp, C.c_int, C.c_long, _dp, _dp, C.c_double,
+                                         C.c_double, C.c_int]
+        lib.orc_b4step2.argtypes = [P, C.c_int, C.c_int, C.c_int, _dp]
+        lib.orc_step2.restype = C.c_double
+        lib.orc_step2.argtypes = [P, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_double,
+                                  C.c_double, C.c_double]
+        lib.orc_src2.argtypes = [P, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_double]
+        lib.orc_riemann_aug_JCP.argtypes = [C.c_int] + [C.c_double] * 18 + [_dp, _dp]
+        lib.orc_riemanntype.argtypes = ([C.c_double] * 4 + [_dp, _dp, _dp, C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.c_int, C.c_double, C.c_double])
+        lib.orc_rpn2.argtypes = [P, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp,
+                                 _dp]
+        lib.orc_rpt2.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
+                                 C.c_int, _dp, _dp, _dp]
+        H = C.POINTER(orc_hydro)
+        ip = C.POINTER(C.c_int)
+        lib.orc_bc2.argtypes = [P, H, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                C.c_double, C.c_double, _dp, _dp, C.c_int, C.c_double, ip]
+        lib.orc_level_ghost_fill.argtypes = [P, H, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                             C.c_int, ip, _dp, _dp, C.c_double, C.c_double,
+                                             C.c_double, ip]
+        _lib = lib
+    return _lib
+
+
+def params(phys=None) -> orc_params:
+    """orc_params from a geoflood_gb300.Phys-like object (or defaults)."""
+    p = orc_params()
+    load().orc_default_params(C.byref(p))
+    if phys is not None:
+        p.grav = phys.grav
+        p.dry_tolerance = phys.dry_tolerance
+        p.sea_level = phys.sea_level
+        p.friction_depth = phys.friction_depth
+        p.friction_forcing = int(bool(phys.friction_forcing))
+        p.num_manning = len(phys.manning_coefficient)
+        for k in range(p.num_manning):
+            p.manning_coefficient[k] = phys.manning_coefficient[k]
+            p.manning_break[k] = phys.manning_break[k]
+        p.variable_friction = int(bool(phys.variable_friction))
+        p.friction_index = int(phys.friction_index)
+        p.order = int(phys.order)
+        p.transverse = int(phys.transverse)
+        for k in range(3):
+            p.mthlim[k] = int(phys.mthlim[k])
+        p.src_term = int(phys.src_term)
+        p.maxcfl_cap = phys.maxcfl_cap
+    return p
+
+
+def _ptr(a):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+def patch_update(q: np.ndarray, aux: np.ndarray, dx: float, dy: float, t: float, dt: float,
+                 phys=None) -> float:
+    """geoclaw_update on one patch (Fortran layout, shape (my+4, mx+4, 3)); in place."""
+    p = params(phys)
+    my4, mx4, _ = q.shape
+    return load().orc_patch_update(C.byref(p), MBC, mx4 - 2 * MBC, my4 - 2 * MBC, _ptr(q),
+                                   _ptr(aux), aux.shape[-1], dx, dy, t, dt)
+
+
+def level_update(q: np.ndarray, aux: np.ndarray, dx, dy, t: float, dt: float, phys=None,
+                 nthreads: int = 0) -> float:
+    """One level step over patches (npatch, my+4, mx+4, 3), in place; returns max CFL."""
+    p = params(phys)
+    n, my4, mx4, _ = q.shape
+    dxa = np.ascontiguousarray(np.broadcast_to(np.asarray(dx, np.float64), (n,)))
+    dya = np.ascontiguousarray(np.broadcast_to(np.asarray(dy, np.float64), (n,)))
+    maux = aux.shape[-1]
+    return load().orc_level_update(C.byref(p), n, MBC, mx4 - 2 * MBC, my4 - 2 * MBC, _ptr(q),
+                                   my4 * mx4 * 3, _ptr(aux), maux, my4 * mx4 * maux, _ptr(dxa),
+                                   _ptr(dya), t, dt, nthreads)
+
+
+def riemann_aug_JCP(hL, hR, huL, huR, hvL, hvR, bL, bR, uL, uR, vL, vR, phiL, phiR, sE1, sE2,
+                    drytol=1e-3, g=9.81):
+    sw = np.zeros(3)
+    fw = np.zeros(9)
+    load().orc_riemann_aug_JCP(1, hL, hR, huL, huR, hvL, hvR, bL, bR, uL, uR, vL, vR, phiL,
+                               phiR, sE1, sE2, drytol, g, _ptr(sw), _ptr(fw))
+    return sw, fw.reshape(3, 3)  # fw[mw, m]
+
+
+def rpn2(ixy: int, q1d: np.ndarray, aux1d: np.ndarray, phys=None):
+    """rpn2 over a slice q1d (n, 3) with n = mx + 2*mbc; returns fwave (n,3,3)
+    [i, mw, m], s (n,3), amdq (n,3), apdq (n,3). q1d is modified like the Fortran."""
+    p = params(phys)
+    n = q1d.shape[0]
+    mx = n - 2 * MBC
+    fwave = np.zeros((n, 3, 3))
+    s = np.zeros((n, 3))
+    amdq = np.zeros((n, 3))
+    apdq = np.zeros((n, 3))
+    load().orc_rpn2(C.byref(p), ixy, MBC, mx, _ptr(q1d), _ptr(aux1d), aux1d.shape[-1],
+                    _ptr(fwave), _ptr(s), _ptr(amdq), _ptr(apdq))
+    return fwave, s, amdq, apdq
+
+
+def level_ghost_fill(q: np.ndarray, aux: np.ndarray, nbr: np.ndarray, xlower, ylower, dx: float,
+                     dy: float, t: float, mthbc=(1, 1, 1, 1), phys=None, hy=None):
+    """Ghost fill of a same-level batch (in place): copies, then bc2."""
+    p = params(phys)
+    n, my4, mx4, _ = q.shape
+    nb = np.ascontiguousarray(nbr, dtype=np.int32).reshape(n, 8)
+    xl = np.ascontiguousarray(xlower, dtype=np.float64)
+    yl = np.ascontiguousarray(ylower, dtype=np.float64)
+    mb = np.ascontiguousarray(mthbc, dtype=np.int32)
+    h = hy if hy is not None else hydro()
+    ip = C.POINTER(C.c_int)
+    load().orc_level_ghost_fill(C.byref(p), C.byref(h), n, MBC, mx4 - 2 * MBC, my4 - 2 * MBC,
+                                _ptr(q), _ptr(aux), aux.shape[-1], nb.ctypes.data_as(ip),
+                                _ptr(xl), _ptr(yl), dx, dy, t, mb.ctypes.data_as(ip))
