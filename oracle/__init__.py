@@ -105,6 +105,10 @@ def load():
                                  _dp]
         lib.orc_rpt2.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                  C.c_int, _dp, _dp, _dp]
+        lib.orc_rpn2_face.argtypes = [P, C.c_int, _dp, _dp, C.c_double, C.c_double, _dp, _dp,
+                                      _dp, _dp]
+        lib.orc_rpt2_face.argtypes = [P, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                      _dp]
         H = C.POINTER(orc_hydro)
         ip = C.POINTER(C.c_int)
         lib.orc_bc2.argtypes = [P, H, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
@@ -206,3 +210,23 @@ def level_ghost_fill(q: np.ndarray, aux: np.ndarray, nbr: np.ndarray, xlower, yl
     load().orc_level_ghost_fill(C.byref(p), C.byref(h), n, MBC, mx4 - 2 * MBC, my4 - 2 * MBC,
                                 _ptr(q), _ptr(aux), aux.shape[-1], nb.ctypes.data_as(ip),
                                 _ptr(xl), _ptr(yl), dx, dy, t, mb.ctypes.data_as(ip))
+
+
+def rpn2_face(ixy: int, ql, qr, bl: float, br: float, phys=None):
+    """Normal solve at one face; returns fwave (3 waves x 3 comps), s, amdq, apdq."""
+    p = params(phys)
+    ql = np.ascontiguousarray(ql, dtype=np.float64)
+    qr = np.ascontiguousarray(qr, dtype=np.float64)
+    fw, s, am, ap = np.zeros(9), np.zeros(3), np.zeros(3), np.zeros(3)
+    load().orc_rpn2_face(C.byref(p), ixy, _ptr(ql), _ptr(qr), bl, br, _ptr(fw), _ptr(s),
+                         _ptr(am), _ptr(ap))
+    return fw.reshape(3, 3), s, am, ap
+
+
+def rpt2_face(ixy: int, imp: int, ql, qr, aux1, aux2, aux3, asdq, phys=None):
+    """Transverse split at one face (imp 1: left cell, 2: right cell)."""
+    p = params(phys)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ql, qr, aux1, aux2, aux3, asdq)]
+    bm, bp = np.zeros(3), np.zeros(3)
+    load().orc_rpt2_face(C.byref(p), ixy, imp, *[_ptr(a) for a in arrs], _ptr(bm), _ptr(bp))
+    return bm, bp

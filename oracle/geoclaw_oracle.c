@@ -960,3 +960,63 @@ double orc_level_update(const orc_params* p, int npatch, int mbc, int mx,
     (void)nthreads;
     return maxcfl;
 }
+
+/* ------------------------------------------------------------------------
+ * Single-face views of rpn2 / rpt2 (for the pin against the reference's
+ * own solver): a slice with mx = 1 whose face 1 separates cell 0 (left
+ * state) from cell 1 (right state); the other slice cells are dry.
+ * fwave[3*mw + m] with m in global order (h, hu, hv).
+ * ---------------------------------------------------------------------- */
+void orc_rpn2_face(const orc_params* p, int ixy, const double* ql, const double* qr, double bl,
+                   double br, double* fwave, double* s, double* amdq, double* apdq)
+{
+    const int mbc = 2, mx = 1, n = mx + 2 * mbc;
+    double q1d[3 * 5], aux[5], fw[3 * 3 * 5], ss[3 * 5], am[3 * 5], ap[3 * 5];
+    int m, mw;
+    memset(q1d, 0, sizeof q1d);
+    memset(aux, 0, sizeof aux);
+    for (m = 0; m < 3; ++m) {
+        q1d[m + 3 * 1] = ql[m]; /* Fortran cell 0 -> slot 0 + mbc - 1 = 1 */
+        q1d[m + 3 * 2] = qr[m]; /* cell 1 -> slot 2 */
+    }
+    aux[1] = bl;
+    aux[2] = br;
+    orc_rpn2(p, ixy, mbc, mx, q1d, aux, 1, fw, ss, am, ap);
+    (void)n;
+    /* face 1 -> slot 1 + mbc - 1 = 2 */
+    for (mw = 0; mw < 3; ++mw) {
+        s[mw] = ss[mw + 3 * 2];
+        for (m = 0; m < 3; ++m) fwave[3 * mw + m] = fw[m + 3 * (mw + 3 * 2)];
+    }
+    for (m = 0; m < 3; ++m) {
+        amdq[m] = am[m + 3 * 2];
+        apdq[m] = ap[m + 3 * 2];
+    }
+}
+
+void orc_rpt2_face(const orc_params* p, int ixy, int imp, const double* ql, const double* qr,
+                   const double* aux1, const double* aux2, const double* aux3, const double* asdq,
+                   double* bmasdq, double* bpasdq)
+{
+    const int mbc = 2, mx = 1;
+    double q1d[3 * 5], a1[5], a2[5], a3[5], as[3 * 5], bm[3 * 5], bp[3 * 5];
+    int m;
+    memset(q1d, 0, sizeof q1d);
+    memset(a1, 0, sizeof a1);
+    memset(a2, 0, sizeof a2);
+    memset(a3, 0, sizeof a3);
+    memset(as, 0, sizeof as);
+    for (m = 0; m < 3; ++m) {
+        q1d[m + 3 * 1] = ql[m];
+        q1d[m + 3 * 2] = qr[m];
+        as[m + 3 * 2] = asdq[m]; /* face 1 -> slot 2 */
+    }
+    a1[1] = aux1[0]; a1[2] = aux1[1];
+    a2[1] = aux2[0]; a2[2] = aux2[1];
+    a3[1] = aux3[0]; a3[2] = aux3[1];
+    orc_rpt2(p, ixy, imp, mbc, mx, q1d, a1, a2, a3, 1, as, bm, bp);
+    for (m = 0; m < 3; ++m) {
+        bmasdq[m] = bm[m + 3 * 2];
+        bpasdq[m] = bp[m + 3 * 2];
+    }
+}

@@ -96,6 +96,13 @@ void orc_rpt2(const orc_params* p, int ixy, int imp, int mbc, int mx,
               const double* aux3, int maux, const double* asdq,
               double* bmasdq, double* bpasdq);
 
+/* Single-face views of rpn2 / rpt2 (see geoclaw_oracle.c). */
+void orc_rpn2_face(const orc_params* p, int ixy, const double* ql, const double* qr, double bl,
+                   double br, double* fwave, double* s, double* amdq, double* apdq);
+void orc_rpt2_face(const orc_params* p, int ixy, int imp, const double* ql, const double* qr,
+                   const double* aux1, const double* aux2, const double* aux3, const double* asdq,
+                   double* bmasdq, double* bpasdq);
+
 #ifdef __cplusplus
 }
 #endif
