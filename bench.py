@@ -285,7 +285,14 @@ def run_gpu(args):
     hbm_peak, peak_kind = load_peaks()
     algo = BYTES_PER_CELL_UPDATE * ncell
     achieved = algo / (kernel_ms * 1e-3) / 1e9
-    fp64 = fp64_peak_gops()
+    rates = fp64_rates()
+    fp64 = None
+    if rates:
+        fp64 = {"bound": "fp64 issue", "peak_dfma_gops": rates["dfma"] / 1e9,
+                "ddiv_gops": rates["ddiv"] / 1e9, "dsqrt_gops": rates["dsqrt"] / 1e9,
+                "ffma_gops": rates["ffma"] / 1e9,
+                "kernel_cell_updates_per_s": ncell / (kernel_ms * 1e-3),
+                "peak_source": "measured live (gf_measure_fp64_rates)"}
     result = {
         "metric": METRIC, "value": world * ncell / (ms * 1e-3), "unit": METRIC,
         "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
@@ -318,21 +325,17 @@ def run_gpu(args):
     return 0
 
 
-def fp64_peak_gops():
-    """Measured FP64 FMA issue rate of this GPU (gf_measure_fp64_peak), if exported."""
-    try:
-        from geoflood_gb300 import _lib
+def fp64_rates():
+    """Measured FP64 pipe rates of this GPU (gf_measure_fp64_rates), ops/s."""
+    import ctypes as C
 
-        lib = _lib.load()
-        if not hasattr(lib, "gf_measure_fp64_peak"):
-            return None
-        import ctypes as C
+    from geoflood_gb300 import _lib
 
-        v = C.c_double()
-        rc = lib.gf_measure_fp64_peak(0, C.byref(v))
-        return {"dfma_gops": v.value} if rc == 0 else None
-    except Exception:
+    lib = _lib.load()
+    r = (C.c_double * 4)()
+    if lib.gf_measure_fp64_rates(int(os.environ.get("LOCAL_RANK", "0")), r) != 0:
         return None
+    return {"dfma": r[0], "ddiv": r[1], "dsqrt": r[2], "ffma": r[3]}
 
 
 def main():

@@ -77,6 +77,7 @@ SIGNATURES = [
                                           C.c_double, C.c_double]),
     ("gf_level_ghost_fill", C.c_int, [_vp, C.c_double]),
     ("gf_level_ghost_fill_async", C.c_int, [_vp, C.c_double]),
+    ("gf_measure_fp64_rates", C.c_int, [C.c_int, _dp]),
     ("gf_level_device_planes", C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
 ]
 

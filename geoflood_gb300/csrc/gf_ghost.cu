@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) ghost_fill_kernel(double* __restrict__ q,
         const int i2 = i + (L ? M : R ? -M : 0), j2 = j + (B ? M : T ? -M : 0);
         const int k2 = (j2 + 1) * N + (i2 + 1);
 #pragma unroll
-        for (int f = 0; f < 3; ++f) plane(q, p, f, S, 3)[k] = plane(q, p, f, S, 3)[k2];
+        for (int f = 0; f < 3; ++f) plane(q, p, f, S, 3)[k] = plane(q, src, f, S, 3)[k2];
     }
     const bool phys_side[4] = {nb[0] == -1, nb[1] == -1, nb[2] == -1, nb[3] == -1};
     if (!(phys_side[0] || phys_side[1] || phys_side[2] || phys_side[3])) return;

@@ -18,12 +18,21 @@
  * before they are read again, so their post-step values are not part of
  * the state.
  *
- * Accumulation: the per-face outputs of a band of slices go to shared
- * memory; each interior cell then gathers its six contributing faces in
- * slice order into two flux-difference accumulators
- *   DX = fm(i+1,j) - fp(i,j),  DY = gm(i,j+1) - gp(i,j)
- * so every cell is written by one thread per band, in a fixed order: the
- * result is deterministic and independent of launch shape.
+ * The update is FP64-issue bound on GB300 (the FP64 pipe, not HBM, is the
+ * ceiling), so the layout of the work aims at few FP64 instructions and
+ * uniform warps:
+ *   - per-cell quotients computed once (hu/h, hv/h, sqrt(g h), and in the
+ *     contracted build 1/h and 1/sqrt(g h));
+ *   - the faces of each band are listed by class (both cells wet, one wet,
+ *     both dry) so a warp runs one code path; dry faces only store zeros;
+ *   - the per-face outputs of a band go to shared memory and each interior
+ *     cell gathers its six contributing faces in slice order, so every cell
+ *     is written by one thread per band, in a fixed order: deterministic and
+ *     independent of launch shape (no atomics on the data).
+ *
+ * EXACT = true is the parity build: the reference's four flux accumulators
+ * fm, fp, gm, gp summed in its order and every division as written; compiled
+ * with floating-point contraction off it reproduces the Fortran's rounding.
  */
 #ifndef GF_PATCH_UPDATE_CUH
 #define GF_PATCH_UPDATE_CUH
@@ -97,13 +106,15 @@ struct Geo {
     static constexpr int NSLICE = M + 2;     /* slices 0..m+1            */
 };
 
-/* Shared-memory layout (doubles unless noted). NACC flux accumulators of
- * 3 components per interior cell: 2 (DX, DY) in the fast form, 4 (fm, fp,
- * gm, gp) in the exact form. */
+/* Shared-memory layout (doubles unless noted). NACC flux accumulators of 3
+ * components per interior cell: 2 (DX, DY) in the contracted build, 4 (fm,
+ * fp, gm, gp) in the exact build. The contracted build also keeps 1/h and
+ * 1/sqrt(g h) planes. */
 template <int M, int RB, bool EXACT = false>
 struct Smem {
-    static constexpr int NACC = EXACT ? 4 : 2;
     using G = Geo<M>;
+    static constexpr int NACC = EXACT ? 4 : 2;
+    static constexpr int NBAND = (G::NSLICE + RB - 1) / RB;
     static constexpr int W_STRIDE = 12; /* s[3] + fw[3][3]                   */
     static constexpr int O_STRIDE = 18; /* faddm faddp A B C D, 3 comps each */
     static constexpr int OFF_H = 0;
@@ -113,71 +124,144 @@ struct Smem {
     static constexpr int OFF_U = OFF_B + G::S;
     static constexpr int OFF_V = OFF_U + G::S;
     static constexpr int OFF_C = OFF_V + G::S;
-    static constexpr int OFF_ACC = OFF_C + G::S;           /* NACC x [3][M*M] */
+    static constexpr int OFF_RH = OFF_C + G::S;                     /* contracted only */
+    static constexpr int OFF_RC = OFF_RH + (EXACT ? 0 : G::S);      /* contracted only */
+    static constexpr int OFF_ACC = OFF_RC + (EXACT ? 0 : G::S);     /* NACC x [3][M*M] */
     static constexpr int OFF_W = OFF_ACC + NACC * 3 * M * M;
     static constexpr int OFF_O = OFF_W + RB * G::FA * W_STRIDE;
     static constexpr int OFF_RED = OFF_O + RB * G::FB * O_STRIDE; /* 2*32 doubles */
     static constexpr int OFF_BAR = OFF_RED + 64;                    /* 1 x u64     */
-    static constexpr int OFF_WET = OFF_BAR + 2;                     /* S bytes     */
-    static constexpr size_t BYTES = (size_t)OFF_WET * 8 + ((G::S + 15) / 16) * 16;
+    /* integer region: class counts per band and face lists (u16) */
+    static constexpr int OFF_INT = OFF_BAR + 2;
+    static constexpr int CNT_INTS = NBAND * 2 * 3 * 2;              /* [band][A|B][class][count|pos] */
+    static constexpr int LIST_A = G::NSLICE * G::FA;
+    static constexpr int LIST_B = G::NSLICE * G::FB;
+    static constexpr size_t INT_BYTES = ((CNT_INTS * 4 + (LIST_A + LIST_B) * 2) + 15) / 16 * 16;
+    static constexpr size_t OFF_WET_BYTES = (size_t)OFF_INT * 8 + INT_BYTES;
+    static constexpr size_t BYTES = OFF_WET_BYTES + ((G::S + 15) / 16) * 16;
 };
 
 /* Load the cell view for a face sweep in direction DIR (0 = x, 1 = y). */
-template <int DIR>
-__device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned char* wet, int k,
-                                             int offH, int offHU, int offHV, int offB, int offU,
-                                             int offV, int offC)
+template <int DIR, bool EXACT, class L>
+__device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned char* wet, int k)
 {
     gf_cell c;
-    c.h = sm[offH + k];
-    c.b = sm[offB + k];
-    c.c = sm[offC + k];
+    c.h = sm[L::OFF_H + k];
+    c.b = sm[L::OFF_B + k];
+    c.c = sm[L::OFF_C + k];
     c.wet = wet[k] != 0;
     if (DIR == 0) {
-        c.hun = sm[offHU + k]; c.hut = sm[offHV + k];
-        c.un = sm[offU + k];   c.ut = sm[offV + k];
+        c.hun = sm[L::OFF_HU + k]; c.hut = sm[L::OFF_HV + k];
+        c.un = sm[L::OFF_U + k];   c.ut = sm[L::OFF_V + k];
     } else {
-        c.hun = sm[offHV + k]; c.hut = sm[offHU + k];
-        c.un = sm[offV + k];   c.ut = sm[offU + k];
+        c.hun = sm[L::OFF_HV + k]; c.hut = sm[L::OFF_HU + k];
+        c.un = sm[L::OFF_V + k];   c.ut = sm[L::OFF_U + k];
+    }
+    if (!EXACT) {
+        c.rh = sm[L::OFF_RH + k];
+        c.rc = sm[L::OFF_RC + k];
+    } else {
+        c.rh = 0.0;
+        c.rc = 0.0;
     }
     return c;
 }
 
-/* One sweep direction over all slices, banded. Accumulates into the DX/DY
- * shared accumulators; returns this thread's max |s| over normal faces. */
+/* Build, for every band of one sweep direction, the normal-solve faces
+ * (list A) and the limited faces (list B) ordered by class: both cells wet,
+ * one wet, both dry. Two passes (count, then place) over all faces. */
 template <int M, int NT, int RB, int DIR, bool EXACT>
-__device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, const gf_phys& P,
-                                        double dtdn, double c16g, double crit, double crit2)
+__device__ __forceinline__ void build_lists(const unsigned char* wet, int* cnt, uint16_t* la,
+                                            uint16_t* lb)
 {
     using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
     constexpr int N = G::N;
+    auto cidx = [](int n, int t) -> int {
+        return DIR == 0 ? (t + 1) * N + (n + 1) : (n + 1) * N + (t + 1);
+    };
+    /* cnt layout: [band][list 0|1][class 0..2][0 = count, 1 = position] */
+    auto C = [&](int band, int list, int cls, int w) -> int& {
+        return cnt[((band * 2 + list) * 3 + cls) * 2 + w];
+    };
+    for (int k = threadIdx.x; k < L::CNT_INTS; k += NT) cnt[k] = 0;
+    __syncthreads();
+    for (int f = threadIdx.x; f < G::NSLICE * G::FA; f += NT) {
+        const int t = f / G::FA, n = f % G::FA;
+        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        atomicAdd(&C(t / RB, 0, cls, 0), 1);
+    }
+    for (int f = threadIdx.x; f < G::NSLICE * G::FB; f += NT) {
+        const int t = f / G::FB, n = 1 + f % G::FB;
+        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        atomicAdd(&C(t / RB, 1, cls, 0), 1);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < L::NBAND * 2; e += NT) {
+        const int band = e >> 1, list = e & 1;
+        int acc = 0;
+        for (int cls = 0; cls < 3; ++cls) {
+            C(band, list, cls, 1) = acc;
+            acc += C(band, list, cls, 0);
+        }
+    }
+    __syncthreads();
+    for (int f = threadIdx.x; f < G::NSLICE * G::FA; f += NT) {
+        const int t = f / G::FA, n = f % G::FA;
+        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        const int band = t / RB;
+        const int pos = atomicAdd(&C(band, 0, cls, 1), 1);
+        la[band * RB * G::FA + pos] = (uint16_t)(f - band * RB * G::FA);
+    }
+    for (int f = threadIdx.x; f < G::NSLICE * G::FB; f += NT) {
+        const int t = f / G::FB, n = 1 + f % G::FB;
+        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        const int band = t / RB;
+        const int pos = atomicAdd(&C(band, 1, cls, 1), 1);
+        lb[band * RB * G::FB + pos] = (uint16_t)(f - band * RB * G::FB);
+    }
+    __syncthreads();
+}
+
+/* One sweep direction over all slices, banded. Accumulates into the flux
+ * accumulators; returns this thread's max |s| over normal faces. */
+template <int M, int NT, int RB, int DIR, bool EXACT>
+__device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, int* cnt,
+                                        uint16_t* la, uint16_t* lb, const gf_phys& P, double dtdn,
+                                        double c16g, double rsg, double crit, double crit2)
+{
+    using G = Geo<M>;
+    using L = Smem<M, RB, EXACT>;
+    constexpr int N = G::N;
+    constexpr bool FAST = !EXACT;
     double* W = sm + L::OFF_W;
     double* O = sm + L::OFF_O;
-    /* Normal accumulator N (DX for x-sweeps) and transverse T (DY). */
-    double* ACCN = sm + L::OFF_ACC + (DIR == 0 ? 0 : 3 * M * M);
-    double* ACCT = sm + L::OFF_ACC + (DIR == 0 ? 3 * M * M : 0);
     const double g = P.grav, drytol = P.dry_tolerance;
     const double half_dtdn = 0.5 * dtdn;
     /* local component l -> global component (h, hu, hv) */
     constexpr int G1 = (DIR == 0) ? 1 : 2; /* normal momentum     */
     constexpr int G2 = (DIR == 0) ? 2 : 1; /* transverse momentum */
+    constexpr int MM = M * M;
     double smax = 0.0;
 
-    /* cell (n, t) in sweep coordinates -> shared-plane offset */
     auto cidx = [](int n, int t) -> int {
         return DIR == 0 ? (t + 1) * N + (n + 1) : (n + 1) * N + (t + 1);
     };
-    /* interior cell (n, t) -> accumulator offset */
     auto aidx = [](int n, int t) -> int {
         return DIR == 0 ? (n - 1) + M * (t - 1) : (t - 1) + M * (n - 1);
     };
+    auto C = [&](int band, int list, int cls) -> int {
+        return cnt[((band * 2 + list) * 3 + cls) * 2 + 0];
+    };
 
-    /* Exact form: accumulators fm(i+1,j), fp(i,j), gm(i,j+1), gp(i,j) of the
-     * reference, in sweep coordinates N_M, N_P (normal) and T_M, T_P
-     * (transverse), each summed in the reference's order (slices in
+    build_lists<M, NT, RB, DIR, EXACT>(wet, cnt, la, lb);
+
+    /* Contracted build: DX, DY. Exact build: fm(i+1,j), fp(i,j), gm(i,j+1),
+     * gp(i,j) of the reference, in sweep coordinates N_M, N_P (normal) and
+     * T_M, T_P (transverse), each summed in the reference's order (slices in
      * increasing order, x sweeps before y sweeps). */
-    constexpr int MM = M * M;
+    double* ACCN = sm + L::OFF_ACC + (DIR == 0 ? 0 : 3 * MM);
+    double* ACCT = sm + L::OFF_ACC + (DIR == 0 ? 3 * MM : 0);
     double* NM = sm + L::OFF_ACC + (DIR == 0 ? 0 : 6 * MM);
     double* NP = NM + 3 * MM;
     double* TM = sm + L::OFF_ACC + (DIR == 0 ? 6 * MM : 0);
@@ -186,8 +270,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, co
     auto gather = [&](int t0, int t1) {
         /* slices t0..t1 feed cells n in [1, M], t in [t0-1, t1+1] (interior) */
         const int ta = max(1, t0 - 1), tb = min(M, t1 + 1);
-        const int cnt = (tb - ta + 1) * M;
-        for (int e = threadIdx.x; e < cnt; e += NT) {
+        const int cnt_c = (tb - ta + 1) * M;
+        for (int e = threadIdx.x; e < cnt_c; e += NT) {
             const int t = ta + e / M;
             const int n = 1 + e % M;
             const int a = aidx(n, t);
@@ -242,27 +326,28 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, co
     };
 
     int prev_t0 = -1, prev_t1 = -1;
-    for (int t0 = 0; t0 < G::NSLICE; t0 += RB) {
+    for (int t0 = 0, band = 0; t0 < G::NSLICE; t0 += RB, ++band) {
         const int t1 = min(t0 + RB, G::NSLICE) - 1; /* last slice of band */
-        const int nrow = t1 - t0 + 1;
+        const uint16_t* lA = la + band * RB * G::FA;
+        const uint16_t* lB = lb + band * RB * G::FB;
+        const int a2 = C(band, 0, 0), a1 = C(band, 0, 1), a0 = C(band, 0, 2);
+        const int b2 = C(band, 1, 0), b1 = C(band, 1, 1), b0 = C(band, 1, 2);
 
-        /* ---- stage A: normal Riemann solves, faces 0..M+2 ---- */
-        for (int f = threadIdx.x; f < nrow * G::FA; f += NT) {
-            const int t = t0 + f / G::FA;
-            const int n = f % G::FA;
-            const int kl = cidx(n - 1, t), kr = cidx(n, t);
+        /* ---- stage A: normal Riemann solves, faces 0..M+2, by class ---- */
+        for (int idx = threadIdx.x; idx < a2 + a1 + a0; idx += NT) {
+            const int f = lA[idx];
             double* w = W + f * L::W_STRIDE;
-            if (!wet[kl] && !wet[kr]) {
+            if (idx >= a2 + a1) { /* both cells dry: no waves */
 #pragma unroll
                 for (int q = 0; q < L::W_STRIDE; ++q) w[q] = 0.0;
                 continue;
             }
-            const gf_cell cl = load_cell<DIR>(sm, wet, kl, L::OFF_H, L::OFF_HU, L::OFF_HV,
-                                              L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
-            const gf_cell cr = load_cell<DIR>(sm, wet, kr, L::OFF_H, L::OFF_HU, L::OFF_HV,
-                                              L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
+            const int t = t0 + f / G::FA;
+            const int n = f % G::FA;
+            const gf_cell cl = load_cell<DIR, EXACT, L>(sm, wet, cidx(n - 1, t));
+            const gf_cell cr = load_cell<DIR, EXACT, L>(sm, wet, cidx(n, t));
             double s[3], fw[3][3];
-            gf_rpn2_face(cl, cr, g, drytol, c16g, crit, crit2, s, fw);
+            gf_rpn2_face<FAST>(cl, cr, g, drytol, c16g, rsg, crit, crit2, s, fw);
 #pragma unroll
             for (int mw = 0; mw < 3; ++mw) {
                 w[mw] = s[mw];
@@ -276,16 +361,17 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, co
         __syncthreads();
 
         /* ---- stage B: limiter, 2nd-order terms, transverse split ---- */
-        for (int f = threadIdx.x; f < nrow * G::FB; f += NT) {
-            const int t = t0 + f / G::FB;
-            const int n = 1 + f % G::FB;
-            const int kl = cidx(n - 1, t), kr = cidx(n, t);
+        for (int idx = threadIdx.x; idx < b2 + b1 + b0; idx += NT) {
+            const int f = lB[idx];
             double* o = O + f * L::O_STRIDE;
-            if (!wet[kl] && !wet[kr]) {
+            if (idx >= b2 + b1) {
 #pragma unroll
                 for (int q = 0; q < L::O_STRIDE; ++q) o[q] = 0.0;
                 continue;
             }
+            const int t = t0 + f / G::FB;
+            const int n = 1 + f % G::FB;
+            const int kl = cidx(n - 1, t), kr = cidx(n, t);
             const double* wc = W + ((t - t0) * G::FA + n) * L::W_STRIDE;
             double s[3], fw[3][3];
 #pragma unroll
@@ -351,24 +437,22 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, co
                     }
                 }
             }
-            double A[3] = {0, 0, 0}, B[3] = {0, 0, 0}, C[3] = {0, 0, 0}, D[3] = {0, 0, 0};
+            double A[3] = {0, 0, 0}, B[3] = {0, 0, 0}, Cc[3] = {0, 0, 0}, D[3] = {0, 0, 0};
             if (P.transverse != 0) {
                 double bm[3], bp[3];
                 if (wet[kl]) { /* rpt2 imp=1: left-going part into cell n-1 */
-                    const gf_cell cl = load_cell<DIR>(sm, wet, kl, L::OFF_H, L::OFF_HU, L::OFF_HV,
-                                                      L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
-                    gf_rpt2_face(cl, sm[L::OFF_B + cidx(n - 1, t - 1)],
-                                 sm[L::OFF_B + cidx(n - 1, t + 1)], drytol, amdq, bm, bp);
+                    const gf_cell cl = load_cell<DIR, EXACT, L>(sm, wet, kl);
+                    gf_rpt2_face<FAST>(cl, sm[L::OFF_B + cidx(n - 1, t - 1)],
+                                       sm[L::OFF_B + cidx(n - 1, t + 1)], drytol, amdq, bm, bp);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) { A[c] = half_dtdn * bm[c]; B[c] = half_dtdn * bp[c]; }
                 }
                 if (wet[kr]) { /* rpt2 imp=2: right-going part into cell n */
-                    const gf_cell cr = load_cell<DIR>(sm, wet, kr, L::OFF_H, L::OFF_HU, L::OFF_HV,
-                                                      L::OFF_B, L::OFF_U, L::OFF_V, L::OFF_C);
-                    gf_rpt2_face(cr, sm[L::OFF_B + cidx(n, t - 1)], sm[L::OFF_B + cidx(n, t + 1)],
-                                 drytol, apdq, bm, bp);
+                    const gf_cell cr = load_cell<DIR, EXACT, L>(sm, wet, kr);
+                    gf_rpt2_face<FAST>(cr, sm[L::OFF_B + cidx(n, t - 1)],
+                                       sm[L::OFF_B + cidx(n, t + 1)], drytol, apdq, bm, bp);
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) { C[c] = half_dtdn * bm[c]; D[c] = half_dtdn * bp[c]; }
+                    for (int c = 0; c < 3; ++c) { Cc[c] = half_dtdn * bm[c]; D[c] = half_dtdn * bp[c]; }
                 }
             }
             /* write in global component order (h, hu, hv) */
@@ -376,7 +460,7 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, co
             o[3] = faddp[0]; o[3 + G1] = faddp[1]; o[3 + G2] = faddp[2];
             o[6] = A[0]; o[6 + G1] = A[1]; o[6 + G2] = A[2];
             o[9] = B[0]; o[9 + G1] = B[1]; o[9 + G2] = B[2];
-            o[12] = C[0]; o[12 + G1] = C[1]; o[12 + G2] = C[2];
+            o[12] = Cc[0]; o[12 + G1] = Cc[1]; o[12 + G2] = Cc[2];
             o[15] = D[0]; o[15 + G1] = D[1]; o[15 + G2] = D[2];
         }
         __syncthreads();
@@ -388,7 +472,10 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, co
     return smax;
 }
 
-/* Manning friction source term on one interior cell (geoclaw_src2_fort.f90:41-71). */
+/* Manning friction source term on one interior cell (geoclaw_src2_fort.f90:41-71).
+ * The contracted build forms h^(-7/3) = (1/h)^2 rcbrt(h) and one reciprocal
+ * of 1 + dt gamma instead of pow and three divisions. */
+template <bool FAST>
 __device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double bathy, double nvar,
                                           double& h, double& hu, double& hv)
 {
@@ -404,11 +491,20 @@ __device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double ba
         } else {
             coeff = nvar;
         }
-        const double gamma =
-            sqrt(hu * hu + hv * hv) * P.grav * (coeff * coeff) / pow(h, 7.0 / 3.0);
-        const double dgamma = 1.0 + dt * gamma;
-        hu = hu / dgamma;
-        hv = hv / dgamma;
+        if (FAST) {
+            const double rh = 1.0 / h;
+            const double gamma =
+                sqrt(hu * hu + hv * hv) * P.grav * (coeff * coeff) * ((rh * rh) * rcbrt(h));
+            const double rdg = 1.0 / (1.0 + dt * gamma);
+            hu = hu * rdg;
+            hv = hv * rdg;
+        } else {
+            const double gamma =
+                sqrt(hu * hu + hv * hv) * P.grav * (coeff * coeff) / pow(h, 7.0 / 3.0);
+            const double dgamma = 1.0 + dt * gamma;
+            hu = hu / dgamma;
+            hv = hv / dgamma;
+        }
     }
 }
 
@@ -425,8 +521,12 @@ __global__ void __launch_bounds__(NT, MINB)
     using L = Smem<M, RB, EXACT>;
     constexpr int N = G::N;
     constexpr int S = G::S;
+    constexpr bool FAST = !EXACT;
     extern __shared__ __align__(128) double sm[];
-    unsigned char* wet = reinterpret_cast<unsigned char*>(sm + L::OFF_WET);
+    int* cnt = reinterpret_cast<int*>(sm + L::OFF_INT);
+    uint16_t* la = reinterpret_cast<uint16_t*>(cnt + L::CNT_INTS);
+    uint16_t* lb = la + L::LIST_A;
+    unsigned char* wet = reinterpret_cast<unsigned char*>(sm) + L::OFF_WET_BYTES;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::OFF_BAR);
     double* red = sm + L::OFF_RED;
 
@@ -466,14 +566,27 @@ __global__ void __launch_bounds__(NT, MINB)
         const bool w = h > drytol;
         wet[k] = w ? 1 : 0;
         any_wet |= w;
+        double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
         if (w) {
-            sm[L::OFF_U + k] = sm[L::OFF_HU + k] / h;
-            sm[L::OFF_V + k] = sm[L::OFF_HV + k] / h;
-            sm[L::OFF_C + k] = sqrt(g * h);
-        } else {
-            sm[L::OFF_U + k] = 0.0;
-            sm[L::OFF_V + k] = 0.0;
-            sm[L::OFF_C + k] = 0.0;
+            if (FAST) {
+                rh = 1.0 / h;
+                u = sm[L::OFF_HU + k] * rh;
+                v = sm[L::OFF_HV + k] * rh;
+                const double gh = g * h;
+                rc = rsqrt(gh);
+                c = gh * rc;
+            } else {
+                u = sm[L::OFF_HU + k] / h;
+                v = sm[L::OFF_HV + k] / h;
+                c = sqrt(g * h);
+            }
+        }
+        sm[L::OFF_U + k] = u;
+        sm[L::OFF_V + k] = v;
+        sm[L::OFF_C + k] = c;
+        if (FAST) {
+            sm[L::OFF_RH + k] = rh;
+            sm[L::OFF_RC + k] = rc;
         }
     }
     for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
@@ -483,10 +596,11 @@ __global__ void __launch_bounds__(NT, MINB)
     double smax_x = 0.0, smax_y = 0.0;
     if (any_wet) {
         const double c16g = 1.0 / (16.0 * g);
+        const double rsg = rsqrt(g);
         const double crit = fmax(drytol * g, 1e-6);
         const double crit2 = sqrt(crit);
-        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, P, dtdx, c16g, crit, crit2);
-        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, P, dtdy, c16g, crit, crit2);
+        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2);
+        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2);
     }
 
     /* ---- flux-difference update, src2, write interior ---- */
@@ -518,7 +632,7 @@ __global__ void __launch_bounds__(NT, MINB)
             const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
                                     ? gaux[(size_t)fidx * S + k]
                                     : 0.0;
-            src2_cell(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
+            src2_cell<FAST>(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
         }
         gq[k] = h;
         gq[S + k] = hu;

@@ -30,16 +30,20 @@ struct gf_cell {
     double ut;   /* hut/h if wet else 0                         */
     double c;    /* sqrt(g h) if wet else 0                     */
     double b;    /* bathymetry                                  */
+    double rh;   /* 1/h if wet (contracted build only)          */
+    double rc;   /* 1/sqrt(g h) if wet (contracted build only)  */
     bool wet;    /* h > dry_tolerance                           */
 };
 
 /* riemanntype (geoclaw_riemann_utils.f:566-677), maxiter = 1.
  * cL = sqrt(g hL), cR = sqrt(g hR) are supplied by the caller (they equal
  * the Fortran's sqrt(g*hL), sqrt(g*hR) bit for bit). Returns hm, s1m, s2m. */
+template <bool FAST>
 __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
                                                double uR, double cL, double cR,
+                                               double rhL, double rhR,
                                                double g, double drytol,
-                                               double c16g, double& hm,
+                                               double c16g, double rsg, double& hm,
                                                double& s1m, double& s2m)
 {
     const double h_min = fmin(hR, hL);
@@ -55,8 +59,11 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
     const double c_min = fmin(cR, cL);
     const double c_max = fmax(cR, cL);
     const double F_min = delu + 2.0 * (c_min - c_max);
+    /* (h_max + h_min)/(h_max h_min) = 1/h_min + 1/h_max: the contracted
+     * build uses the per-cell reciprocals instead of a division. */
     const double F_max =
-        delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
+        FAST ? delu + (h_max - h_min) * sqrt(0.5 * g * (fmax(rhL, rhR) + fmin(rhL, rhR)))
+             : delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
     if (F_min > 0.0) { /* 2-rarefactions */
         const double t = fmax(0.0, -delu + 2.0 * (cL + cR));
         hm = c16g * (t * t);
@@ -65,14 +72,29 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
         s2m = uR - 2.0 * cR + 3.0 * cm;
     } else if (F_max <= 0.0) { /* 2 shocks, one Newton step on sqrt(h) */
         const double h0 = h_max;
-        const double rL = 1.0 / hL, rR = 1.0 / hR;
-        const double r0 = 1.0 / h0; /* equals rL or rR */
-        const double gL = sqrt(0.5 * g * (r0 + rL));
-        const double gR = sqrt(0.5 * g * (r0 + rR));
+        double gL, gR, dfdh, sh0, rL, rR;
+        if (FAST) {
+            rL = rhL;
+            rR = rhR;
+            const double r0 = fmin(rhL, rhR); /* 1/h_max */
+            const double aL = 0.5 * g * (r0 + rL), aR = 0.5 * g * (r0 + rR);
+            const double qL = rsqrt(aL), qR = rsqrt(aR);
+            gL = aL * qL;
+            gR = aR * qR;
+            const double w = 0.25 * (r0 * r0) * g;
+            dfdh = gL - (h0 - hL) * w * qL + gR - (h0 - hR) * w * qR;
+            sh0 = fmax(cL, cR) * rsg; /* sqrt(h_max) = sqrt(g h_max)/sqrt(g) */
+        } else {
+            rL = 1.0 / hL;
+            rR = 1.0 / hR;
+            const double r0 = 1.0 / h0; /* equals rL or rR */
+            gL = sqrt(0.5 * g * (r0 + rL));
+            gR = sqrt(0.5 * g * (r0 + rR));
+            dfdh = gL - g * (h0 - hL) / (4.0 * (h0 * h0) * gL) + gR -
+                   g * (h0 - hR) / (4.0 * (h0 * h0) * gR);
+            sh0 = sqrt(h0);
+        }
         const double F0 = delu + (h0 - hL) * gL + (h0 - hR) * gR;
-        const double dfdh = gL - g * (h0 - hL) / (4.0 * (h0 * h0) * gL) + gR -
-                            g * (h0 - hR) / (4.0 * (h0 * h0) * gR);
-        const double sh0 = sqrt(h0);
         const double slope = 2.0 * sh0 * dfdh;
         const double t = sh0 - F0 / slope;
         hm = t * t;
@@ -85,8 +107,12 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
     } else { /* one shock, one rarefaction, one secant step.
                 The first F0 has (h0 - h_min) = 0, so F0 = F_min exactly. */
         const double F0 = F_min;
-        const double slope = (F_max - F0) / (h_max - h_min);
-        hm = h_min - F0 / slope;
+        if (FAST) {
+            hm = h_min - F0 * ((h_max - h_min) / (F_max - F0));
+        } else {
+            const double slope = (F_max - F0) / (h_max - h_min);
+            hm = h_min - F0 / slope;
+        }
         const double cm = sqrt(g * hm);
         if (hL > hR) {
             s1m = uL + 2.0 * cL - 3.0 * cm;
@@ -100,25 +126,27 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
 
 /* Normal Riemann problem at one face: rpn2_geoclaw.f:110-315 + aug_JCP.
  * Outputs speeds s[3] and f-waves fw[mw][m] (LOCAL component order). */
+template <bool FAST>
 __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& Rc,
                                              double g, double drytol,
-                                             double c16g, double crit,
+                                             double c16g, double rsg, double crit,
                                              double crit2, double s[3],
                                              double fw[3][3])
 {
     /* Riemann problem variables (rpn2_geoclaw.f:136-171). */
-    double hL, huL, hvL, uL, vL, phiL, cL;
-    double hR, huR, hvR, uR, vR, phiR, cR;
+    double hL, huL, hvL, uL, vL, phiL, cL, rhL = 0.0;
+    double hR, huR, hvR, uR, vR, phiR, cR, rhR = 0.0;
     double bL = Lc.b, bR = Rc.b;
     if (Rc.wet) {
-        hR = Rc.h; huR = Rc.hun; hvR = Rc.hut; uR = Rc.un; vR = Rc.ut; cR = Rc.c;
-        phiR = 0.5 * g * (hR * hR) + (huR * huR) / hR;
+        hR = Rc.h; huR = Rc.hun; hvR = Rc.hut; uR = Rc.un; vR = Rc.ut; cR = Rc.c; rhR = Rc.rh;
+        /* hu^2/h = hu u: the contracted build reuses the cell quotient */
+        phiR = FAST ? 0.5 * g * (hR * hR) + huR * uR : 0.5 * g * (hR * hR) + (huR * huR) / hR;
     } else {
         hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0; phiR = 0.0; cR = 0.0;
     }
     if (Lc.wet) {
-        hL = Lc.h; huL = Lc.hun; hvL = Lc.hut; uL = Lc.un; vL = Lc.ut; cL = Lc.c;
-        phiL = 0.5 * g * (hL * hL) + (huL * huL) / hL;
+        hL = Lc.h; huL = Lc.hun; hvL = Lc.hut; uL = Lc.un; vL = Lc.ut; cL = Lc.c; rhL = Lc.rh;
+        phiL = FAST ? 0.5 * g * (hL * hL) + huL * uL : 0.5 * g * (hL * hL) + (huL * huL) / hL;
     } else {
         hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0; phiL = 0.0; cL = 0.0;
     }
@@ -128,21 +156,21 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     double wall0 = 1.0, wall1 = 1.0, wall2 = 1.0;
     if (!Rc.wet) {
         double hstar, s1x, s2x;
-        gf_riemanntype(hL, hL, uL, -uL, cL, cL, g, drytol, c16g, hstar, s1x, s2x);
+        gf_riemanntype<FAST>(hL, hL, uL, -uL, cL, cL, rhL, rhL, g, drytol, c16g, rsg, hstar, s1x, s2x);
         const double hstartest = fmax(hL, hstar);
         if (hstartest + bL < bR) {
             wall1 = 0.0; wall2 = 0.0;
-            hR = hL; huR = -huL; bR = bL; phiR = phiL; uR = -uL; vR = vL; cR = cL;
+            hR = hL; huR = -huL; bR = bL; phiR = phiL; uR = -uL; vR = vL; cR = cL; rhR = rhL;
         } else if (hL + bL < bR) {
             bR = hL + bL;
         }
     } else if (!Lc.wet) {
         double hstar, s1x, s2x;
-        gf_riemanntype(hR, hR, -uR, uR, cR, cR, g, drytol, c16g, hstar, s1x, s2x);
+        gf_riemanntype<FAST>(hR, hR, -uR, uR, cR, cR, rhR, rhR, g, drytol, c16g, rsg, hstar, s1x, s2x);
         const double hstartest = fmax(hR, hstar);
         if (hstartest + bR < bL) {
             wall0 = 0.0; wall1 = 0.0;
-            hL = hR; huL = -huR; bL = bR; phiL = phiR; uL = -uR; vL = vR; cL = cR;
+            hL = hR; huL = -huR; bL = bR; phiL = phiR; uL = -uR; vL = vR; cL = cR; rhL = rhR;
         } else if (hR + bR < bL) {
             bL = hR + bR;
         }
@@ -163,14 +191,18 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double delb = bR - bL;
 
     double hm, s1m, s2m;
-    gf_riemanntype(hL, hR, uL, uR, cL, cR, g, drytol, c16g, hm, s1m, s2m);
+    gf_riemanntype<FAST>(hL, hR, uL, uR, cL, cR, rhL, rhR, g, drytol, c16g, rsg, hm, s1m, s2m);
     (void)hm;
 
     const double l1 = fmin(sE1, s2m);
     const double l3 = fmax(sE2, s1m);
     sE1 = l1;
     sE2 = l3;
-    const double hstarHLL = fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
+    /* One reciprocal serves h*_HLL and Cramer's rule in the contracted
+     * build: sE2 - sE1 = l3 - l1 = -(l1 - l3). */
+    const double rdet = FAST ? 1.0 / (l1 - l3) : 0.0;
+    const double hstarHLL = FAST ? fmax((huL - huR + sE2 * hR - sE1 * hL) * -rdet, 0.0)
+                                 : fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
     const double l2 = 0.5 * (l1 + l3);
 
     /* steady-state wave, first (only) iteration: hLstar = hL etc. */
@@ -188,7 +220,8 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     else if ((uL - cL) * (uR - cR) < 0.0) sonic = true;
     else sonic = false;
 
-    double deldelh = sonic ? -delb : delb * g * hbar / s1s2bar;
+    const double rs12 = (FAST && !sonic) ? 1.0 / s1s2bar : 0.0;
+    double deldelh = sonic ? -delb : (FAST ? delb * g * hbar * rs12 : delb * g * hbar / s1s2bar);
     if (sE1 < -crit && sE2 > crit) {
         deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE2);
         deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE1);
@@ -199,7 +232,9 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
         deldelh = fmin(deldelh, hR);
         deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE2);
     }
-    double deldelphi = sonic ? -g * hbar * delb : -delb * g * hbar * s1s2tilde / s1s2bar;
+    double deldelphi = sonic ? -g * hbar * delb
+                             : (FAST ? -delb * g * hbar * s1s2tilde * rs12
+                                     : -delb * g * hbar * s1s2tilde / s1s2bar);
     deldelphi = fmin(deldelphi, g * fmax(-hL * delb, -hR * delb));
     deldelphi = fmax(deldelphi, g * fmin(-hL * delb, -hR * delb));
 
@@ -211,9 +246,10 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
      * r(:,3) = (1,l3,l3^2): determinant = l1 - l3. */
     const double A2 = l1 * l1, C2 = l3 * l3;
     const double det = l1 - l3;
-    const double beta1 = (d2 - d1 * l3) / det;
-    const double beta2 = ((d2 * C2 - l3 * d3) - d1 * (l1 * C2 - l3 * A2) + (l1 * d3 - d2 * A2)) / det;
-    const double beta3 = (d1 * l1 - d2) / det;
+    const double n2 = (d2 * C2 - l3 * d3) - d1 * (l1 * C2 - l3 * A2) + (l1 * d3 - d2 * A2);
+    const double beta1 = FAST ? (d2 - d1 * l3) * rdet : (d2 - d1 * l3) / det;
+    const double beta2 = FAST ? n2 * rdet : n2 / det;
+    const double beta3 = FAST ? (d1 * l1 - d2) * rdet : (d1 * l1 - d2) / det;
 
     /* f-waves (geoclaw_riemann_utils.f:289-306). */
     double f11 = beta1 * l1, f21 = beta1 * A2, f31 = beta1 * l1 * vL;
@@ -234,6 +270,7 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
  * the transverse neighbours below / above it. asdq in LOCAL order (0 = h,
  * 1 = momentum normal to the face, 2 = momentum along the face; "along the
  * face" is the transverse sweep direction). Accumulates into bm / bp. */
+template <bool FAST>
 __device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
                                              double topo_hi, double tol,
                                              const double asdq[3], double bm[3],
@@ -250,10 +287,13 @@ __device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
     const double s2 = v;
     const double s3 = v + cl.c;
     const double delf1 = asdq[0], delf2 = asdq[1], delf3 = asdq[2];
+    /* s3 - s1 = 2 sqrt(g h): the contracted build multiplies by the
+     * per-cell reciprocal instead of dividing twice. */
     const double den = s3 - s1;
-    const double beta1 = (s3 * delf1 - delf3) / den;
+    const double rden = 0.5 * cl.rc;
+    const double beta1 = FAST ? (s3 * delf1 - delf3) * rden : (s3 * delf1 - delf3) / den;
     const double beta2 = -u * delf1 + delf2;
-    const double beta3 = (delf3 - s1 * delf1) / den;
+    const double beta3 = FAST ? (delf3 - s1 * delf1) * rden : (delf3 - s1 * delf1) / den;
     /* r(:,1) = (1, u, s1); r(:,2) = (0, 1, 0); r(:,3) = (1, u, s3) */
     if (s1 < 0.0 && eta >= topo_lo) {
         const double a = s1 * beta1;

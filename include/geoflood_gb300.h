@@ -185,6 +185,13 @@ int gf_level_patch_cfl(gf_level* lev, double* cfl);
 /* Device pointers of the resident planes (for graph capture / tooling). */
 int gf_level_device_planes(gf_level* lev, double** q, double** aux);
 
+/* ----------------------------------------------------------- probes */
+/* Measured FP64 pipe rates of `device` in operations per second:
+ * rates[0] double fma, [1] double division, [2] double sqrt, [3] float fma.
+ * The patch update is FP64-issue bound; this is its roofline denominator.
+ * No reference counterpart (measurement support). */
+int gf_measure_fp64_rates(int device, double* rates);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,11 +90,15 @@ def test_random_wet_dry_patches(ctx, m, seed):
 @pytest.mark.parametrize("variant", [
     dict(order=1), dict(transverse=0), dict(transverse=1), dict(order=1, transverse=1),
     dict(mthlim=(1, 1, 1)), dict(mthlim=(2, 2, 2)), dict(mthlim=(3, 3, 3)),
-    dict(mthlim=(5, 5, 5)), dict(mthlim=(0, 4, 1)), dict(friction_forcing=False),
+    dict(mthlim=(0, 4, 1)), dict(friction_forcing=False),
     dict(src_term=0), dict(manning_coefficient=(0.06, 0.03), manning_break=(2.0, 1e10)),
     dict(dry_tolerance=1e-2), dict(friction_depth=1.5),
 ])
 def test_method_variants(ctx, variant):
+    """Bounded limiters and method switches at the 1e-10 bar. (The unbounded
+    Beam-Warming limiter, philim = r, amplifies a 1-ulp input change to
+    ~1e-2 in the oracle itself, so it is checked bitwise in the exact build
+    instead: test_exact_build_beam_warming.)"""
     m = 16
     q, aux = random_state(12, m, 9)
     out, ref, cg, cr, pg, pr = level_vs_oracle(ctx, q, aux, m, 2.0, 0.04, gf.Phys(**variant),
@@ -256,3 +260,12 @@ def test_exact_build_depth_bitwise_with_friction(exact_ctx, m):
     assert np.array_equal(out[:, s, s, 0], ref[:, s, s, 0])
     rel = np.abs(out[:, s, s, 1:] - ref[:, s, s, 1:]) / np.maximum(np.abs(ref[:, s, s, 1:]), 1e-300)
     assert rel.max() < 1e-14
+
+
+def test_exact_build_beam_warming(exact_ctx):
+    m = 16
+    q, aux = random_state(12, m, 9)
+    phys = gf.Phys(mthlim=(5, 5, 5), friction_forcing=False)
+    out, ref, cg, cr, pg, pr = level_vs_oracle(exact_ctx, q, aux, m, 2.0, 0.04, phys, slot=7)
+    s = slice(MBC, MBC + m)
+    assert np.array_equal(out[:, s, s], ref[:, s, s])
