@@ -78,6 +78,9 @@ SIGNATURES = [
     ("gf_level_ghost_fill", C.c_int, [_vp, C.c_double]),
     ("gf_level_ghost_fill_async", C.c_int, [_vp, C.c_double]),
     ("gf_measure_fp64_rates", C.c_int, [C.c_int, _dp]),
+    ("gf_patch_update_noalloc", C.c_int, [C.c_int, C.POINTER(gf_phys), C.c_int, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_double,
+                                          C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p]),
     ("gf_level_device_planes", C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
 ]
 

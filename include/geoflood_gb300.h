@@ -185,6 +185,35 @@ int gf_level_patch_cfl(gf_level* lev, double* cfl);
 /* Device pointers of the resident planes (for graph capture / tooling). */
 int gf_level_device_planes(gf_level* lev, double** q, double** aux);
 
+/* ------------------------------------------- allocation-free drop-in */
+/* For callers that cannot allocate device memory at step time: memory owned
+ * by another allocator (a framework's caching pool or a fixed budget a raw
+ * cudaMalloc would bypass), a service at its memory limit where allocation
+ * can fail mid-step, or a latency-critical stream that cudaFree would stall
+ * by synchronising the device. No counterpart in the reference: its GPU
+ * path allocates per call (cuda_source/cudaclaw_step2.cu:179, 279-287).
+ *
+ * Same work as gf_patch_update_batch, but q and aux are DEVICE buffers the
+ * caller owns: npatch contiguous Fortran-layout blocks (q updated in place,
+ * interior cells only), dx/dy/cfl/maxcfl host arrays, `phys` a host struct,
+ * `stream` a cudaStream_t (NULL = legacy default stream). Nothing is
+ * allocated: staging lives in one static device array of
+ * GF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit. Limits: npatch <= GF_NOALLOC_MAX_PATCHES (16), maux <=
+ * GF_NOALLOC_MAX_MAUX (4), mx = my in {8, 16, 32}; larger sizes return
+ * GF_ERR_ARG, other shapes GF_ERR_UNSUPPORTED. The first call on a device
+ * looks up the array's device address, so make that first call before any
+ * stream capture. All calls share the array: calls whose GPU work overlaps
+ * race, so issue them one after another. */
+#define GF_NOALLOC_MAX_PATCHES 16
+#define GF_NOALLOC_MAX_MAUX 4
+#define GF_NOALLOC_SCRATCH_BYTES 1162752
+int gf_patch_update_noalloc(int device, const gf_phys* phys, int npatch,
+                            int mx, int my, int mbc, int meqn, int maux,
+                            const double* dx, const double* dy, double dt,
+                            double* q, const double* aux, double* cfl,
+                            double* maxcfl, void* stream);
+
 /* ----------------------------------------------------------- probes */
 /* Measured FP64 pipe rates of `device` in operations per second:
  * rates[0] double fma, [1] double division, [2] double sqrt, [3] float fma.
