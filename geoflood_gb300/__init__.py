@@ -77,6 +77,41 @@ class Phys:
         return p
 
 
+@dataclass
+class Refine:
+    """Refinement criteria (refinement_data_module) and regions (regions_module).
+    regions: iterable of (x_low, x_hi, y_low, y_hi, t_low, t_hi, min_level, max_level)."""
+    wave_tolerance: float = 0.1
+    speed_tolerance: tuple = (1e12,)
+    deep_depth: float = 1e2
+    max_level_deep: int = 3
+    max_velocity_depth_product: float = 1e20
+    flowgrades: tuple = ()   # (value, variable, type, minlevel)
+    regions: tuple = ()
+
+    def to_c(self) -> _lib.gf_refine:
+        r = _lib.gf_refine()
+        r.wave_tolerance = self.wave_tolerance
+        if len(self.speed_tolerance) > 8 or len(self.flowgrades) > 4 or len(self.regions) > 16:
+            raise ValueError("too many speed tolerances / flowgrades / regions")
+        for k, v in enumerate(self.speed_tolerance):
+            r.speed_tolerance[k] = v
+        r.num_speed_tolerance = len(self.speed_tolerance)
+        r.deep_depth = self.deep_depth
+        r.max_level_deep = self.max_level_deep
+        r.max_velocity_depth_product = self.max_velocity_depth_product
+        r.num_flowgrades = len(self.flowgrades)
+        for k, (val, var, typ, ml) in enumerate(self.flowgrades):
+            r.flowgradevalue[k], r.flowgradevariable[k] = val, var
+            r.flowgradetype[k], r.flowgrademinlevel[k] = typ, ml
+        r.num_regions = len(self.regions)
+        for k, g in enumerate(self.regions):
+            rr = r.regions[k]
+            (rr.x_low, rr.x_hi, rr.y_low, rr.y_hi, rr.t_low, rr.t_hi,
+             rr.min_level, rr.max_level) = g
+        return r
+
+
 def _check(ctx_handle, rc: int):
     if rc != 0:
         lib = _lib.load()
@@ -257,10 +292,40 @@ class Level:
     def ghost_fill_async(self, t: float):
         _check(self.ctx.h, self._lib.gf_level_ghost_fill_async(self.h, t))
 
+    # -- coarse/fine transfers, time interpolation, tags ------------------
+    def transfer(self, fine: "Level", tasks):
+        """tasks: iterable of (kind, coarse_patch, fine_patch, code, ox, oy);
+        self is the coarse level."""
+        tasks = list(tasks)
+        arr = (_lib.gf_transfer * max(1, len(tasks)))()
+        for k, t in enumerate(tasks):
+            arr[k] = _lib.gf_transfer(*[int(v) for v in t])
+        _check(self.ctx.h, self._lib.gf_level_transfer(self.h, fine.h, len(tasks), arr))
+
+    def timeinterp(self, curr: "Level", last: "Level", alpha: float):
+        _check(self.ctx.h, self._lib.gf_level_timeinterp(self.h, curr.h, last.h, alpha))
+
+    def tag4refinement(self, refine: "Refine", level: int, maxlevel: int, init_flag: int,
+                       t: float) -> np.ndarray:
+        r = refine.to_c()
+        out = np.zeros(self.npatch, np.int32)
+        _check(self.ctx.h, self._lib.gf_level_tag4refinement(self.h, C.byref(r), level, maxlevel,
+                                                             init_flag, t, iptr(out)))
+        return out
+
+    def tag4coarsening(self, refine: "Refine", families, level: int, maxlevel: int,
+                       init_flag: int, t: float) -> np.ndarray:
+        r = refine.to_c()
+        fam = np.ascontiguousarray(families, dtype=np.int32).reshape(-1, 4)
+        out = np.zeros(len(fam), np.int32)
+        _check(self.ctx.h, self._lib.gf_level_tag4coarsening(
+            self.h, C.byref(r), len(fam), iptr(fam), level, maxlevel, init_flag, t, iptr(out)))
+        return out
+
     def patch_cfl(self) -> np.ndarray:
         out = np.empty(self.npatch)
         _check(self.ctx.h, self._lib.gf_level_patch_cfl(self.h, dptr(out)))
         return out
 
 
-__all__ = ["Phys", "Context", "Level", "GeoFloodError", "MBC", "MEQN"]
+__all__ = ["Phys", "Refine", "Context", "Level", "GeoFloodError", "MBC", "MEQN"]

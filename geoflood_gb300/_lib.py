@@ -43,6 +43,30 @@ class gf_phys(C.Structure):
     ]
 
 
+class gf_region(C.Structure):
+    _fields_ = [("x_low", C.c_double), ("x_hi", C.c_double), ("y_low", C.c_double),
+                ("y_hi", C.c_double), ("t_low", C.c_double), ("t_hi", C.c_double),
+                ("min_level", C.c_int), ("max_level", C.c_int)]
+
+
+class gf_refine(C.Structure):
+    _fields_ = [("wave_tolerance", C.c_double), ("speed_tolerance", C.c_double * 8),
+                ("num_speed_tolerance", C.c_int), ("deep_depth", C.c_double),
+                ("max_level_deep", C.c_int), ("max_velocity_depth_product", C.c_double),
+                ("num_flowgrades", C.c_int), ("flowgradevalue", C.c_double * 4),
+                ("flowgradevariable", C.c_int * 4), ("flowgradetype", C.c_int * 4),
+                ("flowgrademinlevel", C.c_int * 4), ("num_regions", C.c_int),
+                ("regions", gf_region * 16)]
+
+
+class gf_transfer(C.Structure):
+    _fields_ = [("kind", C.c_int), ("coarse", C.c_int), ("fine", C.c_int), ("code", C.c_int),
+                ("ox", C.c_int), ("oy", C.c_int)]
+
+
+XFER_AVG_FACE, XFER_AVG_CORNER, XFER_INTERP_FACE = 0, 1, 2
+XFER_INTERP_CORNER, XFER_INTERP2FINE, XFER_AVG2COARSE = 3, 4, 5
+
 _dp = C.POINTER(C.c_double)
 _vp = C.c_void_p
 
@@ -78,6 +102,13 @@ SIGNATURES = [
     ("gf_level_ghost_fill", C.c_int, [_vp, C.c_double]),
     ("gf_level_ghost_fill_async", C.c_int, [_vp, C.c_double]),
     ("gf_measure_fp64_rates", C.c_int, [C.c_int, _dp]),
+    ("gf_level_transfer", C.c_int, [_vp, _vp, C.c_int, C.POINTER(gf_transfer)]),
+    ("gf_level_timeinterp", C.c_int, [_vp, _vp, _vp, C.c_double]),
+    ("gf_level_tag4refinement", C.c_int, [_vp, C.POINTER(gf_refine), C.c_int, C.c_int, C.c_int,
+                                          C.c_double, C.POINTER(C.c_int)]),
+    ("gf_level_tag4coarsening", C.c_int, [_vp, C.POINTER(gf_refine), C.c_int,
+                                          C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int,
+                                          C.c_double, C.POINTER(C.c_int)]),
     ("gf_patch_update_noalloc", C.c_int, [C.c_int, C.POINTER(gf_phys), C.c_int, C.c_int, C.c_int,
                                           C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_double,
                                           C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p]),

@@ -37,7 +37,9 @@ def sources() -> list[Path]:
 
 # Per-file flags: the parity build of the patch kernel runs without
 # floating-point contraction.
-PER_FILE = {"gf_kernels_exact.cu": ["-fmad=false"]}
+PER_FILE = {"gf_kernels_exact.cu": ["-fmad=false"],
+            # refinement tags must match the oracle bit for bit: no contraction
+            "gf_amr.cu": ["-fmad=false"]}
 
 
 def _compile(src: Path, extra: list[str]) -> Path:

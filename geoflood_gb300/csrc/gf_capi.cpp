@@ -91,6 +91,12 @@ struct gf_ctx {
     DevBuf<gf_patch_work> work;
     HostBuf<double> h_stage, h_cfl;
     HostBuf<gf_patch_work> h_work;
+    /* coarse/fine transfers and tags */
+    DevBuf<gf_xfer_task> xfer;
+    DevBuf<gf_tinterp_task> tint;
+    DevBuf<gf_tag_task> tagt;
+    DevBuf<int> tags;
+    DevBuf<gf_refine> refine;
 };
 
 struct gf_level {
@@ -253,6 +259,11 @@ void gf_ctx_destroy(gf_ctx* c)
     c->h_stage.release();
     c->h_cfl.release();
     c->h_work.release();
+    c->xfer.release();
+    c->tint.release();
+    c->tagt.release();
+    c->tags.release();
+    c->refine.release();
     if (c->d_phys) cudaFree(c->d_phys);
     if (c->d_status) cudaFree(c->d_status);
     if (c->h_status) cudaFreeHost(c->h_status);
@@ -699,6 +710,163 @@ int gf_level_device_planes(gf_level* L, double** q, double** aux)
     if (q) *q = L->d_q;
     if (aux) *aux = L->d_aux;
     return GF_OK;
+}
+
+/* ----------------------------------------------- coarse/fine, regrid */
+
+int gf_level_transfer(gf_level* Cl, gf_level* Fl, int ntask, const gf_transfer* tasks)
+{
+    if (!Cl || !Fl || (ntask > 0 && !tasks) || ntask < 0) return GF_ERR_ARG;
+    gf_ctx* c = Cl->ctx;
+    if (Fl->ctx != c) return fail(c, GF_ERR_ARG, "levels belong to different contexts");
+    if (Cl->mx != Fl->mx || Cl->maux != Fl->maux)
+        return fail(c, GF_ERR_ARG, "coarse and fine levels need the same patch size and maux");
+    if (ntask == 0) return GF_OK;
+    std::vector<gf_xfer_task> t(ntask);
+    for (int k = 0; k < ntask; ++k) {
+        const gf_transfer& u = tasks[k];
+        if (u.coarse < 0 || u.coarse >= Cl->npatch || u.fine < 0 || u.fine >= Fl->npatch)
+            return fail(c, GF_ERR_ARG, "transfer patch index out of range");
+        if (u.kind < GF_XFER_AVG_FACE || u.kind > GF_XFER_AVG2COARSE || u.code < 0 || u.code > 3)
+            return fail(c, GF_ERR_ARG, "bad transfer kind or code");
+        /* (ox, oy) must keep every fine index inside the array (ghosts included) */
+        if (u.kind <= GF_XFER_INTERP_CORNER &&
+            (u.ox < -2 * Cl->mx - 4 || u.ox > 2 * Cl->mx + 4 || u.oy < -2 * Cl->mx - 4 ||
+             u.oy > 2 * Cl->mx + 4))
+            return fail(c, GF_ERR_ARG, "transfer offset out of range");
+        if (u.kind == GF_XFER_AVG_CORNER || u.kind == GF_XFER_INTERP_CORNER) {
+            /* corner kinds touch all four fine cells unconditionally: require them inside */
+            const int m = Cl->mx;
+            const int i1 = (u.code == 0 || u.code == 2) ? (u.kind == GF_XFER_AVG_CORNER ? -1 : 1)
+                                                         : (u.kind == GF_XFER_AVG_CORNER ? m + 2 : m);
+            const int j1 = (u.code == 0 || u.code == 1) ? (u.kind == GF_XFER_AVG_CORNER ? -1 : 1)
+                                                         : (u.kind == GF_XFER_AVG_CORNER ? m + 2 : m);
+            const int lo = u.kind == GF_XFER_AVG_CORNER ? 1 : -1;
+            const int hi = u.kind == GF_XFER_AVG_CORNER ? m : m + 2;
+            for (int d = 0; d < 2; ++d) {
+                /* both ghost layers (avg) or the single corner cell (interp) */
+                const int ii = u.kind == GF_XFER_AVG_CORNER ? (i1 < 1 ? i1 + d : i1 - d) : i1;
+                const int jj = u.kind == GF_XFER_AVG_CORNER ? (j1 < 1 ? j1 + d : j1 - d) : j1;
+                const int fi0 = 2 * ii - 1 + u.ox, fj0 = 2 * jj - 1 + u.oy;
+                if (fi0 < lo || fi0 + 1 > hi || fj0 < lo || fj0 + 1 > hi)
+                    return fail(c, GF_ERR_ARG, "corner transfer reaches outside the fine patch");
+            }
+        }
+        gf_xfer_task& x = t[k];
+        x.qc = Cl->d_q + (size_t)u.coarse * 3 * Cl->S;
+        x.ac = Cl->d_aux + (size_t)u.coarse * Cl->maux * Cl->S;
+        x.qf = Fl->d_q + (size_t)u.fine * 3 * Fl->S;
+        x.af = Fl->d_aux + (size_t)u.fine * Fl->maux * Fl->S;
+        x.kind = u.kind;
+        x.code = u.code;
+        x.ox = u.ox;
+        x.oy = u.oy;
+        x.phys = Cl->phys[u.coarse];
+        int rc = check_phys_slot(c, x.phys);
+        if (rc) return rc;
+    }
+    GF_CK(c, cudaSetDevice(c->device));
+    GF_CK(c, c->xfer.reserve(ntask));
+    GF_CK(c, cudaMemcpyAsync(c->xfer.p, t.data(), ntask * sizeof(gf_xfer_task),
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_transfer(Cl->mx, c->xfer.p, ntask, c->d_phys, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_level_timeinterp(gf_level* D, gf_level* Cu, gf_level* La, double alpha)
+{
+    if (!D || !Cu || !La) return GF_ERR_ARG;
+    gf_ctx* c = D->ctx;
+    if (Cu->npatch != D->npatch || La->npatch != D->npatch || Cu->mx != D->mx || La->mx != D->mx)
+        return fail(c, GF_ERR_ARG, "time interpolation needs three levels of the same shape");
+    std::vector<gf_tinterp_task> t(D->npatch);
+    for (int k = 0; k < D->npatch; ++k) {
+        t[k].qcurr = Cu->d_q + (size_t)k * 3 * D->S;
+        t[k].qlast = La->d_q + (size_t)k * 3 * D->S;
+        t[k].qinterp = D->d_q + (size_t)k * 3 * D->S;
+    }
+    GF_CK(c, cudaSetDevice(c->device));
+    GF_CK(c, c->tint.reserve(D->npatch));
+    GF_CK(c, cudaMemcpyAsync(c->tint.p, t.data(), t.size() * sizeof(gf_tinterp_task),
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_timeinterp(D->mx, c->tint.p, D->npatch, alpha, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+static int run_tags(gf_level* L, const gf_refine* rf, std::vector<gf_tag_task>& t, int maxlevel,
+                    int init_flag, double tm, int* tags)
+{
+    gf_ctx* c = L->ctx;
+    if (rf->num_speed_tolerance < 0 || rf->num_speed_tolerance > GF_MAX_SPEEDS ||
+        rf->num_flowgrades < 0 || rf->num_flowgrades > GF_MAX_FLOWGRADES ||
+        rf->num_regions < 0 || rf->num_regions > GF_MAX_REGIONS)
+        return fail(c, GF_ERR_ARG, "refinement parameter counts out of range");
+    const int n = (int)t.size();
+    if (n == 0) return GF_OK;
+    GF_CK(c, cudaSetDevice(c->device));
+    GF_CK(c, c->tagt.reserve(n));
+    GF_CK(c, c->tags.reserve(n));
+    GF_CK(c, c->refine.reserve(1));
+    GF_CK(c, cudaMemcpyAsync(c->refine.p, rf, sizeof(gf_refine), cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaMemcpyAsync(c->tagt.p, t.data(), n * sizeof(gf_tag_task), cudaMemcpyHostToDevice,
+                             c->stream));
+    GF_CK(c, gf::launch_tags(L->mx, c->tagt.p, n, c->refine.p, c->d_phys, maxlevel, init_flag, tm,
+                             c->tags.p, c->stream));
+    GF_CK(c, cudaMemcpyAsync(tags, c->tags.p, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_level_tag4refinement(gf_level* L, const gf_refine* rf, int level, int maxlevel,
+                            int init_flag, double t, int* tags)
+{
+    if (!L || !rf || !tags) return GF_ERR_ARG;
+    std::vector<gf_tag_task> tk(L->npatch);
+    for (int k = 0; k < L->npatch; ++k) {
+        int rc = check_phys_slot(L->ctx, L->phys[k]);
+        if (rc) return rc;
+        gf_tag_task& x = tk[k];
+        std::memset(&x, 0, sizeof x);
+        x.q[0] = L->d_q + (size_t)k * 3 * L->S;
+        x.aux[0] = L->d_aux + (size_t)k * L->maux * L->S;
+        x.xlower[0] = L->xlower[k];
+        x.ylower[0] = L->ylower[k];
+        x.dx = L->dx[k];
+        x.dy = L->dy[k];
+        x.level = level;
+        x.nsib = 1;
+        x.phys = L->phys[k];
+    }
+    return run_tags(L, rf, tk, maxlevel, init_flag, t, tags);
+}
+
+int gf_level_tag4coarsening(gf_level* L, const gf_refine* rf, int nfam, const int* fam, int level,
+                            int maxlevel, int init_flag, double t, int* tags)
+{
+    if (!L || !rf || !tags || nfam < 0 || (nfam > 0 && !fam)) return GF_ERR_ARG;
+    std::vector<gf_tag_task> tk(nfam);
+    for (int f = 0; f < nfam; ++f) {
+        gf_tag_task& x = tk[f];
+        std::memset(&x, 0, sizeof x);
+        for (int s = 0; s < 4; ++s) {
+            const int k = fam[4 * f + s];
+            if (k < 0 || k >= L->npatch) return fail(L->ctx, GF_ERR_ARG, "family index out of range");
+            x.q[s] = L->d_q + (size_t)k * 3 * L->S;
+            x.aux[s] = L->d_aux + (size_t)k * L->maux * L->S;
+            x.xlower[s] = L->xlower[k];
+            x.ylower[s] = L->ylower[k];
+        }
+        x.dx = L->dx[fam[4 * f]];
+        x.dy = L->dy[fam[4 * f]];
+        x.level = level;
+        x.nsib = 4;
+        x.phys = L->phys[fam[4 * f]];
+        int rc = check_phys_slot(L->ctx, x.phys);
+        if (rc) return rc;
+    }
+    return run_tags(L, rf, tk, maxlevel, init_flag, t, tags);
 }
 
 } // extern "C"

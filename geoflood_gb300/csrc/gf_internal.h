@@ -27,6 +27,14 @@ cudaError_t launch_ghost_fill(int m, double* q, double* aux, int maux, int npatc
                               const gf_patch_geom* geom, const gf_bc_spec& bc,
                               const gf_phys* phys, const int* phys_of, cudaStream_t st);
 
+cudaError_t launch_transfer(int m, const gf_xfer_task* tasks, int ntask, const gf_phys* phys,
+                            cudaStream_t st);
+cudaError_t launch_timeinterp(int m, const gf_tinterp_task* tasks, int ntask, double alpha,
+                              cudaStream_t st);
+cudaError_t launch_tags(int m, const gf_tag_task* tasks, int ntask, const gf_refine* rf,
+                        const gf_phys* phys, int maxlevel, int init_flag, double t, int* tags,
+                        cudaStream_t st);
+
 } // namespace gf
 
 #endif

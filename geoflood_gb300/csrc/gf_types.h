@@ -40,4 +40,31 @@ typedef struct gf_bc_spec {
     double q0hu;
 } gf_bc_spec;
 
+/* One coarse/fine transfer (gf_amr.cu): kind GF_XFER_*, code = coarse
+ * face / corner or child index, (ox, oy) = fine index of the coarse patch's
+ * lower-left corner minus one. */
+typedef struct gf_xfer_task {
+    double* qc;
+    const double* ac;
+    double* qf;
+    const double* af;
+    int kind, code, ox, oy, phys;
+} gf_xfer_task;
+
+typedef struct gf_tinterp_task {
+    const double* qcurr;
+    const double* qlast;
+    double* qinterp;
+} gf_tinterp_task;
+
+/* A refinement tag task: one patch (nsib = 1) or four siblings (nsib = 4,
+ * order ll, lr, ul, ur). */
+typedef struct gf_tag_task {
+    const double* q[4];
+    const double* aux[4];
+    double xlower[4], ylower[4];
+    double dx, dy;
+    int level, nsib, phys;
+} gf_tag_task;
+
 #endif

@@ -185,6 +185,91 @@ int gf_level_patch_cfl(gf_level* lev, double* cfl);
 /* Device pointers of the resident planes (for graph capture / tooling). */
 int gf_level_device_planes(gf_level* lev, double** q, double** aux);
 
+/* ------------------------------------------ coarse/fine and regrid */
+/* Transfer kinds between a coarse and a fine level (refinement ratio 2,
+ * aligned patches):
+ *   GF_XFER_AVG_FACE / _AVG_CORNER: coarse ghost cells from a fine neighbour
+ *     (fc2d_geoclaw_fort_average_face/_corner, fclaw2d_source/
+ *     fc2d_geoclaw_average_fort.f:33, 323; patch_vt->average_face/_corner);
+ *   GF_XFER_INTERP_FACE / _INTERP_CORNER: fine ghost cells from a coarse
+ *     neighbour (fc2d_geoclaw_interpolate_fort.f:24, 261);
+ *   GF_XFER_INTERP2FINE: child from parent on refinement
+ *     (fc2d_geoclaw_fort_interpolate2fine, interpolate_fort.f:405-579);
+ *   GF_XFER_AVG2COARSE: parent from child on coarsening
+ *     (fc2d_geoclaw_fort_average2coarse, average_fort.f:482-602).
+ * code: the coarse patch's face (0..3) or corner (0..3) toward the fine
+ * patch, or the child index igrid (0..3). (ox, oy): fine-cell index of the
+ * coarse patch's lower-left corner relative to the fine patch's, i.e. the
+ * coarse cell (ic, jc) covers fine cells 2ic-1+ox .. 2ic+ox (unused for the
+ * parent/child kinds). */
+enum gf_xfer_kind {
+    GF_XFER_AVG_FACE = 0,
+    GF_XFER_AVG_CORNER = 1,
+    GF_XFER_INTERP_FACE = 2,
+    GF_XFER_INTERP_CORNER = 3,
+    GF_XFER_INTERP2FINE = 4,
+    GF_XFER_AVG2COARSE = 5
+};
+typedef struct gf_transfer {
+    int kind;
+    int coarse; /* patch index in the coarse level */
+    int fine;   /* patch index in the fine level   */
+    int code;
+    int ox, oy;
+} gf_transfer;
+
+/* Run ntask transfers; tasks of one call must not write a patch another
+ * task of the same call reads (the caller orders averaging before
+ * interpolation, as ForestClaw's ghost fill does). */
+int gf_level_transfer(gf_level* coarse, gf_level* fine, int ntask,
+                      const gf_transfer* tasks);
+
+/* Time interpolation of the 2-cell interior boundary strip of every patch,
+ * dst = last + alpha (curr - last) (fc2d_geoclaw_fort_timeinterp,
+ * fclaw2d_source/fc2d_geoclaw_timeinterp_fort.f:1-69). The three levels
+ * must hold the same patches. */
+int gf_level_timeinterp(gf_level* dst, gf_level* curr, gf_level* last, double alpha);
+
+/* Refinement regions and criteria: regions_module region_type and
+ * refinement_data_module (geolib_source/refinement_data_module.f90:11-40). */
+typedef struct gf_region {
+    double x_low, x_hi, y_low, y_hi, t_low, t_hi;
+    int min_level, max_level;
+} gf_region;
+#define GF_MAX_SPEEDS 8
+#define GF_MAX_FLOWGRADES 4
+#define GF_MAX_REGIONS 16
+typedef struct gf_refine {
+    double wave_tolerance;
+    double speed_tolerance[GF_MAX_SPEEDS];
+    int num_speed_tolerance;
+    double deep_depth;
+    int max_level_deep;
+    double max_velocity_depth_product;
+    int num_flowgrades;
+    double flowgradevalue[GF_MAX_FLOWGRADES];
+    int flowgradevariable[GF_MAX_FLOWGRADES]; /* 1 depth, 2 momentum, 3 surface */
+    int flowgradetype[GF_MAX_FLOWGRADES];
+    int flowgrademinlevel[GF_MAX_FLOWGRADES];
+    int num_regions;
+    gf_region regions[GF_MAX_REGIONS];
+} gf_refine;
+
+/* Refinement tag of every patch of the level (1 refine, 0 not):
+ * geoclaw_patch_tag4refinement (src/fc2d_geoclaw/fc2d_geoclaw.cpp:405-457 ->
+ * fc2d_geoclaw_test_regions, fc2d_geoclaw_fort_tag4refinement,
+ * fc2d_geoflood_flag2refine). The level's xlower/ylower come from
+ * gf_level_set_layout. */
+int gf_level_tag4refinement(gf_level* lev, const gf_refine* rf, int level,
+                            int maxlevel, int init_flag, double t, int* tags);
+
+/* Coarsening tag of nfam sibling families (fam[4k..4k+3] = patches ll, lr,
+ * ul, ur; 1 = may coarsen): geoclaw_patch_tag4coarsening
+ * (fc2d_geoclaw.cpp:461-506 -> fc2d_geoclaw_fort_tag4coarsening). */
+int gf_level_tag4coarsening(gf_level* lev, const gf_refine* rf, int nfam,
+                            const int* fam, int level, int maxlevel,
+                            int init_flag, double t, int* tags);
+
 /* ------------------------------------------- allocation-free drop-in */
 /* For callers that cannot allocate device memory at step time: memory owned
  * by another allocator (a framework's caching pool or a fixed budget a raw

@@ -37,7 +37,7 @@ class orc_params(C.Structure):
 
 
 def build(force: bool = False) -> Path:
-    srcs = [HERE / "geoclaw_oracle.c", HERE / "geoclaw_oracle_ghost.c"]
+    srcs = [HERE / "geoclaw_oracle.c", HERE / "geoclaw_oracle_ghost.c", HERE / "geoclaw_oracle_amr.c"]
     deps = srcs + [HERE / "geoclaw_oracle.h"]
     if not force and LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB
@@ -51,6 +51,29 @@ def build(force: bool = False) -> Path:
 
 _dp = C.POINTER(C.c_double)
 _lib = None
+
+
+class orc_region(C.Structure):
+    _fields_ = [("x_low", C.c_double), ("x_hi", C.c_double), ("y_low", C.c_double),
+                ("y_hi", C.c_double), ("t_low", C.c_double), ("t_hi", C.c_double),
+                ("min_level", C.c_int), ("max_level", C.c_int)]
+
+
+class orc_refine(C.Structure):
+    _fields_ = [("wave_tolerance", C.c_double), ("speed_tolerance", C.c_double * 8),
+                ("num_speed_tolerance", C.c_int), ("deep_depth", C.c_double),
+                ("max_level_deep", C.c_int), ("max_velocity_depth_product", C.c_double),
+                ("num_flowgrades", C.c_int), ("flowgradevalue", C.c_double * 4),
+                ("flowgradevariable", C.c_int * 4), ("flowgradetype", C.c_int * 4),
+                ("flowgrademinlevel", C.c_int * 4), ("num_regions", C.c_int),
+                ("regions", orc_region * 16)]
+
+
+def refine(r) -> orc_refine:
+    """orc_refine from a geoflood_gb300.Refine."""
+    o = orc_refine()
+    C.memmove(C.byref(o), C.byref(r.to_c()), C.sizeof(o))
+    return o
 
 
 class orc_hydro(C.Structure):
@@ -109,6 +132,24 @@ def load():
                                       _dp, _dp]
         lib.orc_rpt2_face.argtypes = [P, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                       _dp]
+        RF = C.POINTER(orc_refine)
+        lib.orc_average_ghost.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp,
+                                          _dp, C.c_int, C.c_int, C.c_int, C.c_int]
+        lib.orc_interpolate_ghost.argtypes = lib.orc_average_ghost.argtypes
+        lib.orc_interpolate2fine.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                             _dp, _dp, C.c_int]
+        lib.orc_average2coarse.argtypes = lib.orc_interpolate2fine.argtypes
+        lib.orc_timeinterp.restype = C.c_int
+        lib.orc_timeinterp.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp,
+                                       C.c_double]
+        lib.orc_tag4refinement.restype = C.c_int
+        lib.orc_tag4refinement.argtypes = [P, RF, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                           C.c_double, C.c_double, C.c_double, C.c_double,
+                                           C.c_double, C.c_int, C.c_int, C.c_int]
+        lib.orc_tag4coarsening.restype = C.c_int
+        lib.orc_tag4coarsening.argtypes = [P, RF, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.POINTER(_dp), C.POINTER(_dp), _dp, _dp, C.c_double,
+                                           C.c_double, C.c_double, C.c_int, C.c_int, C.c_int]
         H = C.POINTER(orc_hydro)
         ip = C.POINTER(C.c_int)
         lib.orc_bc2.argtypes = [P, H, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
@@ -230,3 +271,59 @@ def rpt2_face(ixy: int, imp: int, ql, qr, aux1, aux2, aux3, asdq, phys=None):
     bm, bp = np.zeros(3), np.zeros(3)
     load().orc_rpt2_face(C.byref(p), ixy, imp, *[_ptr(a) for a in arrs], _ptr(bm), _ptr(bp))
     return bm, bp
+
+
+def average_ghost(qc, ac, qf, af, kind, code, ox, oy, phys=None):
+    """kind 0 face / 1 corner; coarse ghost cells from fine (in place on qc)."""
+    p = params(phys)
+    m = qc.shape[0] - 2 * MBC
+    load().orc_average_ghost(C.byref(p), MBC, m, m, ac.shape[-1], _ptr(qc), _ptr(ac), _ptr(qf),
+                             _ptr(af), kind, code, ox, oy)
+
+
+def interpolate_ghost(qc, ac, qf, af, kind, code, ox, oy, phys=None):
+    """kind 0 face / 1 corner; fine ghost cells from coarse (in place on qf)."""
+    p = params(phys)
+    m = qc.shape[0] - 2 * MBC
+    load().orc_interpolate_ghost(C.byref(p), MBC, m, m, ac.shape[-1], _ptr(qc), _ptr(ac),
+                                 _ptr(qf), _ptr(af), kind, code, ox, oy)
+
+
+def interpolate2fine(qc, ac, qf, af, igrid, phys=None):
+    p = params(phys)
+    m = qc.shape[0] - 2 * MBC
+    load().orc_interpolate2fine(C.byref(p), MBC, m, m, ac.shape[-1], _ptr(qc), _ptr(ac),
+                                _ptr(qf), _ptr(af), igrid)
+
+
+def average2coarse(qc, ac, qf, af, igrid, phys=None):
+    p = params(phys)
+    m = qc.shape[0] - 2 * MBC
+    load().orc_average2coarse(C.byref(p), MBC, m, m, ac.shape[-1], _ptr(qc), _ptr(ac),
+                              _ptr(qf), _ptr(af), igrid)
+
+
+def timeinterp(qcurr, qlast, qinterp, alpha):
+    m = qcurr.shape[0] - 2 * MBC
+    psize = 3 * 8 * (m - 2)  # meqn x the strip cell count the Fortran expects
+    return load().orc_timeinterp(MBC, m, m, psize, _ptr(qcurr), _ptr(qlast), _ptr(qinterp), alpha)
+
+
+def tag4refinement(q, aux, xlower, ylower, dx, dy, t, level, maxlevel, init_flag, rf, phys=None):
+    p = params(phys)
+    m = q.shape[0] - 2 * MBC
+    return load().orc_tag4refinement(C.byref(p), C.byref(rf), MBC, m, m, aux.shape[-1], _ptr(q),
+                                     _ptr(aux), xlower, ylower, dx, dy, t, level, maxlevel,
+                                     init_flag)
+
+
+def tag4coarsening(qs, auxs, xlowers, ylowers, dx, dy, t, level, maxlevel, init_flag, rf,
+                   phys=None):
+    p = params(phys)
+    m = qs[0].shape[0] - 2 * MBC
+    qp = (_dp * 4)(*[_ptr(a) for a in qs])
+    ap = (_dp * 4)(*[_ptr(a) for a in auxs])
+    xl = np.ascontiguousarray(xlowers, dtype=np.float64)
+    yl = np.ascontiguousarray(ylowers, dtype=np.float64)
+    return load().orc_tag4coarsening(C.byref(p), C.byref(rf), MBC, m, m, auxs[0].shape[-1], qp, ap,
+                                     _ptr(xl), _ptr(yl), dx, dy, t, level, maxlevel, init_flag)

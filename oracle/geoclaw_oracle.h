@@ -147,3 +147,63 @@ void orc_level_ghost_fill(const orc_params* p, const orc_hydro* hy, int npatch,
 #ifdef __cplusplus
 }
 #endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* Refinement regions (geolib_source/regions_module.f90 region_type). */
+typedef struct orc_region {
+    double x_low, x_hi, y_low, y_hi, t_low, t_hi;
+    int min_level, max_level;
+} orc_region;
+
+/* refinement_data_module (geolib_source/refinement_data_module.f90:11-40). */
+typedef struct orc_refine {
+    double wave_tolerance;
+    double speed_tolerance[8];
+    int num_speed_tolerance;
+    double deep_depth;
+    int max_level_deep;
+    double max_velocity_depth_product;
+    int num_flowgrades;
+    double flowgradevalue[4];
+    int flowgradevariable[4];
+    int flowgradetype[4];
+    int flowgrademinlevel[4];
+    int num_regions;
+    orc_region regions[16];
+} orc_refine;
+
+/* Coarse ghost cells from a fine neighbour (kind 0 face, code = iface of the
+ * coarse patch; kind 1 corner, code = icorner). (ox, oy): fine index of the
+ * coarse patch's cell (1,1) lower-left corner, minus one. */
+void orc_average_ghost(const orc_params* p, int mbc, int mx, int my, int maux, double* qc,
+                       const double* ac, const double* qf, const double* af, int kind, int code,
+                       int ox, int oy);
+/* Fine ghost cells from a coarse neighbour (same conventions). */
+void orc_interpolate_ghost(const orc_params* p, int mbc, int mx, int my, int maux,
+                           const double* qc, const double* ac, double* qf, const double* af,
+                           int kind, int code, int ox, int oy);
+void orc_interpolate2fine(const orc_params* p, int mbc, int mx, int my, int maux,
+                          const double* qc, const double* ac, double* qf, const double* af,
+                          int igrid);
+void orc_average2coarse(const orc_params* p, int mbc, int mx, int my, int maux, double* qc,
+                        const double* ac, const double* qf, const double* af, int igrid);
+int orc_timeinterp(int mbc, int mx, int my, int psize, const double* qcurr, const double* qlast,
+                   double* qinterp, double alpha);
+int orc_test_regions(const orc_refine* rf, int level, double xl, double yl, double xu, double yu,
+                     double t, int refine);
+int orc_flag2refine(const orc_params* p, const orc_refine* rf, int mbc, int mx, int my, int maux,
+                    const double* q, const double* aux, int i, int j, int level, int maxlevel,
+                    int init_flag, int is_coarsening);
+int orc_tag4refinement(const orc_params* p, const orc_refine* rf, int mbc, int mx, int my,
+                       int maux, const double* q, const double* aux, double xlower,
+                       double ylower, double dx, double dy, double t, int level, int maxlevel,
+                       int init_flag);
+int orc_tag4coarsening(const orc_params* p, const orc_refine* rf, int mbc, int mx, int my,
+                       int maux, const double* const* q, const double* const* aux,
+                       const double* xlower, const double* ylower, double dx, double dy, double t,
+                       int level, int maxlevel, int init_flag);
+#ifdef __cplusplus
+}
+#endif
