@@ -149,6 +149,177 @@ def cpu_oracle_rate(q, aux, seconds=12.0, rows=8, threads=0):
     return cells / el, cores, f"{reps} step(s) of {rows} patch rows ({n} patches, {n * M * M} cells)"
 
 
+def plain_per_patch_rate(ctx, q, aux, npatch=256):
+    """The plain per-patch drop-in: gf_patch_update once per patch with host
+    buffers (one launch, host<->device copies per call), as ForestClaw's
+    single_step_update would drive it. Sample: npatch patches across the
+    dam-break front (same wet fraction as the level)."""
+    start = (NPY // 2) * NPX
+    qs = [np.ascontiguousarray(q[start + k]) for k in range(npatch)]
+    aus = [np.ascontiguousarray(aux[start + k]) for k in range(npatch)]
+    for k in range(8):
+        ctx.patch_update(qs[k].copy(), aus[k], DX, DX, 0.0, DT)
+    t0 = time.perf_counter()
+    for k in range(npatch):
+        ctx.patch_update(qs[k], aus[k], DX, DX, 0.0, DT)
+    el = time.perf_counter() - t0
+    return npatch * M * M / el, f"{npatch} patches of 32x32, one gf_patch_update call each"
+
+
+SERVED_SEED = 4242
+
+
+def _pinned(shape):
+    import torch
+
+    return torch.empty(int(np.prod(shape)), dtype=torch.float64,
+                       pin_memory=True).numpy().reshape(shape)
+
+
+def served_stream(args):
+    """Served scenario stream: Poisson arrivals of flood scenarios
+    (finest-level cells log-uniform in [1e4, 4e6], mx drawn from {8,16,32},
+    fractal valley DEM with a channel, hydrograph peak 10-500 m^3/s rising
+    over 0.5-2 h, n ~ U[0.02, 0.08], horizon 1-6 h; times scaled by
+    --served-time-scale) through the continuous-batching server at 80 % of
+    the capacity measured in a calibration pass over the first scenarios."""
+    import queue
+    import threading
+
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+
+    n = args.served_scenarios
+    ts = args.served_time_scale
+    g = np.random.default_rng(SERVED_SEED)
+    cells = np.exp(g.uniform(np.log(1e4), np.log(4e6), n))
+    seeds = [SERVED_SEED + 1 + k for k in range(n)]
+
+    def make(k):
+        sc = synth.flood_scenario(seeds[k], float(cells[k]), time_scale=ts)
+        q = _pinned(sc.q.shape)
+        q[...] = sc.q
+        a = _pinned(sc.aux.shape)
+        a[...] = sc.aux
+        sc.q, sc.aux = q, a
+        return sc, _pinned(sc.q.shape)
+
+    def producer(order, out_q, stop):
+        for k in order:
+            if stop.is_set():
+                return
+            out_q.put((k,) + make(k))
+        out_q.put(None)
+
+    def run_batch(srv, order, arrivals=None, keep=()):
+        """Submit `order` (at `arrivals` on the server clock, else at once)."""
+        stop = threading.Event()
+        q_in = queue.Queue(maxsize=24)
+        th = threading.Thread(target=producer, args=(order, q_in, stop), daemon=True)
+        th.start()
+        ids, late, outs, meta = {}, 0, {}, {}
+        t_base = srv.clock()
+        i = 0
+        while True:
+            item = q_in.get()
+            if item is None:
+                break
+            k, sc, qo = item
+            if arrivals is not None:
+                t_arr = t_base + arrivals[i]
+                while srv.clock() < t_arr:
+                    time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
+                if srv.clock() - t_arr > 0.01:
+                    late += 1
+            ids[k] = srv.submit(sc, qo)
+            meta[k] = (sc.cells, sc.mx, sc.t_final)
+            if k in keep:
+                outs[k] = qo
+            i += 1
+        th.join()
+        infos = {}
+        for k, sid in ids.items():
+            infos[k] = srv.wait(sid, timeout=3600)
+            if k not in keep:
+                srv.release(sid)
+        return infos, outs, late, meta
+
+    srv = gf.Server(device=int(os.environ.get("LOCAL_RANK", "0")))
+    srv.start()
+    # calibration: the first scenarios submitted at once (closed loop)
+    ncal = min(32, n)
+    t0 = srv.clock()
+    cal, _, _, cal_meta = run_batch(srv, list(range(ncal)))
+    t_cal = max(i["t_done"] for i in cal.values()) - t0
+    cap = sum(i["cell_updates"] for i in cal.values()) / t_cal
+    steps_per_sim_s = sum(i["steps"] for i in cal.values()) / sum(m[2] for m in cal_meta.values())
+    # expected work of the stream from its sizes and horizons
+    horizon = [synth.flood_scenario_params(seeds[k], float(cells[k]), time_scale=ts)["horizon"]
+               for k in range(n)]
+    est_work = float(np.mean(cells * np.array(horizon) * steps_per_sim_s))
+    rate = 0.8 * cap / est_work
+    gaps = np.random.default_rng(SERVED_SEED + 7).exponential(1.0 / rate, n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    order = np.argsort(cells)
+    sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 12)})
+    st0 = srv.stats()
+    t_start = srv.clock()
+    infos, outs, late, meta = run_batch(srv, list(range(n)), arrivals, keep=set(sample))
+    t_end = max(i["t_done"] for i in infos.values())
+    st1 = srv.stats()
+    lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
+    work = sum(i["cell_updates"] for i in infos.values())
+    served_rate = work / (t_end - t_start)
+    # isolated re-runs of a size-stratified sample: latency alone, same bits
+    slow, same = [], True
+    for k in sample:
+        iso, iso_out, _, _ = run_batch(srv, [k], keep={k})
+        ik = iso[k]
+        slow.append((infos[k]["t_done"] - infos[k]["t_submit"]) / (ik["t_done"] - ik["t_submit"]))
+        same &= bool(np.array_equal(iso_out[k], outs[k])) and ik["steps"] == infos[k]["steps"]
+    srv.stop()
+    srv.close()
+    # the plain per-patch drop-in on the same work mix
+    ctx = gf.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    rate_mx = {}
+    for mx in (8, 16, 32):
+        sc = synth.flood_scenario(SERVED_SEED, 200000, mx=mx, time_scale=ts)
+        ctx.set_phys(0, sc.phys)
+        npt = min(256, sc.q.shape[0])
+        qs = [np.ascontiguousarray(sc.q[k]) for k in range(npt)]
+        aus = [np.ascontiguousarray(sc.aux[k]) for k in range(npt)]
+        for k in range(min(8, npt)):
+            ctx.patch_update(qs[k].copy(), aus[k], sc.dx, sc.dy, 0.0, 0.2)
+        tp = time.perf_counter()
+        for k in range(npt):
+            ctx.patch_update(qs[k], aus[k], sc.dx, sc.dy, 0.0, 0.2)
+        rate_mx[mx] = npt * mx * mx / (time.perf_counter() - tp)
+    ctx.close()
+    plain_time = sum(i["cell_updates"] / rate_mx[meta[k][1]] for k, i in infos.items())
+    plain_rate = work / plain_time
+    return {
+        "value": served_rate, "unit": METRIC, "scenarios": n,
+        "p50_latency_s": float(np.percentile(lat, 50)),
+        "p99_latency_s": float(np.percentile(lat, 99)),
+        "slowdown_vs_isolated": {"p50": float(np.percentile(slow, 50)),
+                                 "p99": float(np.percentile(slow, 99)), "max": float(max(slow)),
+                                 "sample": len(sample)},
+        "alone_equals_mix": same,
+        "plain_per_patch": {"value": plain_rate, "unit": METRIC,
+                            "per_mx": {str(k): v for k, v in rate_mx.items()},
+                            "note": "gf_patch_update per patch with host buffers, weighted by "
+                                    "the stream's work per mx"},
+        "vs_plain_per_patch": served_rate / plain_rate,
+        "calibration": {"scenarios": ncal, "capacity": cap, "seconds": t_cal},
+        "arrival_rate_per_s": rate, "offered_load": 0.8, "late_submissions": late,
+        "stream_seconds": t_end - t_start, "cell_updates": work,
+        "launches": st1["launches"] - st0["launches"], "rounds": st1["rounds"] - st0["rounds"],
+        "peak_device_bytes": st1["bytes_peak"],
+        "workload": f"{n} flood scenarios, cells log-uniform [1e4, 4e6], mx in {{8,16,32}}, "
+                    f"dx 5 m, times x{ts:.5g} (horizon 1-6 h -> {3600 * ts:.0f}-{21600 * ts:.0f} s)",
+    }
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU patch update (oracle port) on all host threads."""
     if int(os.environ.get("RANK", "0")) != 0:
@@ -282,6 +453,8 @@ def run_gpu(args):
     e2e_ms = max(h0.elapsed_time(h1) / ne, 1e3 * e2e_wall)
     qbytes = q.size * 8
 
+    plain_v, plain_sample = plain_per_patch_rate(ctx, q, aux)
+
     hbm_peak, peak_kind = load_peaks()
     algo = BYTES_PER_CELL_UPDATE * ncell
     achieved = algo / (kernel_ms * 1e-3) / 1e9
@@ -311,7 +484,11 @@ def run_gpu(args):
                      "note": "FP64-issue bound, not HBM bound: see fp64"},
         "fp64": fp64,
         "clocks": clk,
+        "plain_per_patch": {"value": plain_v, "unit": METRIC, "sample": plain_sample,
+                            "note": "single_step_update-style drop-in, host buffers per patch"},
     }
+    if rank == 0 and not args.no_served:
+        result["served"] = served_stream(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
@@ -346,9 +523,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-only", action="store_true")
+    ap.add_argument("--served-scenarios", type=int, default=512)
+    ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.served_only:
+        print(json.dumps({"served": served_stream(args)}))
+        return 0
     return run_gpu(args)
 
 

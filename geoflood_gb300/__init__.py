@@ -328,4 +328,7 @@ class Level:
         return out
 
 
-__all__ = ["Phys", "Refine", "Context", "Level", "GeoFloodError", "MBC", "MEQN"]
+from .serve import Hydrograph, Scenario, Server  # noqa: E402
+
+__all__ = ["Phys", "Refine", "Context", "Level", "GeoFloodError", "MBC", "MEQN", "Hydrograph",
+           "Scenario", "Server"]

@@ -64,6 +64,44 @@ class gf_transfer(C.Structure):
                 ("ox", C.c_int), ("oy", C.c_int)]
 
 
+GF_SERVER_MAX_LANES = 4
+SCEN_QUEUED, SCEN_ACTIVE, SCEN_DONE, SCEN_FAILED, SCEN_CANCELLED = 0, 1, 2, 3, 4
+SCEN_STATE_NAMES = {0: "queued", 1: "active", 2: "done", 3: "failed", 4: "cancelled"}
+
+
+class gf_scenario(C.Structure):
+    _fields_ = [("mx", C.c_int), ("npx", C.c_int), ("npy", C.c_int), ("maux", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("xlower", C.c_double),
+                ("ylower", C.c_double), ("q", C.c_void_p), ("aux", C.c_void_p),
+                ("q_out", C.c_void_p), ("phys", gf_phys), ("mthbc", C.c_int * 4),
+                ("hydro_side", C.c_int * 4), ("nhydro", C.c_int), ("hydro_time", C.c_void_p),
+                ("hydro_hu", C.c_void_p), ("hydro_width", C.c_double), ("hydro_x0", C.c_double),
+                ("hydro_y0", C.c_double), ("t_final", C.c_double), ("nout", C.c_int),
+                ("initial_dt", C.c_double), ("desired_cfl", C.c_double),
+                ("max_cfl", C.c_double)]
+
+
+class gf_server_opts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("nlanes", C.c_int),
+                ("lane_cells", C.c_longlong * GF_SERVER_MAX_LANES), ("priority", C.c_int),
+                ("backfill", C.c_int)]
+
+
+class gf_scenario_info(C.Structure):
+    _fields_ = [("state", C.c_int), ("lane", C.c_int), ("steps", C.c_longlong),
+                ("rejects", C.c_longlong), ("cell_updates", C.c_longlong), ("t", C.c_double),
+                ("dt", C.c_double), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("max_cfl_seen", C.c_double),
+                ("device_bytes", C.c_size_t)]
+
+
+class gf_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("done", C.c_longlong),
+                ("rounds", C.c_longlong), ("launches", C.c_longlong),
+                ("cell_updates", C.c_longlong), ("bytes_in_use", C.c_size_t),
+                ("bytes_peak", C.c_size_t), ("active", C.c_int), ("queued", C.c_int)]
+
+
 XFER_AVG_FACE, XFER_AVG_CORNER, XFER_INTERP_FACE = 0, 1, 2
 XFER_INTERP_CORNER, XFER_INTERP2FINE, XFER_AVG2COARSE = 3, 4, 5
 
@@ -113,6 +151,20 @@ SIGNATURES = [
                                           C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_double,
                                           C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p]),
     ("gf_level_device_planes", C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
+    ("gf_server_opts_default", None, [C.POINTER(gf_server_opts)]),
+    ("gf_server_create", C.c_int, [C.c_int, C.POINTER(gf_server_opts), C.POINTER(_vp)]),
+    ("gf_server_destroy", None, [_vp]),
+    ("gf_server_last_error", C.c_char_p, [_vp]),
+    ("gf_scenario_footprint", C.c_size_t, [C.POINTER(gf_scenario)]),
+    ("gf_server_submit", C.c_int, [_vp, C.POINTER(gf_scenario), C.POINTER(C.c_longlong)]),
+    ("gf_server_pump", C.c_int, [_vp, C.POINTER(C.c_int)]),
+    ("gf_server_start", C.c_int, [_vp]),
+    ("gf_server_stop", C.c_int, [_vp]),
+    ("gf_server_wait", C.c_int, [_vp, C.c_longlong, C.c_double]),
+    ("gf_server_poll", C.c_int, [_vp, C.c_longlong, C.POINTER(gf_scenario_info)]),
+    ("gf_server_cancel", C.c_int, [_vp, C.c_longlong]),
+    ("gf_server_stats_get", C.c_int, [_vp, C.POINTER(gf_server_stats)]),
+    ("gf_server_clock", C.c_double, [_vp]),
 ]
 
 _lib = None

@@ -121,6 +121,7 @@ struct gf_level {
     bool layout_set = false;
     bool geom_dirty = true;
     gf_bc_spec bc{};
+    gf_ghost_block* d_ghost = nullptr; /* one block, rewritten per fill */
     std::vector<double> hy_time, hy_hu;
 };
 
@@ -341,7 +342,7 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
         if (!q[k] || !aux[k]) return fail(c, GF_ERR_ARG, "null patch pointer");
         std::memcpy(hq + (size_t)k * 3 * S, q[k], sizeof(double) * 3 * S);
         std::memcpy(ha + (size_t)k * maux * S, aux[k], sizeof(double) * maux * S);
-        gf_patch_work w;
+        gf_patch_work w{};
         w.q = c->q_soa.p + (size_t)k * 3 * S;
         w.aux = c->aux_soa.p + (size_t)k * maux * S;
         w.dx = dx[k];
@@ -405,6 +406,7 @@ int gf_level_create(gf_ctx* c, int npatch, int mx, int my, int maux, gf_level** 
     if (e == cudaSuccess) e = cudaMalloc(&L->d_nbr, (size_t)npatch * 8 * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&L->d_geom, (size_t)npatch * sizeof(gf_patch_geom));
     if (e == cudaSuccess) e = cudaMalloc(&L->d_phys_of, (size_t)npatch * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_ghost, sizeof(gf_ghost_block));
     if (e == cudaSuccess) e = cudaMemset(L->d_aux, 0, an * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(L->d_q, 0, qn * sizeof(double));
     if (e != cudaSuccess) {
@@ -429,6 +431,7 @@ void gf_level_destroy(gf_level* L)
     if (L->d_nbr) cudaFree(L->d_nbr);
     if (L->d_geom) cudaFree(L->d_geom);
     if (L->d_phys_of) cudaFree(L->d_phys_of);
+    if (L->d_ghost) cudaFree(L->d_ghost);
     delete L;
 }
 
@@ -527,10 +530,18 @@ int gf_level_ghost_fill_async(gf_level* L, double t)
         GF_CK(c, cudaStreamSynchronize(c->stream));
         L->geom_dirty = false;
     }
-    gf_bc_spec bc = L->bc;
-    bc.q0hu = hydro_interp(L, t);
-    GF_CK(c, gf::launch_ghost_fill(L->mx, L->d_q, L->d_aux, L->maux, L->npatch, L->d_nbr, L->d_geom,
-                                   bc, c->d_phys, L->d_phys_of, c->stream));
+    gf_ghost_block blk{};
+    blk.q = L->d_q;
+    blk.aux = L->d_aux;
+    blk.nbr = L->d_nbr;
+    blk.geom = L->d_geom;
+    blk.phys_of = L->d_phys_of;
+    blk.bc = L->bc;
+    blk.bc.q0hu = hydro_interp(L, t);
+    blk.maux = L->maux;
+    /* pageable source: the copy is staged before the call returns */
+    GF_CK(c, cudaMemcpyAsync(L->d_ghost, &blk, sizeof blk, cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_ghost_fill(L->mx, L->d_ghost, nullptr, L->npatch, c->d_phys, c->stream));
     return GF_OK;
 }
 
@@ -613,7 +624,7 @@ static int level_prepare(gf_level* L)
         if (rc) return rc;
     }
     if (!L->work_dirty) return GF_OK;
-    std::vector<gf_patch_work> w(L->npatch);
+    std::vector<gf_patch_work> w(L->npatch, gf_patch_work{});
     for (int k = 0; k < L->npatch; ++k) {
         w[k].q = L->d_q + (size_t)k * 3 * L->S;
         w[k].aux = L->d_aux + (size_t)k * L->maux * L->S;

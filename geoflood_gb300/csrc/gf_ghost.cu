@@ -70,17 +70,20 @@ __device__ bool inflow_state(const gf_phys& P, double q0hu, double h1, double hu
 }
 
 template <int M>
-__global__ void __launch_bounds__(128) ghost_fill_kernel(double* __restrict__ q,
-                                                         double* __restrict__ aux, int maux,
-                                                         int npatch, const int* __restrict__ nbr,
-                                                         const gf_patch_geom* __restrict__ geom,
-                                                         gf_bc_spec bc,
-                                                         const gf_phys* __restrict__ phys_table,
-                                                         const int* __restrict__ phys_of)
+__global__ void __launch_bounds__(128) ghost_fill_kernel(const gf_ghost_block* __restrict__ blocks,
+                                                         const gf_ghost_ref* __restrict__ list,
+                                                         int nlist,
+                                                         const gf_phys* __restrict__ phys_table)
 {
     constexpr int N = M + 4, S = N * N, MBC = 2;
-    const long p = blockIdx.x;
-    if (p >= npatch) return;
+    if ((int)blockIdx.x >= nlist) return;
+    /* list == nullptr: one block, patch = blockIdx.x */
+    const gf_ghost_ref ref = list ? list[blockIdx.x] : gf_ghost_ref{0, (int)blockIdx.x};
+    const gf_ghost_block& blk = blocks[ref.block];
+    const long p = ref.local;
+    double* __restrict__ q = blk.q;
+    const gf_bc_spec bc = blk.bc;
+    const int* __restrict__ nbr = blk.nbr;
     int nb[8];
 #pragma unroll
     for (int s = 0; s < 8; ++s) nb[s] = nbr[8 * p + s];
@@ -103,12 +106,12 @@ __global__ void __launch_bounds__(128) ghost_fill_kernel(double* __restrict__ q,
     if (!(phys_side[0] || phys_side[1] || phys_side[2] || phys_side[3])) return;
     __syncthreads();
 
-    const gf_phys P = phys_table[phys_of ? phys_of[p] : 0];
-    const gf_patch_geom G = geom[p];
+    const gf_phys P = phys_table[blk.phys_of ? blk.phys_of[p] : blk.phys];
+    const gf_patch_geom G = blk.geom[p];
     double* qh = plane(q, p, 0, S, 3);
     double* qu = plane(q, p, 1, S, 3);
     double* qv = plane(q, p, 2, S, 3);
-    double* b = plane(aux, p, 0, S, maux);
+    double* b = plane(blk.aux, p, 0, S, blk.maux);
     auto at = [](int i, int j) { return (j + 1) * N + (i + 1); };
 
     /* ---- step 2a: x sides (left then right are disjoint), all rows ---- */
@@ -186,15 +189,14 @@ __global__ void __launch_bounds__(128) ghost_fill_kernel(double* __restrict__ q,
 
 } // namespace
 
-cudaError_t launch_ghost_fill(int m, double* q, double* aux, int maux, int npatch, const int* nbr,
-                              const gf_patch_geom* geom, const gf_bc_spec& bc,
-                              const gf_phys* phys, const int* phys_of, cudaStream_t st)
+cudaError_t launch_ghost_fill(int m, const gf_ghost_block* blocks, const gf_ghost_ref* list,
+                              int nlist, const gf_phys* phys, cudaStream_t st)
 {
-    if (npatch <= 0) return cudaSuccess;
+    if (nlist <= 0) return cudaSuccess;
     switch (m) {
-    case 32: ghost_fill_kernel<32><<<npatch, 128, 0, st>>>(q, aux, maux, npatch, nbr, geom, bc, phys, phys_of); break;
-    case 16: ghost_fill_kernel<16><<<npatch, 128, 0, st>>>(q, aux, maux, npatch, nbr, geom, bc, phys, phys_of); break;
-    case 8: ghost_fill_kernel<8><<<npatch, 128, 0, st>>>(q, aux, maux, npatch, nbr, geom, bc, phys, phys_of); break;
+    case 32: ghost_fill_kernel<32><<<nlist, 128, 0, st>>>(blocks, list, nlist, phys); break;
+    case 16: ghost_fill_kernel<16><<<nlist, 128, 0, st>>>(blocks, list, nlist, phys); break;
+    case 8: ghost_fill_kernel<8><<<nlist, 128, 0, st>>>(blocks, list, nlist, phys); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -23,9 +23,10 @@ cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int n
 cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int ncell, int nf,
                               long src_stride, long dst_stride, cudaStream_t st);
 
-cudaError_t launch_ghost_fill(int m, double* q, double* aux, int maux, int npatch, const int* nbr,
-                              const gf_patch_geom* geom, const gf_bc_spec& bc,
-                              const gf_phys* phys, const int* phys_of, cudaStream_t st);
+/* list (nullable: one block, nlist patches in order) names the patches to
+ * fill as (block, local) pairs. */
+cudaError_t launch_ghost_fill(int m, const gf_ghost_block* blocks, const gf_ghost_ref* list,
+                              int nlist, const gf_phys* phys, cudaStream_t st);
 
 cudaError_t launch_transfer(int m, const gf_xfer_task* tasks, int ntask, const gf_phys* phys,
                             cudaStream_t st);

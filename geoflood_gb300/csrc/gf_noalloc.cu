@@ -100,7 +100,7 @@ extern "C" int gf_patch_update_noalloc(int device, const gf_phys* phys, int npat
     double* d_q = reinterpret_cast<double*>(base + kOffQ);
     double* d_aux = reinterpret_cast<double*>(base + kOffAux);
 
-    gf_patch_work work[kMaxPatches];
+    gf_patch_work work[kMaxPatches] = {};
     for (int k = 0; k < npatch; ++k) {
         work[k].q = d_q + (size_t)k * 3 * S;
         work[k].aux = d_aux + (size_t)k * maux * S;

@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(NT, MINB)
     }
 
     /* ---- flux-difference update, src2, write interior ---- */
-    double* gq = wk.q;
+    double* gq = wk.qout ? wk.qout : wk.q;
     const double* gaux = wk.aux;
     const int fidx = P.friction_index - 1;
     for (int e = threadIdx.x; e < M * M; e += NT) {

@@ -20,6 +20,7 @@
 /* One unit of work for the patch-update kernel: a patch of any forest. */
 typedef struct gf_patch_work {
     double* q;          /* device: 3 planes of (mx+4)*(my+4) doubles   */
+    double* qout;       /* interior cells of the result; null = q      */
     const double* aux;  /* device: maux planes of (mx+4)*(my+4) doubles */
     double dx, dy;
     int phys;           /* index into the gf_phys table                */
@@ -39,6 +40,25 @@ typedef struct gf_bc_spec {
     double width, x0, y0;
     double q0hu;
 } gf_bc_spec;
+
+/* Ghost fill of one block of same-level patches sharing a layout (a level
+ * of one forest, or one served scenario). nbr holds 8 entries per patch
+ * (left, right, bottom, top, ll, lr, ul, ur) as block-local indices, -1 for
+ * a physical side and -2 for a side filled by another route (coarse/fine). */
+typedef struct gf_ghost_block {
+    double* q;                  /* block's q, patch p at q + 3*S*p             */
+    double* aux;                /* block's aux, patch p at aux + maux*S*p      */
+    const int* nbr;
+    const gf_patch_geom* geom;
+    const int* phys_of;         /* per-patch physics slot, or null = phys      */
+    gf_bc_spec bc;
+    int phys, maux;
+} gf_ghost_block;
+
+/* A patch of a ghost-fill list: (block, block-local patch index). */
+typedef struct gf_ghost_ref {
+    int block, local;
+} gf_ghost_ref;
 
 /* One coarse/fine transfer (gf_amr.cu): kind GF_XFER_*, code = coarse
  * face / corner or child index, (ox, oy) = fine index of the coarse patch's

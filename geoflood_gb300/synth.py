@@ -199,3 +199,95 @@ def brick_layout(py: int, px: int, m: int, dx: float, dy: float | None = None,
             yl[k] = y0 + j * m * dy
     nbr[nbr == np.arange(n)[:, None]] = -1  # a 1-wide periodic grid has no true neighbour
     return nbr, xl, yl
+
+
+_LATTICE_CACHE: dict = {}
+
+
+def _lattice_window(nx: int, ny: int, hurst: float, seed: int, pool: int = 2) -> np.ndarray:
+    """(ny, nx) window of one of `pool` cached diamond-square lattices, picked
+    and offset by `seed`; large scenarios share lattices instead of growing
+    a new 4097^2 surface each."""
+    n = max(nx, ny)
+    lv = max(int(np.ceil(np.log2(max(n, 2)))), 8)
+    if lv >= 11:
+        key = (12, hurst, seed % pool)
+        lv = 12
+    else:
+        key = (lv, hurst, seed)
+    lat = _LATTICE_CACHE.get(key)
+    if lat is None:
+        lat = diamond_square(key[0], hurst, 7919 * key[2] + 17)
+        cell = 0.25 * (lat[:-1, :-1] + lat[1:, :-1] + lat[:-1, 1:] + lat[1:, 1:])
+        lat = cell
+        if len(_LATTICE_CACHE) > 8:
+            _LATTICE_CACHE.clear()
+        _LATTICE_CACHE[key] = lat
+    g = rng(seed + 1)
+    oy = int(g.integers(0, lat.shape[0] - ny + 1))
+    ox = int(g.integers(0, lat.shape[1] - nx + 1))
+    return lat[oy:oy + ny, ox:ox + nx]
+
+
+def flood_scenario_params(seed: int, cells: float, mx: int | None = None, dx: float = 5.0,
+                          time_scale: float = 1.0 / 150.0) -> dict:
+    """The scalar draws of flood_scenario (sizes, channel, hydrograph,
+    friction, horizon) without building any arrays."""
+    g = rng(seed)
+    if mx is None:
+        mx = int(g.choice([8, 16, 32]))
+    npt = max(1, int(round(cells / (mx * mx))))
+    npy = max(1, int(round(np.sqrt(npt / 2.0))))
+    npx = max(1, int(round(npt / npy)))
+    ly = npy * mx * dx
+    width = float(max(g.uniform(30.0, 80.0), 3 * dx))
+    width = min(width, 0.5 * ly)
+    amp = 0.15 * ly * float(g.uniform(0.3, 1.0))
+    peak = float(g.uniform(10.0, 500.0))
+    t_rise = float(g.uniform(0.5, 2.0)) * 3600.0 * time_scale
+    horizon = float(g.uniform(1.0, 6.0)) * 3600.0 * time_scale
+    n = float(g.uniform(0.02, 0.08))
+    return dict(mx=mx, npx=npx, npy=npy, dx=dx, width=width, amp=amp, peak=peak, t_rise=t_rise,
+                horizon=horizon, manning=n)
+
+
+def flood_scenario(seed: int, cells: float, mx: int | None = None, dx: float = 5.0,
+                   time_scale: float = 1.0 / 150.0, relief: float = 10.0):
+    """One served flood scenario: a river valley on a fractal DEM fed by an
+    inflow hydrograph on the left side (mthbc 0 there, extrapolation on the
+    right, walls top and bottom).
+
+    - mx drawn from {8, 16, 32} unless given; npx x npy patches (about 2:1)
+      with about `cells` interior cells at `dx` metres.
+    - DEM: fractal surface (Hurst 0.8, `relief` m) on a 0.002 down-valley
+      slope, with a meandering channel 3 m deep and U[30, 80] m wide.
+    - Water: 2 m in the channel at t = 0, dry elsewhere.
+    - Hydrograph: discharge rising from 10 % of a peak Q ~ U[10, 500] m^3/s
+      to the peak at t_rise ~ U[0.5, 2] h and back by 3 t_rise, per unit
+      channel width; Manning n ~ U[0.02, 0.08]; horizon U[1, 6] h.
+    - All times (rise, horizon) are multiplied by `time_scale`.
+    """
+    from . import Phys
+    from .serve import Hydrograph, Scenario
+    p = flood_scenario_params(seed, cells, mx, dx, time_scale)
+    mx, npx, npy, width = p["mx"], p["npx"], p["npy"], p["width"]
+    nx, ny = npx * mx, npy * mx
+    lx, ly = nx * dx, ny * dx
+    x = (np.arange(nx) + 0.5) * dx
+    y = (np.arange(ny) + 0.5) * dx
+    surf = _lattice_window(nx, ny, 0.8, seed)
+    surf = (surf - surf.min()) / max(surf.max() - surf.min(), 1e-300) * relief
+    yc = 0.5 * ly + p["amp"] * np.sin(2.0 * np.pi * x / max(lx, 1.0))
+    inside = np.abs(y[:, None] - yc[None, :]) <= 0.5 * width
+    b = surf + 0.002 * (lx - x)[None, :] - 3.0 * inside
+    q = np.zeros((ny, nx, 3))
+    q[..., 0] = np.where(inside, 2.0, 0.0)
+    peak, t_rise = p["peak"], p["t_rise"]
+    hy = Hydrograph(time=np.array([0.0, t_rise, 3.0 * t_rise]),
+                    hu=np.array([0.1 * peak, peak, 0.1 * peak]) / width,
+                    side=(1, 0, 0, 0), width=width, x0=0.0, y0=0.5 * ly)
+    qt = np.ascontiguousarray(tile_level(pad_extrap(q), mx))
+    at = np.ascontiguousarray(tile_level(pad_extrap(b[..., None]), mx))
+    return Scenario(mx=mx, npx=npx, npy=npy, dx=dx, dy=dx, q=qt, aux=at, t_final=p["horizon"],
+                    phys=Phys(manning_coefficient=(p["manning"],), manning_break=(1.0e10,)),
+                    mthbc=(0, 1, 3, 3), hydro=hy, nout=4, initial_dt=0.2, seed=seed)

@@ -299,6 +299,104 @@ int gf_patch_update_noalloc(int device, const gf_phys* phys, int npatch,
                             double* q, const double* aux, double* cfl,
                             double* maxcfl, void* stream);
 
+/* ------------------------------------------------- served scenarios */
+/* A request loop over flood scenarios (continuous batching). Each admitted
+ * scenario keeps its state resident on the device; every batching round
+ * steps all active scenarios of a size lane with shared launches (one ghost
+ * fill and one patch update per mx present), each scenario with its own dt
+ * and CFL slot. Time stepping per scenario follows ForestClaw's outstyle 1
+ * loop (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395): dt clipped to hit each
+ * output time with the 1% tolerance, a step whose CFL exceeds max_cfl is
+ * retaken with dt * desired_cfl / cfl, otherwise the next dt is
+ * dt * desired_cfl / cfl. A rejected step costs no copy: the update writes
+ * into the second of two state buffers and the scenario's current buffer
+ * only flips on acceptance. Replaces the per-rank driver loop for many
+ * independent runs; the single level per scenario is a one-level forest.
+ *
+ * The caller keeps q, aux and q_out alive until the scenario is DONE,
+ * FAILED or CANCELLED (pinned memory keeps the copies asynchronous). */
+typedef struct gf_server gf_server;
+
+enum gf_scenario_state {
+    GF_SCEN_QUEUED = 0,
+    GF_SCEN_ACTIVE = 1,
+    GF_SCEN_DONE = 2,
+    GF_SCEN_FAILED = 3,
+    GF_SCEN_CANCELLED = 4
+};
+
+#define GF_SERVER_MAX_LANES 4
+
+typedef struct gf_scenario {
+    int mx;                /* 8, 16 or 32 (my = mx)                              */
+    int npx, npy;          /* patch grid of the level, patch index = py*npx + px */
+    int maux;              /* aux fields, bathymetry first (1..3)                */
+    double dx, dy;         /* cell size                                          */
+    double xlower, ylower; /* lower-left corner of the domain                    */
+    const double* q;       /* host, Fortran layout per patch: q(3, mx+4, mx+4)   */
+    const double* aux;     /* host, aux(maux, mx+4, mx+4) per patch, ghosts set  */
+    double* q_out;         /* host, final state in the layout of q (nullable)    */
+    gf_phys phys;
+    int mthbc[4];          /* left, right, bottom, top: 0 inflow, 1 extrap, 3 wall */
+    int hydro_side[4];     /* sides fed by the hydrograph (rule 0)               */
+    int nhydro;            /* hydrograph samples (0 = none)                      */
+    const double* hydro_time;
+    const double* hydro_hu; /* discharge per unit width at hydro_time            */
+    double hydro_width, hydro_x0, hydro_y0;
+    double t_final;        /* simulated horizon                                  */
+    int nout;              /* output intervals (dt lands on each output time)    */
+    double initial_dt, desired_cfl, max_cfl;
+} gf_scenario;
+
+typedef struct gf_server_opts {
+    size_t hbm_budget;      /* device bytes all admitted scenarios may hold      */
+    int max_active;         /* scenarios admitted at once (<= 1024)              */
+    int nlanes;             /* size lanes, each with its own stream (1..4)       */
+    long long lane_cells[GF_SERVER_MAX_LANES]; /* lane k: cells < lane_cells[k]; last lane takes the rest */
+    int priority;           /* 1: smaller lanes on higher-priority streams       */
+    int backfill;           /* 1: admit later arrivals that fit while the head waits */
+} gf_server_opts;
+
+typedef struct gf_scenario_info {
+    int state;              /* gf_scenario_state                                 */
+    int lane;
+    long long steps, rejects, cell_updates; /* accepted steps; interior cells x steps */
+    double t;               /* simulated time reached                            */
+    double dt;              /* current dt of the controller                      */
+    double t_submit, t_admit, t_done; /* seconds on the server clock (-1: not yet) */
+    double max_cfl_seen;
+    size_t device_bytes;
+} gf_scenario_info;
+
+typedef struct gf_server_stats {
+    long long submitted, admitted, done, rounds, launches;
+    long long cell_updates;  /* accepted steps over all scenarios               */
+    size_t bytes_in_use, bytes_peak;
+    int active, queued;
+} gf_server_stats;
+
+void gf_server_opts_default(gf_server_opts* o);
+int gf_server_create(int device, const gf_server_opts* opts, gf_server** out);
+void gf_server_destroy(gf_server* s);
+const char* gf_server_last_error(const gf_server* s);
+/* Device bytes a scenario holds while admitted (0 for an invalid one). */
+size_t gf_scenario_footprint(const gf_scenario* sc);
+/* Queue a scenario (validated here; GF_ERR_NOMEM if it can never fit). */
+int gf_server_submit(gf_server* s, const gf_scenario* sc, long long* id);
+/* One non-blocking pass of the request loop: finish completed rounds, admit,
+ * launch the next rounds. *busy = 1 while any work is queued or in flight. */
+int gf_server_pump(gf_server* s, int* busy);
+/* Run the request loop on a background thread / stop it. */
+int gf_server_start(gf_server* s);
+int gf_server_stop(gf_server* s);
+/* Pump (or, with the loop thread running, sleep) until the scenario ends or
+ * timeout_s passes (GF_ERR_STATE on timeout). */
+int gf_server_wait(gf_server* s, long long id, double timeout_s);
+int gf_server_poll(gf_server* s, long long id, gf_scenario_info* info);
+int gf_server_cancel(gf_server* s, long long id);
+int gf_server_stats_get(gf_server* s, gf_server_stats* st);
+double gf_server_clock(const gf_server* s);
+
 /* ----------------------------------------------------------- probes */
 /* Measured FP64 pipe rates of `device` in operations per second:
  * rates[0] double fma, [1] double division, [2] double sqrt, [3] float fma.

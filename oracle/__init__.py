@@ -327,3 +327,65 @@ def tag4coarsening(qs, auxs, xlowers, ylowers, dx, dy, t, level, maxlevel, init_
     yl = np.ascontiguousarray(ylowers, dtype=np.float64)
     return load().orc_tag4coarsening(C.byref(p), C.byref(rf), MBC, m, m, auxs[0].shape[-1], qp, ap,
                                      _ptr(xl), _ptr(yl), dx, dy, t, level, maxlevel, init_flag)
+
+
+def brick_neighbours(npx: int, npy: int, mx: int, dx: float, dy: float, x0: float = 0.0,
+                     y0: float = 0.0):
+    """Neighbour table (left, right, bottom, top, ll, lr, ul, ur; -1 physical)
+    and patch origins of an npx x npy brick, patch = py*npx + px."""
+    n = npx * npy
+    nbr = -np.ones((n, 8), np.int32)
+    xl, yl = np.zeros(n), np.zeros(n)
+
+    def at(px, py):
+        return py * npx + px if 0 <= px < npx and 0 <= py < npy else -1
+
+    for py in range(npy):
+        for px in range(npx):
+            k = py * npx + px
+            nbr[k] = [at(px - 1, py), at(px + 1, py), at(px, py - 1), at(px, py + 1),
+                      at(px - 1, py - 1), at(px + 1, py - 1), at(px - 1, py + 1),
+                      at(px + 1, py + 1)]
+            xl[k], yl[k] = x0 + px * mx * dx, y0 + py * mx * dy
+    return nbr, xl, yl
+
+
+def run_scenario(q, aux, mx, npx, npy, dx, dy, t_final, nout, initial_dt, desired_cfl,
+                 max_cfl, mthbc, phys=None, hy=None, xlower=0.0, ylower=0.0, nthreads=0):
+    """Single-level run with ForestClaw's outstyle-1 time stepping
+    (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395, variable dt, reduce_cfl on):
+    per step, ghost fill at the step's start time, level update, CFL test.
+
+    q (npatch, mx+4, mx+4, 3) is advanced in place; returns
+    (accepted steps, rejected steps, list of accepted dt)."""
+    nbr, xl, yl = brick_neighbours(npx, npy, mx, dx, dy, xlower, ylower)
+    dt_outer = t_final / nout
+    t_curr = 0.0
+    dt_minlevel = initial_dt
+    steps, rejects, dts = 0, 0, []
+    for _ in range(nout):
+        tend = t_curr + dt_outer
+        while t_curr < tend:
+            dt_step = dt_minlevel
+            tol = 1e-2 * dt_step
+            took_small = False
+            small_step = tend - (t_curr + dt_step)
+            if small_step < tol:
+                dt_step = tend - t_curr
+                if small_step < 0:
+                    took_small = True
+            save = q.copy()
+            level_ghost_fill(q, aux, nbr, xl, yl, dx, dy, t_curr, mthbc, phys, hy)
+            cfl = level_update(q, aux, dx, dy, t_curr, dt_step, phys, nthreads)
+            if cfl > max_cfl:
+                q[...] = save
+                dt_minlevel = dt_minlevel * desired_cfl / cfl
+                rejects += 1
+                continue
+            steps += 1
+            t_curr += dt_step
+            dts.append(dt_step)
+            dt_new = dt_minlevel * desired_cfl / cfl if cfl > 0.0 else float("inf")
+            if not took_small:
+                dt_minlevel = dt_new
+    return steps, rejects, dts
