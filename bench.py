@@ -182,8 +182,7 @@ def served_stream(args):
     fractal valley DEM with a channel, hydrograph peak 10-500 m^3/s rising
     over 0.5-2 h, n ~ U[0.02, 0.08], horizon 1-6 h; times scaled by
     --served-time-scale) through the continuous-batching server at 80 % of
-    the capacity measured in a calibration pass over the first scenarios."""
-    import queue
+    the capacity measured in a saturated calibration pass."""
     import threading
 
     import geoflood_gb300 as gf
@@ -191,96 +190,138 @@ def served_stream(args):
 
     n = args.served_scenarios
     ts = args.served_time_scale
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
     g = np.random.default_rng(SERVED_SEED)
     cells = np.exp(g.uniform(np.log(1e4), np.log(4e6), n))
     seeds = [SERVED_SEED + 1 + k for k in range(n)]
+    params = [synth.flood_scenario_params(seeds[k], float(cells[k]), time_scale=ts)
+              for k in range(n)]
 
     def make(k):
-        sc = synth.flood_scenario(seeds[k], float(cells[k]), time_scale=ts)
-        q = _pinned(sc.q.shape)
-        q[...] = sc.q
-        a = _pinned(sc.aux.shape)
-        a[...] = sc.aux
-        sc.q, sc.aux = q, a
+        sc = synth.flood_scenario(seeds[k], float(cells[k]), time_scale=ts, alloc=_pinned)
         return sc, _pinned(sc.q.shape)
 
-    def producer(order, out_q, stop):
-        for k in order:
-            if stop.is_set():
-                return
-            out_q.put((k,) + make(k))
-        out_q.put(None)
+    # warm the shared DEM lattices so generation keeps ahead of arrivals
+    synth.flood_scenario(1, 3e6, mx=32, time_scale=ts)
+    synth.flood_scenario(2, 3e6, mx=32, time_scale=ts)
 
-    def run_batch(srv, order, arrivals=None, keep=()):
-        """Submit `order` (at `arrivals` on the server clock, else at once)."""
-        stop = threading.Event()
-        q_in = queue.Queue(maxsize=24)
-        th = threading.Thread(target=producer, args=(order, q_in, stop), daemon=True)
-        th.start()
-        ids, late, outs, meta = {}, 0, {}, {}
-        t_base = srv.clock()
-        i = 0
-        while True:
-            item = q_in.get()
-            if item is None:
-                break
-            k, sc, qo = item
-            if arrivals is not None:
-                t_arr = t_base + arrivals[i]
-                while srv.clock() < t_arr:
-                    time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
-                if srv.clock() - t_arr > 0.01:
-                    late += 1
-            ids[k] = srv.submit(sc, qo)
-            meta[k] = (sc.cells, sc.mx, sc.t_final)
-            if k in keep:
-                outs[k] = qo
-            i += 1
-        th.join()
-        infos = {}
-        for k, sid in ids.items():
-            infos[k] = srv.wait(sid, timeout=3600)
-            if k not in keep:
-                srv.release(sid)
-        return infos, outs, late, meta
-
-    srv = gf.Server(device=int(os.environ.get("LOCAL_RANK", "0")))
+    srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms)
     srv.start()
-    # calibration: the first scenarios submitted at once (closed loop)
+
+    # -- calibration: a saturated batch, throughput while most are in flight
     ncal = min(32, n)
+    cal_items = [make(k) for k in range(ncal)]
+    st_a = srv.stats()
     t0 = srv.clock()
-    cal, _, _, cal_meta = run_batch(srv, list(range(ncal)))
-    t_cal = max(i["t_done"] for i in cal.values()) - t0
-    cap = sum(i["cell_updates"] for i in cal.values()) / t_cal
-    steps_per_sim_s = sum(i["steps"] for i in cal.values()) / sum(m[2] for m in cal_meta.values())
-    # expected work of the stream from its sizes and horizons
-    horizon = [synth.flood_scenario_params(seeds[k], float(cells[k]), time_scale=ts)["horizon"]
-               for k in range(n)]
-    est_work = float(np.mean(cells * np.array(horizon) * steps_per_sim_s))
+    cal_ids = [srv.submit(sc, qo) for sc, qo in cal_items]
+    samples = []
+    while True:
+        st = srv.stats()
+        samples.append((srv.clock(), st["cell_updates"] - st_a["cell_updates"],
+                        st["active"] + st["queued"]))
+        if st["active"] + st["queued"] == 0:
+            break
+        time.sleep(0.002)
+    half = next((t, w) for t, w, left in samples if left <= ncal // 2)
+    cap = half[1] / (half[0] - t0)
+    cal_info = [srv.wait(i, timeout=600) for i in cal_ids]
+    for i in cal_ids:
+        srv.release(i)
+    del cal_items
+    steps_per_sim_s = sum(i["steps"] for i in cal_info) / sum(p["horizon"] for p in params[:ncal])
+    est_work = float(np.mean([cells[k] * params[k]["horizon"] * steps_per_sim_s for k in range(n)]))
     rate = 0.8 * cap / est_work
     gaps = np.random.default_rng(SERVED_SEED + 7).exponential(1.0 / rate, n)
     arrivals = np.cumsum(gaps) - gaps[0]
     order = np.argsort(cells)
     sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 12)})
+
+    # -- the stream: producer threads keep generated scenarios ahead of the
+    #    arrivals (numpy releases the GIL in the array work)
+    ready, cond, nxt, taken = {}, threading.Condition(), [0], [0]
+    ahead = 48
+
+    def producer():
+        while True:
+            with cond:
+                while nxt[0] < n and nxt[0] >= taken[0] + ahead:
+                    cond.wait()
+                if nxt[0] >= n:
+                    return
+                k = nxt[0]
+                nxt[0] += 1
+            item = make(k)
+            with cond:
+                ready[k] = item
+                cond.notify_all()
+
+    def take(k):
+        with cond:
+            while k not in ready:
+                cond.wait()
+            taken[0] = k + 1
+            cond.notify_all()
+            return ready.pop(k)
+
+    workers = [threading.Thread(target=producer, daemon=True)
+               for _ in range(max(2, min(8, (os.cpu_count() or 4) // 2)))]
+    for w in workers:
+        w.start()
+    with cond:
+        while len(ready) < min(ahead, n) and any(w.is_alive() for w in workers):
+            cond.wait(0.05)
     st0 = srv.stats()
     t_start = srv.clock()
-    infos, outs, late, meta = run_batch(srv, list(range(n)), arrivals, keep=set(sample))
+    ids, pending, infos, outs, late, mx_of = {}, [], {}, {}, 0, {}
+
+    def sweep(block=False):
+        for k in list(pending):
+            info = srv.wait(ids[k], timeout=3600) if block else srv.poll(ids[k])
+            if info["state"] in ("done", "failed", "cancelled"):
+                infos[k] = info
+                pending.remove(k)
+                if k not in sample:
+                    srv.release(ids[k])
+
+    for i in range(n):
+        k = i
+        sc, qo = take(k)
+        t_arr = t_start + arrivals[i]
+        while srv.clock() < t_arr:
+            time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
+        if srv.clock() - t_arr > 0.01:
+            late += 1
+        ids[k] = srv.submit(sc, qo)
+        mx_of[k] = sc.mx
+        pending.append(k)
+        if k in sample:
+            outs[k] = qo
+        del sc, qo
+        sweep()
+    for w in workers:
+        w.join()
+    sweep(block=True)
     t_end = max(i["t_done"] for i in infos.values())
     st1 = srv.stats()
+    failed = sum(1 for i in infos.values() if i["state"] != "done")
     lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
     work = sum(i["cell_updates"] for i in infos.values())
     served_rate = work / (t_end - t_start)
-    # isolated re-runs of a size-stratified sample: latency alone, same bits
+
+    # -- isolated re-runs of a size-stratified sample: latency alone, same bits
     slow, same = [], True
     for k in sample:
-        iso, iso_out, _, _ = run_batch(srv, [k], keep={k})
-        ik = iso[k]
+        sc, qo = make(k)
+        sid = srv.submit(sc, qo)
+        ik = srv.wait(sid, timeout=600)
         slow.append((infos[k]["t_done"] - infos[k]["t_submit"]) / (ik["t_done"] - ik["t_submit"]))
-        same &= bool(np.array_equal(iso_out[k], outs[k])) and ik["steps"] == infos[k]["steps"]
+        same &= bool(np.array_equal(qo, outs[k])) and ik["steps"] == infos[k]["steps"]
+        srv.release(sid)
     srv.stop()
     srv.close()
-    # the plain per-patch drop-in on the same work mix
-    ctx = gf.Context(int(os.environ.get("LOCAL_RANK", "0")))
+
+    # -- the plain per-patch drop-in on the same work mix
+    ctx = gf.Context(dev)
     rate_mx = {}
     for mx in (8, 16, 32):
         sc = synth.flood_scenario(SERVED_SEED, 200000, mx=mx, time_scale=ts)
@@ -295,10 +336,10 @@ def served_stream(args):
             ctx.patch_update(qs[k], aus[k], sc.dx, sc.dy, 0.0, 0.2)
         rate_mx[mx] = npt * mx * mx / (time.perf_counter() - tp)
     ctx.close()
-    plain_time = sum(i["cell_updates"] / rate_mx[meta[k][1]] for k, i in infos.items())
+    plain_time = sum(i["cell_updates"] / rate_mx[mx_of[k]] for k, i in infos.items())
     plain_rate = work / plain_time
     return {
-        "value": served_rate, "unit": METRIC, "scenarios": n,
+        "value": served_rate, "unit": METRIC, "scenarios": n, "failed": failed,
         "p50_latency_s": float(np.percentile(lat, 50)),
         "p99_latency_s": float(np.percentile(lat, 99)),
         "slowdown_vs_isolated": {"p50": float(np.percentile(slow, 50)),
@@ -310,7 +351,9 @@ def served_stream(args):
                             "note": "gf_patch_update per patch with host buffers, weighted by "
                                     "the stream's work per mx"},
         "vs_plain_per_patch": served_rate / plain_rate,
-        "calibration": {"scenarios": ncal, "capacity": cap, "seconds": t_cal},
+        "capacity": {"value": cap, "unit": METRIC, "scenarios": ncal,
+                     "window_s": half[0] - t0,
+                     "note": "saturated batch, until half of it has finished"},
         "arrival_rate_per_s": rate, "offered_load": 0.8, "late_submissions": late,
         "stream_seconds": t_end - t_start, "cell_updates": work,
         "launches": st1["launches"] - st0["launches"], "rounds": st1["rounds"] - st0["rounds"],
@@ -527,6 +570,7 @@ def main():
     ap.add_argument("--served-only", action="store_true")
     ap.add_argument("--served-scenarios", type=int, default=512)
     ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
+    ap.add_argument("--served-reserve-sms", type=int, default=None)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

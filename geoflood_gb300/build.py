@@ -20,7 +20,9 @@ BUILD = PKG / "_build"
 LIB = PKG / "libgeoflood_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
+# host code: no FMA contraction (gcc contracts by default on aarch64), so
+# the host-side hydrograph and controller arithmetic matches the oracle bits
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
           f"-I{ROOT / 'include'}", f"-I{CSRC}", "-diag-suppress", "550"]
 
 
@@ -38,8 +40,10 @@ def sources() -> list[Path]:
 # Per-file flags: the parity build of the patch kernel runs without
 # floating-point contraction.
 PER_FILE = {"gf_kernels_exact.cu": ["-fmad=false"],
-            # refinement tags must match the oracle bit for bit: no contraction
-            "gf_amr.cu": ["-fmad=false"]}
+            # refinement tags, transfers and the served time-step controller
+            # must match the oracle bit for bit: no contraction
+            "gf_amr.cu": ["-fmad=false"],
+            "gf_served.cu": ["-fmad=false"]}
 
 
 def _compile(src: Path, extra: list[str]) -> Path:

@@ -161,7 +161,7 @@ int enqueue_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int 
         GF_CK(c, gf::launch_patch_update_exact(m, d_work, nwork, c->d_phys, dt, nullptr, maux,
                                                d_cfl, &d_status->gmax, &d_status->err, c->stream));
     else
-        GF_CK(c, gf::launch_patch_update(m, d_work, nwork, c->d_phys, dt, nullptr, maux, d_cfl,
+        GF_CK(c, gf::launch_patch_update(m, d_work, nwork, c->d_phys, dt, nullptr, nullptr, maux, d_cfl,
                                          &d_status->gmax, &d_status->err, c->stream));
     return GF_OK;
 }

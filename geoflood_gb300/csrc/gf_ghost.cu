@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(128) ghost_fill_kernel(const gf_ghost_block* _
     /* list == nullptr: one block, patch = blockIdx.x */
     const gf_ghost_ref ref = list ? list[blockIdx.x] : gf_ghost_ref{0, (int)blockIdx.x};
     const gf_ghost_block& blk = blocks[ref.block];
+    if (blk.skip) return;
     const long p = ref.local;
     double* __restrict__ q = blk.q;
     const gf_bc_spec bc = blk.bc;

@@ -9,10 +9,16 @@
 
 namespace gf {
 
+/* gdt / gpar (nullable): per-group dt (<= 0 skips the group) and state
+ * parity (1: the group's state is in the work items' qout buffers). */
+/* max_ctas > 0 caps the grid: each CTA then walks the work list with a
+ * grid stride, leaving the other SMs to concurrent launches. */
 cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, const gf_phys* phys,
-                                double dt, const double* gdt, int maux, double* cfl,
-                                unsigned long long* gmax, int* err, cudaStream_t st);
+                                double dt, const double* gdt, const int* gpar, int maux, double* cfl,
+                                unsigned long long* gmax, int* err, cudaStream_t st,
+                                int max_ctas = 0);
 size_t patch_update_smem_bytes(int m);
+int patch_update_occupancy(int m); /* resident CTAs per SM */
 cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwork,
                                       const gf_phys* phys, double dt, const double* gdt, int maux,
                                       double* cfl, unsigned long long* gmax, int* err,
@@ -22,6 +28,14 @@ cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int n
                               long src_stride, long dst_stride, cudaStream_t st);
 cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int ncell, int nf,
                               long src_stride, long dst_stride, cudaStream_t st);
+
+/* Served scenarios: device-side time-step control around a round. */
+cudaError_t launch_served_prepare(gf_group_state* gs, gf_ghost_block* blocks, double* gdt, int* gpar,
+                                  unsigned long long* gmax, const double* hy_t,
+                                  const double* hy_hu, int ng, cudaStream_t st);
+cudaError_t launch_served_finish(gf_group_state* gs, const double* gdt,
+                                 const unsigned long long* gmax, const int* err, int ng,
+                                 cudaStream_t st);
 
 /* list (nullable: one block, nlist patches in order) names the patches to
  * fill as (block, local) pairs. */

@@ -17,8 +17,8 @@ namespace gf {
 
 template <int M, int NT, int RB, int MINB>
 static cudaError_t launch_update(const gf_patch_work* work, int nwork, const gf_phys* phys,
-                                 double dt, const double* gdt, int maux, double* cfl,
-                                 unsigned long long* gmax, int* err, cudaStream_t st)
+                                 double dt, const double* gdt, const int* gpar, int maux, double* cfl,
+                                 unsigned long long* gmax, int* err, int max_ctas, cudaStream_t st)
 {
     using L = Smem<M, RB, false>;
     auto kern = patch_update_kernel<M, NT, RB, MINB, false>;
@@ -30,19 +30,43 @@ static cudaError_t launch_update(const gf_patch_work* work, int nwork, const gf_
         attr_set = true;
     }
     if (nwork <= 0) return cudaSuccess;
-    kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err);
+    const int grid = (max_ctas > 0 && max_ctas < nwork) ? max_ctas : nwork;
+    kern<<<grid, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, const gf_phys* phys,
-                                double dt, const double* gdt, int maux, double* cfl,
-                                unsigned long long* gmax, int* err, cudaStream_t st)
+                                double dt, const double* gdt, const int* gpar, int maux, double* cfl,
+                                unsigned long long* gmax, int* err, cudaStream_t st, int max_ctas)
 {
     switch (m) {
-    case 32: return launch_update<32, 256, 7, 1>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
-    case 16: return launch_update<16, 128, 6, 1>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
-    case 8: return launch_update<8, 64, 5, 1>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
+    case 32: return launch_update<32, 256, 7, 1>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
+    case 16: return launch_update<16, 128, 6, 1>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
+    case 8: return launch_update<8, 64, 5, 1>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
     default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int M, int NT, int RB>
+static int occupancy_of()
+{
+    using L = Smem<M, RB, false>;
+    auto kern = patch_update_kernel<M, NT, RB, 1, false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES) !=
+        cudaSuccess)
+        return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, NT, L::BYTES) != cudaSuccess) return 0;
+    return n;
+}
+
+int patch_update_occupancy(int m)
+{
+    switch (m) {
+    case 32: return occupancy_of<32, 256, 7>();
+    case 16: return occupancy_of<16, 128, 6>();
+    case 8: return occupancy_of<8, 64, 5>();
+    default: return 0;
     }
 }
 

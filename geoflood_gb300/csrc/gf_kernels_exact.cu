@@ -30,7 +30,7 @@ static cudaError_t launch_exact(const gf_patch_work* work, int nwork, const gf_p
         attr_set = true;
     }
     if (nwork <= 0) return cudaSuccess;
-    kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err);
+    kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, nullptr, maux, cfl, gmax, err);
     return cudaGetLastError();
 }
 

@@ -118,7 +118,7 @@ extern "C" int gf_patch_update_noalloc(int device, const gf_phys* phys, int npat
     GF_NA_CK(cudaMemcpyAsync(d_work, work, npatch * sizeof(gf_patch_work), cudaMemcpyHostToDevice, st));
     GF_NA_CK(gf::launch_aos_to_soa(q, d_q, npatch, (int)S, 3, 3 * S, 3 * S, st));
     GF_NA_CK(gf::launch_aos_to_soa(aux, d_aux, npatch, (int)S, maux, maux * S, maux * S, st));
-    GF_NA_CK(gf::launch_patch_update(mx, d_work, npatch, d_phys, dt, nullptr, maux, d_cfl,
+    GF_NA_CK(gf::launch_patch_update(mx, d_work, npatch, d_phys, dt, nullptr, nullptr, maux, d_cfl,
                                      &d_status->gmax, &d_status->err, st));
     GF_NA_CK(gf::launch_soa_to_aos(d_q, q, npatch, (int)S, 3, 3 * S, 3 * S, st));
     NoallocStatus hs;

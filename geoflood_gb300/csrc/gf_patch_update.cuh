@@ -513,9 +513,9 @@ template <int M, int NT, int RB, int MINB, bool EXACT>
 __global__ void __launch_bounds__(NT, MINB)
     patch_update_kernel(const gf_patch_work* __restrict__ work, int nwork,
                         const gf_phys* __restrict__ phys_table, double dt_uniform,
-                        const double* __restrict__ group_dt, int maux,
-                        double* __restrict__ cfl_out, unsigned long long* __restrict__ group_max,
-                        int* __restrict__ err)
+                        const double* __restrict__ group_dt, const int* __restrict__ group_par,
+                        int maux, double* __restrict__ cfl_out,
+                        unsigned long long* __restrict__ group_max, int* __restrict__ err)
 {
     using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
@@ -530,139 +530,153 @@ __global__ void __launch_bounds__(NT, MINB)
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::OFF_BAR);
     double* red = sm + L::OFF_RED;
 
-    const int wi = blockIdx.x;
-    if (wi >= nwork) return;
-    const gf_patch_work wk = work[wi];
-    const gf_phys P = phys_table[wk.phys];
-    const double g = P.grav, drytol = P.dry_tolerance;
-    const double dt = group_dt ? group_dt[wk.group] : dt_uniform;
-
-    /* ---- stage the patch (h, hu, hv planes and b) with bulk copies ---- */
-    if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-    }
+    if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(bar, (uint32_t)(4 * S * sizeof(double)));
-        bulk_g2s(sm + L::OFF_H, wk.q, (uint32_t)(3 * S * sizeof(double)), bar);
-        bulk_g2s(sm + L::OFF_B, wk.aux, (uint32_t)(S * sizeof(double)), bar);
-    }
-    if (!mbar_wait(bar, 0, 1u << 22)) {
-        if (threadIdx.x == 0) atomicExch(err, 1);
-        mbar_wait(bar, 0, 1u << 22); /* let any copy in flight land */
-        return;
-    }
-
-    /* ---- b4step2 on all cells + per-cell quotients ---- */
-    int any_wet = 0;
-    for (int k = threadIdx.x; k < S; k += NT) {
-        double h = sm[L::OFF_H + k];
-        if (h < drytol) {
-            h = fmax(h, 0.0);
-            sm[L::OFF_H + k] = h;
-            sm[L::OFF_HU + k] = 0.0;
-            sm[L::OFF_HV + k] = 0.0;
+    uint32_t phase = 0;
+    /* persistent over the work list: one patch at a time per CTA */
+    for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
+        gf_patch_work wk = work[wi];
+        const double dt = group_dt ? group_dt[wk.group] : dt_uniform;
+        /* a group with no step this round (dt <= 0) is skipped as a whole */
+        if (group_dt && !(dt > 0.0)) continue;
+        if (group_par && group_par[wk.group]) {
+            /* the group's state lives in the second buffer: read there, write back */
+            double* t = wk.q;
+            wk.q = wk.qout;
+            wk.qout = t;
         }
-        const bool w = h > drytol;
-        wet[k] = w ? 1 : 0;
-        any_wet |= w;
-        double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
-        if (w) {
+        const gf_phys P = phys_table[wk.phys];
+        const double g = P.grav, drytol = P.dry_tolerance;
+
+        /* ---- stage the patch (h, hu, hv planes and b) with bulk copies ---- */
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(bar, (uint32_t)(4 * S * sizeof(double)));
+            bulk_g2s(sm + L::OFF_H, wk.q, (uint32_t)(3 * S * sizeof(double)), bar);
+            bulk_g2s(sm + L::OFF_B, wk.aux, (uint32_t)(S * sizeof(double)), bar);
+        }
+        const uint32_t ph = phase;
+        phase ^= 1u;
+        if (!__syncthreads_and(mbar_wait(bar, ph, 1u << 22))) {
+            if (threadIdx.x == 0) atomicExch(err, 1);
+            mbar_wait(bar, ph, 1u << 22); /* let any copy in flight land */
+            return;
+        }
+
+        /* ---- b4step2 on all cells + per-cell quotients ---- */
+        int any_wet = 0;
+        for (int k = threadIdx.x; k < S; k += NT) {
+            double h = sm[L::OFF_H + k];
+            if (h < drytol) {
+                h = fmax(h, 0.0);
+                sm[L::OFF_H + k] = h;
+                sm[L::OFF_HU + k] = 0.0;
+                sm[L::OFF_HV + k] = 0.0;
+            }
+            const bool w = h > drytol;
+            wet[k] = w ? 1 : 0;
+            any_wet |= w;
+            double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
+            if (w) {
+                if (FAST) {
+                    rh = 1.0 / h;
+                    u = sm[L::OFF_HU + k] * rh;
+                    v = sm[L::OFF_HV + k] * rh;
+                    const double gh = g * h;
+                    rc = rsqrt(gh);
+                    c = gh * rc;
+                } else {
+                    u = sm[L::OFF_HU + k] / h;
+                    v = sm[L::OFF_HV + k] / h;
+                    c = sqrt(g * h);
+                }
+            }
+            sm[L::OFF_U + k] = u;
+            sm[L::OFF_V + k] = v;
+            sm[L::OFF_C + k] = c;
             if (FAST) {
-                rh = 1.0 / h;
-                u = sm[L::OFF_HU + k] * rh;
-                v = sm[L::OFF_HV + k] * rh;
-                const double gh = g * h;
-                rc = rsqrt(gh);
-                c = gh * rc;
-            } else {
-                u = sm[L::OFF_HU + k] / h;
-                v = sm[L::OFF_HV + k] / h;
-                c = sqrt(g * h);
+                sm[L::OFF_RH + k] = rh;
+                sm[L::OFF_RC + k] = rc;
             }
         }
-        sm[L::OFF_U + k] = u;
-        sm[L::OFF_V + k] = v;
-        sm[L::OFF_C + k] = c;
-        if (FAST) {
-            sm[L::OFF_RH + k] = rh;
-            sm[L::OFF_RC + k] = rc;
-        }
-    }
-    for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
-    any_wet = __syncthreads_or(any_wet);
+        for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
+        any_wet = __syncthreads_or(any_wet);
 
-    const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
-    double smax_x = 0.0, smax_y = 0.0;
-    if (any_wet) {
-        const double c16g = 1.0 / (16.0 * g);
-        const double rsg = rsqrt(g);
-        const double crit = fmax(drytol * g, 1e-6);
-        const double crit2 = sqrt(crit);
-        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2);
-        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2);
-    }
+        const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
+        double smax_x = 0.0, smax_y = 0.0;
+        if (any_wet) {
+            const double c16g = 1.0 / (16.0 * g);
+            const double rsg = rsqrt(g);
+            const double crit = fmax(drytol * g, 1e-6);
+            const double crit2 = sqrt(crit);
+            smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2);
+            smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2);
+        }
 
-    /* ---- flux-difference update, src2, write interior ---- */
-    double* gq = wk.qout ? wk.qout : wk.q;
-    const double* gaux = wk.aux;
-    const int fidx = P.friction_index - 1;
-    for (int e = threadIdx.x; e < M * M; e += NT) {
-        const int i = 1 + e % M, j = 1 + e / M;
-        const int k = (j + 1) * N + (i + 1);
-        double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
-        if (EXACT) {
-            /* q - dtdx*(fm(i+1,j) - fp(i,j)) - dtdy*(gm(i,j+1) - gp(i,j)) */
-            const double* FM = sm + L::OFF_ACC;
-            const double* FP = FM + 3 * M * M;
-            const double* GM = FP + 3 * M * M;
-            const double* GP = GM + 3 * M * M;
-            h = h - dtdx * (FM[e] - FP[e]) - dtdy * (GM[e] - GP[e]);
-            hu = hu - dtdx * (FM[e + M * M] - FP[e + M * M]) - dtdy * (GM[e + M * M] - GP[e + M * M]);
-            hv = hv - dtdx * (FM[e + 2 * M * M] - FP[e + 2 * M * M]) -
-                 dtdy * (GM[e + 2 * M * M] - GP[e + 2 * M * M]);
-        } else {
-            const double* DX = sm + L::OFF_ACC;
-            const double* DY = sm + L::OFF_ACC + 3 * M * M;
-            h = h - dtdx * DX[e] - dtdy * DY[e];
-            hu = hu - dtdx * DX[e + M * M] - dtdy * DY[e + M * M];
-            hv = hv - dtdx * DX[e + 2 * M * M] - dtdy * DY[e + 2 * M * M];
+        /* ---- flux-difference update, src2, write interior ---- */
+        double* gq = wk.qout ? wk.qout : wk.q;
+        const double* gaux = wk.aux;
+        const int fidx = P.friction_index - 1;
+        for (int e = threadIdx.x; e < M * M; e += NT) {
+            const int i = 1 + e % M, j = 1 + e / M;
+            const int k = (j + 1) * N + (i + 1);
+            double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
+            if (EXACT) {
+                /* q - dtdx*(fm(i+1,j) - fp(i,j)) - dtdy*(gm(i,j+1) - gp(i,j)) */
+                const double* FM = sm + L::OFF_ACC;
+                const double* FP = FM + 3 * M * M;
+                const double* GM = FP + 3 * M * M;
+                const double* GP = GM + 3 * M * M;
+                h = h - dtdx * (FM[e] - FP[e]) - dtdy * (GM[e] - GP[e]);
+                hu = hu - dtdx * (FM[e + M * M] - FP[e + M * M]) - dtdy * (GM[e + M * M] - GP[e + M * M]);
+                hv = hv - dtdx * (FM[e + 2 * M * M] - FP[e + 2 * M * M]) -
+                     dtdy * (GM[e + 2 * M * M] - GP[e + 2 * M * M]);
+            } else {
+                const double* DX = sm + L::OFF_ACC;
+                const double* DY = sm + L::OFF_ACC + 3 * M * M;
+                h = h - dtdx * DX[e] - dtdy * DY[e];
+                hu = hu - dtdx * DX[e + M * M] - dtdy * DY[e + M * M];
+                hv = hv - dtdx * DX[e + 2 * M * M] - dtdy * DY[e + 2 * M * M];
+            }
+            if (P.src_term > 0) {
+                const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
+                                        ? gaux[(size_t)fidx * S + k]
+                                        : 0.0;
+                src2_cell<FAST>(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
+            }
+            gq[k] = h;
+            gq[S + k] = hu;
+            gq[2 * S + k] = hv;
         }
-        if (P.src_term > 0) {
-            const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
-                                    ? gaux[(size_t)fidx * S + k]
-                                    : 0.0;
-            src2_cell<FAST>(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
-        }
-        gq[k] = h;
-        gq[S + k] = hu;
-        gq[2 * S + k] = hv;
-    }
 
-    /* ---- CFL: warp-shuffle max, then across warps ---- */
-    double cx = smax_x, cy = smax_y;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
-        cy = fmax(cy, __shfl_xor_sync(0xffffffffu, cy, o));
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        red[warp] = cx;
-        red[32 + warp] = cy;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double mx = 0.0, my = 0.0;
-        for (int w2 = 0; w2 < NT / 32; ++w2) {
-            mx = fmax(mx, red[w2]);
-            my = fmax(my, red[32 + w2]);
+        /* ---- CFL: warp-shuffle max, then across warps ---- */
+        double cx = smax_x, cy = smax_y;
+    #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
+            cy = fmax(cy, __shfl_xor_sync(0xffffffffu, cy, o));
         }
-        double cfl = fmax(dtdx * mx, dtdy * my);
-        if (cfl > P.maxcfl_cap) cfl = 0.0;
-        if (cfl_out) cfl_out[wi] = cfl;
-        if (group_max) atomicMax(group_max + wk.group, dkey(cfl));
-    }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) {
+            red[warp] = cx;
+            red[32 + warp] = cy;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double mx = 0.0, my = 0.0;
+            for (int w2 = 0; w2 < NT / 32; ++w2) {
+                mx = fmax(mx, red[w2]);
+                my = fmax(my, red[32 + w2]);
+            }
+            double cfl = fmax(dtdx * mx, dtdy * my);
+            if (cfl > P.maxcfl_cap) cfl = 0.0;
+            if (cfl_out) cfl_out[wi] = cfl;
+            if (group_max) atomicMax(group_max + wk.group, dkey(cfl));
+        }
+        /* shared memory is restaged by the bulk (async-proxy) copies of the next
+         * work item: order this item's generic-proxy accesses before them */
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+    } /* work list */
 }
 
 } // namespace GF_KNS

@@ -4,19 +4,30 @@
  * Scenarios are single-level forests (a brick of npx x npy patches of one
  * mx). On admission a scenario gets one stream-ordered device allocation
  * (two state buffers, aux, neighbour table, geometry) and a physics slot;
- * its state then stays on the device until it finishes. Scenarios are
- * sorted into size lanes; each lane has its own stream and runs rounds: a
- * round steps every active scenario of the lane once, with one ghost-fill
- * launch and one patch-update launch per mx present, each scenario in its
- * own dt / CFL group. The host reads the group maxima back at the end of a
- * round and runs each scenario's time-step controller. Lanes overlap on the
- * device, and small lanes can run on higher-priority streams so that their
- * short rounds are not held behind the large scenarios' launches.
+ * its state then stays on the device until it finishes.
  *
- * Time stepping follows ForestClaw's outstyle 1 loop
- * (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395) with variable dt and
- * reduce_cfl on: save / restore around a rejected step (:239-243, :326-340)
- * becomes a flip between the two state buffers.
+ * Scenarios are sorted into size lanes; each lane has its own stream and a
+ * fixed membership (an epoch) between admissions and completions. A round
+ * of a lane steps every member once:
+ *
+ *   prepare (1 thread / scenario: dt, buffer parity, inflow state)
+ *   -> ghost fill (one launch per mx present)
+ *   -> patch update (one launch per mx present, each scenario its own
+ *      dt and CFL group)
+ *   -> finish (1 thread / scenario: accept or retake, next dt).
+ *
+ * The time-step control runs on the device (gf_served.cu), so rounds of a
+ * lane are enqueued back to back in chunks sized to about half a
+ * millisecond, two chunks in flight; the host reads the controllers back at
+ * each chunk end to notice finished scenarios, and changes the membership
+ * only when the lane has drained. Lanes overlap on the device, and smaller
+ * lanes run on higher-priority streams so that their short rounds are not
+ * held behind the large scenarios' launches.
+ *
+ * A rejected step costs no copy: the update writes into the second state
+ * buffer and the controller flips the current buffer only on acceptance
+ * (ForestClaw's save/restore, src/fc2d_geoclaw/fc2d_geoclaw_run.c:239-243,
+ * :326-340).
  */
 #include <cuda_runtime.h>
 
@@ -39,8 +50,11 @@ namespace {
 
 constexpr int kMaxSlots = 1024; /* physics slots = active scenarios */
 constexpr int kLaneMaux = 3;     /* largest maux a served scenario may have */
+constexpr int kMaxRounds = 64;   /* rounds per chunk */
+constexpr double kChunkTargetMs = 0.5;
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+inline int mclass(int mx) { return mx == 8 ? 0 : mx == 16 ? 1 : 2; }
 
 using Clock = std::chrono::steady_clock;
 
@@ -49,42 +63,46 @@ struct Scen {
     gf_scenario sc{};
     std::vector<double> hy_t, hy_hu;
     gf_scenario_info info{};
+    gf_group_state gst{}; /* host copy of the device controller */
     int lane = -1, slot = -1;
     int np = 0;
-    long S = 0;         /* cells per patch incl. halo */
+    long S = 0;          /* cells per patch incl. halo */
     long long cells = 0; /* interior cells */
     size_t bytes = 0;
-    /* device */
     char* dev = nullptr;
     double* qbuf[2] = {nullptr, nullptr};
     double* aux = nullptr;
     int* nbr = nullptr;
     gf_patch_geom* geom = nullptr;
-    int cur = 0;
-    /* outstyle-1 controller */
-    double dt_outer = 0, t_curr = 0, tend = 0, dt_minlevel = 0;
-    double dt_step = 0;
-    int nint = 0;           /* output interval in progress */
-    bool took_small = false;
     bool cancel_req = false;
-    bool finishing = false;
+    bool failed = false;
     cudaEvent_t ev_fin = nullptr;
+};
+
+struct Chunk {
+    int slot = 0;
+    int rounds = 0;
 };
 
 struct Lane {
     int idx = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev = nullptr;
-    bool in_flight = false;
-    std::vector<Scen*> act;     /* admitted, not finishing */
-    std::vector<Scen*> members; /* stepped by the round in flight */
+    std::vector<Scen*> members; /* group g of the epoch = members[g] */
+    std::vector<Scen*> joining; /* admitted, enter at the next epoch */
     std::vector<Scen*> fin;     /* final download in flight */
-    /* one pinned upload area and its device twin, one readback area */
-    char* h_up = nullptr;
-    char* d_up = nullptr;
-    size_t up_cap = 0;
-    unsigned long long* h_rb = nullptr; /* [0] err, [1..] group maxima */
-    unsigned long long* d_rb = nullptr;
+    std::deque<Chunk> inflight; /* at most two */
+    cudaEvent_t ev_start[2] = {nullptr, nullptr}, ev_end[2] = {nullptr, nullptr};
+    int next_slot = 0;
+    double round_ms = 0.05;
+    /* epoch area: pinned mirror and device copy */
+    char* h_ep = nullptr;
+    char* d_ep = nullptr;
+    size_t ep_cap = 0;
+    size_t off_blk = 0, off_gs = 0, off_dt = 0, off_par = 0, off_rb = 0, off_hyt = 0, off_hyu = 0;
+    size_t off_ref[3] = {0, 0, 0}, off_work[3] = {0, 0, 0};
+    int npm[3] = {0, 0, 0};
+    /* two readback slots: [err (8 B)][states] */
+    char* h_rb[2] = {nullptr, nullptr};
     size_t rb_cap = 0;
 };
 
@@ -106,6 +124,7 @@ struct gf_server {
     std::vector<gf_phys> h_phys;
     std::vector<int> free_slots;
     gf_server_stats stats{};
+    int cta_cap[GF_SERVER_MAX_LANES][3] = {}; /* update-kernel grid caps per lane and mx */
     std::thread loop;
     std::atomic<bool> running{false};
 
@@ -127,10 +146,10 @@ int scuda(gf_server* s, cudaError_t e, const char* where)
     return GF_ERR_CUDA;
 }
 
-#define SV_CK(s, call)                                        \
-    do {                                                      \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return scuda((s), e_, #call);  \
+#define SV_CK(s, call)                                       \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return scuda((s), e_, #call); \
     } while (0)
 
 size_t footprint_of(const gf_scenario& sc)
@@ -168,20 +187,6 @@ const char* validate(const gf_scenario& sc)
     return nullptr;
 }
 
-/* hydrograph/hydrograh_module.f90:176-221, discharge type */
-double hydro_at(const Scen& s, double t)
-{
-    const size_t n = s.hy_t.size();
-    if (n == 0) return 0.0;
-    if (t < s.hy_t[0]) return s.hy_hu[0];
-    if (t > s.hy_t[n - 1]) return s.hy_hu[n - 1];
-    for (size_t i = 0; i + 1 < n; ++i)
-        if (t >= s.hy_t[i] && t <= s.hy_t[i + 1])
-            return s.hy_hu[i] +
-                   (s.hy_hu[i + 1] - s.hy_hu[i]) / (s.hy_t[i + 1] - s.hy_t[i]) * (t - s.hy_t[i]);
-    return 0.0;
-}
-
 int lane_of(const gf_server* s, long long cells)
 {
     for (int k = 0; k < s->o.nlanes - 1; ++k)
@@ -189,44 +194,14 @@ int lane_of(const gf_server* s, long long cells)
     return s->o.nlanes - 1;
 }
 
-/* Advance the controller to the next step; false when the run is over
- * (the outer loop over output intervals, fc2d_geoclaw_run.c:229-236). */
-bool prepare_step(Scen* s)
+void sync_info(Scen* s)
 {
-    while (!(s->t_curr < s->tend)) {
-        if (++s->nint >= s->sc.nout) return false;
-        s->tend = s->t_curr + s->dt_outer;
-    }
-    /* fc2d_geoclaw_run.c:251-278: hit tend without a tiny trailing step */
-    double dt_step = s->dt_minlevel;
-    const double tol = 1e-2 * dt_step;
-    s->took_small = false;
-    const double small_step = s->tend - (s->t_curr + dt_step);
-    if (small_step < tol) {
-        dt_step = s->tend - s->t_curr;
-        if (small_step < 0) s->took_small = true;
-    }
-    s->dt_step = dt_step;
-    return true;
-}
-
-/* fc2d_geoclaw_run.c:326-376: reject and retake, or accept and set dt. */
-void finish_step(Scen* s, double cfl)
-{
-    s->info.max_cfl_seen = std::max(s->info.max_cfl_seen, cfl);
-    if (cfl > s->sc.max_cfl) {
-        s->dt_minlevel = s->dt_minlevel * s->sc.desired_cfl / cfl;
-        s->info.rejects++;
-    } else {
-        s->info.steps++;
-        s->info.cell_updates += s->cells;
-        s->t_curr += s->dt_step;
-        s->cur ^= 1;
-        const double dt_new = s->dt_minlevel * s->sc.desired_cfl / cfl;
-        if (!s->took_small) s->dt_minlevel = dt_new;
-    }
-    s->info.t = s->t_curr;
-    s->info.dt = s->dt_minlevel;
+    s->info.t = s->gst.t_curr;
+    s->info.dt = s->gst.dt_minlevel;
+    s->info.steps = s->gst.steps;
+    s->info.rejects = s->gst.rejects;
+    s->info.cell_updates = s->gst.steps * s->cells;
+    s->info.max_cfl_seen = s->gst.max_cfl_seen;
 }
 
 void release_device(gf_server* srv, Scen* s, cudaStream_t st)
@@ -310,21 +285,28 @@ int admit(gf_server* srv, Scen* s)
                                cudaMemcpyHostToDevice, L.st));
     SV_CK(srv, gf::launch_aos_to_soa(spare, s->aux, np, (int)S, sc.maux, sc.maux * S, sc.maux * S, L.st));
     srv->stats.launches += 2;
-    s->cur = 0;
-    /* controller state (fc2d_geoclaw_run.c:197-225) */
-    s->dt_outer = sc.t_final / sc.nout;
-    s->t_curr = 0.0;
-    s->nint = 0;
-    s->tend = s->dt_outer;
-    s->dt_minlevel = sc.initial_dt;
+    /* controller at t = 0 (fc2d_geoclaw_run.c:197-225) */
+    gf_group_state& g = s->gst;
+    std::memset(&g, 0, sizeof g);
+    g.qb[0] = s->qbuf[0];
+    g.qb[1] = s->qbuf[1];
+    g.dt_outer = sc.t_final / sc.nout;
+    g.t_curr = 0.0;
+    g.tend = g.dt_outer;
+    g.dt_minlevel = sc.initial_dt;
+    g.desired_cfl = sc.desired_cfl;
+    g.max_cfl = sc.max_cfl;
+    g.nout = sc.nout;
+    g.active = 1;
+    g.cur = 0;
+    g.nhydro = (int)s->hy_t.size();
     s->info.state = GF_SCEN_ACTIVE;
     s->info.t_admit = srv->now();
-    s->info.dt = s->dt_minlevel;
     s->info.device_bytes = s->bytes;
-    L.act.push_back(s);
+    sync_info(s);
+    L.joining.push_back(s);
     srv->stats.admitted++;
     srv->stats.active++;
-    srv->stats.queued--;
     return GF_OK;
 }
 
@@ -346,23 +328,36 @@ int admit_queued(gf_server* srv)
     return GF_OK;
 }
 
-/* Launch the next round of a lane (lane idle on entry). */
-int launch_round(gf_server* srv, Lane& L)
+template <typename T>
+int grow_pinned(gf_server* srv, T** p, size_t& cap, size_t need)
 {
-    L.members.clear();
-    for (size_t k = 0; k < L.act.size();) {
-        Scen* s = L.act[k];
-        if (s->cancel_req) {
+    if (need <= cap) return GF_OK;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    cap = 0;
+    const size_t c = std::max(need * 2, (size_t)1 << 16);
+    SV_CK(srv, cudaMallocHost(reinterpret_cast<void**>(p), c));
+    cap = c;
+    return GF_OK;
+}
+
+/* New epoch of a drained lane: drop finished / cancelled / failed members,
+ * start their final downloads, take in the joining scenarios, and upload
+ * the round tables. */
+int rebuild_epoch(gf_server* srv, Lane& L)
+{
+    std::vector<Scen*> keep;
+    for (Scen* s : L.members) {
+        if (s->failed) {
+            release_device(srv, s, L.st);
+            end_scenario(srv, s, GF_SCEN_FAILED);
+        } else if (s->cancel_req) {
             release_device(srv, s, L.st);
             end_scenario(srv, s, GF_SCEN_CANCELLED);
-            L.act.erase(L.act.begin() + k);
-            continue;
-        }
-        if (!prepare_step(s)) {
-            /* run over: final state out through the spare buffer */
+        } else if (!s->gst.active) {
             const long S = s->S;
-            double* curq = s->qbuf[s->cur];
-            double* spare = s->qbuf[s->cur ^ 1];
+            double* curq = s->qbuf[s->gst.cur];
+            double* spare = s->qbuf[s->gst.cur ^ 1];
             if (s->sc.q_out) {
                 SV_CK(srv, gf::launch_soa_to_aos(curq, spare, s->np, (int)S, 3, 3 * S, 3 * S, L.st));
                 SV_CK(srv, cudaMemcpyAsync(s->sc.q_out, spare, (size_t)s->np * 3 * S * sizeof(double),
@@ -371,70 +366,89 @@ int launch_round(gf_server* srv, Lane& L)
             }
             SV_CK(srv, cudaEventCreateWithFlags(&s->ev_fin, cudaEventDisableTiming));
             SV_CK(srv, cudaEventRecord(s->ev_fin, L.st));
-            s->finishing = true;
             L.fin.push_back(s);
-            L.act.erase(L.act.begin() + k);
-            continue;
+        } else {
+            keep.push_back(s);
         }
-        L.members.push_back(s);
-        ++k;
     }
+    for (Scen* s : L.joining) {
+        if (s->cancel_req) {
+            release_device(srv, s, L.st);
+            end_scenario(srv, s, GF_SCEN_CANCELLED);
+        } else {
+            keep.push_back(s);
+        }
+    }
+    L.joining.clear();
+    L.members.swap(keep);
     const int nm = (int)L.members.size();
     if (nm == 0) return GF_OK;
 
-    /* upload area: [blocks][group dt][refs m=8][work m=8][refs 16][work 16][refs 32][work 32] */
-    static const int ms[3] = {8, 16, 32};
     int npm[3] = {0, 0, 0};
-    for (Scen* s : L.members) npm[s->sc.mx == 8 ? 0 : s->sc.mx == 16 ? 1 : 2] += s->np;
-    size_t off_blk = 0;
-    size_t off_dt = align256(off_blk + nm * sizeof(gf_ghost_block));
-    size_t off = align256(off_dt + nm * sizeof(double));
-    size_t off_ref[3], off_work[3];
+    size_t nhy = 0;
+    for (Scen* s : L.members) {
+        npm[mclass(s->sc.mx)] += s->np;
+        nhy += s->hy_t.size();
+    }
+    size_t off = 0;
+    L.off_blk = off;
+    off = align256(off + nm * sizeof(gf_ghost_block));
+    L.off_gs = off;
+    off = align256(off + nm * sizeof(gf_group_state));
+    L.off_dt = off;
+    off = align256(off + nm * sizeof(double));
+    L.off_par = off;
+    off = align256(off + nm * sizeof(int));
+    L.off_rb = off; /* [err][gmax per group] */
+    off = align256(off + (nm + 1) * sizeof(unsigned long long));
+    L.off_hyt = off;
+    off = align256(off + std::max<size_t>(nhy, 1) * sizeof(double));
+    L.off_hyu = off;
+    off = align256(off + std::max<size_t>(nhy, 1) * sizeof(double));
     for (int c = 0; c < 3; ++c) {
-        off_ref[c] = off;
+        L.off_ref[c] = off;
         off = align256(off + npm[c] * sizeof(gf_ghost_ref));
-        off_work[c] = off;
+        L.off_work[c] = off;
         off = align256(off + npm[c] * sizeof(gf_patch_work));
+        L.npm[c] = npm[c];
     }
     const size_t need = off;
-    if (need > L.up_cap) {
-        if (L.h_up) cudaFreeHost(L.h_up);
-        if (L.d_up) cudaFreeAsync(L.d_up, L.st);
-        L.h_up = nullptr;
-        L.d_up = nullptr;
-        L.up_cap = 0;
-        const size_t cap = std::max(need * 2, (size_t)1 << 20);
-        SV_CK(srv, cudaMallocHost(reinterpret_cast<void**>(&L.h_up), cap));
-        SV_CK(srv, cudaMallocAsync(reinterpret_cast<void**>(&L.d_up), cap, L.st));
-        L.up_cap = cap;
+    if (need > L.ep_cap) {
+        if (L.d_ep) cudaFreeAsync(L.d_ep, L.st);
+        L.d_ep = nullptr;
+        size_t cap = L.ep_cap;
+        int rc = grow_pinned(srv, &L.h_ep, cap, need);
+        if (rc) return rc;
+        SV_CK(srv, cudaMallocAsync(reinterpret_cast<void**>(&L.d_ep), cap, L.st));
+        L.ep_cap = cap;
     }
-    if ((size_t)nm + 1 > L.rb_cap) {
-        if (L.h_rb) cudaFreeHost(L.h_rb);
-        if (L.d_rb) cudaFreeAsync(L.d_rb, L.st);
-        L.h_rb = nullptr;
-        L.d_rb = nullptr;
-        L.rb_cap = 0;
-        const size_t cap = std::max<size_t>(2 * (nm + 1), 64);
-        SV_CK(srv, cudaMallocHost(reinterpret_cast<void**>(&L.h_rb), cap * sizeof(unsigned long long)));
-        SV_CK(srv, cudaMallocAsync(reinterpret_cast<void**>(&L.d_rb), cap * sizeof(unsigned long long), L.st));
-        L.rb_cap = cap;
+    const size_t rb_need = 8 + nm * sizeof(gf_group_state);
+    if (rb_need > L.rb_cap) {
+        size_t c0 = L.rb_cap, c1 = L.rb_cap;
+        int rc = grow_pinned(srv, &L.h_rb[0], c0, rb_need);
+        if (!rc) rc = grow_pinned(srv, &L.h_rb[1], c1, rb_need);
+        if (rc) return rc;
+        L.rb_cap = std::min(c0, c1);
     }
-    gf_ghost_block* hb = reinterpret_cast<gf_ghost_block*>(L.h_up + off_blk);
-    double* hdt = reinterpret_cast<double*>(L.h_up + off_dt);
+    char* h = L.h_ep;
+    std::memset(h + L.off_rb, 0, (nm + 1) * sizeof(unsigned long long));
+    gf_ghost_block* hb = reinterpret_cast<gf_ghost_block*>(h + L.off_blk);
+    gf_group_state* hg = reinterpret_cast<gf_group_state*>(h + L.off_gs);
+    double* hyt = reinterpret_cast<double*>(h + L.off_hyt);
+    double* hyu = reinterpret_cast<double*>(h + L.off_hyu);
     gf_ghost_ref* href[3];
     gf_patch_work* hwork[3];
     int fill[3] = {0, 0, 0};
     for (int c = 0; c < 3; ++c) {
-        href[c] = reinterpret_cast<gf_ghost_ref*>(L.h_up + off_ref[c]);
-        hwork[c] = reinterpret_cast<gf_patch_work*>(L.h_up + off_work[c]);
+        href[c] = reinterpret_cast<gf_ghost_ref*>(h + L.off_ref[c]);
+        hwork[c] = reinterpret_cast<gf_patch_work*>(h + L.off_work[c]);
     }
+    size_t hoff = 0;
     for (int g = 0; g < nm; ++g) {
         Scen* s = L.members[g];
         const long S = s->S;
-        double* qc = s->qbuf[s->cur];
-        double* qn = s->qbuf[s->cur ^ 1];
         gf_ghost_block blk{};
-        blk.q = qc;
+        blk.q = s->qbuf[s->gst.cur];
         blk.aux = s->aux;
         blk.nbr = s->nbr;
         blk.geom = s->geom;
@@ -446,17 +460,22 @@ int launch_round(gf_server* srv, Lane& L)
         blk.bc.width = s->sc.hydro_width;
         blk.bc.x0 = s->sc.hydro_x0;
         blk.bc.y0 = s->sc.hydro_y0;
-        blk.bc.q0hu = hydro_at(*s, s->t_curr);
         blk.phys = s->slot;
         blk.maux = s->sc.maux;
+        blk.skip = 1;
         hb[g] = blk;
-        hdt[g] = s->dt_step;
-        const int c = s->sc.mx == 8 ? 0 : s->sc.mx == 16 ? 1 : 2;
+        s->gst.hydro_off = (int)hoff;
+        s->gst.nhydro = (int)s->hy_t.size();
+        std::copy(s->hy_t.begin(), s->hy_t.end(), hyt + hoff);
+        std::copy(s->hy_hu.begin(), s->hy_hu.end(), hyu + hoff);
+        hoff += s->hy_t.size();
+        hg[g] = s->gst;
+        const int c = mclass(s->sc.mx);
         for (int p = 0; p < s->np; ++p) {
             href[c][fill[c]] = gf_ghost_ref{g, p};
             gf_patch_work w{};
-            w.q = qc + (size_t)p * 3 * S;
-            w.qout = qn + (size_t)p * 3 * S;
+            w.q = s->qbuf[0] + (size_t)p * 3 * S;
+            w.qout = s->qbuf[1] + (size_t)p * 3 * S;
             w.aux = s->aux + (size_t)p * s->sc.maux * S;
             w.dx = s->sc.dx;
             w.dy = s->sc.dy;
@@ -466,67 +485,87 @@ int launch_round(gf_server* srv, Lane& L)
             ++fill[c];
         }
     }
-    SV_CK(srv, cudaMemcpyAsync(L.d_up, L.h_up, need, cudaMemcpyHostToDevice, L.st));
-    SV_CK(srv, cudaMemsetAsync(L.d_rb, 0, (nm + 1) * sizeof(unsigned long long), L.st));
-    const gf_ghost_block* db = reinterpret_cast<const gf_ghost_block*>(L.d_up + off_blk);
-    const double* ddt = reinterpret_cast<const double*>(L.d_up + off_dt);
-    for (int c = 0; c < 3; ++c) {
-        if (!npm[c]) continue;
-        SV_CK(srv, gf::launch_ghost_fill(ms[c], db, reinterpret_cast<const gf_ghost_ref*>(L.d_up + off_ref[c]),
-                                         npm[c], srv->d_phys, L.st));
-        srv->stats.launches++;
-    }
-    for (int c = 0; c < 3; ++c) {
-        if (!npm[c]) continue;
-        SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(L.d_up + off_work[c]),
-                                           npm[c], srv->d_phys, 0.0, ddt, kLaneMaux, nullptr, L.d_rb + 1,
-                                           reinterpret_cast<int*>(L.d_rb), L.st));
-        srv->stats.launches++;
-    }
-    SV_CK(srv, cudaMemcpyAsync(L.h_rb, L.d_rb, (nm + 1) * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, L.st));
-    SV_CK(srv, cudaEventRecord(L.ev, L.st));
-    L.in_flight = true;
-    srv->stats.rounds++;
+    SV_CK(srv, cudaMemcpyAsync(L.d_ep, L.h_ep, need, cudaMemcpyHostToDevice, L.st));
     return GF_OK;
 }
 
-/* A lane's round has completed: run the controllers. */
-int finish_round(gf_server* srv, Lane& L)
+/* Enqueue a chunk of rounds on an idle-or-running lane (epoch unchanged). */
+int launch_chunk(gf_server* srv, Lane& L)
 {
-    L.in_flight = false;
-    const int err = (int)L.h_rb[0];
+    static const int ms[3] = {8, 16, 32};
+    const int nm = (int)L.members.size();
+    char* d = L.d_ep;
+    gf_ghost_block* blk = reinterpret_cast<gf_ghost_block*>(d + L.off_blk);
+    gf_group_state* gs = reinterpret_cast<gf_group_state*>(d + L.off_gs);
+    double* gdt = reinterpret_cast<double*>(d + L.off_dt);
+    int* gpar = reinterpret_cast<int*>(d + L.off_par);
+    unsigned long long* rb = reinterpret_cast<unsigned long long*>(d + L.off_rb);
+    int* err = reinterpret_cast<int*>(rb);
+    const double* hyt = reinterpret_cast<const double*>(d + L.off_hyt);
+    const double* hyu = reinterpret_cast<const double*>(d + L.off_hyu);
+    int rounds = (int)std::ceil(kChunkTargetMs / std::max(L.round_ms, 1e-3));
+    rounds = std::max(1, std::min(kMaxRounds, rounds));
+    const int slot = L.next_slot;
+    L.next_slot ^= 1;
+    SV_CK(srv, cudaEventRecord(L.ev_start[slot], L.st));
+    for (int r = 0; r < rounds; ++r) {
+        SV_CK(srv, gf::launch_served_prepare(gs, blk, gdt, gpar, rb + 1, hyt, hyu, nm, L.st));
+        for (int c = 0; c < 3; ++c)
+            if (L.npm[c])
+                SV_CK(srv, gf::launch_ghost_fill(ms[c], blk,
+                                                 reinterpret_cast<const gf_ghost_ref*>(d + L.off_ref[c]),
+                                                 L.npm[c], srv->d_phys, L.st));
+        for (int c = 0; c < 3; ++c)
+            if (L.npm[c])
+                SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
+                                                   L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux,
+                                                   nullptr, rb + 1, err, L.st, srv->cta_cap[L.idx][c]));
+        SV_CK(srv, gf::launch_served_finish(gs, gdt, rb + 1, err, nm, L.st));
+        int ncls = (L.npm[0] > 0) + (L.npm[1] > 0) + (L.npm[2] > 0);
+        srv->stats.launches += 2 + 2 * ncls;
+    }
+    SV_CK(srv, cudaMemcpyAsync(L.h_rb[slot], rb, 8, cudaMemcpyDeviceToHost, L.st));
+    SV_CK(srv, cudaMemcpyAsync(L.h_rb[slot] + 8, gs, nm * sizeof(gf_group_state),
+                               cudaMemcpyDeviceToHost, L.st));
+    SV_CK(srv, cudaEventRecord(L.ev_end[slot], L.st));
+    L.inflight.push_back(Chunk{slot, rounds});
+    srv->stats.rounds += rounds;
+    return GF_OK;
+}
+
+/* A chunk has completed: copy the controllers back to the scenarios. */
+void finish_chunk(gf_server* srv, Lane& L, const Chunk& ch)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, L.ev_start[ch.slot], L.ev_end[ch.slot]) == cudaSuccess && ch.rounds > 0)
+        L.round_ms = std::max(1e-3, (double)ms / ch.rounds);
+    const char* rb = L.h_rb[ch.slot];
+    int err;
+    std::memcpy(&err, rb, sizeof err);
+    const gf_group_state* st = reinterpret_cast<const gf_group_state*>(rb + 8);
     for (size_t g = 0; g < L.members.size(); ++g) {
         Scen* s = L.members[g];
-        if (err) {
-            continue;
-        }
-        double cfl;
-        std::memcpy(&cfl, &L.h_rb[1 + g], sizeof cfl);
-        const long long before = s->info.cell_updates;
-        finish_step(s, cfl);
-        srv->stats.cell_updates += s->info.cell_updates - before;
+        const long long before = s->gst.steps;
+        s->gst = st[g];
+        srv->stats.cell_updates += (s->gst.steps - before) * s->cells;
+        sync_info(s);
+        if (err) s->failed = true;
     }
-    if (err) {
-        /* a bounded wait in the kernel expired: the round is void */
-        for (Scen* s : L.members) {
-            auto it = std::find(L.act.begin(), L.act.end(), s);
-            if (it != L.act.end()) L.act.erase(it);
-            release_device(srv, s, L.st);
-            end_scenario(srv, s, GF_SCEN_FAILED);
-        }
-        L.members.clear();
-        return sfail(srv, GF_ERR_DEVICE, "a patch-update copy wait timed out; scenarios failed");
-    }
-    L.members.clear();
-    return GF_OK;
+    if (err) srv->last_error = "a patch-update copy wait timed out; the lane's scenarios failed";
+}
+
+bool lane_needs_epoch(const Lane& L)
+{
+    if (!L.joining.empty()) return true;
+    for (const Scen* s : L.members)
+        if (!s->gst.active || s->cancel_req || s->failed) return true;
+    return false;
 }
 
 int pump_locked(gf_server* srv, int* busy)
 {
     if (srv->broken) return GF_ERR_STATE;
     SV_CK(srv, cudaSetDevice(srv->device));
-    int rc = GF_OK;
     for (int k = 0; k < srv->o.nlanes; ++k) {
         Lane& L = srv->lanes[k];
         for (size_t i = 0; i < L.fin.size();) {
@@ -538,30 +577,37 @@ int pump_locked(gf_server* srv, int* busy)
             end_scenario(srv, s, GF_SCEN_DONE);
             L.fin.erase(L.fin.begin() + i);
         }
-        if (L.in_flight) {
-            cudaError_t e = cudaEventQuery(L.ev);
-            if (e == cudaErrorNotReady) continue;
-            if (e != cudaSuccess) return scuda(srv, e, "round");
-            int r = finish_round(srv, L);
-            if (r && !rc) rc = r;
+        while (!L.inflight.empty()) {
+            const Chunk ch = L.inflight.front();
+            cudaError_t e = cudaEventQuery(L.ev_end[ch.slot]);
+            if (e == cudaErrorNotReady) break;
+            if (e != cudaSuccess) return scuda(srv, e, "round chunk");
+            finish_chunk(srv, L, ch);
+            L.inflight.pop_front();
         }
     }
-    int r = admit_queued(srv);
-    if (r) return r;
+    int rc = admit_queued(srv);
+    if (rc) return rc;
     for (int k = 0; k < srv->o.nlanes; ++k) {
         Lane& L = srv->lanes[k];
-        if (!L.in_flight) {
-            r = launch_round(srv, L);
-            if (r) return r;
+        if (lane_needs_epoch(L)) {
+            if (!L.inflight.empty()) continue; /* drain first */
+            rc = rebuild_epoch(srv, L);
+            if (rc) return rc;
+        }
+        if (L.members.empty()) continue;
+        while (L.inflight.size() < 2) {
+            rc = launch_chunk(srv, L);
+            if (rc) return rc;
         }
     }
     int b = !srv->queue.empty();
     for (int k = 0; k < srv->o.nlanes; ++k) {
         const Lane& L = srv->lanes[k];
-        b |= L.in_flight || !L.act.empty() || !L.fin.empty();
+        b |= !L.inflight.empty() || !L.members.empty() || !L.joining.empty() || !L.fin.empty();
     }
     if (busy) *busy = b;
-    return rc;
+    return GF_OK;
 }
 
 void loop_main(gf_server* srv)
@@ -572,14 +618,13 @@ void loop_main(gf_server* srv)
         {
             std::lock_guard<std::mutex> g(srv->mu);
             rc = pump_locked(srv, &busy);
-        }
-        if (rc == GF_ERR_CUDA || rc == GF_ERR_STATE) {
-            std::lock_guard<std::mutex> g(srv->mu);
-            srv->cv.notify_all();
-            break;
+            if (rc == GF_ERR_CUDA || rc == GF_ERR_STATE) {
+                srv->cv.notify_all();
+                break;
+            }
         }
         if (!busy) std::this_thread::sleep_for(std::chrono::microseconds(200));
-        else std::this_thread::yield();
+        else std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
@@ -599,6 +644,7 @@ void gf_server_opts_default(gf_server_opts* o)
     o->lane_cells[2] = 0;
     o->priority = 1;
     o->backfill = 1;
+    o->reserve_sms = 16;
 }
 
 int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
@@ -628,7 +674,10 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
         int prio = lo;
         if (o.priority && o.nlanes > 1) prio = hi + (lo - hi) * k / (o.nlanes - 1);
         e = cudaStreamCreateWithPriority(&L.st, cudaStreamNonBlocking, prio);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
+        for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+            e = cudaEventCreate(&L.ev_start[j]);
+            if (e == cudaSuccess) e = cudaEventCreate(&L.ev_end[j]);
+        }
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->d_phys, kMaxSlots * sizeof(gf_phys));
     if (e == cudaSuccess) {
@@ -643,6 +692,18 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
         gf_server_destroy(s);
         return GF_ERR_CUDA;
     }
+    /* later lanes run persistent update grids that leave reserve_sms SMs to
+     * the first lane, whose short rounds then start without waiting for
+     * resident CTAs of the large scenarios to retire */
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    static const int ms[3] = {8, 16, 32};
+    for (int k = 1; k < o.nlanes; ++k)
+        for (int c = 0; c < 3; ++c) {
+            const int occ = gf::patch_update_occupancy(ms[c]);
+            const int sms = nsm - o.reserve_sms;
+            s->cta_cap[k][c] = (o.reserve_sms > 0 && sms > 0 && occ > 0) ? sms * occ : 0;
+        }
     s->h_phys.resize(kMaxSlots);
     for (int k = kMaxSlots - 1; k >= 0; --k) s->free_slots.push_back(k);
     *out = s;
@@ -666,11 +727,13 @@ void gf_server_destroy(gf_server* s)
     }
     for (int k = 0; k < GF_SERVER_MAX_LANES; ++k) {
         Lane& L = s->lanes[k];
-        if (L.d_up) cudaFree(L.d_up);
-        if (L.d_rb) cudaFree(L.d_rb);
-        if (L.h_up) cudaFreeHost(L.h_up);
-        if (L.h_rb) cudaFreeHost(L.h_rb);
-        if (L.ev) cudaEventDestroy(L.ev);
+        if (L.d_ep) cudaFree(L.d_ep);
+        if (L.h_ep) cudaFreeHost(L.h_ep);
+        for (int j = 0; j < 2; ++j) {
+            if (L.h_rb[j]) cudaFreeHost(L.h_rb[j]);
+            if (L.ev_start[j]) cudaEventDestroy(L.ev_start[j]);
+            if (L.ev_end[j]) cudaEventDestroy(L.ev_end[j]);
+        }
         if (L.st) cudaStreamDestroy(L.st);
     }
     if (s->d_phys) cudaFree(s->d_phys);
@@ -713,7 +776,6 @@ int gf_server_submit(gf_server* s, const gf_scenario* sc, long long* id)
     s->all[x->id] = x;
     s->queue.push_back(x);
     s->stats.submitted++;
-    s->stats.queued++;
     if (id) *id = x->id;
     return GF_OK;
 }
@@ -761,7 +823,7 @@ int gf_server_wait(gf_server* s, long long id, double timeout_s)
             if (rc) return rc;
             if (busy) {
                 g.unlock();
-                std::this_thread::yield();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
                 g.lock();
             }
         }
@@ -788,12 +850,11 @@ int gf_server_cancel(gf_server* s, long long id)
     Scen* x = it->second;
     if (x->info.state == GF_SCEN_QUEUED) {
         s->queue.erase(std::find(s->queue.begin(), s->queue.end(), x));
-        s->stats.queued--;
         x->info.state = GF_SCEN_CANCELLED;
         x->info.t_done = s->now();
         s->cv.notify_all();
-    } else if (x->info.state == GF_SCEN_ACTIVE && !x->finishing) {
-        x->cancel_req = true;
+    } else if (x->info.state == GF_SCEN_ACTIVE) {
+        x->cancel_req = true; /* taken out at the lane's next epoch */
     }
     return GF_OK;
 }

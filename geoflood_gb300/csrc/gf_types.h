@@ -53,12 +53,29 @@ typedef struct gf_ghost_block {
     const int* phys_of;         /* per-patch physics slot, or null = phys      */
     gf_bc_spec bc;
     int phys, maux;
+    int skip;                   /* non-zero: leave this block alone this round */
+    int pad;
 } gf_ghost_block;
 
 /* A patch of a ghost-fill list: (block, block-local patch index). */
 typedef struct gf_ghost_ref {
     int block, local;
 } gf_ghost_ref;
+
+/* Time-step controller of one served scenario, kept on the device
+ * (ForestClaw outstyle 1, src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395). */
+typedef struct gf_group_state {
+    double* qb[2];             /* the scenario's two state buffers            */
+    double t_curr, tend, dt_outer, dt_minlevel, dt_step;
+    double desired_cfl, max_cfl, max_cfl_seen;
+    long long steps, rejects;
+    int nint, nout;            /* output interval in progress / count         */
+    int took_small;
+    int active;                /* 0: the run is over (or never started)       */
+    int cur;                   /* state buffer holding the current solution   */
+    int hydro_off, nhydro;     /* samples in the lane's hydrograph table      */
+    int pad;
+} gf_group_state;
 
 /* One coarse/fine transfer (gf_amr.cu): kind GF_XFER_*, code = coarse
  * face / corner or child index, (ox, oy) = fine index of the coarse patch's

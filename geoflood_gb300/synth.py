@@ -122,20 +122,22 @@ def pad_wall(q: np.ndarray, mbc: int = MBC) -> np.ndarray:
     return out
 
 
-def tile_level(field: np.ndarray, m: int, mbc: int = MBC) -> np.ndarray:
+def tile_level(field: np.ndarray, m: int, mbc: int = MBC, out: np.ndarray | None = None) -> np.ndarray:
     """Cut a haloed global array (NY+2mbc, NX+2mbc, nf) into patches of m x m
     interior cells, each with its mbc-wide ghost ring taken from the global
-    array. Returns (npatch, m+2mbc, m+2mbc, nf), patches row-major in (py, px)."""
+    array. Returns (npatch, m+2mbc, m+2mbc, nf), patches row-major in (py, px),
+    written into `out` when given."""
     NY, NX = field.shape[0] - 2 * mbc, field.shape[1] - 2 * mbc
     assert NX % m == 0 and NY % m == 0
     py, px = NY // m, NX // m
     n4 = m + 2 * mbc
-    out = np.empty((py * px, n4, n4, field.shape[2]))
-    k = 0
-    for j in range(py):
-        for i in range(px):
-            out[k] = field[j * m:j * m + n4, i * m:i * m + n4]
-            k += 1
+    f = np.ascontiguousarray(field)
+    s0, s1, s2 = f.strides
+    view = np.lib.stride_tricks.as_strided(f, shape=(py, px, n4, n4, f.shape[2]),
+                                           strides=(m * s0, m * s1, s0, s1, s2), writeable=False)
+    if out is None:
+        return np.ascontiguousarray(view).reshape(py * px, n4, n4, f.shape[2])
+    np.copyto(out.reshape(py, px, n4, n4, f.shape[2]), view)
     return out
 
 
@@ -252,7 +254,7 @@ def flood_scenario_params(seed: int, cells: float, mx: int | None = None, dx: fl
 
 
 def flood_scenario(seed: int, cells: float, mx: int | None = None, dx: float = 5.0,
-                   time_scale: float = 1.0 / 150.0, relief: float = 10.0):
+                   time_scale: float = 1.0 / 150.0, relief: float = 10.0, alloc=None):
     """One served flood scenario: a river valley on a fractal DEM fed by an
     inflow hydrograph on the left side (mthbc 0 there, extrapolation on the
     right, walls top and bottom).
@@ -266,6 +268,8 @@ def flood_scenario(seed: int, cells: float, mx: int | None = None, dx: float = 5
       to the peak at t_rise ~ U[0.5, 2] h and back by 3 t_rise, per unit
       channel width; Manning n ~ U[0.02, 0.08]; horizon U[1, 6] h.
     - All times (rise, horizon) are multiplied by `time_scale`.
+
+    `alloc(shape)` (optional) provides the q and aux arrays (e.g. pinned).
     """
     from . import Phys
     from .serve import Hydrograph, Scenario
@@ -286,8 +290,11 @@ def flood_scenario(seed: int, cells: float, mx: int | None = None, dx: float = 5
     hy = Hydrograph(time=np.array([0.0, t_rise, 3.0 * t_rise]),
                     hu=np.array([0.1 * peak, peak, 0.1 * peak]) / width,
                     side=(1, 0, 0, 0), width=width, x0=0.0, y0=0.5 * ly)
-    qt = np.ascontiguousarray(tile_level(pad_extrap(q), mx))
-    at = np.ascontiguousarray(tile_level(pad_extrap(b[..., None]), mx))
+    n4 = mx + 2 * MBC
+    qt = alloc((npx * npy, n4, n4, 3)) if alloc else None
+    at = alloc((npx * npy, n4, n4, 1)) if alloc else None
+    qt = tile_level(pad_extrap(q), mx, out=qt)
+    at = tile_level(pad_extrap(b[..., None]), mx, out=at)
     return Scenario(mx=mx, npx=npx, npy=npy, dx=dx, dy=dx, q=qt, aux=at, t_final=p["horizon"],
                     phys=Phys(manning_coefficient=(p["manning"],), manning_break=(1.0e10,)),
                     mthbc=(0, 1, 3, 3), hydro=hy, nout=4, initial_dt=0.2, seed=seed)

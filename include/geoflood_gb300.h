@@ -355,6 +355,7 @@ typedef struct gf_server_opts {
     long long lane_cells[GF_SERVER_MAX_LANES]; /* lane k: cells < lane_cells[k]; last lane takes the rest */
     int priority;           /* 1: smaller lanes on higher-priority streams       */
     int backfill;           /* 1: admit later arrivals that fit while the head waits */
+    int reserve_sms;        /* lanes after the first leave this many SMs free for it */
 } gf_server_opts;
 
 typedef struct gf_scenario_info {
