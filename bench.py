@@ -205,7 +205,8 @@ def served_stream(args):
     synth.flood_scenario(1, 3e6, mx=32, time_scale=ts)
     synth.flood_scenario(2, 3e6, mx=32, time_scale=ts)
 
-    srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms)
+    lanes = tuple(int(float(v)) for v in args.served_lanes.split(",") if v.strip())
+    srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms, lanes=lanes)
     srv.start()
 
     # -- calibration: a saturated batch, throughput while most are in flight
@@ -309,13 +310,18 @@ def served_stream(args):
     served_rate = work / (t_end - t_start)
 
     # -- isolated re-runs of a size-stratified sample: latency alone, same bits
-    slow, same = [], True
+    slow, same, detail = [], True, []
     for k in sample:
         sc, qo = make(k)
         sid = srv.submit(sc, qo)
         ik = srv.wait(sid, timeout=600)
-        slow.append((infos[k]["t_done"] - infos[k]["t_submit"]) / (ik["t_done"] - ik["t_submit"]))
+        t_iso = ik["t_done"] - ik["t_submit"]
+        t_mix = infos[k]["t_done"] - infos[k]["t_submit"]
+        slow.append(t_mix / t_iso)
         same &= bool(np.array_equal(qo, outs[k])) and ik["steps"] == infos[k]["steps"]
+        detail.append({"cells": int(sc.cells), "mx": sc.mx, "lane": ik["lane"], "steps": ik["steps"],
+                       "isolated_s": t_iso, "mixed_s": t_mix,
+                       "queued_s": infos[k]["t_admit"] - infos[k]["t_submit"]})
         srv.release(sid)
     srv.stop()
     srv.close()
@@ -344,7 +350,7 @@ def served_stream(args):
         "p99_latency_s": float(np.percentile(lat, 99)),
         "slowdown_vs_isolated": {"p50": float(np.percentile(slow, 50)),
                                  "p99": float(np.percentile(slow, 99)), "max": float(max(slow)),
-                                 "sample": len(sample)},
+                                 "sample": len(sample), "detail": detail},
         "alone_equals_mix": same,
         "plain_per_patch": {"value": plain_rate, "unit": METRIC,
                             "per_mx": {str(k): v for k, v in rate_mx.items()},
@@ -571,6 +577,8 @@ def main():
     ap.add_argument("--served-scenarios", type=int, default=512)
     ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
     ap.add_argument("--served-reserve-sms", type=int, default=None)
+    ap.add_argument("--served-lanes", default="1e5,1e6",
+                    help="cell-count boundaries between the server's size lanes")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -30,6 +30,7 @@
  * :326-340).
  */
 #include <cuda_runtime.h>
+#include <sys/prctl.h>
 
 #include <algorithm>
 #include <atomic>
@@ -104,6 +105,10 @@ struct Lane {
     /* two readback slots: [err (8 B)][states] */
     char* h_rb[2] = {nullptr, nullptr};
     size_t rb_cap = 0;
+    /* one round of the epoch, captured once and replayed per round */
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int launches_per_round = 0;
 };
 
 } // namespace
@@ -341,6 +346,9 @@ int grow_pinned(gf_server* srv, T** p, size_t& cap, size_t need)
     return GF_OK;
 }
 
+int capture_round(gf_server* srv, Lane& L);
+void drop_graph(Lane& L);
+
 /* New epoch of a drained lane: drop finished / cancelled / failed members,
  * start their final downloads, take in the joining scenarios, and upload
  * the round tables. */
@@ -382,7 +390,10 @@ int rebuild_epoch(gf_server* srv, Lane& L)
     L.joining.clear();
     L.members.swap(keep);
     const int nm = (int)L.members.size();
-    if (nm == 0) return GF_OK;
+    if (nm == 0) {
+        drop_graph(L);
+        return GF_OK;
+    }
 
     int npm[3] = {0, 0, 0};
     size_t nhy = 0;
@@ -486,11 +497,12 @@ int rebuild_epoch(gf_server* srv, Lane& L)
         }
     }
     SV_CK(srv, cudaMemcpyAsync(L.d_ep, L.h_ep, need, cudaMemcpyHostToDevice, L.st));
-    return GF_OK;
+    return capture_round(srv, L);
 }
 
-/* Enqueue a chunk of rounds on an idle-or-running lane (epoch unchanged). */
-int launch_chunk(gf_server* srv, Lane& L)
+/* Enqueue one round of the lane's epoch on its stream (used once per epoch,
+ * under stream capture). */
+int enqueue_round(gf_server* srv, Lane& L)
 {
     static const int ms[3] = {8, 16, 32};
     const int nm = (int)L.members.size();
@@ -503,27 +515,68 @@ int launch_chunk(gf_server* srv, Lane& L)
     int* err = reinterpret_cast<int*>(rb);
     const double* hyt = reinterpret_cast<const double*>(d + L.off_hyt);
     const double* hyu = reinterpret_cast<const double*>(d + L.off_hyu);
+    int n = 0;
+    SV_CK(srv, gf::launch_served_prepare(gs, blk, gdt, gpar, rb + 1, hyt, hyu, nm, L.st));
+    ++n;
+    for (int c = 0; c < 3; ++c)
+        if (L.npm[c]) {
+            SV_CK(srv, gf::launch_ghost_fill(ms[c], blk, reinterpret_cast<const gf_ghost_ref*>(d + L.off_ref[c]),
+                                             L.npm[c], srv->d_phys, L.st));
+            ++n;
+        }
+    for (int c = 0; c < 3; ++c)
+        if (L.npm[c]) {
+            SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
+                                               L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux, nullptr,
+                                               rb + 1, err, L.st, srv->cta_cap[L.idx][c]));
+            ++n;
+        }
+    SV_CK(srv, gf::launch_served_finish(gs, gdt, rb + 1, err, nm, L.st));
+    ++n;
+    L.launches_per_round = n;
+    return GF_OK;
+}
+
+void drop_graph(Lane& L)
+{
+    if (L.exec) cudaGraphExecDestroy(L.exec);
+    if (L.graph) cudaGraphDestroy(L.graph);
+    L.exec = nullptr;
+    L.graph = nullptr;
+}
+
+/* Capture the epoch's round as a graph (one graph launch per round). */
+int capture_round(gf_server* srv, Lane& L)
+{
+    drop_graph(L);
+    SV_CK(srv, cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_round(srv, L);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(L.st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    SV_CK(srv, e);
+    L.graph = g;
+    SV_CK(srv, cudaGraphInstantiate(&L.exec, L.graph, 0));
+    return GF_OK;
+}
+
+/* Enqueue a chunk of rounds (epoch unchanged) and the controllers' readback. */
+int launch_chunk(gf_server* srv, Lane& L)
+{
+    const int nm = (int)L.members.size();
+    char* d = L.d_ep;
+    const gf_group_state* gs = reinterpret_cast<const gf_group_state*>(d + L.off_gs);
+    const unsigned long long* rb = reinterpret_cast<const unsigned long long*>(d + L.off_rb);
     int rounds = (int)std::ceil(kChunkTargetMs / std::max(L.round_ms, 1e-3));
     rounds = std::max(1, std::min(kMaxRounds, rounds));
     const int slot = L.next_slot;
     L.next_slot ^= 1;
     SV_CK(srv, cudaEventRecord(L.ev_start[slot], L.st));
-    for (int r = 0; r < rounds; ++r) {
-        SV_CK(srv, gf::launch_served_prepare(gs, blk, gdt, gpar, rb + 1, hyt, hyu, nm, L.st));
-        for (int c = 0; c < 3; ++c)
-            if (L.npm[c])
-                SV_CK(srv, gf::launch_ghost_fill(ms[c], blk,
-                                                 reinterpret_cast<const gf_ghost_ref*>(d + L.off_ref[c]),
-                                                 L.npm[c], srv->d_phys, L.st));
-        for (int c = 0; c < 3; ++c)
-            if (L.npm[c])
-                SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
-                                                   L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux,
-                                                   nullptr, rb + 1, err, L.st, srv->cta_cap[L.idx][c]));
-        SV_CK(srv, gf::launch_served_finish(gs, gdt, rb + 1, err, nm, L.st));
-        int ncls = (L.npm[0] > 0) + (L.npm[1] > 0) + (L.npm[2] > 0);
-        srv->stats.launches += 2 + 2 * ncls;
-    }
+    for (int r = 0; r < rounds; ++r) SV_CK(srv, cudaGraphLaunch(L.exec, L.st));
+    srv->stats.launches += (long long)rounds * L.launches_per_round;
     SV_CK(srv, cudaMemcpyAsync(L.h_rb[slot], rb, 8, cudaMemcpyDeviceToHost, L.st));
     SV_CK(srv, cudaMemcpyAsync(L.h_rb[slot] + 8, gs, nm * sizeof(gf_group_state),
                                cudaMemcpyDeviceToHost, L.st));
@@ -612,6 +665,8 @@ int pump_locked(gf_server* srv, int* busy)
 
 void loop_main(gf_server* srv)
 {
+    /* short sleeps between passes: ask for fine timer slack on this thread */
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0, 0, 0);
     while (srv->running.load()) {
         int busy = 0;
         int rc;
@@ -623,8 +678,8 @@ void loop_main(gf_server* srv)
                 break;
             }
         }
-        if (!busy) std::this_thread::sleep_for(std::chrono::microseconds(200));
-        else std::this_thread::sleep_for(std::chrono::microseconds(20));
+        /* outside the lock, so that submitters and pollers get their turn */
+        std::this_thread::sleep_for(std::chrono::microseconds(busy ? 10 : 200));
     }
 }
 
@@ -698,6 +753,9 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     static const int ms[3] = {8, 16, 32};
+    for (int c = 0; c < 3; ++c) /* sets the kernels' shared-memory attribute outside capture */
+        gf::launch_patch_update(ms[c], nullptr, 0, nullptr, 0.0, nullptr, nullptr, 0, nullptr,
+                                nullptr, nullptr, nullptr);
     for (int k = 1; k < o.nlanes; ++k)
         for (int c = 0; c < 3; ++c) {
             const int occ = gf::patch_update_occupancy(ms[c]);
@@ -734,6 +792,7 @@ void gf_server_destroy(gf_server* s)
             if (L.ev_start[j]) cudaEventDestroy(L.ev_start[j]);
             if (L.ev_end[j]) cudaEventDestroy(L.ev_end[j]);
         }
+        drop_graph(L);
         if (L.st) cudaStreamDestroy(L.st);
     }
     if (s->d_phys) cudaFree(s->d_phys);
