@@ -17,6 +17,7 @@ library; there is no host fallback.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -129,10 +130,17 @@ class Context:
         if rc != 0:
             raise GeoFloodError(rc, f"gf_ctx_create(device={device}) failed")
         self.h = h
+        # levels and forests live on this context: they are closed before it
+        self._children = weakref.WeakSet()
         self.set_phys(0, phys or Phys())
+
+    def _adopt(self, child):
+        self._children.add(child)
 
     def close(self):
         if getattr(self, "h", None):
+            for ch in list(self._children):
+                ch.close()
             self._lib.gf_ctx_destroy(self.h)
             self.h = None
 
@@ -204,6 +212,7 @@ class Level:
         _check(ctx.h, self._lib.gf_level_create(ctx.h, self.npatch, self.m, self.m, self.maux,
                                                 C.byref(h)))
         self.h = h
+        ctx._adopt(self)
 
     @property
     def shape_q(self):
@@ -329,6 +338,7 @@ class Level:
 
 
 from .serve import Hydrograph, Scenario, Server  # noqa: E402
+from .forest import Forest  # noqa: E402
 
 __all__ = ["Phys", "Refine", "Context", "Level", "GeoFloodError", "MBC", "MEQN", "Hydrograph",
-           "Scenario", "Server"]
+           "Scenario", "Server", "Forest"]

@@ -102,6 +102,21 @@ class gf_server_stats(C.Structure):
                 ("bytes_peak", C.c_size_t), ("active", C.c_int), ("queued", C.c_int)]
 
 
+class gf_forest_opts(C.Structure):
+    _fields_ = [("mx", C.c_int), ("maux", C.c_int), ("nbx", C.c_int), ("nby", C.c_int),
+                ("minlevel", C.c_int), ("maxlevel", C.c_int), ("x0", C.c_double),
+                ("y0", C.c_double), ("dx0", C.c_double), ("dy0", C.c_double),
+                ("phys_slot", C.c_int), ("mthbc", C.c_int * 4), ("regrid_interval", C.c_int),
+                ("max_patches", C.c_int), ("refine", gf_refine)]
+
+
+class gf_forest_stats(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("rejects", C.c_longlong), ("regrids", C.c_longlong),
+                ("cell_updates", C.c_longlong), ("t", C.c_double), ("dt", C.c_double),
+                ("max_cfl_seen", C.c_double), ("npatch", C.c_int), ("npatch_max", C.c_int),
+                ("levels_used", C.c_int)]
+
+
 XFER_AVG_FACE, XFER_AVG_CORNER, XFER_INTERP_FACE = 0, 1, 2
 XFER_INTERP_CORNER, XFER_INTERP2FINE, XFER_AVG2COARSE = 3, 4, 5
 
@@ -151,6 +166,25 @@ SIGNATURES = [
                                           C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_double,
                                           C.c_void_p, C.c_void_p, _dp, _dp, C.c_void_p]),
     ("gf_level_device_planes", C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp)]),
+    ("gf_forest_opts_default", None, [C.POINTER(gf_forest_opts)]),
+    ("gf_forest_create", C.c_int, [_vp, C.POINTER(gf_forest_opts), _dp, C.POINTER(_vp)]),
+    ("gf_forest_destroy", None, [_vp]),
+    ("gf_forest_set_hydrograph", C.c_int, [_vp, C.c_int, _dp, _dp, C.POINTER(C.c_int),
+                                           C.c_double, C.c_double, C.c_double]),
+    ("gf_forest_init", C.c_int, [_vp]),
+    ("gf_forest_ghost_fill", C.c_int, [_vp, C.c_double]),
+    ("gf_forest_step", C.c_int, [_vp, C.c_double, C.c_double, _dp]),
+    ("gf_forest_accept", C.c_int, [_vp, C.c_int]),
+    ("gf_forest_regrid", C.c_int, [_vp, C.c_double, C.POINTER(C.c_int)]),
+    ("gf_forest_run", C.c_int, [_vp, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double,
+                                C.c_int, C.POINTER(gf_forest_stats)]),
+    ("gf_forest_get_stats", C.c_int, [_vp, C.POINTER(gf_forest_stats)]),
+    ("gf_forest_npatch", C.c_int, [_vp]),
+    ("gf_forest_patches", C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]),
+    ("gf_forest_download", C.c_int, [_vp, _dp]),
+    ("gf_forest_download_aux", C.c_int, [_vp, _dp]),
+    ("gf_forest_upload", C.c_int, [_vp, _dp]),
     ("gf_server_opts_default", None, [C.POINTER(gf_server_opts)]),
     ("gf_server_create", C.c_int, [C.c_int, C.POINTER(gf_server_opts), C.POINTER(_vp)]),
     ("gf_server_destroy", None, [_vp]),

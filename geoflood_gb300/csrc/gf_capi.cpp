@@ -158,7 +158,7 @@ int enqueue_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int 
 {
     GF_CK(c, cudaMemsetAsync(d_status, 0, sizeof(DevStatus), c->stream));
     if (c->exact)
-        GF_CK(c, gf::launch_patch_update_exact(m, d_work, nwork, c->d_phys, dt, nullptr, maux,
+        GF_CK(c, gf::launch_patch_update_exact(m, d_work, nwork, c->d_phys, dt, nullptr, nullptr, maux,
                                                d_cfl, &d_status->gmax, &d_status->err, c->stream));
     else
         GF_CK(c, gf::launch_patch_update(m, d_work, nwork, c->d_phys, dt, nullptr, nullptr, maux, d_cfl,
@@ -881,3 +881,15 @@ int gf_level_tag4coarsening(gf_level* L, const gf_refine* rf, int nfam, const in
 }
 
 } // extern "C"
+
+/* Context access for the other host translation units (gf_forest.cpp). */
+namespace gf {
+cudaStream_t ctx_stream(gf_ctx* c) { return c->stream; }
+int ctx_device(gf_ctx* c) { return c->device; }
+bool ctx_exact(gf_ctx* c) { return c->exact; }
+const gf_phys* ctx_device_phys(gf_ctx* c) { return c->d_phys; }
+const gf_phys* ctx_host_phys(gf_ctx* c, int slot) { return &c->h_phys[slot]; }
+int ctx_check_phys(gf_ctx* c, int slot) { return check_phys_slot(c, slot); }
+int ctx_fail(gf_ctx* c, int code, const char* msg) { return fail(c, code, msg); }
+int ctx_cuda_fail(gf_ctx* c, cudaError_t e, const char* what) { return cuda_fail(c, e, what); }
+} // namespace gf

@@ -1,0 +1,1081 @@
+/*
+ * Multi-level forests on one GPU: the ForestClaw machinery around the
+ * patch update (quadtree leaves, 2:1 balance, ghost exchange between
+ * levels, regrid, outstyle-1 time stepping), restated for a device-resident
+ * slot pool. ForestClaw / p4est are external to the reference tree; the
+ * rules below are this file's statement of them, followed equally by the
+ * oracle's driver (oracle/forest.py):
+ *
+ *  - Leaves (level, I, J): I in [0, nbx*2^level), J in [0, nby*2^level).
+ *    Canonical order: level, then J, then I.
+ *  - Balance: leaves sharing a face or a corner differ by at most one
+ *    level. Refinement ripples outward (a leaf next to a split leaf two
+ *    levels finer splits too); a family coarsens only if every leaf along
+ *    the parent's boundary stays within one level.
+ *  - Ghost fill at t: (1) fine->coarse face and corner averages into coarse
+ *    ghost cells; (2) same-level copies and physical boundaries on every
+ *    leaf; (3) for each level above minlevel, coarse->fine face and corner
+ *    interpolation into its leaves, then the physical boundaries again on
+ *    those of them with a physical side. A corner that lies inside a
+ *    coarser neighbour's face is filled by that face's interpolation.
+ *  - Regrid (every regrid_interval accepted steps, after a ghost fill at
+ *    the new time): refinement tags on leaves below maxlevel, coarsening
+ *    tags on complete families above minlevel; tagged leaves split one
+ *    level; balance; families whose four leaves are tagged, unsplit, and
+ *    whose parent stays balanced merge; children take interpolate2fine of
+ *    their parent, parents average2coarse of their children; every new
+ *    patch takes its aux fields from the raster pyramid.
+ *  - Initialisation: leaves at minlevel, then initial-refinement passes
+ *    (init_flag = 1, no coarsening); every new patch takes the rasters.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "gf_internal.h"
+
+namespace {
+
+template <typename T>
+struct DArr {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t want)
+    {
+        if (want <= n) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t c = std::max<size_t>(want + want / 2, 16);
+        cudaError_t e = cudaMalloc(&p, c * sizeof(T));
+        if (e == cudaSuccess) n = c;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct Leaf {
+    int level, I, J, slot;
+};
+
+inline uint64_t lkey(int l, int I, int J)
+{
+    return ((uint64_t)l << 56) | ((uint64_t)(uint32_t)J << 28) | (uint64_t)(uint32_t)I;
+}
+
+inline bool canon_less(const Leaf& a, const Leaf& b)
+{
+    if (a.level != b.level) return a.level < b.level;
+    if (a.J != b.J) return a.J < b.J;
+    return a.I < b.I;
+}
+
+/* faces: left, right, bottom, top; corners: ll, lr, ul, ur */
+const int FDI[4] = {-1, 1, 0, 0}, FDJ[4] = {0, 0, -1, 1};
+const int CDI[4] = {-1, 1, -1, 1}, CDJ[4] = {-1, -1, 1, 1};
+
+} // namespace
+
+struct gf_forest {
+    gf_ctx* ctx = nullptr;
+    int device = 0; /* kept so that destroy does not need the context */
+    gf_forest_opts o{};
+    int M = 0;
+    long S = 0;
+    int nf = 0; /* raster fields: maux aux, then h, hu, hv */
+    int cap = 0;
+    /* raster pyramid: level l, field f at pyr[(l - minlevel) * nf + f] */
+    std::vector<double*> pyr;
+    /* slot pool */
+    double* qbuf[2] = {nullptr, nullptr};
+    double* aux = nullptr;
+    int par = 0; /* buffer holding the current state */
+    std::vector<int> free_slots;
+    /* leaves */
+    std::vector<Leaf> leaves;
+    std::unordered_map<uint64_t, int> index; /* key -> position in leaves */
+    /* boundary conditions */
+    gf_bc_spec bc{};
+    std::vector<double> hy_t, hy_hu;
+    /* tables of the current leaves (rebuilt after every change) */
+    bool dirty = true;
+    DArr<int> d_nbr;               /* 8 per slot */
+    DArr<gf_patch_geom> d_geom;    /* per slot   */
+    DArr<gf_patch_work> d_work;
+    DArr<gf_ghost_ref> d_refs_all;
+    DArr<gf_ghost_ref> d_refs_lv;  /* refresh lists, concatenated by level */
+    DArr<gf_xfer_task> d_avg[2];   /* per parity */
+    DArr<gf_xfer_task> d_itp[2];   /* concatenated by level, per parity */
+    DArr<gf_ghost_block> d_block;
+    DArr<double> d_gdt;
+    DArr<int> d_gpar;
+    DArr<unsigned long long> d_rb; /* [err][gmax] */
+    DArr<gf_tag_task> d_tagt;
+    DArr<int> d_tags;
+    DArr<gf_refine> d_refine;
+    DArr<gf_xfer_task> d_rgx;
+    DArr<gf_fill_task> d_fill;
+    int n_avg = 0;
+    std::vector<int> itp_off, itp_n, ref_off, ref_n; /* per level */
+    unsigned long long* h_rb = nullptr;              /* pinned */
+    long long cells = 0;                             /* interior cells of all leaves */
+    gf_forest_stats st{};
+};
+
+namespace {
+
+int ffail(gf_forest* f, int code, const char* msg) { return gf::ctx_fail(f->ctx, code, msg); }
+
+#define FK(f, call)                                                               \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) return gf::ctx_cuda_fail((f)->ctx, e_, #call);     \
+    } while (0)
+
+inline int nx_at(const gf_forest* f, int l) { return f->o.nbx * f->M << l; }
+inline int ny_at(const gf_forest* f, int l) { return f->o.nby * f->M << l; }
+inline int npx_at(const gf_forest* f, int l) { return f->o.nbx << l; }
+inline int npy_at(const gf_forest* f, int l) { return f->o.nby << l; }
+inline double dx_at(const gf_forest* f, int l) { return f->o.dx0 / (double)(1 << l); }
+inline double dy_at(const gf_forest* f, int l) { return f->o.dy0 / (double)(1 << l); }
+
+inline double* qslot(gf_forest* f, int b, int slot) { return f->qbuf[b] + (size_t)slot * 3 * f->S; }
+inline double* aslot(gf_forest* f, int slot) { return f->aux + (size_t)slot * f->o.maux * f->S; }
+
+int find(const gf_forest* f, int l, int I, int J)
+{
+    auto it = f->index.find(lkey(l, I, J));
+    return it == f->index.end() ? -1 : it->second;
+}
+
+/* leaf containing the level-l cell block (I, J) at level <= l, or -1 */
+int containing(const gf_forest* f, int l, int I, int J)
+{
+    for (int k = l; k >= f->o.minlevel; --k) {
+        int p = find(f, k, I >> (l - k), J >> (l - k));
+        if (p >= 0) return p;
+    }
+    return -1;
+}
+
+inline bool inside(const gf_forest* f, int l, int I, int J)
+{
+    return I >= 0 && J >= 0 && I < npx_at(f, l) && J < npy_at(f, l);
+}
+
+void reindex(gf_forest* f)
+{
+    std::sort(f->leaves.begin(), f->leaves.end(), canon_less);
+    f->index.clear();
+    f->index.reserve(f->leaves.size() * 2);
+    f->cells = 0;
+    for (size_t k = 0; k < f->leaves.size(); ++k) {
+        const Leaf& L = f->leaves[k];
+        f->index[lkey(L.level, L.I, L.J)] = (int)k;
+        f->cells += (long long)f->M * f->M;
+    }
+    f->dirty = true;
+}
+
+int alloc_slot(gf_forest* f)
+{
+    if (f->free_slots.empty()) return -1;
+    int s = f->free_slots.back();
+    f->free_slots.pop_back();
+    return s;
+}
+
+/* build the raster pyramid from the finest-level rasters (host) */
+int build_pyramid(gf_forest* f, const double* fields)
+{
+    const gf_forest_opts& o = f->o;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const int nlev = o.maxlevel - o.minlevel + 1;
+    f->pyr.assign((size_t)nlev * f->nf, nullptr);
+    for (int l = o.minlevel; l <= o.maxlevel; ++l)
+        for (int k = 0; k < f->nf; ++k) {
+            const size_t n = (size_t)(nx_at(f, l) + 2 * GF_MBC) * (ny_at(f, l) + 2 * GF_MBC);
+            FK(f, cudaMalloc(&f->pyr[(size_t)(l - o.minlevel) * f->nf + k], n * sizeof(double)));
+        }
+    const int nx = nx_at(f, o.maxlevel), ny = ny_at(f, o.maxlevel);
+    double* stage = nullptr;
+    FK(f, cudaMalloc(&stage, (size_t)nx * ny * sizeof(double)));
+    int rc = GF_OK;
+    for (int k = 0; k < f->nf && !rc; ++k) {
+        cudaError_t e = cudaMemcpyAsync(stage, fields + (size_t)k * nx * ny,
+                                        (size_t)nx * ny * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = gf::launch_pyramid_top(stage, f->pyr[(size_t)(o.maxlevel - o.minlevel) * f->nf + k], nx,
+                                       ny, st);
+        for (int l = o.maxlevel - 1; l >= o.minlevel && e == cudaSuccess; --l)
+            e = gf::launch_pyramid_down(f->pyr[(size_t)(l + 1 - o.minlevel) * f->nf + k],
+                                        f->pyr[(size_t)(l - o.minlevel) * f->nf + k], nx_at(f, l),
+                                        ny_at(f, l), st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st); /* the stage is reused */
+        if (e != cudaSuccess) rc = gf::ctx_cuda_fail(f->ctx, e, "raster pyramid");
+    }
+    cudaFree(stage);
+    return rc;
+}
+
+/* fill new leaves' planes from the pyramid: aux fields, and q when with_q */
+int fill_from_pyramid(gf_forest* f, const std::vector<Leaf>& fresh, bool with_q)
+{
+    if (fresh.empty()) return GF_OK;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    std::vector<gf_fill_task> t(fresh.size());
+    for (size_t k = 0; k < fresh.size(); ++k) {
+        const Leaf& L = fresh[k];
+        gf_fill_task& x = t[k];
+        std::memset(&x, 0, sizeof x);
+        int n = 0;
+        const size_t base = (size_t)(L.level - f->o.minlevel) * f->nf;
+        for (int a = 0; a < f->o.maux; ++a, ++n) {
+            x.src[n] = f->pyr[base + a];
+            x.dst[n] = aslot(f, L.slot) + (size_t)a * f->S;
+        }
+        if (with_q)
+            for (int m = 0; m < 3; ++m, ++n) {
+                x.src[n] = f->pyr[base + f->o.maux + m];
+                x.dst[n] = qslot(f, f->par, L.slot) + (size_t)m * f->S;
+            }
+        x.nfield = n;
+        x.nx = nx_at(f, L.level);
+        x.I = L.I;
+        x.J = L.J;
+    }
+    FK(f, f->d_fill.reserve(t.size()));
+    FK(f, cudaMemcpyAsync(f->d_fill.p, t.data(), t.size() * sizeof(gf_fill_task),
+                          cudaMemcpyHostToDevice, st));
+    FK(f, gf::launch_patch_fill(f->M, f->d_fill.p, (int)t.size(), st));
+    FK(f, cudaStreamSynchronize(st)); /* the task vector is pageable and about to go */
+    return GF_OK;
+}
+
+} // namespace
+
+namespace {
+
+gf_xfer_task xtask(gf_forest* f, int b, int kind, int cslot, int fslot, int code, int ox, int oy)
+{
+    gf_xfer_task t;
+    t.qc = qslot(f, b, cslot);
+    t.ac = aslot(f, cslot);
+    t.qf = qslot(f, b, fslot);
+    t.af = aslot(f, fslot);
+    t.kind = kind;
+    t.code = code;
+    t.ox = ox;
+    t.oy = oy;
+    t.phys = f->o.phys_slot;
+    return t;
+}
+
+/* Neighbour tables and transfer lists of the current leaves. */
+int build_tables(gf_forest* f)
+{
+    if (!f->dirty) return GF_OK;
+    const gf_forest_opts& o = f->o;
+    const int M = f->M;
+    const int nlev = o.maxlevel + 1;
+    std::vector<int> nbr((size_t)f->cap * 8, -1);
+    std::vector<gf_patch_geom> geom(f->cap, gf_patch_geom{0, 0, 1, 1});
+    std::vector<gf_patch_work> work(f->leaves.size(), gf_patch_work{});
+    std::vector<gf_ghost_ref> refs_all(f->leaves.size());
+    std::vector<gf_xfer_task> avg[2];
+    std::vector<std::vector<gf_xfer_task>> itp[2];
+    std::vector<std::vector<gf_ghost_ref>> refresh(nlev);
+    itp[0].resize(nlev);
+    itp[1].resize(nlev);
+    for (size_t k = 0; k < f->leaves.size(); ++k) {
+        const Leaf& P = f->leaves[k];
+        const int l = P.level, I = P.I, J = P.J, s = P.slot;
+        const double dx = dx_at(f, l), dy = dy_at(f, l);
+        geom[s] = {o.x0 + (double)I * M * dx, o.y0 + (double)J * M * dy, dx, dy};
+        gf_patch_work& w = work[k];
+        w.q = qslot(f, 0, s);
+        w.qout = qslot(f, 1, s);
+        w.aux = aslot(f, s);
+        w.dx = dx;
+        w.dy = dy;
+        w.phys = o.phys_slot;
+        w.group = 0;
+        refs_all[k] = gf_ghost_ref{0, s};
+        bool interp = false, physical = false;
+        for (int fc = 0; fc < 4; ++fc) {
+            const int NI = I + FDI[fc], NJ = J + FDJ[fc];
+            int& nb = nbr[(size_t)8 * s + fc];
+            if (!inside(f, l, NI, NJ)) {
+                nb = -1;
+                physical = true;
+                continue;
+            }
+            int q = find(f, l, NI, NJ);
+            if (q >= 0) {
+                nb = f->leaves[q].slot;
+                continue;
+            }
+            nb = -2;
+            q = l > o.minlevel ? find(f, l - 1, NI >> 1, NJ >> 1) : -1;
+            if (q >= 0) {
+                /* coarser neighbour: its face toward P is the opposite one */
+                const Leaf& C = f->leaves[q];
+                for (int b = 0; b < 2; ++b)
+                    itp[b][l].push_back(xtask(f, b, GF_XFER_INTERP_FACE, C.slot, s, fc ^ 1,
+                                              M * (2 * C.I - I), M * (2 * C.J - J)));
+                interp = true;
+                continue;
+            }
+            /* finer: the two children of the neighbour region next to P */
+            for (int c = 0; c < 2; ++c) {
+                int FI, FJ;
+                if (fc < 2) {
+                    FI = 2 * NI + (FDI[fc] < 0 ? 1 : 0);
+                    FJ = 2 * J + c;
+                } else {
+                    FI = 2 * I + c;
+                    FJ = 2 * NJ + (FDJ[fc] < 0 ? 1 : 0);
+                }
+                const int r = find(f, l + 1, FI, FJ);
+                if (r < 0) return ffail(f, GF_ERR_STATE, "forest is not 2:1 balanced across a face");
+                for (int b = 0; b < 2; ++b)
+                    avg[b].push_back(xtask(f, b, GF_XFER_AVG_FACE, s, f->leaves[r].slot, fc,
+                                           M * (2 * I - FI), M * (2 * J - FJ)));
+            }
+        }
+        for (int cc = 0; cc < 4; ++cc) {
+            const int DI = I + CDI[cc], DJ = J + CDJ[cc];
+            int& nb = nbr[(size_t)8 * s + 4 + cc];
+            if (!inside(f, l, DI, DJ)) {
+                nb = -1;
+                continue;
+            }
+            int q = find(f, l, DI, DJ);
+            if (q >= 0) {
+                nb = f->leaves[q].slot;
+                continue;
+            }
+            nb = -2;
+            q = l > o.minlevel ? find(f, l - 1, DI >> 1, DJ >> 1) : -1;
+            if (q >= 0) {
+                const Leaf& C = f->leaves[q];
+                const bool dxok = CDI[cc] > 0 ? 2 * C.I == DI : 2 * C.I + 1 == DI;
+                const bool dyok = CDJ[cc] > 0 ? 2 * C.J == DJ : 2 * C.J + 1 == DJ;
+                if (dxok && dyok) {
+                    /* diagonal coarser neighbour: its corner toward P is 3 - cc */
+                    for (int b = 0; b < 2; ++b)
+                        itp[b][l].push_back(xtask(f, b, GF_XFER_INTERP_CORNER, C.slot, s, 3 - cc,
+                                                  M * (2 * C.I - I), M * (2 * C.J - J)));
+                    interp = true;
+                }
+                /* otherwise the corner lies inside C's face: face interpolation fills it */
+                continue;
+            }
+            if (containing(f, l, DI, DJ) >= 0)
+                return ffail(f, GF_ERR_STATE, "forest is not 2:1 balanced across a corner");
+            const int FI = 2 * DI + (CDI[cc] < 0 ? 1 : 0), FJ = 2 * DJ + (CDJ[cc] < 0 ? 1 : 0);
+            const int r = find(f, l + 1, FI, FJ);
+            if (r < 0) return ffail(f, GF_ERR_STATE, "forest is not 2:1 balanced across a corner");
+            for (int b = 0; b < 2; ++b)
+                avg[b].push_back(xtask(f, b, GF_XFER_AVG_CORNER, s, f->leaves[r].slot, cc,
+                                       M * (2 * I - FI), M * (2 * J - FJ)));
+        }
+        if (interp && physical) refresh[l].push_back(gf_ghost_ref{0, s});
+    }
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    FK(f, f->d_nbr.reserve(nbr.size()));
+    FK(f, f->d_geom.reserve(geom.size()));
+    FK(f, f->d_work.reserve(work.size()));
+    FK(f, f->d_refs_all.reserve(refs_all.size()));
+    FK(f, cudaMemcpyAsync(f->d_nbr.p, nbr.data(), nbr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    FK(f, cudaMemcpyAsync(f->d_geom.p, geom.data(), geom.size() * sizeof(gf_patch_geom),
+                          cudaMemcpyHostToDevice, st));
+    FK(f, cudaMemcpyAsync(f->d_work.p, work.data(), work.size() * sizeof(gf_patch_work),
+                          cudaMemcpyHostToDevice, st));
+    FK(f, cudaMemcpyAsync(f->d_refs_all.p, refs_all.data(), refs_all.size() * sizeof(gf_ghost_ref),
+                          cudaMemcpyHostToDevice, st));
+    f->n_avg = (int)avg[0].size();
+    f->itp_off.assign(nlev, 0);
+    f->itp_n.assign(nlev, 0);
+    f->ref_off.assign(nlev, 0);
+    f->ref_n.assign(nlev, 0);
+    std::vector<gf_xfer_task> itp_all[2];
+    std::vector<gf_ghost_ref> ref_all;
+    for (int l = 0; l < nlev; ++l) {
+        f->itp_off[l] = (int)itp_all[0].size();
+        f->itp_n[l] = (int)itp[0][l].size();
+        for (int b = 0; b < 2; ++b) itp_all[b].insert(itp_all[b].end(), itp[b][l].begin(), itp[b][l].end());
+        f->ref_off[l] = (int)ref_all.size();
+        f->ref_n[l] = (int)refresh[l].size();
+        ref_all.insert(ref_all.end(), refresh[l].begin(), refresh[l].end());
+    }
+    for (int b = 0; b < 2; ++b) {
+        FK(f, f->d_avg[b].reserve(avg[b].size() + 1));
+        FK(f, f->d_itp[b].reserve(itp_all[b].size() + 1));
+        if (!avg[b].empty())
+            FK(f, cudaMemcpyAsync(f->d_avg[b].p, avg[b].data(), avg[b].size() * sizeof(gf_xfer_task),
+                                  cudaMemcpyHostToDevice, st));
+        if (!itp_all[b].empty())
+            FK(f, cudaMemcpyAsync(f->d_itp[b].p, itp_all[b].data(),
+                                  itp_all[b].size() * sizeof(gf_xfer_task), cudaMemcpyHostToDevice, st));
+    }
+    FK(f, f->d_refs_lv.reserve(ref_all.size() + 1));
+    if (!ref_all.empty())
+        FK(f, cudaMemcpyAsync(f->d_refs_lv.p, ref_all.data(), ref_all.size() * sizeof(gf_ghost_ref),
+                              cudaMemcpyHostToDevice, st));
+    FK(f, cudaStreamSynchronize(st)); /* host vectors go out of scope */
+    f->dirty = false;
+    return GF_OK;
+}
+
+/* hydrograph/hydrograh_module.f90:176-221, discharge type */
+double hydro_at(const gf_forest* f, double t)
+{
+    const size_t n = f->hy_t.size();
+    if (n == 0) return 0.0;
+    if (t < f->hy_t[0]) return f->hy_hu[0];
+    if (t > f->hy_t[n - 1]) return f->hy_hu[n - 1];
+    for (size_t i = 0; i + 1 < n; ++i)
+        if (t >= f->hy_t[i] && t <= f->hy_t[i + 1])
+            return f->hy_hu[i] + (f->hy_hu[i + 1] - f->hy_hu[i]) / (f->hy_t[i + 1] - f->hy_t[i]) *
+                                     (t - f->hy_t[i]);
+    return 0.0;
+}
+
+int ghost_fill(gf_forest* f, double t)
+{
+    int rc = build_tables(f);
+    if (rc) return rc;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const gf_phys* phys = gf::ctx_device_phys(f->ctx);
+    gf_ghost_block blk{};
+    blk.q = f->qbuf[f->par];
+    blk.aux = f->aux;
+    blk.nbr = f->d_nbr.p;
+    blk.geom = f->d_geom.p;
+    blk.phys_of = nullptr;
+    blk.bc = f->bc;
+    blk.bc.q0hu = hydro_at(f, t);
+    blk.phys = f->o.phys_slot;
+    blk.maux = f->o.maux;
+    blk.skip = 0;
+    FK(f, f->d_block.reserve(1));
+    /* pageable source: staged before the call returns */
+    FK(f, cudaMemcpyAsync(f->d_block.p, &blk, sizeof blk, cudaMemcpyHostToDevice, st));
+    if (f->n_avg) FK(f, gf::launch_transfer(f->M, f->d_avg[f->par].p, f->n_avg, phys, st));
+    FK(f, gf::launch_ghost_fill(f->M, f->d_block.p, f->d_refs_all.p, (int)f->leaves.size(), phys, st));
+    for (int l = f->o.minlevel + 1; l <= f->o.maxlevel; ++l) {
+        if (f->itp_n[l])
+            FK(f, gf::launch_transfer(f->M, f->d_itp[f->par].p + f->itp_off[l], f->itp_n[l], phys, st));
+        if (f->ref_n[l])
+            FK(f, gf::launch_ghost_fill(f->M, f->d_block.p, f->d_refs_lv.p + f->ref_off[l], f->ref_n[l],
+                                        phys, st));
+    }
+    return GF_OK;
+}
+
+int step(gf_forest* f, double t, double dt, double* cfl)
+{
+    int rc = ghost_fill(f, t);
+    if (rc) return rc;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    FK(f, f->d_gdt.reserve(1));
+    FK(f, f->d_gpar.reserve(1));
+    FK(f, f->d_rb.reserve(2));
+    FK(f, cudaMemcpyAsync(f->d_gdt.p, &dt, sizeof dt, cudaMemcpyHostToDevice, st));
+    FK(f, cudaMemcpyAsync(f->d_gpar.p, &f->par, sizeof(int), cudaMemcpyHostToDevice, st));
+    FK(f, cudaMemsetAsync(f->d_rb.p, 0, 2 * sizeof(unsigned long long), st));
+    const gf_phys* phys = gf::ctx_device_phys(f->ctx);
+    int* err = reinterpret_cast<int*>(f->d_rb.p);
+    if (gf::ctx_exact(f->ctx))
+        FK(f, gf::launch_patch_update_exact(f->M, f->d_work.p, (int)f->leaves.size(), phys, 0.0,
+                                            f->d_gdt.p, f->d_gpar.p, f->o.maux, nullptr, f->d_rb.p + 1,
+                                            err, st));
+    else
+        FK(f, gf::launch_patch_update(f->M, f->d_work.p, (int)f->leaves.size(), phys, 0.0, f->d_gdt.p,
+                                      f->d_gpar.p, f->o.maux, nullptr, f->d_rb.p + 1, err, st));
+    FK(f, cudaMemcpyAsync(f->h_rb, f->d_rb.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    FK(f, cudaStreamSynchronize(st));
+    if ((int)f->h_rb[0]) return ffail(f, GF_ERR_DEVICE, "a patch-update copy wait timed out");
+    double c;
+    std::memcpy(&c, &f->h_rb[1], sizeof c);
+    if (cfl) *cfl = c;
+    return GF_OK;
+}
+
+} // namespace
+
+namespace {
+
+/* Refinement tags (leaves below maxlevel) and coarsening tags (complete
+ * families above minlevel, children ll, lr, ul, ur). */
+int run_tags(gf_forest* f, double t, int init_flag, std::vector<char>& refine,
+             std::vector<std::array<int, 4>>& fams, std::vector<char>& coarsen)
+{
+    const gf_forest_opts& o = f->o;
+    std::vector<gf_tag_task> tk;
+    std::vector<int> who;
+    for (size_t k = 0; k < f->leaves.size(); ++k) {
+        const Leaf& L = f->leaves[k];
+        if (L.level >= o.maxlevel) continue;
+        gf_tag_task x;
+        std::memset(&x, 0, sizeof x);
+        x.q[0] = qslot(f, f->par, L.slot);
+        x.aux[0] = aslot(f, L.slot);
+        x.xlower[0] = o.x0 + (double)L.I * f->M * dx_at(f, L.level);
+        x.ylower[0] = o.y0 + (double)L.J * f->M * dy_at(f, L.level);
+        x.dx = dx_at(f, L.level);
+        x.dy = dy_at(f, L.level);
+        x.level = L.level;
+        x.nsib = 1;
+        x.phys = o.phys_slot;
+        tk.push_back(x);
+        who.push_back((int)k);
+    }
+    const size_t nref = tk.size();
+    fams.clear();
+    if (!init_flag) {
+        for (size_t k = 0; k < f->leaves.size(); ++k) {
+            const Leaf& L = f->leaves[k];
+            if (L.level <= o.minlevel || (L.I & 1) || (L.J & 1)) continue;
+            std::array<int, 4> fam;
+            bool full = true;
+            for (int c = 0; c < 4 && full; ++c) {
+                fam[c] = find(f, L.level, L.I + (c & 1), L.J + (c >> 1));
+                full = fam[c] >= 0;
+            }
+            if (!full) continue;
+            gf_tag_task x;
+            std::memset(&x, 0, sizeof x);
+            for (int c = 0; c < 4; ++c) {
+                const Leaf& C = f->leaves[fam[c]];
+                x.q[c] = qslot(f, f->par, C.slot);
+                x.aux[c] = aslot(f, C.slot);
+                x.xlower[c] = o.x0 + (double)C.I * f->M * dx_at(f, C.level);
+                x.ylower[c] = o.y0 + (double)C.J * f->M * dy_at(f, C.level);
+            }
+            x.dx = dx_at(f, L.level);
+            x.dy = dy_at(f, L.level);
+            x.level = L.level;
+            x.nsib = 4;
+            x.phys = o.phys_slot;
+            tk.push_back(x);
+            fams.push_back(fam);
+        }
+    }
+    refine.assign(f->leaves.size(), 0);
+    coarsen.assign(fams.size(), 0);
+    if (tk.empty()) return GF_OK;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    std::vector<int> tags(tk.size());
+    FK(f, f->d_tagt.reserve(tk.size()));
+    FK(f, f->d_tags.reserve(tk.size()));
+    FK(f, f->d_refine.reserve(1));
+    FK(f, cudaMemcpyAsync(f->d_refine.p, &o.refine, sizeof(gf_refine), cudaMemcpyHostToDevice, st));
+    FK(f, cudaMemcpyAsync(f->d_tagt.p, tk.data(), tk.size() * sizeof(gf_tag_task), cudaMemcpyHostToDevice, st));
+    FK(f, gf::launch_tags(f->M, f->d_tagt.p, (int)tk.size(), f->d_refine.p, gf::ctx_device_phys(f->ctx),
+                          o.maxlevel, init_flag, t, f->d_tags.p, st));
+    FK(f, cudaMemcpyAsync(tags.data(), f->d_tags.p, tk.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+    FK(f, cudaStreamSynchronize(st));
+    for (size_t k = 0; k < nref; ++k) refine[who[k]] = tags[k] != 0;
+    for (size_t k = 0; k < fams.size(); ++k) coarsen[k] = tags[nref + k] != 0;
+    return GF_OK;
+}
+
+/* Grow the split set until the refined forest is 2:1 balanced. */
+void balance_splits(const gf_forest* f, std::vector<char>& split)
+{
+    std::vector<int> work;
+    for (size_t k = 0; k < split.size(); ++k)
+        if (split[k]) work.push_back((int)k);
+    while (!work.empty()) {
+        const int k = work.back();
+        work.pop_back();
+        const Leaf& P = f->leaves[k];
+        const int l = P.level;
+        for (int d = 0; d < 8; ++d) {
+            const int di = d < 4 ? FDI[d] : CDI[d - 4], dj = d < 4 ? FDJ[d] : CDJ[d - 4];
+            const int NI = P.I + di, NJ = P.J + dj;
+            if (!inside(f, l, NI, NJ)) continue;
+            const int q = containing(f, l, NI, NJ);
+            if (q < 0) continue; /* finer there */
+            if (f->leaves[q].level <= l - 1 && !split[q]) {
+                split[q] = 1; /* P's children at l + 1 would touch a leaf at <= l - 1 */
+                work.push_back(q);
+            }
+        }
+    }
+}
+
+/* May the family under parent (l - 1, PI, PJ) merge, given the splits? */
+bool family_can_merge(const gf_forest* f, int l, int PI, int PJ, const std::vector<char>& split)
+{
+    /* leaves along the parent's boundary, as level-l cell blocks */
+    for (int a = -1; a <= 2; ++a)
+        for (int b = -1; b <= 2; ++b) {
+            if (a >= 0 && a <= 1 && b >= 0 && b <= 1) continue;
+            const int I = 2 * PI + a, J = 2 * PJ + b;
+            if (!inside(f, l, I, J)) continue;
+            const int q = containing(f, l, I, J);
+            if (q < 0) return false;                                   /* finer than l */
+            if (f->leaves[q].level == l && split[q]) return false;     /* will be l + 1 */
+        }
+    return true;
+}
+
+} // namespace
+
+namespace {
+
+/* Replace split leaves by their children and merged families by their
+ * parents. Children / parents take interpolate2fine / average2coarse of
+ * the current state (or, at initialisation, the rasters); every new patch
+ * takes its aux fields from the pyramid. */
+int apply_changes(gf_forest* f, const std::vector<char>& split,
+                  const std::vector<std::array<int, 4>>& fams, const std::vector<char>& merge,
+                  bool init, bool* changed)
+{
+    size_t need = 0;
+    std::vector<char> in_merge(f->leaves.size(), 0);
+    for (size_t k = 0; k < split.size(); ++k) need += split[k] ? 4 : 0;
+    for (size_t m = 0; m < fams.size(); ++m)
+        if (merge[m]) {
+            need += 1;
+            for (int c = 0; c < 4; ++c) in_merge[fams[m][c]] = 1;
+        }
+    if (changed) *changed = need > 0;
+    if (need == 0) return GF_OK;
+    if (need > f->free_slots.size())
+        return ffail(f, GF_ERR_NOMEM, "forest slot pool exhausted (raise max_patches)");
+    std::vector<Leaf> next, fresh;
+    std::vector<gf_xfer_task> xt;
+    std::vector<int> freed;
+    const int b = f->par;
+    for (size_t k = 0; k < f->leaves.size(); ++k) {
+        const Leaf& P = f->leaves[k];
+        if (in_merge[k]) continue;
+        if (!split[k]) {
+            next.push_back(P);
+            continue;
+        }
+        for (int c = 0; c < 4; ++c) {
+            Leaf C{P.level + 1, 2 * P.I + (c & 1), 2 * P.J + (c >> 1), alloc_slot(f)};
+            next.push_back(C);
+            fresh.push_back(C);
+            if (!init) xt.push_back(xtask(f, b, GF_XFER_INTERP2FINE, P.slot, C.slot, c, 0, 0));
+        }
+        freed.push_back(P.slot);
+    }
+    for (size_t m = 0; m < fams.size(); ++m) {
+        if (!merge[m]) continue;
+        const Leaf& C0 = f->leaves[fams[m][0]];
+        Leaf Pn{C0.level - 1, C0.I >> 1, C0.J >> 1, alloc_slot(f)};
+        next.push_back(Pn);
+        fresh.push_back(Pn);
+        for (int c = 0; c < 4; ++c) {
+            const Leaf& C = f->leaves[fams[m][c]];
+            xt.push_back(xtask(f, b, GF_XFER_AVG2COARSE, Pn.slot, C.slot, c, 0, 0));
+            freed.push_back(C.slot);
+        }
+    }
+    int rc = fill_from_pyramid(f, fresh, init);
+    if (rc) return rc;
+    if (!xt.empty()) {
+        cudaStream_t st = gf::ctx_stream(f->ctx);
+        FK(f, f->d_rgx.reserve(xt.size()));
+        FK(f, cudaMemcpyAsync(f->d_rgx.p, xt.data(), xt.size() * sizeof(gf_xfer_task),
+                              cudaMemcpyHostToDevice, st));
+        FK(f, gf::launch_transfer(f->M, f->d_rgx.p, (int)xt.size(), gf::ctx_device_phys(f->ctx), st));
+        FK(f, cudaStreamSynchronize(st));
+    }
+    /* old slots return to the pool only after the transfers read them */
+    for (int s : freed) f->free_slots.push_back(s);
+    f->leaves.swap(next);
+    reindex(f);
+    f->st.npatch = (int)f->leaves.size();
+    f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+    return GF_OK;
+}
+
+int regrid(gf_forest* f, double t, bool* changed)
+{
+    int rc = ghost_fill(f, t);
+    if (rc) return rc;
+    std::vector<char> refine, coarsen;
+    std::vector<std::array<int, 4>> fams;
+    if ((rc = run_tags(f, t, 0, refine, fams, coarsen))) return rc;
+    std::vector<char> split = refine;
+    balance_splits(f, split);
+    std::vector<char> merge(fams.size(), 0);
+    for (size_t m = 0; m < fams.size(); ++m) {
+        if (!coarsen[m]) continue;
+        bool any_split = false;
+        for (int c = 0; c < 4; ++c) any_split |= split[fams[m][c]] != 0;
+        const Leaf& C0 = f->leaves[fams[m][0]];
+        merge[m] = !any_split && family_can_merge(f, C0.level, C0.I >> 1, C0.J >> 1, split);
+    }
+    rc = apply_changes(f, split, fams, merge, false, changed);
+    if (!rc) f->st.regrids++;
+    return rc;
+}
+
+int init_forest(gf_forest* f)
+{
+    const gf_forest_opts& o = f->o;
+    /* all slots free, leaves at minlevel */
+    f->free_slots.clear();
+    for (int s = f->cap - 1; s >= 0; --s) f->free_slots.push_back(s);
+    f->leaves.clear();
+    const size_t n0 = (size_t)npx_at(f, o.minlevel) * npy_at(f, o.minlevel);
+    if (n0 > f->free_slots.size()) return ffail(f, GF_ERR_NOMEM, "max_patches below the minlevel patch count");
+    for (int J = 0; J < npy_at(f, o.minlevel); ++J)
+        for (int I = 0; I < npx_at(f, o.minlevel); ++I)
+            f->leaves.push_back(Leaf{o.minlevel, I, J, alloc_slot(f)});
+    f->par = 0;
+    reindex(f);
+    int rc = fill_from_pyramid(f, f->leaves, true);
+    if (rc) return rc;
+    f->st = gf_forest_stats{};
+    for (int pass = o.minlevel; pass < o.maxlevel; ++pass) {
+        std::vector<char> refine, coarsen;
+        std::vector<std::array<int, 4>> fams;
+        if ((rc = run_tags(f, 0.0, 1, refine, fams, coarsen))) return rc;
+        std::vector<char> split = refine;
+        balance_splits(f, split);
+        bool changed = false;
+        if ((rc = apply_changes(f, split, fams, std::vector<char>(fams.size(), 0), true, &changed)))
+            return rc;
+        if (!changed) break;
+    }
+    f->st.npatch = (int)f->leaves.size();
+    f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+    return build_tables(f);
+}
+
+/* ForestClaw outstyle 1 (fc2d_geoclaw_run.c:190-395) with variable dt,
+ * reduce_cfl, advance-one-step (the step is the minlevel dt over
+ * 2^(maxlevel - minlevel)) and no subcycling. */
+int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
+                  double max_cfl, int max_steps)
+{
+    const gf_forest_opts& o = f->o;
+    const double level_factor = (double)(1 << (o.maxlevel - o.minlevel));
+    const double dt_outer = t_final / nout;
+    double t_curr = f->st.t;
+    double dt_minlevel = initial_dt;
+    long long taken = 0;
+    for (int n = 0; n < nout; ++n) {
+        const double tend = t_curr + dt_outer;
+        while (t_curr < tend) {
+            if (max_steps > 0 && taken >= max_steps) goto out;
+            double dt_step = dt_minlevel / level_factor;
+            const double tol = 1e-2 * dt_step;
+            bool took_small = false;
+            const double small_step = tend - (t_curr + dt_step);
+            if (small_step < tol) {
+                dt_step = tend - t_curr;
+                if (small_step < 0) took_small = true;
+            }
+            double cfl = 0.0;
+            int rc = step(f, t_curr, dt_step, &cfl);
+            if (rc) return rc;
+            ++taken;
+            f->st.max_cfl_seen = std::max(f->st.max_cfl_seen, cfl);
+            if (cfl > max_cfl) {
+                dt_minlevel = dt_minlevel * desired_cfl / cfl;
+                f->st.rejects++;
+                continue;
+            }
+            f->par ^= 1;
+            f->st.steps++;
+            f->st.cell_updates += f->cells;
+            t_curr += dt_step;
+            const double dt_new = dt_minlevel * desired_cfl / cfl;
+            if (!took_small) dt_minlevel = dt_new;
+            f->st.t = t_curr;
+            f->st.dt = dt_minlevel;
+            if (o.regrid_interval > 0 && f->st.steps % o.regrid_interval == 0) {
+                bool changed = false;
+                if ((rc = regrid(f, t_curr, &changed))) return rc;
+            }
+        }
+    }
+out:
+    f->st.t = t_curr;
+    f->st.dt = dt_minlevel;
+    return GF_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+void gf_forest_opts_default(gf_forest_opts* o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->mx = 16;
+    o->maux = 1;
+    o->nbx = o->nby = 1;
+    o->minlevel = 0;
+    o->maxlevel = 0;
+    o->dx0 = o->dy0 = 1.0;
+    for (int s = 0; s < 4; ++s) o->mthbc[s] = 1;
+    o->regrid_interval = 0;
+    o->refine.wave_tolerance = 0.1;
+    o->refine.speed_tolerance[0] = 1e12;
+    o->refine.num_speed_tolerance = 1;
+    o->refine.deep_depth = 1e10;
+    o->refine.max_level_deep = 0;
+    o->refine.max_velocity_depth_product = 1e20;
+}
+
+void gf_forest_destroy(gf_forest* f)
+{
+    if (!f) return;
+    /* the caller destroys forests before their context; the frees below
+     * synchronise the device, so no stream of the context is needed */
+    cudaSetDevice(f->device);
+    for (double* p : f->pyr)
+        if (p) cudaFree(p);
+    for (int b = 0; b < 2; ++b)
+        if (f->qbuf[b]) cudaFree(f->qbuf[b]);
+    if (f->aux) cudaFree(f->aux);
+    f->d_nbr.release();
+    f->d_geom.release();
+    f->d_work.release();
+    f->d_refs_all.release();
+    f->d_refs_lv.release();
+    for (int b = 0; b < 2; ++b) {
+        f->d_avg[b].release();
+        f->d_itp[b].release();
+    }
+    f->d_block.release();
+    f->d_gdt.release();
+    f->d_gpar.release();
+    f->d_rb.release();
+    f->d_tagt.release();
+    f->d_tags.release();
+    f->d_refine.release();
+    f->d_rgx.release();
+    f->d_fill.release();
+    if (f->h_rb) cudaFreeHost(f->h_rb);
+    delete f;
+}
+
+int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, gf_forest** out)
+{
+    if (!c || !o || !fields || !out) return GF_ERR_ARG;
+    *out = nullptr;
+    if (!(o->mx == 8 || o->mx == 16 || o->mx == 32)) return gf::ctx_fail(c, GF_ERR_ARG, "mx must be 8, 16 or 32");
+    if (o->maux < 1 || o->maux > 3) return gf::ctx_fail(c, GF_ERR_ARG, "maux must be 1..3");
+    if (o->nbx < 1 || o->nby < 1) return gf::ctx_fail(c, GF_ERR_ARG, "nbx, nby must be positive");
+    if (o->minlevel < 0 || o->maxlevel < o->minlevel || o->maxlevel > 10)
+        return gf::ctx_fail(c, GF_ERR_ARG, "need 0 <= minlevel <= maxlevel <= 10");
+    if (!(o->dx0 > 0) || !(o->dy0 > 0)) return gf::ctx_fail(c, GF_ERR_ARG, "dx0, dy0 must be positive");
+    for (int s = 0; s < 4; ++s)
+        if (!(o->mthbc[s] == 0 || o->mthbc[s] == 1 || o->mthbc[s] == 3))
+            return gf::ctx_fail(c, GF_ERR_ARG, "forest mthbc must be 0, 1 or 3");
+    if (o->regrid_interval < 0) return gf::ctx_fail(c, GF_ERR_ARG, "regrid_interval must be >= 0");
+    int rc = gf::ctx_check_phys(c, o->phys_slot);
+    if (rc) return rc;
+    const long long full = (long long)o->nbx * o->nby << (2 * o->maxlevel);
+    long long cap = o->max_patches > 0 ? std::min<long long>(o->max_patches, full) : full;
+    if (cap > (1LL << 22)) return gf::ctx_fail(c, GF_ERR_ARG, "set max_patches (full refinement is too large)");
+    gf_forest* f = new gf_forest;
+    f->ctx = c;
+    f->device = gf::ctx_device(c);
+    f->o = *o;
+    f->M = o->mx;
+    f->S = (long)(o->mx + 2 * GF_MBC) * (o->mx + 2 * GF_MBC);
+    f->nf = o->maux + 3;
+    f->cap = (int)cap;
+    for (int s = 0; s < 4; ++s) f->bc.mthbc[s] = o->mthbc[s];
+    cudaError_t e = cudaSetDevice(gf::ctx_device(c));
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b)
+        e = cudaMalloc(&f->qbuf[b], (size_t)cap * 3 * f->S * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&f->aux, (size_t)cap * o->maux * f->S * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&f->h_rb, 2 * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        gf_forest_destroy(f);
+        return gf::ctx_cuda_fail(c, e, "forest pool allocation");
+    }
+    if ((rc = build_pyramid(f, fields))) {
+        gf_forest_destroy(f);
+        return rc;
+    }
+    *out = f;
+    return GF_OK;
+}
+
+int gf_forest_set_hydrograph(gf_forest* f, int n, const double* time, const double* hu,
+                             const int* side, double width, double x0, double y0)
+{
+    if (!f || n < 0 || (n > 0 && (!time || !hu || !side))) return GF_ERR_ARG;
+    for (int i = 1; i < n; ++i)
+        if (!(time[i] >= time[i - 1])) return ffail(f, GF_ERR_ARG, "hydrograph times must increase");
+    f->hy_t.assign(time, time + n);
+    f->hy_hu.assign(hu, hu + n);
+    for (int s = 0; s < 4; ++s) f->bc.hydro_side[s] = n > 0 ? (side[s] != 0) : 0;
+    f->bc.width = width;
+    f->bc.x0 = x0;
+    f->bc.y0 = y0;
+    return GF_OK;
+}
+
+int gf_forest_init(gf_forest* f)
+{
+    if (!f) return GF_ERR_ARG;
+    for (int s = 0; s < 4; ++s)
+        if (f->o.mthbc[s] == 0 && !f->bc.hydro_side[s])
+            return ffail(f, GF_ERR_ARG, "mthbc = 0 needs a hydrograph on that side (the reference stops here)");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return init_forest(f);
+}
+
+int gf_forest_ghost_fill(gf_forest* f, double t)
+{
+    if (!f) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    int rc = ghost_fill(f, t);
+    if (rc) return rc;
+    FK(f, cudaStreamSynchronize(gf::ctx_stream(f->ctx)));
+    return GF_OK;
+}
+
+int gf_forest_step(gf_forest* f, double t, double dt, double* cfl)
+{
+    if (!f || !(dt > 0)) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return step(f, t, dt, cfl);
+}
+
+int gf_forest_accept(gf_forest* f, int accept)
+{
+    if (!f) return GF_ERR_ARG;
+    if (accept) {
+        f->par ^= 1;
+        f->st.steps++;
+        f->st.cell_updates += f->cells;
+    } else {
+        f->st.rejects++;
+    }
+    return GF_OK;
+}
+
+int gf_forest_regrid(gf_forest* f, double t, int* changed)
+{
+    if (!f) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    bool ch = false;
+    int rc = regrid(f, t, &ch);
+    if (changed) *changed = ch;
+    return rc;
+}
+
+int gf_forest_run(gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
+                  double max_cfl, int max_steps, gf_forest_stats* st)
+{
+    if (!f || !(t_final > 0) || nout < 1 || !(initial_dt > 0) || !(desired_cfl > 0) || !(max_cfl > 0))
+        return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    int rc = run_outstyle1(f, t_final, nout, initial_dt, desired_cfl, max_cfl, max_steps);
+    if (st) gf_forest_get_stats(f, st);
+    return rc;
+}
+
+int gf_forest_get_stats(gf_forest* f, gf_forest_stats* st)
+{
+    if (!f || !st) return GF_ERR_ARG;
+    *st = f->st;
+    st->npatch = (int)f->leaves.size();
+    st->levels_used = 0;
+    for (const Leaf& L : f->leaves) st->levels_used = std::max(st->levels_used, L.level);
+    return GF_OK;
+}
+
+int gf_forest_npatch(const gf_forest* f) { return f ? (int)f->leaves.size() : -1; }
+
+int gf_forest_patches(const gf_forest* f, int* level, int* I, int* J)
+{
+    if (!f) return GF_ERR_ARG;
+    for (size_t k = 0; k < f->leaves.size(); ++k) {
+        if (level) level[k] = f->leaves[k].level;
+        if (I) I[k] = f->leaves[k].I;
+        if (J) J[k] = f->leaves[k].J;
+    }
+    return GF_OK;
+}
+
+} // extern "C"
+
+namespace {
+
+/* planes of the leaves' slots <-> Fortran layout in canonical order */
+int move_leaves(gf_forest* f, double* host, int nfield, bool to_host, bool aux)
+{
+    const size_t per = (size_t)nfield * f->S;
+    const size_t n = f->leaves.size();
+    std::vector<double> tmp(per);
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    for (size_t k = 0; k < n; ++k) {
+        const int s = f->leaves[k].slot;
+        double* dev = aux ? aslot(f, s) : qslot(f, f->par, s);
+        double* h = host + k * per;
+        if (to_host) {
+            FK(f, cudaMemcpyAsync(tmp.data(), dev, per * sizeof(double), cudaMemcpyDeviceToHost, st));
+            FK(f, cudaStreamSynchronize(st));
+            for (long c = 0; c < f->S; ++c)
+                for (int m = 0; m < nfield; ++m) h[(size_t)c * nfield + m] = tmp[(size_t)m * f->S + c];
+        } else {
+            for (long c = 0; c < f->S; ++c)
+                for (int m = 0; m < nfield; ++m) tmp[(size_t)m * f->S + c] = h[(size_t)c * nfield + m];
+            FK(f, cudaMemcpyAsync(dev, tmp.data(), per * sizeof(double), cudaMemcpyHostToDevice, st));
+            FK(f, cudaStreamSynchronize(st));
+        }
+    }
+    return GF_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int gf_forest_download(gf_forest* f, double* q)
+{
+    if (!f || !q) return GF_ERR_ARG;
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return move_leaves(f, q, 3, true, false);
+}
+
+int gf_forest_download_aux(gf_forest* f, double* aux)
+{
+    if (!f || !aux) return GF_ERR_ARG;
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return move_leaves(f, aux, f->o.maux, true, true);
+}
+
+int gf_forest_upload(gf_forest* f, const double* q)
+{
+    if (!f || !q) return GF_ERR_ARG;
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return move_leaves(f, const_cast<double*>(q), 3, false, false);
+}
+
+} // extern "C"

@@ -20,9 +20,9 @@ cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, con
 size_t patch_update_smem_bytes(int m);
 int patch_update_occupancy(int m); /* resident CTAs per SM */
 cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwork,
-                                      const gf_phys* phys, double dt, const double* gdt, int maux,
-                                      double* cfl, unsigned long long* gmax, int* err,
-                                      cudaStream_t st);
+                                      const gf_phys* phys, double dt, const double* gdt,
+                                      const int* gpar, int maux, double* cfl,
+                                      unsigned long long* gmax, int* err, cudaStream_t st);
 
 cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int ncell, int nf,
                               long src_stride, long dst_stride, cudaStream_t st);
@@ -49,6 +49,22 @@ cudaError_t launch_timeinterp(int m, const gf_tinterp_task* tasks, int ntask, do
 cudaError_t launch_tags(int m, const gf_tag_task* tasks, int ntask, const gf_refine* rf,
                         const gf_phys* phys, int maxlevel, int init_flag, double t, int* tags,
                         cudaStream_t st);
+
+/* Context access from host translation units other than gf_capi.cpp. */
+cudaStream_t ctx_stream(gf_ctx* c);
+int ctx_device(gf_ctx* c);
+bool ctx_exact(gf_ctx* c); /* contraction-free update build selected */
+const gf_phys* ctx_device_phys(gf_ctx* c);
+const gf_phys* ctx_host_phys(gf_ctx* c, int slot);
+int ctx_check_phys(gf_ctx* c, int slot);
+int ctx_fail(gf_ctx* c, int code, const char* msg);
+int ctx_cuda_fail(gf_ctx* c, cudaError_t e, const char* what);
+
+/* Forest raster pyramid (gf_forest_kernels.cu); levels are padded by 2. */
+cudaError_t launch_pyramid_top(const double* src, double* dst, int nx, int ny, cudaStream_t st);
+cudaError_t launch_pyramid_down(const double* fine, double* coarse, int nxc, int nyc,
+                                cudaStream_t st);
+cudaError_t launch_patch_fill(int m, const gf_fill_task* tasks, int ntask, cudaStream_t st);
 
 } // namespace gf
 

@@ -17,7 +17,7 @@ namespace gf {
 
 template <int M, int NT, int RB>
 static cudaError_t launch_exact(const gf_patch_work* work, int nwork, const gf_phys* phys,
-                                double dt, const double* gdt, int maux, double* cfl,
+                                double dt, const double* gdt, const int* gpar, int maux, double* cfl,
                                 unsigned long long* gmax, int* err, cudaStream_t st)
 {
     using L = gf_exact::Smem<M, RB, true>;
@@ -30,19 +30,19 @@ static cudaError_t launch_exact(const gf_patch_work* work, int nwork, const gf_p
         attr_set = true;
     }
     if (nwork <= 0) return cudaSuccess;
-    kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, nullptr, maux, cfl, gmax, err);
+    kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwork,
-                                      const gf_phys* phys, double dt, const double* gdt, int maux,
-                                      double* cfl, unsigned long long* gmax, int* err,
-                                      cudaStream_t st)
+                                      const gf_phys* phys, double dt, const double* gdt,
+                                      const int* gpar, int maux, double* cfl,
+                                      unsigned long long* gmax, int* err, cudaStream_t st)
 {
     switch (m) {
-    case 32: return launch_exact<32, 256, 4>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
-    case 16: return launch_exact<16, 128, 6>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
-    case 8: return launch_exact<8, 64, 5>(work, nwork, phys, dt, gdt, maux, cfl, gmax, err, st);
+    case 32: return launch_exact<32, 256, 4>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, st);
+    case 16: return launch_exact<16, 128, 6>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, st);
+    case 8: return launch_exact<8, 64, 5>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, st);
     default: return cudaErrorInvalidValue;
     }
 }

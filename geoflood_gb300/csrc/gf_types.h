@@ -77,6 +77,19 @@ typedef struct gf_group_state {
     int pad;
 } gf_group_state;
 
+/* Fill of one patch's planes from pyramid windows (gf_forest_kernels.cu):
+ * field f of the patch (slot planes dst[f]) is the (mx+4)^2 window of the
+ * padded level raster src[f] (row length nx + 4) starting at patch
+ * (I, J) of that level. */
+#define GF_FILL_MAX_FIELDS 8
+typedef struct gf_fill_task {
+    const double* src[GF_FILL_MAX_FIELDS];
+    double* dst[GF_FILL_MAX_FIELDS];
+    int nfield;
+    int nx;          /* interior cells per row of the level */
+    int I, J;        /* patch index at that level */
+} gf_fill_task;
+
 /* One coarse/fine transfer (gf_amr.cu): kind GF_XFER_*, code = coarse
  * face / corner or child index, (ox, oy) = fine index of the coarse patch's
  * lower-left corner minus one. */

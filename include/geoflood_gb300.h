@@ -299,6 +299,83 @@ int gf_patch_update_noalloc(int device, const gf_phys* phys, int npatch,
                             double* q, const double* aux, double* cfl,
                             double* maxcfl, void* stream);
 
+/* ------------------------------------------------ multi-level forests */
+/* A forest of nbx x nby root blocks refined as quadtrees between minlevel
+ * and maxlevel, patches of mx x mx cells, resident on the device. This is
+ * the ForestClaw level machinery the patch-update path sits in, restated
+ * for one GPU (ForestClaw itself is an external library, absent from the
+ * reference tree): leaves with full (face and corner) 2:1 balance; ghost
+ * fill = fine->coarse averages (fc2d_geoclaw_average_fort.f:33,323), same-
+ * level copies and physical boundaries (fc2d_geoclaw_copy_fort.f,
+ * geoflood_bc2_fort.f90), then coarse->fine interpolation level by level
+ * (fc2d_geoclaw_interpolate_fort.f:24,261) with the boundaries re-applied
+ * to interpolated patches; regrid from the reference's tags
+ * (fc2d_geoclaw_tag4refinement_fort.f90, _tag4coarsening_fort.f90) with
+ * interpolate2fine / average2coarse for the new patches; time stepping by
+ * outstyle 1 (fc2d_geoclaw_run.c:190-395) with all levels advanced by the
+ * same step (subcycle = F, advance-one-step = T, as the reference's
+ * examples set them) and a regrid every regrid_interval accepted steps.
+ *
+ * Static fields and the initial state come as rasters at the finest level
+ * (maxlevel): maux aux fields then h, hu, hv, each ny x nx doubles with x
+ * fastest, nx = nbx*mx*2^maxlevel, ny = nby*mx*2^maxlevel. A patch at a
+ * coarser level takes the cell averages of the raster (a pyramid of 2 x 2
+ * averages), like setaux's cell-averaged topography. */
+typedef struct gf_forest gf_forest;
+
+typedef struct gf_forest_opts {
+    int mx;                /* 8, 16 or 32 (my = mx)                          */
+    int maux;              /* aux fields, bathymetry first (1..3)            */
+    int nbx, nby;          /* root blocks                                    */
+    int minlevel, maxlevel; /* 0 <= minlevel <= maxlevel <= 10               */
+    double x0, y0;         /* lower-left corner of the domain                */
+    double dx0, dy0;       /* cell size at level 0                           */
+    int phys_slot;         /* physics set in the context's table             */
+    int mthbc[4];          /* left, right, bottom, top: 0 inflow, 1 extrap, 3 wall */
+    int regrid_interval;   /* accepted steps between regrids (0: never)      */
+    int max_patches;       /* slot capacity (0: nbx*nby*4^maxlevel)          */
+    gf_refine refine;      /* refinement criteria                            */
+} gf_forest_opts;
+
+typedef struct gf_forest_stats {
+    long long steps, rejects, regrids;
+    long long cell_updates;  /* interior cells x accepted steps, all leaves */
+    double t;                /* simulated time reached                      */
+    double dt;               /* controller's dt at minlevel                 */
+    double max_cfl_seen;
+    int npatch, npatch_max;  /* leaves now / at most                        */
+    int levels_used;         /* finest level present                        */
+} gf_forest_stats;
+
+void gf_forest_opts_default(gf_forest_opts* o);
+/* fields: (maux + 3) rasters at maxlevel, see above (host memory). */
+int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, gf_forest** out);
+void gf_forest_destroy(gf_forest* f);
+/* Inflow hydrograph (as gf_level_set_hydrograph); call before gf_forest_init. */
+int gf_forest_set_hydrograph(gf_forest* f, int n, const double* time, const double* hu,
+                             const int* side, double width, double x0, double y0);
+/* Leaves at minlevel, then initial refinement (init_flag = 1) until no tag
+ * fires or maxlevel is reached; every new patch takes the rasters. */
+int gf_forest_init(gf_forest* f);
+int gf_forest_ghost_fill(gf_forest* f, double t);
+/* One step of every leaf with dt from its state at t (ghost fill included);
+ * the result is held until gf_forest_accept. *cfl = max over leaves. */
+int gf_forest_step(gf_forest* f, double t, double dt, double* cfl);
+int gf_forest_accept(gf_forest* f, int accept);
+/* Tag, refine/coarsen, balance, transfer; *changed = 1 if the leaves changed. */
+int gf_forest_regrid(gf_forest* f, double t, int* changed);
+/* outstyle-1 run from t = 0 to t_final with nout output intervals. */
+int gf_forest_run(gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
+                  double max_cfl, int max_steps, gf_forest_stats* st);
+int gf_forest_get_stats(gf_forest* f, gf_forest_stats* st);
+/* Leaves in canonical order (level, then J, then I). */
+int gf_forest_npatch(const gf_forest* f);
+int gf_forest_patches(const gf_forest* f, int* level, int* I, int* J);
+/* State / aux of the leaves in canonical order, Fortran layout per patch. */
+int gf_forest_download(gf_forest* f, double* q);
+int gf_forest_download_aux(gf_forest* f, double* aux);
+int gf_forest_upload(gf_forest* f, const double* q);
+
 /* ------------------------------------------------- served scenarios */
 /* A request loop over flood scenarios (continuous batching). Each admitted
  * scenario keeps its state resident on the device; every batching round

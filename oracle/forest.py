@@ -1,0 +1,371 @@
+"""CPU oracle for multi-level forests -- TEST INFRASTRUCTURE ONLY.
+
+A plain-Python restatement of the forest rules (leaves, 2:1 balance, ghost
+exchange between levels, regrid, initial refinement, outstyle-1 stepping)
+on top of the oracle's C kernels, which restate the reference's Fortran:
+copies and bc2 (fclaw2d_source/fc2d_geoclaw_copy_fort.f,
+fortran_source/geoflood_bc2_fort.f90), averaging and interpolation
+(fclaw2d_source/fc2d_geoclaw_average_fort.f,
+fclaw2d_source/fc2d_geoclaw_interpolate_fort.f), tags
+(fclaw2d_source/fc2d_geoclaw_tag4refinement_fort.f90,
+fc2d_geoclaw_tag4coarsening_fort.f90) and the patch update. The level
+machinery itself belongs to ForestClaw / p4est, which the reference tree
+does not contain, so this driver states the rules the device driver
+follows; its agreement with ForestClaw is unpinned.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import (MBC, average2coarse, average_ghost, interpolate2fine, interpolate_ghost,
+               level_ghost_fill, level_update, refine as c_refine, tag4coarsening,
+               tag4refinement)
+
+FACES = ((-1, 0), (1, 0), (0, -1), (0, 1))          # left, right, bottom, top
+CORNERS = ((-1, -1), (1, -1), (-1, 1), (1, 1))       # ll, lr, ul, ur
+
+
+def pyramid(fields: np.ndarray, levels: int) -> list:
+    """fields (nf, ny, nx) at the finest level -> [finest, ..., coarsest],
+    each (nf, ny_l + 4, nx_l + 4) padded by edge copies; coarser interiors are
+    ((a + b) + (c + d)) * 0.25 of the 2 x 2 block below."""
+    out = []
+    cur = np.asarray(fields, np.float64)
+    for k in range(levels):
+        out.append(np.pad(cur, ((0, 0), (MBC, MBC), (MBC, MBC)), mode="edge"))
+        if k + 1 < levels:
+            cur = ((cur[:, 0::2, 0::2] + cur[:, 0::2, 1::2])
+                   + (cur[:, 1::2, 0::2] + cur[:, 1::2, 1::2])) * 0.25
+    return out
+
+
+class Forest:
+    def __init__(self, mx, nbx, nby, minlevel, maxlevel, dx0, dy0, aux, q, x0=0.0, y0=0.0,
+                 phys=None, mthbc=(1, 1, 1, 1), regrid_interval=0, rf=None, hy=None):
+        self.m, self.nbx, self.nby = mx, nbx, nby
+        self.lmin, self.lmax = minlevel, maxlevel
+        self.dx0, self.dy0, self.x0, self.y0 = dx0, dy0, x0, y0
+        self.phys, self.mthbc, self.hy = phys, tuple(mthbc), hy
+        self.regrid_interval = regrid_interval
+        self.rf = c_refine(rf) if rf is not None else None
+        aux = np.asarray(aux, np.float64)
+        if aux.ndim == 2:
+            aux = aux[None]
+        self.maux = aux.shape[0]
+        fields = np.concatenate([aux, np.moveaxis(np.asarray(q, np.float64), 2, 0)], axis=0)
+        pyr = pyramid(fields, maxlevel - minlevel + 1)
+        self.pyr = {maxlevel - k: p for k, p in enumerate(pyr)}
+        self.leaves = {}            # (l, I, J) -> [q (n4, n4, 3), aux (n4, n4, maux)]
+        self.steps = self.rejects = self.regrids = 0
+        self.cell_updates = 0
+        self.t = 0.0
+        self.dt = 0.0
+        self.max_cfl_seen = 0.0
+
+    # ---- geometry -------------------------------------------------------
+    def npx(self, l):
+        return self.nbx << l
+
+    def npy(self, l):
+        return self.nby << l
+
+    def inside(self, l, I, J):
+        return 0 <= I < self.npx(l) and 0 <= J < self.npy(l)
+
+    def dx(self, l):
+        return self.dx0 / (1 << l)
+
+    def dy(self, l):
+        return self.dy0 / (1 << l)
+
+    def origin(self, l, I, J):
+        return (self.x0 + I * self.m * self.dx(l), self.y0 + J * self.m * self.dy(l))
+
+    def containing(self, l, I, J):
+        for k in range(l, self.lmin - 1, -1):
+            key = (k, I >> (l - k), J >> (l - k))
+            if key in self.leaves:
+                return key
+        return None
+
+    def canonical(self):
+        return sorted(self.leaves, key=lambda k: (k[0], k[2], k[1]))
+
+    def window(self, l, I, J):
+        n4 = self.m + 2 * MBC
+        p = self.pyr[l]
+        w = p[:, J * self.m:J * self.m + n4, I * self.m:I * self.m + n4]
+        return np.ascontiguousarray(np.moveaxis(w, 0, 2))   # (n4, n4, nf)
+
+    def new_patch(self, key, with_q):
+        w = self.window(*key)
+        aux = np.ascontiguousarray(w[..., :self.maux])
+        q = np.ascontiguousarray(w[..., self.maux:]) if with_q else np.zeros(w.shape[:2] + (3,))
+        return [q, aux]
+
+    # ---- ghost exchange -------------------------------------------------
+    def _level_fill(self, l, t):
+        keys = [k for k in self.canonical() if k[0] == l]
+        if not keys:
+            return
+        pos = {k: n for n, k in enumerate(keys)}
+        nbr = -np.ones((len(keys), 8), np.int32)
+        for n, (_, I, J) in enumerate(keys):
+            for s, (di, dj) in enumerate(FACES + CORNERS):
+                if not self.inside(l, I + di, J + dj):
+                    nbr[n, s] = -1
+                else:
+                    nbr[n, s] = pos.get((l, I + di, J + dj), -2)
+        q = np.stack([self.leaves[k][0] for k in keys])
+        aux = np.stack([self.leaves[k][1] for k in keys])
+        xl = np.array([self.origin(*k)[0] for k in keys])
+        yl = np.array([self.origin(*k)[1] for k in keys])
+        level_ghost_fill(q, aux, nbr, xl, yl, self.dx(l), self.dy(l), t, self.mthbc, self.phys,
+                         self.hy)
+        for n, k in enumerate(keys):
+            self.leaves[k][0][...] = q[n]
+            self.leaves[k][1][...] = aux[n]
+
+    def ghost_fill(self, t):
+        m = self.m
+        # (1) fine -> coarse averages into coarse ghost cells
+        for (l, I, J), (qc, ac) in self.leaves.items():
+            for fc, (di, dj) in enumerate(FACES):
+                NI, NJ = I + di, J + dj
+                if not self.inside(l, NI, NJ) or (l, NI, NJ) in self.leaves:
+                    continue
+                if l > self.lmin and (l - 1, NI >> 1, NJ >> 1) in self.leaves:
+                    continue
+                for c in range(2):
+                    if fc < 2:
+                        FI, FJ = 2 * NI + (1 if di < 0 else 0), 2 * J + c
+                    else:
+                        FI, FJ = 2 * I + c, 2 * NJ + (1 if dj < 0 else 0)
+                    qf, af = self.leaves[(l + 1, FI, FJ)]
+                    average_ghost(qc, ac, qf, af, 0, fc, m * (2 * I - FI), m * (2 * J - FJ),
+                                  self.phys)
+            for cc, (di, dj) in enumerate(CORNERS):
+                DI, DJ = I + di, J + dj
+                if not self.inside(l, DI, DJ) or (l, DI, DJ) in self.leaves:
+                    continue
+                if self.containing(l, DI, DJ) is not None:
+                    continue
+                FI, FJ = 2 * DI + (1 if di < 0 else 0), 2 * DJ + (1 if dj < 0 else 0)
+                qf, af = self.leaves[(l + 1, FI, FJ)]
+                average_ghost(qc, ac, qf, af, 1, cc, m * (2 * I - FI), m * (2 * J - FJ), self.phys)
+        # (2) same-level copies and physical boundaries, every level
+        for l in range(self.lmin, self.lmax + 1):
+            self._level_fill(l, t)
+        # (3) coarse -> fine interpolation, level by level, boundaries again
+        for l in range(self.lmin + 1, self.lmax + 1):
+            for (lp, I, J), (qf, af) in self.leaves.items():
+                if lp != l:
+                    continue
+                for fc, (di, dj) in enumerate(FACES):
+                    NI, NJ = I + di, J + dj
+                    if not self.inside(l, NI, NJ) or (l, NI, NJ) in self.leaves:
+                        continue
+                    ck = (l - 1, NI >> 1, NJ >> 1)
+                    if ck in self.leaves:
+                        qc, ac = self.leaves[ck]
+                        interpolate_ghost(qc, ac, qf, af, 0, fc ^ 1, m * (2 * ck[1] - I),
+                                          m * (2 * ck[2] - J), self.phys)
+                for cc, (di, dj) in enumerate(CORNERS):
+                    DI, DJ = I + di, J + dj
+                    if not self.inside(l, DI, DJ) or (l, DI, DJ) in self.leaves:
+                        continue
+                    ck = (l - 1, DI >> 1, DJ >> 1)
+                    if ck not in self.leaves:
+                        continue
+                    xok = 2 * ck[1] == DI if di > 0 else 2 * ck[1] + 1 == DI
+                    yok = 2 * ck[2] == DJ if dj > 0 else 2 * ck[2] + 1 == DJ
+                    if xok and yok:
+                        qc, ac = self.leaves[ck]
+                        interpolate_ghost(qc, ac, qf, af, 1, 3 - cc, m * (2 * ck[1] - I),
+                                          m * (2 * ck[2] - J), self.phys)
+            self._level_fill(l, t)
+
+    # ---- tags, balance, regrid ------------------------------------------
+    def _tags(self, t, init_flag):
+        refine = {}
+        for k in self.canonical():
+            l, I, J = k
+            if l >= self.lmax:
+                continue
+            q, aux = self.leaves[k]
+            xl, yl = self.origin(*k)
+            refine[k] = tag4refinement(q, aux, xl, yl, self.dx(l), self.dy(l), t, l, self.lmax,
+                                       init_flag, self.rf, self.phys) != 0
+        fams = []
+        if not init_flag:
+            for k in self.canonical():
+                l, I, J = k
+                if l <= self.lmin or I & 1 or J & 1:
+                    continue
+                fam = [(l, I + (c & 1), J + (c >> 1)) for c in range(4)]
+                if not all(f in self.leaves for f in fam):
+                    continue
+                qs = [self.leaves[f][0] for f in fam]
+                auxs = [self.leaves[f][1] for f in fam]
+                xs = [self.origin(*f)[0] for f in fam]
+                ys = [self.origin(*f)[1] for f in fam]
+                c = tag4coarsening(qs, auxs, xs, ys, self.dx(l), self.dy(l), t, l, self.lmax,
+                                   init_flag, self.rf, self.phys)
+                fams.append((fam, c != 0))
+        return refine, fams
+
+    def _balance(self, split):
+        """Split every leaf that a split neighbour's children would touch
+        across a two-level jump (face or corner), until none is left."""
+        work = [k for k in split]
+        while work:
+            l, I, J = work.pop()
+            for di, dj in FACES + CORNERS:
+                if not self.inside(l, I + di, J + dj):
+                    continue
+                q = self.containing(l, I + di, J + dj)
+                if q is not None and q[0] <= l - 1 and q not in split:
+                    split.add(q)
+                    work.append(q)
+
+    def _can_merge(self, l, PI, PJ, split):
+        for a in range(-1, 3):
+            for b in range(-1, 3):
+                if 0 <= a <= 1 and 0 <= b <= 1:
+                    continue
+                I, J = 2 * PI + a, 2 * PJ + b
+                if not self.inside(l, I, J):
+                    continue
+                q = self.containing(l, I, J)
+                if q is None or (q[0] == l and q in split):
+                    return False
+        return True
+
+    def _apply(self, split, merges, init):
+        new = {}
+        for k, (q, aux) in self.leaves.items():
+            if k in split:
+                l, I, J = k
+                for c in range(4):
+                    ck = (l + 1, 2 * I + (c & 1), 2 * J + (c >> 1))
+                    child = self.new_patch(ck, init)
+                    if not init:
+                        interpolate2fine(q, aux, child[0], child[1], c, self.phys)
+                    new[ck] = child
+            elif not any(k in fam for fam in merges):
+                new[k] = [q, aux]
+        for fam in merges:
+            l, I, J = fam[0]
+            pk = (l - 1, I >> 1, J >> 1)
+            parent = self.new_patch(pk, False)
+            for c, ck in enumerate(fam):
+                average2coarse(parent[0], parent[1], self.leaves[ck][0], self.leaves[ck][1], c,
+                               self.phys)
+            new[pk] = parent
+        changed = bool(split) or bool(merges)
+        self.leaves = new
+        return changed
+
+    def regrid(self, t):
+        self.ghost_fill(t)
+        refine, fams = self._tags(t, 0)
+        split = {k for k, v in refine.items() if v}
+        self._balance(split)
+        merges = []
+        for fam, c in fams:
+            if c and not any(f in split for f in fam) and \
+                    self._can_merge(fam[0][0], fam[0][1] >> 1, fam[0][2] >> 1, split):
+                merges.append(fam)
+        self.regrids += 1
+        return self._apply(split, merges, False)
+
+    def init(self):
+        self.leaves = {}
+        for J in range(self.npy(self.lmin)):
+            for I in range(self.npx(self.lmin)):
+                k = (self.lmin, I, J)
+                self.leaves[k] = self.new_patch(k, True)
+        for _ in range(self.lmin, self.lmax):
+            refine, _ = self._tags(0.0, 1)
+            split = {k for k, v in refine.items() if v}
+            self._balance(split)
+            if not self._apply(split, [], True):
+                break
+
+    # ---- stepping -------------------------------------------------------
+    def step(self, t, dt):
+        """Ghost fill at t and one update of every leaf; returns max CFL."""
+        self.ghost_fill(t)
+        keys = self.canonical()
+        q = np.stack([self.leaves[k][0] for k in keys])
+        aux = np.stack([self.leaves[k][1] for k in keys])
+        dx = np.array([self.dx(k[0]) for k in keys])
+        dy = np.array([self.dy(k[0]) for k in keys])
+        cfl = level_update(q, aux, dx, dy, t, dt, self.phys)
+        for n, k in enumerate(keys):
+            self.leaves[k][0][...] = q[n]
+        return cfl
+
+    def snapshot(self):
+        return {k: v[0].copy() for k, v in self.leaves.items()}
+
+    def restore(self, snap):
+        for k, q in snap.items():
+            self.leaves[k][0][...] = q
+
+    def run(self, t_final, nout, initial_dt, desired_cfl, max_cfl, max_steps=0):
+        """outstyle 1 (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395), variable dt,
+        advance-one-step, no subcycling; returns the accepted dt list."""
+        level_factor = float(1 << (self.lmax - self.lmin))
+        dt_outer = t_final / nout
+        t_curr = self.t
+        dt_minlevel = initial_dt
+        taken = 0
+        dts = []
+        for _ in range(nout):
+            tend = t_curr + dt_outer
+            while t_curr < tend:
+                if max_steps and taken >= max_steps:
+                    self.t, self.dt = t_curr, dt_minlevel
+                    return dts
+                dt_step = dt_minlevel / level_factor
+                tol = 1e-2 * dt_step
+                took_small = False
+                small_step = tend - (t_curr + dt_step)
+                if small_step < tol:
+                    dt_step = tend - t_curr
+                    if small_step < 0:
+                        took_small = True
+                snap = self.snapshot()
+                cfl = self.step(t_curr, dt_step)
+                taken += 1
+                self.max_cfl_seen = max(self.max_cfl_seen, cfl)
+                if cfl > max_cfl:
+                    self.restore(snap)
+                    dt_minlevel = dt_minlevel * desired_cfl / cfl
+                    self.rejects += 1
+                    continue
+                self.steps += 1
+                self.cell_updates += len(self.leaves) * self.m * self.m
+                t_curr += dt_step
+                dts.append(dt_step)
+                dt_new = dt_minlevel * desired_cfl / cfl if cfl > 0.0 else float("inf")
+                if not took_small:
+                    dt_minlevel = dt_new
+                if self.regrid_interval > 0 and self.steps % self.regrid_interval == 0:
+                    self.regrid(t_curr)
+        self.t, self.dt = t_curr, dt_minlevel
+        return dts
+
+    def patches(self):
+        return np.array(self.canonical(), np.int32).reshape(-1, 3)
+
+    def download(self):
+        return np.stack([self.leaves[k][0] for k in self.canonical()])
+
+    def download_aux(self):
+        return np.stack([self.leaves[k][1] for k in self.canonical()])
+
+    def upload(self, q):
+        for n, k in enumerate(self.canonical()):
+            self.leaves[k][0][...] = q[n]
