@@ -538,6 +538,8 @@ def run_gpu(args):
     }
     if rank == 0 and not args.no_served:
         result["served"] = served_stream(args)
+    if rank == 0 and not args.no_forest:
+        result["forest"] = forest_leg(args, local)
     if rank == 0:
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
@@ -549,6 +551,70 @@ def run_gpu(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def forest_dambreak_config(mx=16, lmin=1, lmax=3, seed=SEED):
+    """The CPU dam break as a forest: 2000 x 1000 m as a 2 x 1 brick of
+    1000 m blocks, levels 1..3 (dx 31.25 m .. 7.8125 m at mx = 16), bump-and-
+    ramp bed, surface 10 m above the bed for x < 600 m, dry beyond, n =
+    0.035, walls; refinement follows moving water (flowgrade on momentum
+    > 1 m^2/s up to level 3), regrid every 2 steps."""
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+
+    nbx, nby = 2, 1
+    dx0 = 1000.0 / mx
+    nx, ny = nbx * mx << lmax, nby * mx << lmax
+    dxf = dx0 / (1 << lmax)
+    b = synth.bump_ramp_dem(nx, ny, dxf, dxf, seed=seed)
+    x = (np.arange(nx) + 0.5) * dxf
+    q = np.zeros((ny, nx, 3))
+    q[..., 0] = np.where(x[None, :] < 600.0, 10.0, 0.0)
+    rf = gf.Refine(wave_tolerance=1e9, flowgrades=((1.0, 2, 1, lmax),))
+    phys = gf.Phys(manning_coefficient=(0.035,), manning_break=(1e10,))
+    return dict(mx=mx, nbx=nbx, nby=nby, lmin=lmin, lmax=lmax, dx0=dx0, b=b, q=q, rf=rf,
+                phys=phys, mthbc=(3, 3, 3, 3), regrid=2)
+
+
+def forest_leg(args, dev=0):
+    """Config-1 dam break (AMR forest) on the GPU forest and on the oracle's
+    forest driver (CPU, same rules), same number of accepted steps."""
+    import geoflood_gb300 as gf
+    import oracle
+    from oracle import forest as of
+
+    c = forest_dambreak_config()
+    steps = args.forest_steps
+    ctx = gf.Context(dev)
+    ctx.set_phys(0, c["phys"])
+    F = gf.Forest(ctx, c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"],
+                  c["b"], c["q"], mthbc=c["mthbc"], regrid_interval=c["regrid"], refine=c["rf"])
+    F.init()
+    t0 = time.perf_counter()
+    st = F.run(1e9, 1, 5.0, 0.9, 1.0, max_steps=steps)
+    gpu_s = time.perf_counter() - t0
+    gpu_patches = F.patches()
+    F.close()
+    ctx.close()
+    oracle.load()
+    O = of.Forest(c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"], c["b"],
+                  c["q"], phys=c["phys"], mthbc=c["mthbc"], regrid_interval=c["regrid"],
+                  rf=c["rf"])
+    O.init()
+    t0 = time.perf_counter()
+    O.run(1e9, 1, 5.0, 0.9, 1.0, max_steps=steps)
+    cpu_s = time.perf_counter() - t0
+    return {
+        "workload": "dam break forest, 2x1 blocks of 1000 m, mx 16, levels 1-3, "
+                    f"{steps} step attempts (accepted + rejected), regrid every 2",
+        "value": st["cell_updates"] / gpu_s, "unit": METRIC, "seconds": gpu_s,
+        "steps": st["steps"], "rejects": st["rejects"], "regrids": st["regrids"],
+        "patches_end": int(len(gpu_patches)), "patches_max": st["npatch_max"],
+        "cpu_oracle": {"value": O.cell_updates / cpu_s, "unit": METRIC, "seconds": cpu_s,
+                       "cores": 1, "kind": "port",
+                       "note": "oracle forest driver (Python tree + C kernels, one thread)"},
+        "patch_lists_equal_to_oracle": bool(np.array_equal(gpu_patches, O.patches())),
+    }
 
 
 def fp64_rates():
@@ -574,6 +640,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--served-only", action="store_true")
+    ap.add_argument("--no-forest", action="store_true")
+    ap.add_argument("--forest-only", action="store_true")
+    ap.add_argument("--forest-steps", type=int, default=200)
     ap.add_argument("--served-scenarios", type=int, default=512)
     ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
     ap.add_argument("--served-reserve-sms", type=int, default=None)
@@ -582,6 +651,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.forest_only:
+        print(json.dumps({"forest": forest_leg(args)}))
+        return 0
     if args.served_only:
         print(json.dumps({"served": served_stream(args)}))
         return 0
