@@ -117,6 +117,11 @@ class gf_forest_stats(C.Structure):
                 ("levels_used", C.c_int)]
 
 
+class gf_forest_batch_stats(C.Structure):
+    _fields_ = [("rounds", C.c_longlong), ("epochs", C.c_longlong), ("regrids", C.c_longlong),
+                ("launches", C.c_longlong), ("cell_updates", C.c_longlong)]
+
+
 XFER_AVG_FACE, XFER_AVG_CORNER, XFER_INTERP_FACE = 0, 1, 2
 XFER_INTERP_CORNER, XFER_INTERP2FINE, XFER_AVG2COARSE = 3, 4, 5
 
@@ -185,6 +190,8 @@ SIGNATURES = [
     ("gf_forest_download", C.c_int, [_vp, _dp]),
     ("gf_forest_download_aux", C.c_int, [_vp, _dp]),
     ("gf_forest_upload", C.c_int, [_vp, _dp]),
+    ("gf_forest_batch_run", C.c_int, [C.POINTER(_vp), C.c_int, C.c_double, C.c_int, C.c_double,
+                                      C.c_double, C.c_double, C.POINTER(gf_forest_batch_stats)]),
     ("gf_server_opts_default", None, [C.POINTER(gf_server_opts)]),
     ("gf_server_create", C.c_int, [C.c_int, C.POINTER(gf_server_opts), C.POINTER(_vp)]),
     ("gf_server_destroy", None, [_vp]),

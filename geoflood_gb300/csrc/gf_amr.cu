@@ -133,13 +133,21 @@ __device__ __forceinline__ void under(int ic, int jc, int ox, int oy, int* i2, i
 template <int M>
 __global__ void __launch_bounds__(128) transfer_kernel(const gf_xfer_task* __restrict__ tasks,
                                                        int ntask,
-                                                       const gf_phys* __restrict__ phys_table)
+                                                       const gf_phys* __restrict__ phys_table,
+                                                       const long long* __restrict__ qdelta)
 {
     using G = AmrGeo<M>;
     constexpr int MBC = 2;
     const int ti = blockIdx.x;
     if (ti >= ntask) return;
-    const gf_xfer_task T = tasks[ti];
+    gf_xfer_task T = tasks[ti];
+    if (qdelta) {
+        const long long d = qdelta[T.group];
+        if (d == GF_QDELTA_SKIP) return; /* the group does not step this round */
+        /* shift to the buffer holding the group's current state */
+        T.qc += d;
+        T.qf += d;
+    }
     const double drytol = phys_table[T.phys].dry_tolerance;
     const double sea = phys_table[T.phys].sea_level;
     const double* bc = T.ac; /* aux field 0 = bathymetry */
@@ -399,13 +407,13 @@ __global__ void __launch_bounds__(128) tag_kernel(const gf_tag_task* __restrict_
 } // namespace
 
 cudaError_t launch_transfer(int m, const gf_xfer_task* tasks, int ntask, const gf_phys* phys,
-                            cudaStream_t st)
+                            cudaStream_t st, const long long* qdelta)
 {
     if (ntask <= 0) return cudaSuccess;
     switch (m) {
-    case 32: transfer_kernel<32><<<ntask, 128, 0, st>>>(tasks, ntask, phys); break;
-    case 16: transfer_kernel<16><<<ntask, 128, 0, st>>>(tasks, ntask, phys); break;
-    case 8: transfer_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask, phys); break;
+    case 32: transfer_kernel<32><<<ntask, 128, 0, st>>>(tasks, ntask, phys, qdelta); break;
+    case 16: transfer_kernel<16><<<ntask, 128, 0, st>>>(tasks, ntask, phys, qdelta); break;
+    case 8: transfer_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask, phys, qdelta); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -132,6 +132,12 @@ struct gf_forest {
     unsigned long long* h_rb = nullptr;              /* pinned */
     long long cells = 0;                             /* interior cells of all leaves */
     gf_forest_stats st{};
+    /* host copies of the tables (buffer-0 pointers), for batched epochs */
+    std::vector<gf_patch_work> h_work;
+    std::vector<gf_xfer_task> h_avg;
+    std::vector<std::vector<gf_xfer_task>> h_itp; /* per level */
+    std::vector<std::vector<int>> h_refresh;      /* slots per level */
+    gf_group_state gst{};                         /* controller during a batched run */
 };
 
 namespace {
@@ -280,6 +286,7 @@ gf_xfer_task xtask(gf_forest* f, int b, int kind, int cslot, int fslot, int code
     t.ox = ox;
     t.oy = oy;
     t.phys = f->o.phys_slot;
+    t.group = 0;
     return t;
 }
 
@@ -436,6 +443,14 @@ int build_tables(gf_forest* f)
         FK(f, cudaMemcpyAsync(f->d_refs_lv.p, ref_all.data(), ref_all.size() * sizeof(gf_ghost_ref),
                               cudaMemcpyHostToDevice, st));
     FK(f, cudaStreamSynchronize(st)); /* host vectors go out of scope */
+    f->h_work.swap(work);
+    f->h_avg.swap(avg[0]);
+    f->h_itp.assign(nlev, {});
+    f->h_refresh.assign(nlev, {});
+    for (int l = 0; l < nlev; ++l) {
+        f->h_itp[l].swap(itp[0][l]);
+        for (const gf_ghost_ref& r : refresh[l]) f->h_refresh[l].push_back(r.local);
+    }
     f->dirty = false;
     return GF_OK;
 }
@@ -1079,3 +1094,389 @@ int gf_forest_upload(gf_forest* f, const double* q)
 }
 
 } // extern "C"
+
+/* ------------------------------------------------------------------------
+ * Batched form: many forests in shared launches, device-side time-step
+ * control, one captured round per epoch.
+ * --------------------------------------------------------------------- */
+namespace {
+
+inline int cls_of(int mx) { return mx == 8 ? 0 : mx == 16 ? 1 : 2; }
+inline size_t align_up(size_t b) { return (b + 255) & ~(size_t)255; }
+const int kCls[3] = {8, 16, 32};
+constexpr int kBatchLevels = 11;
+
+struct Batch {
+    gf_ctx* ctx = nullptr;
+    std::vector<gf_forest*> fs;     /* members: group g = fs[g] */
+    cudaStream_t st = nullptr;
+    /* epoch area (pinned mirror + device) */
+    char* h = nullptr;
+    char* d = nullptr;
+    size_t cap = 0;
+    size_t off_blk = 0, off_gs = 0, off_dt = 0, off_par = 0, off_dl = 0, off_rb = 0, off_hyt = 0,
+           off_hyu = 0;
+    size_t off_refs[3] = {}, off_avg[3] = {}, off_work[3] = {};
+    size_t off_itp[3][kBatchLevels] = {}, off_ref[3][kBatchLevels] = {};
+    int n_refs[3] = {}, n_avg[3] = {}, n_work[3] = {};
+    int n_itp[3][kBatchLevels] = {}, n_ref[3][kBatchLevels] = {};
+    char* h_rb = nullptr;           /* readback: [err 8 B][states] */
+    size_t rb_cap = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int launches_per_round = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ~Batch()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (d) cudaFree(d);
+        if (h) cudaFreeHost(h);
+        if (h_rb) cudaFreeHost(h_rb);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+};
+
+#define BK(b, call)                                                               \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) return gf::ctx_cuda_fail((b).ctx, e_, #call);      \
+    } while (0)
+
+/* one round of the epoch on the batch stream (captured) */
+int enqueue_batch_round(Batch& B)
+{
+    const int ng = (int)B.fs.size();
+    char* d = B.d;
+    const gf_phys* phys = gf::ctx_device_phys(B.ctx);
+    gf_ghost_block* blk = reinterpret_cast<gf_ghost_block*>(d + B.off_blk);
+    gf_group_state* gs = reinterpret_cast<gf_group_state*>(d + B.off_gs);
+    double* gdt = reinterpret_cast<double*>(d + B.off_dt);
+    int* gpar = reinterpret_cast<int*>(d + B.off_par);
+    long long* dl = reinterpret_cast<long long*>(d + B.off_dl);
+    unsigned long long* rb = reinterpret_cast<unsigned long long*>(d + B.off_rb);
+    int* err = reinterpret_cast<int*>(rb);
+    const double* hyt = reinterpret_cast<const double*>(d + B.off_hyt);
+    const double* hyu = reinterpret_cast<const double*>(d + B.off_hyu);
+    int n = 0;
+    BK(B, gf::launch_served_prepare(gs, blk, gdt, gpar, rb + 1, hyt, hyu, ng, B.st, dl));
+    ++n;
+    for (int c = 0; c < 3; ++c) {
+        const int m = kCls[c];
+        if (!B.n_refs[c]) continue;
+        if (B.n_avg[c]) {
+            BK(B, gf::launch_transfer(m, reinterpret_cast<gf_xfer_task*>(d + B.off_avg[c]), B.n_avg[c],
+                                      phys, B.st, dl));
+            ++n;
+        }
+        BK(B, gf::launch_ghost_fill(m, blk, reinterpret_cast<gf_ghost_ref*>(d + B.off_refs[c]),
+                                    B.n_refs[c], phys, B.st));
+        ++n;
+        for (int l = 0; l < kBatchLevels; ++l) {
+            if (B.n_itp[c][l]) {
+                BK(B, gf::launch_transfer(m, reinterpret_cast<gf_xfer_task*>(d + B.off_itp[c][l]),
+                                          B.n_itp[c][l], phys, B.st, dl));
+                ++n;
+            }
+            if (B.n_ref[c][l]) {
+                BK(B, gf::launch_ghost_fill(m, blk, reinterpret_cast<gf_ghost_ref*>(d + B.off_ref[c][l]),
+                                            B.n_ref[c][l], phys, B.st));
+                ++n;
+            }
+        }
+    }
+    const bool exact = gf::ctx_exact(B.ctx);
+    for (int c = 0; c < 3; ++c) {
+        if (!B.n_work[c]) continue;
+        const gf_patch_work* w = reinterpret_cast<gf_patch_work*>(d + B.off_work[c]);
+        if (exact)
+            BK(B, gf::launch_patch_update_exact(kCls[c], w, B.n_work[c], phys, 0.0, gdt, gpar, 3, nullptr,
+                                                rb + 1, err, B.st));
+        else
+            BK(B, gf::launch_patch_update(kCls[c], w, B.n_work[c], phys, 0.0, gdt, gpar, 3, nullptr,
+                                          rb + 1, err, B.st));
+        ++n;
+    }
+    BK(B, gf::launch_served_finish(gs, gdt, rb + 1, err, ng, B.st));
+    ++n;
+    B.launches_per_round = n;
+    return GF_OK;
+}
+
+/* Concatenate the members' tables into a new epoch and capture its round. */
+int build_epoch(Batch& B)
+{
+    const int ng = (int)B.fs.size();
+    for (gf_forest* f : B.fs) {
+        int rc = build_tables(f);
+        if (rc) return rc;
+    }
+    /* sizes */
+    size_t nhy = 0;
+    std::memset(B.n_refs, 0, sizeof B.n_refs);
+    std::memset(B.n_avg, 0, sizeof B.n_avg);
+    std::memset(B.n_work, 0, sizeof B.n_work);
+    std::memset(B.n_itp, 0, sizeof B.n_itp);
+    std::memset(B.n_ref, 0, sizeof B.n_ref);
+    for (gf_forest* f : B.fs) {
+        const int c = cls_of(f->M);
+        nhy += f->hy_t.size();
+        B.n_refs[c] += (int)f->leaves.size();
+        B.n_work[c] += (int)f->h_work.size();
+        B.n_avg[c] += (int)f->h_avg.size();
+        for (size_t l = 0; l < f->h_itp.size(); ++l) {
+            B.n_itp[c][l] += (int)f->h_itp[l].size();
+            B.n_ref[c][l] += (int)f->h_refresh[l].size();
+        }
+    }
+    size_t off = 0;
+    auto take = [&off](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes);
+        return o;
+    };
+    B.off_blk = take(ng * sizeof(gf_ghost_block));
+    B.off_gs = take(ng * sizeof(gf_group_state));
+    B.off_dt = take(ng * sizeof(double));
+    B.off_par = take(ng * sizeof(int));
+    B.off_dl = take(ng * sizeof(long long));
+    B.off_rb = take((ng + 1) * sizeof(unsigned long long));
+    B.off_hyt = take(std::max<size_t>(nhy, 1) * sizeof(double));
+    B.off_hyu = take(std::max<size_t>(nhy, 1) * sizeof(double));
+    for (int c = 0; c < 3; ++c) {
+        B.off_refs[c] = take(B.n_refs[c] * sizeof(gf_ghost_ref));
+        B.off_avg[c] = take(B.n_avg[c] * sizeof(gf_xfer_task));
+        B.off_work[c] = take(B.n_work[c] * sizeof(gf_patch_work));
+        for (int l = 0; l < kBatchLevels; ++l) {
+            B.off_itp[c][l] = take(B.n_itp[c][l] * sizeof(gf_xfer_task));
+            B.off_ref[c][l] = take(B.n_ref[c][l] * sizeof(gf_ghost_ref));
+        }
+    }
+    const size_t need = off;
+    if (need > B.cap) {
+        if (B.d) cudaFree(B.d);
+        if (B.h) cudaFreeHost(B.h);
+        B.d = nullptr;
+        B.h = nullptr;
+        B.cap = 0;
+        const size_t c2 = need + need / 2;
+        BK(B, cudaMalloc(reinterpret_cast<void**>(&B.d), c2));
+        BK(B, cudaMallocHost(reinterpret_cast<void**>(&B.h), c2));
+        B.cap = c2;
+    }
+    const size_t rbn = 8 + ng * sizeof(gf_group_state);
+    if (rbn > B.rb_cap) {
+        if (B.h_rb) cudaFreeHost(B.h_rb);
+        B.h_rb = nullptr;
+        BK(B, cudaMallocHost(reinterpret_cast<void**>(&B.h_rb), rbn * 2));
+        B.rb_cap = rbn * 2;
+    }
+    char* h = B.h;
+    /* every per-group table starts defined: the round's prepare kernel
+     * rewrites them, but only for groups that step */
+    std::memset(h, 0, need);
+    int fill_refs[3] = {}, fill_avg[3] = {}, fill_work[3] = {};
+    int fill_itp[3][kBatchLevels] = {}, fill_ref[3][kBatchLevels] = {};
+    size_t hoff = 0;
+    for (int g = 0; g < ng; ++g) {
+        gf_forest* f = B.fs[g];
+        const int c = cls_of(f->M);
+        gf_ghost_block blk{};
+        blk.q = f->qbuf[f->gst.cur];
+        blk.aux = f->aux;
+        blk.nbr = f->d_nbr.p;
+        blk.geom = f->d_geom.p;
+        blk.phys_of = nullptr;
+        blk.bc = f->bc;
+        blk.phys = f->o.phys_slot;
+        blk.maux = f->o.maux;
+        blk.skip = 1;
+        reinterpret_cast<gf_ghost_block*>(h + B.off_blk)[g] = blk;
+        f->gst.hydro_off = (int)hoff;
+        f->gst.nhydro = (int)f->hy_t.size();
+        std::copy(f->hy_t.begin(), f->hy_t.end(), reinterpret_cast<double*>(h + B.off_hyt) + hoff);
+        std::copy(f->hy_hu.begin(), f->hy_hu.end(), reinterpret_cast<double*>(h + B.off_hyu) + hoff);
+        hoff += f->hy_t.size();
+        reinterpret_cast<gf_group_state*>(h + B.off_gs)[g] = f->gst;
+        gf_ghost_ref* refs = reinterpret_cast<gf_ghost_ref*>(h + B.off_refs[c]);
+        for (const Leaf& L : f->leaves) refs[fill_refs[c]++] = gf_ghost_ref{g, L.slot};
+        gf_xfer_task* av = reinterpret_cast<gf_xfer_task*>(h + B.off_avg[c]);
+        for (gf_xfer_task t : f->h_avg) {
+            t.group = g;
+            av[fill_avg[c]++] = t;
+        }
+        gf_patch_work* wk = reinterpret_cast<gf_patch_work*>(h + B.off_work[c]);
+        for (gf_patch_work w : f->h_work) {
+            w.group = g;
+            wk[fill_work[c]++] = w;
+        }
+        for (size_t l = 0; l < f->h_itp.size(); ++l) {
+            gf_xfer_task* it = reinterpret_cast<gf_xfer_task*>(h + B.off_itp[c][l]);
+            for (gf_xfer_task t : f->h_itp[l]) {
+                t.group = g;
+                it[fill_itp[c][l]++] = t;
+            }
+            gf_ghost_ref* rr = reinterpret_cast<gf_ghost_ref*>(h + B.off_ref[c][l]);
+            for (int slot : f->h_refresh[l]) rr[fill_ref[c][l]++] = gf_ghost_ref{g, slot};
+        }
+    }
+    BK(B, cudaMemcpyAsync(B.d, B.h, need, cudaMemcpyHostToDevice, B.st));
+    /* capture one round */
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    if (B.graph) cudaGraphDestroy(B.graph);
+    B.exec = nullptr;
+    B.graph = nullptr;
+    BK(B, cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_batch_round(B);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(B.st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    BK(B, e);
+    B.graph = g;
+    BK(B, cudaGraphInstantiate(&B.exec, B.graph, 0));
+    return GF_OK;
+}
+
+} // namespace
+
+extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout,
+                                   double initial_dt, double desired_cfl, double max_cfl,
+                                   gf_forest_batch_stats* bst)
+{
+    if (!forests || n < 1 || !(t_final > 0) || nout < 1 || !(initial_dt > 0) || !(desired_cfl > 0) ||
+        !(max_cfl > 0))
+        return GF_ERR_ARG;
+    gf_ctx* ctx = forests[0]->ctx;
+    for (int k = 0; k < n; ++k) {
+        if (!forests[k] || forests[k]->ctx != ctx) return GF_ERR_ARG;
+        if (forests[k]->leaves.empty()) return ffail(forests[k], GF_ERR_STATE, "forest not initialised");
+        if (forests[k]->o.maxlevel >= kBatchLevels) return ffail(forests[k], GF_ERR_ARG, "maxlevel too deep");
+        for (int j = 0; j < k; ++j)
+            if (forests[j] == forests[k]) return ffail(forests[k], GF_ERR_ARG, "a forest appears twice");
+    }
+    if (cudaSetDevice(gf::ctx_device(ctx)) != cudaSuccess) return GF_ERR_CUDA;
+    Batch B;
+    B.ctx = ctx;
+    B.st = gf::ctx_stream(ctx);
+    BK(B, cudaEventCreate(&B.ev0));
+    BK(B, cudaEventCreate(&B.ev1));
+    /* kernel attributes are set outside stream capture */
+    for (int c = 0; c < 3; ++c) {
+        gf::launch_patch_update(kCls[c], nullptr, 0, nullptr, 0.0, nullptr, nullptr, 0, nullptr, nullptr,
+                                nullptr, B.st);
+        gf::launch_patch_update_exact(kCls[c], nullptr, 0, nullptr, 0.0, nullptr, nullptr, 0, nullptr,
+                                      nullptr, nullptr, B.st);
+    }
+    gf_forest_batch_stats S{};
+    /* controllers at the start (fc2d_geoclaw_run.c:197-225) */
+    for (int k = 0; k < n; ++k) {
+        gf_forest* f = forests[k];
+        gf_group_state& g = f->gst;
+        std::memset(&g, 0, sizeof g);
+        g.qb[0] = f->qbuf[0];
+        g.qb[1] = f->qbuf[1];
+        g.dt_outer = t_final / nout;
+        g.t_curr = f->st.t;
+        g.tend = g.t_curr + g.dt_outer;
+        g.dt_minlevel = initial_dt;
+        g.desired_cfl = desired_cfl;
+        g.max_cfl = max_cfl;
+        g.max_cfl_seen = f->st.max_cfl_seen;
+        g.level_factor = (double)(1 << (f->o.maxlevel - f->o.minlevel));
+        g.steps = f->st.steps;
+        g.rejects = f->st.rejects;
+        g.nout = nout;
+        g.active = 1;
+        g.cur = f->par;
+        g.regrid_interval = f->o.regrid_interval;
+        g.since_regrid = f->o.regrid_interval > 0 ? (int)(f->st.steps % f->o.regrid_interval) : 0;
+        B.fs.push_back(f);
+    }
+    double round_ms = 0.05;
+    int rounds_paused = 0;
+    bool rebuild = true;
+    while (true) {
+        /* drop finished forests; stop when none is left */
+        std::vector<gf_forest*> live;
+        for (gf_forest* f : B.fs)
+            if (f->gst.active) live.push_back(f);
+        if (live.empty()) break;
+        if (live.size() != B.fs.size()) {
+            B.fs.swap(live);
+            rebuild = true;
+        }
+        if (rebuild) {
+            int rc = build_epoch(B);
+            if (rc) return rc;
+            S.epochs++;
+            rebuild = false;
+            rounds_paused = 0;
+        }
+        const int ng = (int)B.fs.size();
+        int rounds = (int)std::ceil(0.5 / std::max(round_ms, 1e-3));
+        rounds = std::max(1, std::min(64, rounds));
+        BK(B, cudaEventRecord(B.ev0, B.st));
+        for (int r = 0; r < rounds; ++r) BK(B, cudaGraphLaunch(B.exec, B.st));
+        BK(B, cudaMemcpyAsync(B.h_rb, B.d + B.off_rb, 8, cudaMemcpyDeviceToHost, B.st));
+        BK(B, cudaMemcpyAsync(B.h_rb + 8, B.d + B.off_gs, ng * sizeof(gf_group_state),
+                              cudaMemcpyDeviceToHost, B.st));
+        BK(B, cudaEventRecord(B.ev1, B.st));
+        BK(B, cudaStreamSynchronize(B.st));
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) round_ms = std::max(1e-3, (double)ms / rounds);
+        S.rounds += rounds;
+        S.launches += (long long)rounds * B.launches_per_round;
+        int err;
+        std::memcpy(&err, B.h_rb, sizeof err);
+        if (err) return ffail(B.fs[0], GF_ERR_DEVICE, "a patch-update copy wait timed out");
+        const gf_group_state* gs = reinterpret_cast<const gf_group_state*>(B.h_rb + 8);
+        int npaused = 0, nactive = 0;
+        for (int g = 0; g < ng; ++g) {
+            gf_forest* f = B.fs[g];
+            const long long before = f->gst.steps;
+            const int hoff = f->gst.hydro_off;
+            f->gst = gs[g];
+            f->gst.hydro_off = hoff;
+            f->par = f->gst.cur;
+            f->st.cell_updates += (f->gst.steps - before) * f->cells;
+            S.cell_updates += (f->gst.steps - before) * f->cells;
+            f->st.steps = f->gst.steps;
+            f->st.rejects = f->gst.rejects;
+            f->st.t = f->gst.t_curr;
+            f->st.dt = f->gst.dt_minlevel;
+            f->st.max_cfl_seen = f->gst.max_cfl_seen;
+            if (f->gst.active) {
+                ++nactive;
+                npaused += f->gst.paused != 0;
+            }
+        }
+        if (npaused) rounds_paused += rounds;
+        /* regrid the waiting forests together once all live ones wait, or
+         * after a while (the others keep stepping meanwhile) */
+        if (npaused && (npaused == nactive || rounds_paused >= 16)) {
+            for (gf_forest* f : B.fs) {
+                if (!f->gst.active || !f->gst.paused) continue;
+                bool changed = false;
+                int rc = regrid(f, f->gst.t_curr, &changed);
+                if (rc) return rc;
+                f->gst.paused = 0;
+                f->gst.since_regrid = 0;
+                S.regrids++;
+            }
+            rebuild = true;
+        } else if (nactive < ng) {
+            rebuild = true; /* finished forests leave the epoch */
+        }
+    }
+    for (int k = 0; k < n; ++k) {
+        gf_forest* f = forests[k];
+        f->st.npatch = (int)f->leaves.size();
+        f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+    }
+    if (bst) *bst = S;
+    return GF_OK;
+}

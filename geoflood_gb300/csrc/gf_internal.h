@@ -32,7 +32,8 @@ cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int n
 /* Served scenarios: device-side time-step control around a round. */
 cudaError_t launch_served_prepare(gf_group_state* gs, gf_ghost_block* blocks, double* gdt, int* gpar,
                                   unsigned long long* gmax, const double* hy_t,
-                                  const double* hy_hu, int ng, cudaStream_t st);
+                                  const double* hy_hu, int ng, cudaStream_t st,
+                                  long long* qdelta = nullptr);
 cudaError_t launch_served_finish(gf_group_state* gs, const double* gdt,
                                  const unsigned long long* gmax, const int* err, int ng,
                                  cudaStream_t st);
@@ -42,8 +43,10 @@ cudaError_t launch_served_finish(gf_group_state* gs, const double* gdt,
 cudaError_t launch_ghost_fill(int m, const gf_ghost_block* blocks, const gf_ghost_ref* list,
                               int nlist, const gf_phys* phys, cudaStream_t st);
 
+/* qdelta (nullable): per-group offset (in doubles) added to the tasks' q
+ * pointers, selecting each group's current state buffer. */
 cudaError_t launch_transfer(int m, const gf_xfer_task* tasks, int ntask, const gf_phys* phys,
-                            cudaStream_t st);
+                            cudaStream_t st, const long long* qdelta = nullptr);
 cudaError_t launch_timeinterp(int m, const gf_tinterp_task* tasks, int ntask, double alpha,
                               cudaStream_t st);
 cudaError_t launch_tags(int m, const gf_tag_task* tasks, int ntask, const gf_refine* rf,

@@ -4,8 +4,9 @@
  * arithmetic is the same IEEE sequence as the host restatement of
  * ForestClaw's outstyle 1 loop (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395):
  *
- *   prepare: close finished output intervals (:229-236), stop after the
- *            last one, pick dt_step = dt_minlevel clipped to land on the
+ *   prepare: hold the group for a due regrid, close finished output
+ *            intervals (:229-236), stop after the last one, pick
+ *            dt_step = dt_minlevel / level_factor clipped to land on the
  *            interval end with the 1 % tolerance (:251-278), select the
  *            current state buffer and the hydrograph inflow at t_curr
  *            (hydrograph/hydrograh_module.f90:176-221).
@@ -39,13 +40,20 @@ __global__ void served_prepare_kernel(gf_group_state* __restrict__ gs,
                                       double* __restrict__ gdt, int* __restrict__ gpar,
                                       unsigned long long* __restrict__ gmax,
                                       const double* __restrict__ hy_t,
-                                      const double* __restrict__ hy_hu, int ng)
+                                      const double* __restrict__ hy_hu, int ng,
+                                      long long* __restrict__ qdelta)
 {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     gf_group_state s = gs[g];
     gmax[g] = 0ull;
     bool go = s.active != 0;
+    /* a regrid is due right after the accepted step that completes the
+     * interval (fc2d_geoclaw_run.c:388-395): wait for the host */
+    if (go && s.regrid_interval > 0 && s.since_regrid >= s.regrid_interval) {
+        s.paused = 1;
+        go = false;
+    }
     while (go && !(s.t_curr < s.tend)) {
         if (++s.nint >= s.nout) {
             s.active = 0;
@@ -57,10 +65,12 @@ __global__ void served_prepare_kernel(gf_group_state* __restrict__ gs,
     if (!go) {
         gdt[g] = 0.0;
         blocks[g].skip = 1;
+        if (qdelta) qdelta[g] = GF_QDELTA_SKIP;
         gs[g] = s;
         return;
     }
-    double dt_step = s.dt_minlevel;
+    /* advance-one-step: the step is the minlevel dt over 2^(maxlevel-minlevel) */
+    double dt_step = s.dt_minlevel / s.level_factor;
     const double tol = 1e-2 * dt_step;
     s.took_small = 0;
     const double small_step = s.tend - (s.t_curr + dt_step);
@@ -71,6 +81,7 @@ __global__ void served_prepare_kernel(gf_group_state* __restrict__ gs,
     s.dt_step = dt_step;
     gdt[g] = dt_step;
     gpar[g] = s.cur;
+    if (qdelta) qdelta[g] = s.cur ? (long long)(s.qb[1] - s.qb[0]) : 0ll;
     blocks[g].q = s.qb[s.cur];
     blocks[g].skip = 0;
     blocks[g].bc.q0hu = hydro_at(hy_t + s.hydro_off, hy_hu + s.hydro_off, s.nhydro, s.t_curr);
@@ -99,6 +110,7 @@ __global__ void served_finish_kernel(gf_group_state* __restrict__ gs,
         s.rejects++;
     } else {
         s.steps++;
+        s.since_regrid++;
         s.t_curr += s.dt_step;
         s.cur ^= 1;
         const double dt_new = s.dt_minlevel * s.desired_cfl / cfl;
@@ -111,11 +123,11 @@ __global__ void served_finish_kernel(gf_group_state* __restrict__ gs,
 
 cudaError_t launch_served_prepare(gf_group_state* gs, gf_ghost_block* blocks, double* gdt, int* gpar,
                                   unsigned long long* gmax, const double* hy_t,
-                                  const double* hy_hu, int ng, cudaStream_t st)
+                                  const double* hy_hu, int ng, cudaStream_t st, long long* qdelta)
 {
     if (ng <= 0) return cudaSuccess;
     served_prepare_kernel<<<(ng + 127) / 128, 128, 0, st>>>(gs, blocks, gdt, gpar, gmax, hy_t, hy_hu,
-                                                            ng);
+                                                            ng, qdelta);
     return cudaGetLastError();
 }
 

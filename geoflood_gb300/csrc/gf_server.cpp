@@ -302,6 +302,7 @@ int admit(gf_server* srv, Scen* s)
     g.desired_cfl = sc.desired_cfl;
     g.max_cfl = sc.max_cfl;
     g.nout = sc.nout;
+    g.level_factor = 1.0; /* one level */
     g.active = 1;
     g.cur = 0;
     g.nhydro = (int)s->hy_t.size();

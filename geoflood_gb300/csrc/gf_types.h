@@ -57,6 +57,10 @@ typedef struct gf_ghost_block {
     int pad;
 } gf_ghost_block;
 
+/* Per-group q-pointer offset of a group with no step this round: its
+ * coarse/fine transfer tasks are skipped. */
+#define GF_QDELTA_SKIP (-0x7fffffffffffffffLL - 1)
+
 /* A patch of a ghost-fill list: (block, block-local patch index). */
 typedef struct gf_ghost_ref {
     int block, local;
@@ -68,13 +72,16 @@ typedef struct gf_group_state {
     double* qb[2];             /* the scenario's two state buffers            */
     double t_curr, tend, dt_outer, dt_minlevel, dt_step;
     double desired_cfl, max_cfl, max_cfl_seen;
+    double level_factor;       /* step = dt_minlevel / level_factor           */
     long long steps, rejects;
     int nint, nout;            /* output interval in progress / count         */
     int took_small;
     int active;                /* 0: the run is over (or never started)       */
     int cur;                   /* state buffer holding the current solution   */
     int hydro_off, nhydro;     /* samples in the lane's hydrograph table      */
-    int pad;
+    int regrid_interval;       /* accepted steps between regrids (0: never)   */
+    int since_regrid;          /* accepted steps since the last regrid        */
+    int paused;                /* 1: waiting for the host to regrid           */
 } gf_group_state;
 
 /* Fill of one patch's planes from pyramid windows (gf_forest_kernels.cu):
@@ -99,6 +106,7 @@ typedef struct gf_xfer_task {
     double* qf;
     const double* af;
     int kind, code, ox, oy, phys;
+    int group; /* with a per-group offset table: q pointers are shifted by it */
 } gf_xfer_task;
 
 typedef struct gf_tinterp_task {

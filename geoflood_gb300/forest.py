@@ -145,3 +145,20 @@ class Forest:
         if q.shape != (self.npatch, self.mx + 4, self.mx + 4, 3):
             raise GeoFloodError(-1, "q must match the current leaves")
         _check(self.ctx.h, self._lib.gf_forest_upload(self.h, dptr(q)))
+
+
+def batch_run(forests, t_final: float, nout: int = 1, initial_dt: float = 1.0,
+              desired_cfl: float = 0.9, max_cfl: float = 1.0) -> dict:
+    """Run several forests of one context together (gf_forest_batch_run):
+    shared launches, device-side time-step control, one captured round per
+    epoch. Each forest ends exactly as its own Forest.run would."""
+    forests = list(forests)
+    if not forests:
+        raise ValueError("no forests")
+    ctx = forests[0].ctx
+    arr = (C.c_void_p * len(forests))(*[f.h for f in forests])
+    st = _lib.gf_forest_batch_stats()
+    _check(ctx.h, _lib.load().gf_forest_batch_run(arr, len(forests), t_final, nout, initial_dt,
+                                                  desired_cfl, max_cfl, C.byref(st)))
+    return {k: getattr(st, k) for k, _ in _lib.gf_forest_batch_stats._fields_}
+

@@ -376,6 +376,24 @@ int gf_forest_download(gf_forest* f, double* q);
 int gf_forest_download_aux(gf_forest* f, double* aux);
 int gf_forest_upload(gf_forest* f, const double* q);
 
+/* Batched form: n forests of one context run the same outstyle-1 loop
+ * (each with its own dt, CFL, output times and regrid cadence) in shared
+ * launches. The time-step control runs on the device; one round (step
+ * control, coarse/fine exchange, ghost fill, patch update of every leaf of
+ * every forest, CFL reduction) is captured as a CUDA graph per epoch and
+ * replayed; a forest whose regrid is due waits on the device until the
+ * host regrids it, after which the epoch is rebuilt and captured again.
+ * Each forest's result equals its own gf_forest_run. */
+typedef struct gf_forest_batch_stats {
+    long long rounds;        /* graph replays                               */
+    long long epochs;        /* captures (membership or tables changed)     */
+    long long regrids;       /* forest regrids                              */
+    long long launches;      /* kernel launches inside the replayed rounds  */
+    long long cell_updates;  /* all forests                                 */
+} gf_forest_batch_stats;
+int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout, double initial_dt,
+                        double desired_cfl, double max_cfl, gf_forest_batch_stats* st);
+
 /* ------------------------------------------------- served scenarios */
 /* A request loop over flood scenarios (continuous batching). Each admitted
  * scenario keeps its state resident on the device; every batching round

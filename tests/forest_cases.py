@@ -8,9 +8,9 @@ M, NBX, NBY, LMIN, LMAX = 8, 2, 1, 1, 3
 DX0 = 1000.0 / M            # 1000 m root blocks
 
 
-def rasters(kind="dambreak", seed=3):
-    nx, ny = NBX * M << LMAX, NBY * M << LMAX
-    dxf = DX0 / (1 << LMAX)
+def rasters(kind="dambreak", seed=3, m=M, lmax=LMAX):
+    nx, ny = NBX * m << lmax, NBY * m << lmax
+    dxf = 1000.0 / m / (1 << lmax)
     b = synth.bump_ramp_dem(nx, ny, dxf, dxf, seed=seed)
     q = np.zeros((ny, nx, 3))
     if kind == "lake":
