@@ -540,6 +540,7 @@ def run_gpu(args):
         result["served"] = served_stream(args)
     if rank == 0 and not args.no_forest:
         result["forest"] = forest_leg(args, local)
+        result["batched"] = batched_leg(args, local)
     if rank == 0:
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
@@ -617,6 +618,79 @@ def forest_leg(args, dev=0):
     }
 
 
+def batched_leg(args, dev=0):
+    """Batched AMR (config 3): forests with mx drawn from {8, 16, 32},
+    levels 2..5, target patch counts log-uniform in [50, 5000], fractal
+    valley DEM, reservoir + inflow hydrograph, n ~ U[0.02, 0.08], regrid every
+    4 steps; a bounded simulated time. The same forests run once as one
+    batch (shared launches, device-side control, captured rounds) and once
+    one after another with Forest.run; a sample is checked bit for bit."""
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+    from geoflood_gb300.forest import batch_run
+
+    n = args.batch_forests
+    T = args.batch_time
+    g = np.random.default_rng(SEED + 3)
+    targets = np.exp(g.uniform(np.log(50), np.log(5000), n))
+    specs = [synth.flood_forest(SEED + 100 + k, float(targets[k])) for k in range(n)]
+    ctx = gf.Context(dev)
+
+    def build():
+        fs = []
+        for k, sp in enumerate(specs):
+            ctx.set_phys(1 + k, sp["phys"])
+            F = gf.Forest(ctx, sp["mx"], sp["nbx"], sp["nby"], sp["minlevel"], sp["maxlevel"],
+                          sp["dx0"], sp["dy0"], sp["aux"], sp["q"], mthbc=sp["mthbc"],
+                          regrid_interval=sp["regrid_interval"], refine=sp["refine"],
+                          phys_slot=1 + k)
+            F.set_hydrograph(*sp["hydro"])
+            F.init()
+            fs.append(F)
+        return fs
+
+    A = build()
+    patches0 = [F.npatch for F in A]
+    t0 = time.perf_counter()
+    bst = batch_run(A, T, 1, 1.6, 0.9, 1.0)
+    el_b = time.perf_counter() - t0
+    sample = list(range(0, n, max(1, n // 8)))
+    ref = {k: (A[k].patches(), A[k].download(), A[k].stats()) for k in sample}
+    work = sum(F.stats()["cell_updates"] for F in A)
+    pmax = [F.stats()["npatch_max"] for F in A]
+    for F in A:
+        F.close()
+    B = build()
+    t0 = time.perf_counter()
+    for F in B:
+        F.run(T, 1, 1.6, 0.9, 1.0)
+    el_s = time.perf_counter() - t0
+    work_s = sum(F.stats()["cell_updates"] for F in B)
+    same = all(np.array_equal(ref[k][0], B[k].patches())
+               and np.array_equal(ref[k][1][:, 2:-2, 2:-2], B[k].download()[:, 2:-2, 2:-2])
+               and ref[k][2]["steps"] == B[k].stats()["steps"] for k in sample)
+    for F in B:
+        F.close()
+    ctx.close()
+    mxs = [sp["mx"] for sp in specs]
+    return {
+        "workload": f"{n} forests, mx in {{8,16,32}} ({mxs.count(8)}/{mxs.count(16)}/"
+                    f"{mxs.count(32)}), levels 2-5, target patches log-uniform [50, 5000], "
+                    f"{T:g} s simulated, regrid every 4 steps",
+        "value": work / el_b, "unit": METRIC, "seconds": el_b,
+        "one_by_one": {"value": work_s / el_s, "unit": METRIC, "seconds": el_s,
+                       "note": "same forests, Forest.run one after another"},
+        "speedup_vs_one_by_one": (work / el_b) / (work_s / el_s),
+        "batch_equals_one_by_one": bool(same), "checked_forests": len(sample),
+        "patches_initial": [int(min(patches0)), int(max(patches0)), int(sum(patches0))],
+        "patches_max": [int(min(pmax)), int(max(pmax))],
+        "rounds": bst["rounds"], "epochs": bst["epochs"], "regrids": bst["regrids"],
+        "launches": bst["launches"], "cell_updates": work,
+        "host_seconds": {"rounds": bst["s_rounds"], "regrid": bst["s_regrid"],
+                         "epoch": bst["s_epoch"]},
+    }
+
+
 def fp64_rates():
     """Measured FP64 pipe rates of this GPU (gf_measure_fp64_rates), ops/s."""
     import ctypes as C
@@ -643,6 +717,9 @@ def main():
     ap.add_argument("--no-forest", action="store_true")
     ap.add_argument("--forest-only", action="store_true")
     ap.add_argument("--forest-steps", type=int, default=200)
+    ap.add_argument("--batch-forests", type=int, default=64)
+    ap.add_argument("--batch-time", type=float, default=10.0)
+    ap.add_argument("--batched-only", action="store_true")
     ap.add_argument("--served-scenarios", type=int, default=512)
     ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
     ap.add_argument("--served-reserve-sms", type=int, default=None)
@@ -651,6 +728,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.batched_only:
+        print(json.dumps({"batched": batched_leg(args)}))
+        return 0
     if args.forest_only:
         print(json.dumps({"forest": forest_leg(args)}))
         return 0

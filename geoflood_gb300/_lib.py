@@ -119,7 +119,8 @@ class gf_forest_stats(C.Structure):
 
 class gf_forest_batch_stats(C.Structure):
     _fields_ = [("rounds", C.c_longlong), ("epochs", C.c_longlong), ("regrids", C.c_longlong),
-                ("launches", C.c_longlong), ("cell_updates", C.c_longlong)]
+                ("launches", C.c_longlong), ("cell_updates", C.c_longlong),
+                ("s_rounds", C.c_double), ("s_regrid", C.c_double), ("s_epoch", C.c_double)]
 
 
 XFER_AVG_FACE, XFER_AVG_CORNER, XFER_INTERP_FACE = 0, 1, 2

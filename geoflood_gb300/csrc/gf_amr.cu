@@ -375,7 +375,12 @@ __global__ void __launch_bounds__(128) tag_kernel(const gf_tag_task* __restrict_
     const int ti = blockIdx.x;
     if (ti >= ntask) return;
     const gf_tag_task T = tasks[ti];
-    const gf_refine& rf = *rfp;
+    const gf_refine& rf = T.rf ? *T.rf : *rfp;
+    if (T.rf) {
+        maxlevel = T.maxlevel;
+        init_flag = T.init_flag;
+        t = T.t;
+    }
     const gf_phys& P = phys_table[T.phys];
     const bool coarsen = T.nsib == 4;
     __shared__ int verdict;

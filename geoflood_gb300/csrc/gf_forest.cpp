@@ -32,11 +32,11 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "gf_internal.h"
@@ -70,11 +70,6 @@ struct Leaf {
     int level, I, J, slot;
 };
 
-inline uint64_t lkey(int l, int I, int J)
-{
-    return ((uint64_t)l << 56) | ((uint64_t)(uint32_t)J << 28) | (uint64_t)(uint32_t)I;
-}
-
 inline bool canon_less(const Leaf& a, const Leaf& b)
 {
     if (a.level != b.level) return a.level < b.level;
@@ -105,7 +100,7 @@ struct gf_forest {
     std::vector<int> free_slots;
     /* leaves */
     std::vector<Leaf> leaves;
-    std::unordered_map<uint64_t, int> index; /* key -> position in leaves */
+    std::vector<std::vector<int>> grid; /* per level: position in leaves at (I, J), or -1 */
     /* boundary conditions */
     gf_bc_spec bc{};
     std::vector<double> hy_t, hy_hu;
@@ -162,8 +157,10 @@ inline double* aslot(gf_forest* f, int slot) { return f->aux + (size_t)slot * f-
 
 int find(const gf_forest* f, int l, int I, int J)
 {
-    auto it = f->index.find(lkey(l, I, J));
-    return it == f->index.end() ? -1 : it->second;
+    if (l < f->o.minlevel || l > f->o.maxlevel || I < 0 || J < 0) return -1;
+    const int nx = f->o.nbx << l;
+    if (I >= nx || J >= (f->o.nby << l)) return -1;
+    return f->grid[l][(size_t)J * nx + I];
 }
 
 /* leaf containing the level-l cell block (I, J) at level <= l, or -1 */
@@ -184,12 +181,18 @@ inline bool inside(const gf_forest* f, int l, int I, int J)
 void reindex(gf_forest* f)
 {
     std::sort(f->leaves.begin(), f->leaves.end(), canon_less);
-    f->index.clear();
-    f->index.reserve(f->leaves.size() * 2);
+    if ((int)f->grid.size() != f->o.maxlevel + 1) {
+        f->grid.assign(f->o.maxlevel + 1, {});
+        for (int l = f->o.minlevel; l <= f->o.maxlevel; ++l)
+            f->grid[l].assign((size_t)(f->o.nbx << l) * (f->o.nby << l), -1);
+    } else {
+        for (int l = f->o.minlevel; l <= f->o.maxlevel; ++l)
+            std::fill(f->grid[l].begin(), f->grid[l].end(), -1);
+    }
     f->cells = 0;
     for (size_t k = 0; k < f->leaves.size(); ++k) {
         const Leaf& L = f->leaves[k];
-        f->index[lkey(L.level, L.I, L.J)] = (int)k;
+        f->grid[L.level][(size_t)L.J * (f->o.nbx << L.level) + L.I] = (int)k;
         f->cells += (long long)f->M * f->M;
     }
     f->dirty = true;
@@ -234,40 +237,6 @@ int build_pyramid(gf_forest* f, const double* fields)
     }
     cudaFree(stage);
     return rc;
-}
-
-/* fill new leaves' planes from the pyramid: aux fields, and q when with_q */
-int fill_from_pyramid(gf_forest* f, const std::vector<Leaf>& fresh, bool with_q)
-{
-    if (fresh.empty()) return GF_OK;
-    cudaStream_t st = gf::ctx_stream(f->ctx);
-    std::vector<gf_fill_task> t(fresh.size());
-    for (size_t k = 0; k < fresh.size(); ++k) {
-        const Leaf& L = fresh[k];
-        gf_fill_task& x = t[k];
-        std::memset(&x, 0, sizeof x);
-        int n = 0;
-        const size_t base = (size_t)(L.level - f->o.minlevel) * f->nf;
-        for (int a = 0; a < f->o.maux; ++a, ++n) {
-            x.src[n] = f->pyr[base + a];
-            x.dst[n] = aslot(f, L.slot) + (size_t)a * f->S;
-        }
-        if (with_q)
-            for (int m = 0; m < 3; ++m, ++n) {
-                x.src[n] = f->pyr[base + f->o.maux + m];
-                x.dst[n] = qslot(f, f->par, L.slot) + (size_t)m * f->S;
-            }
-        x.nfield = n;
-        x.nx = nx_at(f, L.level);
-        x.I = L.I;
-        x.J = L.J;
-    }
-    FK(f, f->d_fill.reserve(t.size()));
-    FK(f, cudaMemcpyAsync(f->d_fill.p, t.data(), t.size() * sizeof(gf_fill_task),
-                          cudaMemcpyHostToDevice, st));
-    FK(f, gf::launch_patch_fill(f->M, f->d_fill.p, (int)t.size(), st));
-    FK(f, cudaStreamSynchronize(st)); /* the task vector is pageable and about to go */
-    return GF_OK;
 }
 
 } // namespace
@@ -442,7 +411,7 @@ int build_tables(gf_forest* f)
     if (!ref_all.empty())
         FK(f, cudaMemcpyAsync(f->d_refs_lv.p, ref_all.data(), ref_all.size() * sizeof(gf_ghost_ref),
                               cudaMemcpyHostToDevice, st));
-    FK(f, cudaStreamSynchronize(st)); /* host vectors go out of scope */
+    /* pageable sources are staged before each copy call returns */
     f->h_work.swap(work);
     f->h_avg.swap(avg[0]);
     f->h_itp.assign(nlev, {});
@@ -534,78 +503,116 @@ int step(gf_forest* f, double t, double dt, double* cfl)
 
 namespace {
 
-/* Refinement tags (leaves below maxlevel) and coarsening tags (complete
- * families above minlevel, children ll, lr, ul, ur). */
-int run_tags(gf_forest* f, double t, int init_flag, std::vector<char>& refine,
-             std::vector<std::array<int, 4>>& fams, std::vector<char>& coarsen)
+/* One forest's regrid in flight: tags, then the new leaves. */
+struct Regrid {
+    gf_forest* f = nullptr;
+    double t = 0.0;
+    int init_flag = 0;
+    std::vector<int> who;                   /* leaf of each refinement-tag task */
+    std::vector<std::array<int, 4>> fams;   /* complete families (ll, lr, ul, ur) */
+    std::vector<char> refine, coarsen;
+    size_t base = 0;                        /* first tag of this forest in its class */
+    bool changed = false;
+};
+
+inline int mclass_of(int mx) { return mx == 8 ? 0 : mx == 16 ? 1 : 2; }
+const int kMx[3] = {8, 16, 32};
+
+gf_tag_task tag_task(gf_forest* f, const Regrid& R, int level, int nsib)
 {
-    const gf_forest_opts& o = f->o;
-    std::vector<gf_tag_task> tk;
-    std::vector<int> who;
-    for (size_t k = 0; k < f->leaves.size(); ++k) {
-        const Leaf& L = f->leaves[k];
-        if (L.level >= o.maxlevel) continue;
-        gf_tag_task x;
-        std::memset(&x, 0, sizeof x);
-        x.q[0] = qslot(f, f->par, L.slot);
-        x.aux[0] = aslot(f, L.slot);
-        x.xlower[0] = o.x0 + (double)L.I * f->M * dx_at(f, L.level);
-        x.ylower[0] = o.y0 + (double)L.J * f->M * dy_at(f, L.level);
-        x.dx = dx_at(f, L.level);
-        x.dy = dy_at(f, L.level);
-        x.level = L.level;
-        x.nsib = 1;
-        x.phys = o.phys_slot;
-        tk.push_back(x);
-        who.push_back((int)k);
-    }
-    const size_t nref = tk.size();
-    fams.clear();
-    if (!init_flag) {
+    gf_tag_task x;
+    std::memset(&x, 0, sizeof x);
+    x.dx = dx_at(f, level);
+    x.dy = dy_at(f, level);
+    x.level = level;
+    x.nsib = nsib;
+    x.phys = f->o.phys_slot;
+    x.rf = f->d_refine.p;
+    x.t = R.t;
+    x.maxlevel = f->o.maxlevel;
+    x.init_flag = R.init_flag;
+    return x;
+}
+
+/* Refinement tags (leaves below maxlevel) and coarsening tags (complete
+ * families above minlevel) of several forests: one launch per patch size. */
+int run_tags(gf_ctx* ctx, std::vector<Regrid>& W)
+{
+    std::vector<gf_tag_task> tk[3];
+    for (Regrid& R : W) {
+        gf_forest* f = R.f;
+        const gf_forest_opts& o = f->o;
+        const int c = mclass_of(f->M);
+        R.base = tk[c].size();
+        R.who.clear();
+        R.fams.clear();
         for (size_t k = 0; k < f->leaves.size(); ++k) {
             const Leaf& L = f->leaves[k];
-            if (L.level <= o.minlevel || (L.I & 1) || (L.J & 1)) continue;
-            std::array<int, 4> fam;
-            bool full = true;
-            for (int c = 0; c < 4 && full; ++c) {
-                fam[c] = find(f, L.level, L.I + (c & 1), L.J + (c >> 1));
-                full = fam[c] >= 0;
-            }
-            if (!full) continue;
-            gf_tag_task x;
-            std::memset(&x, 0, sizeof x);
-            for (int c = 0; c < 4; ++c) {
-                const Leaf& C = f->leaves[fam[c]];
-                x.q[c] = qslot(f, f->par, C.slot);
-                x.aux[c] = aslot(f, C.slot);
-                x.xlower[c] = o.x0 + (double)C.I * f->M * dx_at(f, C.level);
-                x.ylower[c] = o.y0 + (double)C.J * f->M * dy_at(f, C.level);
-            }
-            x.dx = dx_at(f, L.level);
-            x.dy = dy_at(f, L.level);
-            x.level = L.level;
-            x.nsib = 4;
-            x.phys = o.phys_slot;
-            tk.push_back(x);
-            fams.push_back(fam);
+            if (L.level >= o.maxlevel) continue;
+            gf_tag_task x = tag_task(f, R, L.level, 1);
+            x.q[0] = qslot(f, f->par, L.slot);
+            x.aux[0] = aslot(f, L.slot);
+            x.xlower[0] = o.x0 + (double)L.I * f->M * dx_at(f, L.level);
+            x.ylower[0] = o.y0 + (double)L.J * f->M * dy_at(f, L.level);
+            tk[c].push_back(x);
+            R.who.push_back((int)k);
         }
+        if (!R.init_flag) {
+            for (size_t k = 0; k < f->leaves.size(); ++k) {
+                const Leaf& L = f->leaves[k];
+                if (L.level <= o.minlevel || (L.I & 1) || (L.J & 1)) continue;
+                std::array<int, 4> fam;
+                bool full = true;
+                for (int cc = 0; cc < 4 && full; ++cc) {
+                    fam[cc] = find(f, L.level, L.I + (cc & 1), L.J + (cc >> 1));
+                    full = fam[cc] >= 0;
+                }
+                if (!full) continue;
+                gf_tag_task x = tag_task(f, R, L.level, 4);
+                for (int cc = 0; cc < 4; ++cc) {
+                    const Leaf& C = f->leaves[fam[cc]];
+                    x.q[cc] = qslot(f, f->par, C.slot);
+                    x.aux[cc] = aslot(f, C.slot);
+                    x.xlower[cc] = o.x0 + (double)C.I * f->M * dx_at(f, C.level);
+                    x.ylower[cc] = o.y0 + (double)C.J * f->M * dy_at(f, C.level);
+                }
+                tk[c].push_back(x);
+                R.fams.push_back(fam);
+            }
+        }
+        R.refine.assign(f->leaves.size(), 0);
+        R.coarsen.assign(R.fams.size(), 0);
     }
-    refine.assign(f->leaves.size(), 0);
-    coarsen.assign(fams.size(), 0);
-    if (tk.empty()) return GF_OK;
-    cudaStream_t st = gf::ctx_stream(f->ctx);
-    std::vector<int> tags(tk.size());
-    FK(f, f->d_tagt.reserve(tk.size()));
-    FK(f, f->d_tags.reserve(tk.size()));
-    FK(f, f->d_refine.reserve(1));
-    FK(f, cudaMemcpyAsync(f->d_refine.p, &o.refine, sizeof(gf_refine), cudaMemcpyHostToDevice, st));
-    FK(f, cudaMemcpyAsync(f->d_tagt.p, tk.data(), tk.size() * sizeof(gf_tag_task), cudaMemcpyHostToDevice, st));
-    FK(f, gf::launch_tags(f->M, f->d_tagt.p, (int)tk.size(), f->d_refine.p, gf::ctx_device_phys(f->ctx),
-                          o.maxlevel, init_flag, t, f->d_tags.p, st));
-    FK(f, cudaMemcpyAsync(tags.data(), f->d_tags.p, tk.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
-    FK(f, cudaStreamSynchronize(st));
-    for (size_t k = 0; k < nref; ++k) refine[who[k]] = tags[k] != 0;
-    for (size_t k = 0; k < fams.size(); ++k) coarsen[k] = tags[nref + k] != 0;
+    size_t total = tk[0].size() + tk[1].size() + tk[2].size();
+    if (total == 0) return GF_OK;
+    cudaStream_t st = gf::ctx_stream(ctx);
+    gf_tag_task* d_t = nullptr;
+    int* d_tags = nullptr;
+    std::vector<int> tags(total);
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&d_t), total * sizeof(gf_tag_task), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&d_tags), total * sizeof(int), st);
+    size_t off = 0;
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+        if (tk[c].empty()) continue;
+        e = cudaMemcpyAsync(d_t + off, tk[c].data(), tk[c].size() * sizeof(gf_tag_task),
+                            cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = gf::launch_tags(kMx[c], d_t + off, (int)tk[c].size(), nullptr, gf::ctx_device_phys(ctx), 0,
+                                0, 0.0, d_tags + off, st);
+        off += tk[c].size();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(tags.data(), d_tags, total * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (d_t) cudaFreeAsync(d_t, st);
+    if (d_tags) cudaFreeAsync(d_tags, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return gf::ctx_cuda_fail(ctx, e, "refinement tags");
+    size_t cbase[3] = {0, tk[0].size(), tk[0].size() + tk[1].size()};
+    for (Regrid& R : W) {
+        const int* tg = tags.data() + cbase[mclass_of(R.f->M)] + R.base;
+        for (size_t k = 0; k < R.who.size(); ++k) R.refine[R.who[k]] = tg[k] != 0;
+        for (size_t m = 0; m < R.fams.size(); ++m) R.coarsen[m] = tg[R.who.size() + m] != 0;
+    }
     return GF_OK;
 }
 
@@ -644,114 +651,195 @@ bool family_can_merge(const gf_forest* f, int l, int PI, int PJ, const std::vect
             const int I = 2 * PI + a, J = 2 * PJ + b;
             if (!inside(f, l, I, J)) continue;
             const int q = containing(f, l, I, J);
-            if (q < 0) return false;                                   /* finer than l */
-            if (f->leaves[q].level == l && split[q]) return false;     /* will be l + 1 */
+            if (q < 0) return false;                               /* finer than l */
+            if (f->leaves[q].level == l && split[q]) return false; /* will be l + 1 */
         }
     return true;
 }
 
-} // namespace
-
-namespace {
-
-/* Replace split leaves by their children and merged families by their
- * parents. Children / parents take interpolate2fine / average2coarse of
- * the current state (or, at initialisation, the rasters); every new patch
- * takes its aux fields from the pyramid. */
-int apply_changes(gf_forest* f, const std::vector<char>& split,
-                  const std::vector<std::array<int, 4>>& fams, const std::vector<char>& merge,
-                  bool init, bool* changed)
+gf_fill_task fill_task(gf_forest* f, const Leaf& L, bool with_q)
 {
-    size_t need = 0;
-    std::vector<char> in_merge(f->leaves.size(), 0);
-    for (size_t k = 0; k < split.size(); ++k) need += split[k] ? 4 : 0;
-    for (size_t m = 0; m < fams.size(); ++m)
-        if (merge[m]) {
-            need += 1;
-            for (int c = 0; c < 4; ++c) in_merge[fams[m][c]] = 1;
-        }
-    if (changed) *changed = need > 0;
-    if (need == 0) return GF_OK;
-    if (need > f->free_slots.size())
-        return ffail(f, GF_ERR_NOMEM, "forest slot pool exhausted (raise max_patches)");
-    std::vector<Leaf> next, fresh;
-    std::vector<gf_xfer_task> xt;
-    std::vector<int> freed;
-    const int b = f->par;
-    for (size_t k = 0; k < f->leaves.size(); ++k) {
-        const Leaf& P = f->leaves[k];
-        if (in_merge[k]) continue;
-        if (!split[k]) {
-            next.push_back(P);
-            continue;
-        }
-        for (int c = 0; c < 4; ++c) {
-            Leaf C{P.level + 1, 2 * P.I + (c & 1), 2 * P.J + (c >> 1), alloc_slot(f)};
-            next.push_back(C);
-            fresh.push_back(C);
-            if (!init) xt.push_back(xtask(f, b, GF_XFER_INTERP2FINE, P.slot, C.slot, c, 0, 0));
-        }
-        freed.push_back(P.slot);
+    gf_fill_task x;
+    std::memset(&x, 0, sizeof x);
+    int n = 0;
+    const size_t base = (size_t)(L.level - f->o.minlevel) * f->nf;
+    for (int a = 0; a < f->o.maux; ++a, ++n) {
+        x.src[n] = f->pyr[base + a];
+        x.dst[n] = aslot(f, L.slot) + (size_t)a * f->S;
     }
-    for (size_t m = 0; m < fams.size(); ++m) {
-        if (!merge[m]) continue;
-        const Leaf& C0 = f->leaves[fams[m][0]];
-        Leaf Pn{C0.level - 1, C0.I >> 1, C0.J >> 1, alloc_slot(f)};
-        next.push_back(Pn);
-        fresh.push_back(Pn);
-        for (int c = 0; c < 4; ++c) {
-            const Leaf& C = f->leaves[fams[m][c]];
-            xt.push_back(xtask(f, b, GF_XFER_AVG2COARSE, Pn.slot, C.slot, c, 0, 0));
-            freed.push_back(C.slot);
+    if (with_q)
+        for (int m = 0; m < 3; ++m, ++n) {
+            x.src[n] = f->pyr[base + f->o.maux + m];
+            x.dst[n] = qslot(f, f->par, L.slot) + (size_t)m * f->S;
         }
+    x.nfield = n;
+    x.nx = nx_at(f, L.level);
+    x.I = L.I;
+    x.J = L.J;
+    return x;
+}
+
+/* Fill tasks and transfer tasks, one launch of each per patch size. */
+int launch_fills_and_transfers(gf_ctx* ctx, std::vector<gf_fill_task>* fill,
+                               std::vector<gf_xfer_task>* xfer)
+{
+    size_t nf = 0, nx = 0;
+    for (int c = 0; c < 3; ++c) {
+        nf += fill[c].size();
+        nx += xfer[c].size();
     }
-    int rc = fill_from_pyramid(f, fresh, init);
-    if (rc) return rc;
-    if (!xt.empty()) {
-        cudaStream_t st = gf::ctx_stream(f->ctx);
-        FK(f, f->d_rgx.reserve(xt.size()));
-        FK(f, cudaMemcpyAsync(f->d_rgx.p, xt.data(), xt.size() * sizeof(gf_xfer_task),
-                              cudaMemcpyHostToDevice, st));
-        FK(f, gf::launch_transfer(f->M, f->d_rgx.p, (int)xt.size(), gf::ctx_device_phys(f->ctx), st));
-        FK(f, cudaStreamSynchronize(st));
+    if (nf + nx == 0) return GF_OK;
+    cudaStream_t st = gf::ctx_stream(ctx);
+    gf_fill_task* d_f = nullptr;
+    gf_xfer_task* d_x = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (nf) e = cudaMallocAsync(reinterpret_cast<void**>(&d_f), nf * sizeof(gf_fill_task), st);
+    if (e == cudaSuccess && nx) e = cudaMallocAsync(reinterpret_cast<void**>(&d_x), nx * sizeof(gf_xfer_task), st);
+    size_t of = 0, ox = 0;
+    /* fills first: interpolate2fine reads the children's bathymetry */
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+        if (fill[c].empty()) continue;
+        e = cudaMemcpyAsync(d_f + of, fill[c].data(), fill[c].size() * sizeof(gf_fill_task),
+                            cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = gf::launch_patch_fill(kMx[c], d_f + of, (int)fill[c].size(), st);
+        of += fill[c].size();
     }
-    /* old slots return to the pool only after the transfers read them */
-    for (int s : freed) f->free_slots.push_back(s);
-    f->leaves.swap(next);
-    reindex(f);
-    f->st.npatch = (int)f->leaves.size();
-    f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+    for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+        if (xfer[c].empty()) continue;
+        e = cudaMemcpyAsync(d_x + ox, xfer[c].data(), xfer[c].size() * sizeof(gf_xfer_task),
+                            cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = gf::launch_transfer(kMx[c], d_x + ox, (int)xfer[c].size(), gf::ctx_device_phys(ctx), st);
+        ox += xfer[c].size();
+    }
+    if (d_f) cudaFreeAsync(d_f, st);
+    if (d_x) cudaFreeAsync(d_x, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st); /* old slots are read before reuse */
+    if (e != cudaSuccess) return gf::ctx_cuda_fail(ctx, e, "regrid transfers");
     return GF_OK;
+}
+
+/* Decide splits and merges from the tags and replace the leaves of every
+ * forest; children / parents take interpolate2fine / average2coarse of the
+ * current state (at initialisation: the rasters); new patches take their aux
+ * fields from the pyramid. */
+int apply_regrids(gf_ctx* ctx, std::vector<Regrid>& W, bool init)
+{
+    std::vector<gf_fill_task> fill[3];
+    std::vector<gf_xfer_task> xfer[3];
+    std::vector<std::vector<Leaf>> next(W.size());
+    std::vector<std::vector<int>> freed(W.size());
+    for (size_t w = 0; w < W.size(); ++w) {
+        Regrid& R = W[w];
+        gf_forest* f = R.f;
+        const int c = mclass_of(f->M);
+        std::vector<char> split = R.refine;
+        balance_splits(f, split);
+        std::vector<char> merge(R.fams.size(), 0);
+        for (size_t m = 0; m < R.fams.size(); ++m) {
+            if (!R.coarsen[m]) continue;
+            bool any_split = false;
+            for (int cc = 0; cc < 4; ++cc) any_split |= split[R.fams[m][cc]] != 0;
+            const Leaf& C0 = f->leaves[R.fams[m][0]];
+            merge[m] = !any_split && family_can_merge(f, C0.level, C0.I >> 1, C0.J >> 1, split);
+        }
+        size_t need = 0;
+        std::vector<char> in_merge(f->leaves.size(), 0);
+        for (size_t k = 0; k < split.size(); ++k) need += split[k] ? 4 : 0;
+        for (size_t m = 0; m < R.fams.size(); ++m)
+            if (merge[m]) {
+                need += 1;
+                for (int cc = 0; cc < 4; ++cc) in_merge[R.fams[m][cc]] = 1;
+            }
+        R.changed = need > 0;
+        if (!R.changed) continue;
+        if (need > f->free_slots.size())
+            return ffail(f, GF_ERR_NOMEM, "forest slot pool exhausted (raise max_patches)");
+        const int b = f->par;
+        std::vector<Leaf>& nx = next[w];
+        for (size_t k = 0; k < f->leaves.size(); ++k) {
+            const Leaf& P = f->leaves[k];
+            if (in_merge[k]) continue;
+            if (!split[k]) {
+                nx.push_back(P);
+                continue;
+            }
+            for (int cc = 0; cc < 4; ++cc) {
+                Leaf C{P.level + 1, 2 * P.I + (cc & 1), 2 * P.J + (cc >> 1), alloc_slot(f)};
+                nx.push_back(C);
+                fill[c].push_back(fill_task(f, C, init));
+                if (!init) xfer[c].push_back(xtask(f, b, GF_XFER_INTERP2FINE, P.slot, C.slot, cc, 0, 0));
+            }
+            freed[w].push_back(P.slot);
+        }
+        for (size_t m = 0; m < R.fams.size(); ++m) {
+            if (!merge[m]) continue;
+            const Leaf& C0 = f->leaves[R.fams[m][0]];
+            Leaf Pn{C0.level - 1, C0.I >> 1, C0.J >> 1, alloc_slot(f)};
+            nx.push_back(Pn);
+            fill[c].push_back(fill_task(f, Pn, false));
+            for (int cc = 0; cc < 4; ++cc) {
+                const Leaf& C = f->leaves[R.fams[m][cc]];
+                xfer[c].push_back(xtask(f, b, GF_XFER_AVG2COARSE, Pn.slot, C.slot, cc, 0, 0));
+                freed[w].push_back(C.slot);
+            }
+        }
+    }
+    int rc = launch_fills_and_transfers(ctx, fill, xfer);
+    if (rc) return rc;
+    for (size_t w = 0; w < W.size(); ++w) {
+        Regrid& R = W[w];
+        if (!R.changed) continue;
+        gf_forest* f = R.f;
+        for (int sl : freed[w]) f->free_slots.push_back(sl);
+        f->leaves.swap(next[w]);
+        reindex(f);
+        f->st.npatch = (int)f->leaves.size();
+        f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+    }
+    return GF_OK;
+}
+
+/* Regrid several forests, each at its own time, with shared launches. */
+int regrid_many(gf_ctx* ctx, std::vector<gf_forest*>& fs, const std::vector<double>& ts)
+{
+    std::vector<Regrid> W(fs.size());
+    for (size_t k = 0; k < fs.size(); ++k) {
+        int rc = ghost_fill(fs[k], ts[k]); /* interpolate2fine reads the parents' ghost cells */
+        if (rc) return rc;
+        W[k].f = fs[k];
+        W[k].t = ts[k];
+        W[k].init_flag = 0;
+    }
+    int rc = run_tags(ctx, W);
+    if (!rc) rc = apply_regrids(ctx, W, false);
+    if (!rc)
+        for (gf_forest* f : fs) f->st.regrids++;
+    return rc;
 }
 
 int regrid(gf_forest* f, double t, bool* changed)
 {
-    int rc = ghost_fill(f, t);
-    if (rc) return rc;
-    std::vector<char> refine, coarsen;
-    std::vector<std::array<int, 4>> fams;
-    if ((rc = run_tags(f, t, 0, refine, fams, coarsen))) return rc;
-    std::vector<char> split = refine;
-    balance_splits(f, split);
-    std::vector<char> merge(fams.size(), 0);
-    for (size_t m = 0; m < fams.size(); ++m) {
-        if (!coarsen[m]) continue;
-        bool any_split = false;
-        for (int c = 0; c < 4; ++c) any_split |= split[fams[m][c]] != 0;
-        const Leaf& C0 = f->leaves[fams[m][0]];
-        merge[m] = !any_split && family_can_merge(f, C0.level, C0.I >> 1, C0.J >> 1, split);
+    std::vector<gf_forest*> fs{f};
+    std::vector<double> ts{t};
+    const size_t n0 = f->leaves.size();
+    std::vector<Leaf> before = f->leaves;
+    int rc = regrid_many(f->ctx, fs, ts);
+    if (changed) {
+        bool ch = f->leaves.size() != n0;
+        for (size_t k = 0; !ch && k < n0; ++k)
+            ch = f->leaves[k].level != before[k].level || f->leaves[k].I != before[k].I ||
+                 f->leaves[k].J != before[k].J;
+        *changed = ch;
     }
-    rc = apply_changes(f, split, fams, merge, false, changed);
-    if (!rc) f->st.regrids++;
     return rc;
 }
 
 int init_forest(gf_forest* f)
 {
     const gf_forest_opts& o = f->o;
-    /* all slots free, leaves at minlevel */
     f->free_slots.clear();
-    for (int s = f->cap - 1; s >= 0; --s) f->free_slots.push_back(s);
+    for (int s2 = f->cap - 1; s2 >= 0; --s2) f->free_slots.push_back(s2);
     f->leaves.clear();
     const size_t n0 = (size_t)npx_at(f, o.minlevel) * npy_at(f, o.minlevel);
     if (n0 > f->free_slots.size()) return ffail(f, GF_ERR_NOMEM, "max_patches below the minlevel patch count");
@@ -760,19 +848,23 @@ int init_forest(gf_forest* f)
             f->leaves.push_back(Leaf{o.minlevel, I, J, alloc_slot(f)});
     f->par = 0;
     reindex(f);
-    int rc = fill_from_pyramid(f, f->leaves, true);
-    if (rc) return rc;
+    {
+        std::vector<gf_fill_task> fill[3];
+        std::vector<gf_xfer_task> none[3];
+        for (const Leaf& L : f->leaves) fill[mclass_of(f->M)].push_back(fill_task(f, L, true));
+        int rc = launch_fills_and_transfers(f->ctx, fill, none);
+        if (rc) return rc;
+    }
     f->st = gf_forest_stats{};
     for (int pass = o.minlevel; pass < o.maxlevel; ++pass) {
-        std::vector<char> refine, coarsen;
-        std::vector<std::array<int, 4>> fams;
-        if ((rc = run_tags(f, 0.0, 1, refine, fams, coarsen))) return rc;
-        std::vector<char> split = refine;
-        balance_splits(f, split);
-        bool changed = false;
-        if ((rc = apply_changes(f, split, fams, std::vector<char>(fams.size(), 0), true, &changed)))
-            return rc;
-        if (!changed) break;
+        std::vector<Regrid> W(1);
+        W[0].f = f;
+        W[0].t = 0.0;
+        W[0].init_flag = 1;
+        int rc = run_tags(f->ctx, W);
+        if (!rc) rc = apply_regrids(f->ctx, W, true);
+        if (rc) return rc;
+        if (!W[0].changed) break;
     }
     f->st.npatch = (int)f->leaves.size();
     f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
@@ -904,6 +996,10 @@ int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, g
         if (!(o->mthbc[s] == 0 || o->mthbc[s] == 1 || o->mthbc[s] == 3))
             return gf::ctx_fail(c, GF_ERR_ARG, "forest mthbc must be 0, 1 or 3");
     if (o->regrid_interval < 0) return gf::ctx_fail(c, GF_ERR_ARG, "regrid_interval must be >= 0");
+    if (o->refine.num_speed_tolerance < 0 || o->refine.num_speed_tolerance > GF_MAX_SPEEDS ||
+        o->refine.num_flowgrades < 0 || o->refine.num_flowgrades > GF_MAX_FLOWGRADES ||
+        o->refine.num_regions < 0 || o->refine.num_regions > GF_MAX_REGIONS)
+        return gf::ctx_fail(c, GF_ERR_ARG, "refinement parameter counts out of range");
     int rc = gf::ctx_check_phys(c, o->phys_slot);
     if (rc) return rc;
     const long long full = (long long)o->nbx * o->nby << (2 * o->maxlevel);
@@ -930,6 +1026,14 @@ int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, g
     if ((rc = build_pyramid(f, fields))) {
         gf_forest_destroy(f);
         return rc;
+    }
+    /* the refinement criteria live on the device for the tag launches */
+    e = f->d_refine.reserve(1);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(f->d_refine.p, &o->refine, sizeof(gf_refine), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        gf_forest_destroy(f);
+        return gf::ctx_cuda_fail(c, e, "forest refinement criteria");
     }
     *out = f;
     return GF_OK;
@@ -1409,8 +1513,12 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
             B.fs.swap(live);
             rebuild = true;
         }
+        using clk = std::chrono::steady_clock;
+        auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
         if (rebuild) {
+            const auto te = clk::now();
             int rc = build_epoch(B);
+            S.s_epoch += secs(te);
             if (rc) return rc;
             S.epochs++;
             rebuild = false;
@@ -1419,6 +1527,7 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
         const int ng = (int)B.fs.size();
         int rounds = (int)std::ceil(0.5 / std::max(round_ms, 1e-3));
         rounds = std::max(1, std::min(64, rounds));
+        const auto tr = clk::now();
         BK(B, cudaEventRecord(B.ev0, B.st));
         for (int r = 0; r < rounds; ++r) BK(B, cudaGraphLaunch(B.exec, B.st));
         BK(B, cudaMemcpyAsync(B.h_rb, B.d + B.off_rb, 8, cudaMemcpyDeviceToHost, B.st));
@@ -1426,6 +1535,7 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
                               cudaMemcpyDeviceToHost, B.st));
         BK(B, cudaEventRecord(B.ev1, B.st));
         BK(B, cudaStreamSynchronize(B.st));
+        S.s_rounds += secs(tr);
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) round_ms = std::max(1e-3, (double)ms / rounds);
         S.rounds += rounds;
@@ -1458,11 +1568,18 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
         /* regrid the waiting forests together once all live ones wait, or
          * after a while (the others keep stepping meanwhile) */
         if (npaused && (npaused == nactive || rounds_paused >= 16)) {
-            for (gf_forest* f : B.fs) {
-                if (!f->gst.active || !f->gst.paused) continue;
-                bool changed = false;
-                int rc = regrid(f, f->gst.t_curr, &changed);
-                if (rc) return rc;
+            std::vector<gf_forest*> due;
+            std::vector<double> ts;
+            for (gf_forest* f : B.fs)
+                if (f->gst.active && f->gst.paused) {
+                    due.push_back(f);
+                    ts.push_back(f->gst.t_curr);
+                }
+            const auto tg = clk::now();
+            int rc = regrid_many(ctx, due, ts);
+            S.s_regrid += secs(tg);
+            if (rc) return rc;
+            for (gf_forest* f : due) {
                 f->gst.paused = 0;
                 f->gst.since_regrid = 0;
                 S.regrids++;

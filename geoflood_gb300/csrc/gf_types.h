@@ -123,6 +123,11 @@ typedef struct gf_tag_task {
     double xlower[4], ylower[4];
     double dx, dy;
     int level, nsib, phys;
+    /* rf != null: this task's criteria, time, maxlevel and init_flag replace
+     * the launch's (one launch then tags many forests) */
+    const gf_refine* rf;
+    double t;
+    int maxlevel, init_flag;
 } gf_tag_task;
 
 #endif

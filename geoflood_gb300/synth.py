@@ -298,3 +298,45 @@ def flood_scenario(seed: int, cells: float, mx: int | None = None, dx: float = 5
     return Scenario(mx=mx, npx=npx, npy=npy, dx=dx, dy=dx, q=qt, aux=at, t_final=p["horizon"],
                     phys=Phys(manning_coefficient=(p["manning"],), manning_break=(1.0e10,)),
                     mthbc=(0, 1, 3, 3), hydro=hy, nout=4, initial_dt=0.2, seed=seed)
+
+
+def flood_forest(seed: int, target_patches: float, mx: int | None = None, minlevel: int = 2,
+                 maxlevel: int = 5, wet_fraction: float = 0.5):
+    """One batched-AMR forest: nbx x nby root blocks (at most 4 x 2) sized so
+    that refining the wet part of the domain to maxlevel gives about
+    `target_patches` patches; fractal valley DEM (Hurst 0.8, 10 m relief,
+    0.002 slope), a reservoir at the left end sized for the target (surface
+    0.5 m above the 70th percentile of its bed), inflow hydrograph on the left
+    (peak Q ~ U[10, 500] m^3/s over a 40 m window, per unit width), n ~
+    U[0.02, 0.08]; finest cells are 2 m. Refinement: depth > 0.01 m up to
+    maxlevel. Returns the Forest keyword arguments plus 'hydro' and 'phys'."""
+    from . import Phys, Refine
+    g = rng(seed)
+    if mx is None:
+        mx = int(g.choice([8, 16, 32]))
+    full_per_block = 4 ** maxlevel
+    need = target_patches / max(wet_fraction, 1e-3)
+    layouts = [(1, 1), (2, 1), (2, 2), (4, 2)]
+    nbx, nby = next(((a, b) for a, b in layouts if a * b * full_per_block >= need), layouts[-1])
+    dxf = 2.0
+    nx, ny = nbx * mx << maxlevel, nby * mx << maxlevel
+    dx0 = dxf * (1 << maxlevel)
+    x = (np.arange(nx) + 0.5) * dxf
+    surf = _lattice_window(nx, ny, 0.8, seed)
+    surf = (surf - surf.min()) / max(surf.max() - surf.min(), 1e-300) * 10.0
+    b = surf + 0.002 * (nx * dxf - x)[None, :]
+    frac = min(1.0, target_patches / (0.7 * nbx * nby * full_per_block))
+    x_res = max(frac, 1.0 / nx) * nx * dxf
+    inres = np.broadcast_to(x[None, :] < x_res, b.shape)
+    level = float(np.percentile(b[inres], 70.0)) + 0.5
+    q = np.zeros((ny, nx, 3))
+    q[..., 0] = np.where(inres, np.maximum(level - b, 0.0), 0.0)
+    peak = float(g.uniform(10.0, 500.0))
+    width = 40.0
+    n = float(g.uniform(0.02, 0.08))
+    hydro = ([0.0, 60.0, 600.0], [0.1 * peak / width, peak / width, 0.1 * peak / width],
+             [1, 0, 0, 0], width, 0.0, 0.5 * ny * dxf)
+    return dict(mx=mx, nbx=nbx, nby=nby, minlevel=minlevel, maxlevel=maxlevel, dx0=dx0, dy0=dx0,
+                aux=b, q=q, mthbc=(0, 1, 3, 3), regrid_interval=4,
+                refine=Refine(wave_tolerance=1e9, flowgrades=((0.01, 1, 1, maxlevel),)),
+                hydro=hydro, phys=Phys(manning_coefficient=(n,), manning_break=(1e10,)))

@@ -390,6 +390,9 @@ typedef struct gf_forest_batch_stats {
     long long regrids;       /* forest regrids                              */
     long long launches;      /* kernel launches inside the replayed rounds  */
     long long cell_updates;  /* all forests                                 */
+    double s_rounds;         /* host seconds waiting on replayed rounds      */
+    double s_regrid;         /* host seconds in regrids                      */
+    double s_epoch;          /* host seconds building and capturing epochs   */
 } gf_forest_batch_stats;
 int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout, double initial_dt,
                         double desired_cfl, double max_cfl, gf_forest_batch_stats* st);
