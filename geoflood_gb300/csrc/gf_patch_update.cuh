@@ -354,7 +354,7 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 w[3 + 3 * mw + 0] = fw[mw][0];
                 w[3 + 3 * mw + 1] = fw[mw][1];
                 w[3 + 3 * mw + 2] = fw[mw][2];
-                smax = fmax(smax, fabs(s[mw]));
+                smax = d_max_nn<FAST>(smax, fabs(s[mw]));
             }
         }
         if (prev_t0 >= 0) gather(prev_t0, prev_t1);
@@ -383,9 +383,9 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
             double amdq[3] = {0.0, 0.0, 0.0}, apdq[3] = {0.0, 0.0, 0.0};
 #pragma unroll
             for (int mw = 0; mw < 3; ++mw) {
-                if (s[mw] < 0.0) {
+                if (d_ltz<FAST>(s[mw])) {
                     amdq[0] += fw[mw][0]; amdq[1] += fw[mw][1]; amdq[2] += fw[mw][2];
-                } else if (s[mw] > 0.0) {
+                } else if (d_gtz<FAST>(s[mw])) {
                     apdq[0] += fw[mw][0]; apdq[1] += fw[mw][1]; apdq[2] += fw[mw][2];
                 } else {
                     amdq[0] += 0.5 * fw[mw][0]; amdq[1] += 0.5 * fw[mw][1]; amdq[2] += 0.5 * fw[mw][2];
@@ -413,10 +413,11 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                         const double r0 = qr[0], r1 = (DIR == 0) ? qr[1] : qr[2],
                                      r2 = (DIR == 0) ? qr[2] : qr[1];
                         const double wnorm2 = a0 * a0 + a1 * a1 + a2 * a2;
-                        if (wnorm2 != 0.0) {
+                        if (!d_eqz<FAST>(wnorm2)) {
                             const double dotl = l0 * a0 + l1 * a1 + l2 * a2;
                             const double dotr = a0 * r0 + a1 * r1 + a2 * r2;
-                            lim = gf_philim(wnorm2, s[mw] > 0.0 ? dotl : dotr, P.mthlim[mw]);
+                            lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[mw]) ? dotl : dotr,
+                                                  P.mthlim[mw]);
                         }
                     }
                     const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
@@ -566,13 +567,13 @@ __global__ void __launch_bounds__(NT, MINB)
         int any_wet = 0;
         for (int k = threadIdx.x; k < S; k += NT) {
             double h = sm[L::OFF_H + k];
-            if (h < drytol) {
-                h = fmax(h, 0.0);
+            if (d_lt<FAST>(h, drytol)) {
+                h = d_max<FAST>(h, 0.0);
                 sm[L::OFF_H + k] = h;
                 sm[L::OFF_HU + k] = 0.0;
                 sm[L::OFF_HV + k] = 0.0;
             }
-            const bool w = h > drytol;
+            const bool w = d_gt<FAST>(h, drytol);
             wet[k] = w ? 1 : 0;
             any_wet |= w;
             double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;

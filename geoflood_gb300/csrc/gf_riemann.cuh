@@ -21,6 +21,7 @@
 #define GF_RIEMANN_CUH
 
 #include "gf_types.h"
+#include "gf_cmp.cuh"
 
 struct gf_cell {
     double h;    /* depth after b4step2                         */
@@ -46,44 +47,44 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
                                                double c16g, double rsg, double& hm,
                                                double& s1m, double& s2m)
 {
-    const double h_min = fmin(hR, hL);
-    const double h_max = fmax(hR, hL);
+    const double h_min = d_min<FAST>(hR, hL);
+    const double h_max = d_max<FAST>(hR, hL);
     const double delu = uR - uL;
-    if (h_min <= drytol) {
+    if (d_le<FAST>(h_min, drytol)) {
         hm = 0.0;
         s1m = uR + uL - 2.0 * cR + 2.0 * cL;
         s2m = s1m;
         return;
     }
     /* sqrt is monotone, so sqrt(g*h_min) = min(cL, cR). */
-    const double c_min = fmin(cR, cL);
-    const double c_max = fmax(cR, cL);
+    const double c_min = d_min<FAST>(cR, cL);
+    const double c_max = d_max<FAST>(cR, cL);
     const double F_min = delu + 2.0 * (c_min - c_max);
     /* (h_max + h_min)/(h_max h_min) = 1/h_min + 1/h_max: the contracted
      * build uses the per-cell reciprocals instead of a division. */
     const double F_max =
-        FAST ? delu + (h_max - h_min) * sqrt(0.5 * g * (fmax(rhL, rhR) + fmin(rhL, rhR)))
+        FAST ? delu + (h_max - h_min) * sqrt(0.5 * g * (d_max<FAST>(rhL, rhR) + d_min<FAST>(rhL, rhR)))
              : delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
-    if (F_min > 0.0) { /* 2-rarefactions */
-        const double t = fmax(0.0, -delu + 2.0 * (cL + cR));
+    if (d_gtz<FAST>(F_min)) { /* 2-rarefactions */
+        const double t = d_max<FAST>(0.0, -delu + 2.0 * (cL + cR));
         hm = c16g * (t * t);
         const double cm = sqrt(g * hm);
         s1m = uL + 2.0 * cL - 3.0 * cm;
         s2m = uR - 2.0 * cR + 3.0 * cm;
-    } else if (F_max <= 0.0) { /* 2 shocks, one Newton step on sqrt(h) */
+    } else if (d_lez<FAST>(F_max)) { /* 2 shocks, one Newton step on sqrt(h) */
         const double h0 = h_max;
         double gL, gR, dfdh, sh0, rL, rR;
         if (FAST) {
             rL = rhL;
             rR = rhR;
-            const double r0 = fmin(rhL, rhR); /* 1/h_max */
+            const double r0 = d_min<FAST>(rhL, rhR); /* 1/h_max */
             const double aL = 0.5 * g * (r0 + rL), aR = 0.5 * g * (r0 + rR);
             const double qL = rsqrt(aL), qR = rsqrt(aR);
             gL = aL * qL;
             gR = aR * qR;
             const double w = 0.25 * (r0 * r0) * g;
             dfdh = gL - (h0 - hL) * w * qL + gR - (h0 - hR) * w * qR;
-            sh0 = fmax(cL, cR) * rsg; /* sqrt(h_max) = sqrt(g h_max)/sqrt(g) */
+            sh0 = d_max<FAST>(cL, cR) * rsg; /* sqrt(h_max) = sqrt(g h_max)/sqrt(g) */
         } else {
             rL = 1.0 / hL;
             rR = 1.0 / hR;
@@ -114,7 +115,7 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
             hm = h_min - F0 / slope;
         }
         const double cm = sqrt(g * hm);
-        if (hL > hR) {
+        if (d_gt<FAST>(hL, hR)) {
             s1m = uL + 2.0 * cL - 3.0 * cm;
             s2m = uL + 2.0 * cL - cm;
         } else {
@@ -157,21 +158,21 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     if (!Rc.wet) {
         double hstar, s1x, s2x;
         gf_riemanntype<FAST>(hL, hL, uL, -uL, cL, cL, rhL, rhL, g, drytol, c16g, rsg, hstar, s1x, s2x);
-        const double hstartest = fmax(hL, hstar);
-        if (hstartest + bL < bR) {
+        const double hstartest = d_max<FAST>(hL, hstar);
+        if (d_lt<FAST>(hstartest + bL, bR)) {
             wall1 = 0.0; wall2 = 0.0;
             hR = hL; huR = -huL; bR = bL; phiR = phiL; uR = -uL; vR = vL; cR = cL; rhR = rhL;
-        } else if (hL + bL < bR) {
+        } else if (d_lt<FAST>(hL + bL, bR)) {
             bR = hL + bL;
         }
     } else if (!Lc.wet) {
         double hstar, s1x, s2x;
         gf_riemanntype<FAST>(hR, hR, -uR, uR, cR, cR, rhR, rhR, g, drytol, c16g, rsg, hstar, s1x, s2x);
-        const double hstartest = fmax(hR, hstar);
-        if (hstartest + bR < bL) {
+        const double hstartest = d_max<FAST>(hR, hstar);
+        if (d_lt<FAST>(hstartest + bR, bL)) {
             wall0 = 0.0; wall1 = 0.0;
             hL = hR; huL = -huR; bL = bR; phiL = phiR; uL = -uR; vL = vR; cL = cR; rhL = rhR;
-        } else if (hR + bR < bL) {
+        } else if (d_lt<FAST>(hR + bR, bL)) {
             bL = hR + bR;
         }
     }
@@ -181,8 +182,8 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double sR = uR + cR;
     const double uhat = (cL * uL + cR * uR) / (cR + cL);
     const double chat = sqrt(g * 0.5 * (hR + hL));
-    double sE1 = fmin(sL, uhat - chat);
-    double sE2 = fmax(sR, uhat + chat);
+    double sE1 = d_min<FAST>(sL, uhat - chat);
+    double sE2 = d_max<FAST>(sR, uhat + chat);
 
     /* ---- riemann_aug_JCP (geoclaw_riemann_utils.f:57-306) ---- */
     const double delh = hR - hL;
@@ -194,49 +195,50 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     gf_riemanntype<FAST>(hL, hR, uL, uR, cL, cR, rhL, rhR, g, drytol, c16g, rsg, hm, s1m, s2m);
     (void)hm;
 
-    const double l1 = fmin(sE1, s2m);
-    const double l3 = fmax(sE2, s1m);
+    const double l1 = d_min<FAST>(sE1, s2m);
+    const double l3 = d_max<FAST>(sE2, s1m);
     sE1 = l1;
     sE2 = l3;
     /* One reciprocal serves h*_HLL and Cramer's rule in the contracted
      * build: sE2 - sE1 = l3 - l1 = -(l1 - l3). */
     const double rdet = FAST ? 1.0 / (l1 - l3) : 0.0;
-    const double hstarHLL = FAST ? fmax((huL - huR + sE2 * hR - sE1 * hL) * -rdet, 0.0)
+    const double hstarHLL = FAST ? d_max<FAST>((huL - huR + sE2 * hR - sE1 * hL) * -rdet, 0.0)
                                  : fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
     const double l2 = 0.5 * (l1 + l3);
 
     /* steady-state wave, first (only) iteration: hLstar = hL etc. */
-    const double hbar = fmax(0.5 * (hL + hR), 0.0);
+    const double hbar = d_max<FAST>(0.5 * (hL + hR), 0.0);
     const double s1s2bar = 0.25 * ((uL + uR) * (uL + uR)) - g * hbar;
-    const double s1s2tilde = fmax(0.0, uL * uR) - g * hbar;
+    const double s1s2tilde = d_max<FAST>(0.0, uL * uR) - g * hbar;
+    const double crit_sq = crit * crit;
     bool sonic;
-    if (fabs(s1s2bar) <= crit) sonic = true;
-    else if (s1s2bar * s1s2tilde <= crit * crit) sonic = true;
-    else if (s1s2bar * sE1 * sE2 <= crit * crit) sonic = true;
-    else if (fmin(fabs(sE1), fabs(sE2)) < crit2) sonic = true;
-    else if (sE1 < crit2 && s1m > -crit2) sonic = true;
-    else if (sE2 > -crit2 && s2m < crit2) sonic = true;
-    else if ((uL + cL) * (uR + cR) < 0.0) sonic = true;
-    else if ((uL - cL) * (uR - cR) < 0.0) sonic = true;
+    if (d_le<FAST>(fabs(s1s2bar), crit)) sonic = true;
+    else if (d_le<FAST>(s1s2bar * s1s2tilde, crit_sq)) sonic = true;
+    else if (d_le<FAST>(s1s2bar * sE1 * sE2, crit_sq)) sonic = true;
+    else if (d_lt<FAST>(d_min<FAST>(fabs(sE1), fabs(sE2)), crit2)) sonic = true;
+    else if (d_lt<FAST>(sE1, crit2) && d_gt<FAST>(s1m, -crit2)) sonic = true;
+    else if (d_gt<FAST>(sE2, -crit2) && d_lt<FAST>(s2m, crit2)) sonic = true;
+    else if (d_ltz<FAST>((uL + cL) * (uR + cR))) sonic = true;
+    else if (d_ltz<FAST>((uL - cL) * (uR - cR))) sonic = true;
     else sonic = false;
 
     const double rs12 = (FAST && !sonic) ? 1.0 / s1s2bar : 0.0;
     double deldelh = sonic ? -delb : (FAST ? delb * g * hbar * rs12 : delb * g * hbar / s1s2bar);
-    if (sE1 < -crit && sE2 > crit) {
-        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE2);
-        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE1);
-    } else if (sE1 >= crit) {
-        deldelh = fmin(deldelh, hstarHLL * (sE2 - sE1) / sE1);
-        deldelh = fmax(deldelh, -hL);
-    } else if (sE2 <= -crit) {
-        deldelh = fmin(deldelh, hR);
-        deldelh = fmax(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+    if (d_lt<FAST>(sE1, -crit) && d_gt<FAST>(sE2, crit)) {
+        deldelh = d_min<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+        deldelh = d_max<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+    } else if (d_ge<FAST>(sE1, crit)) {
+        deldelh = d_min<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = d_max<FAST>(deldelh, -hL);
+    } else if (d_le<FAST>(sE2, -crit)) {
+        deldelh = d_min<FAST>(deldelh, hR);
+        deldelh = d_max<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE2);
     }
     double deldelphi = sonic ? -g * hbar * delb
                              : (FAST ? -delb * g * hbar * s1s2tilde * rs12
                                      : -delb * g * hbar * s1s2tilde / s1s2bar);
-    deldelphi = fmin(deldelphi, g * fmax(-hL * delb, -hR * delb));
-    deldelphi = fmax(deldelphi, g * fmin(-hL * delb, -hR * delb));
+    deldelphi = d_min<FAST>(deldelphi, g * d_max<FAST>(-hL * delb, -hR * delb));
+    deldelphi = d_max<FAST>(deldelphi, g * d_min<FAST>(-hL * delb, -hR * delb));
 
     const double d1 = delh - deldelh;
     const double d2 = delhu;
@@ -255,7 +257,7 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     double f11 = beta1 * l1, f21 = beta1 * A2, f31 = beta1 * l1 * vL;
     double f13 = beta3 * l3, f23 = beta3 * C2, f33 = beta3 * l3 * vR;
     const double corr = hR * uR * vR - hL * uL * vL - f31 - f33;
-    if (huL + f11 <= 0.0) f31 = f31 + corr;
+    if (d_lez<FAST>(huL + f11)) f31 = f31 + corr;
     else f33 = f33 + corr;
 
     /* Wall masking (rpn2_geoclaw.f:303-309). */
@@ -278,9 +280,10 @@ __device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
 {
     bm[0] = bm[1] = bm[2] = 0.0;
     bp[0] = bp[1] = bp[2] = 0.0;
-    if (cl.h <= tol) return;
+    if (d_le<FAST>(cl.h, tol)) return;
     const double eta = cl.h + cl.b;
-    if (eta < fmin(topo_lo, topo_hi)) return;
+    if (d_lt<FAST>(eta, d_min<FAST>(topo_lo, topo_hi))) return;
+    const bool up_lo = d_ge<FAST>(eta, topo_lo), up_hi = d_ge<FAST>(eta, topo_hi);
     const double u = cl.un;  /* q(mu)/h */
     const double v = cl.ut;  /* q(mv)/h */
     const double s1 = v - cl.c;
@@ -295,22 +298,22 @@ __device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
     const double beta2 = -u * delf1 + delf2;
     const double beta3 = FAST ? (delf3 - s1 * delf1) * rden : (delf3 - s1 * delf1) / den;
     /* r(:,1) = (1, u, s1); r(:,2) = (0, 1, 0); r(:,3) = (1, u, s3) */
-    if (s1 < 0.0 && eta >= topo_lo) {
+    if (d_ltz<FAST>(s1) && up_lo) {
         const double a = s1 * beta1;
         bm[0] += a; bm[1] += a * u; bm[2] += a * s1;
-    } else if (s1 > 0.0 && eta >= topo_hi) {
+    } else if (d_gtz<FAST>(s1) && up_hi) {
         const double a = s1 * beta1;
         bp[0] += a; bp[1] += a * u; bp[2] += a * s1;
     }
-    if (s2 < 0.0 && eta >= topo_lo) {
+    if (d_ltz<FAST>(s2) && up_lo) {
         bm[1] += s2 * beta2;
-    } else if (s2 > 0.0 && eta >= topo_hi) {
+    } else if (d_gtz<FAST>(s2) && up_hi) {
         bp[1] += s2 * beta2;
     }
-    if (s3 < 0.0 && eta >= topo_lo) {
+    if (d_ltz<FAST>(s3) && up_lo) {
         const double a = s3 * beta3;
         bm[0] += a; bm[1] += a * u; bm[2] += a * s3;
-    } else if (s3 > 0.0 && eta >= topo_hi) {
+    } else if (d_gtz<FAST>(s3) && up_hi) {
         const double a = s3 * beta3;
         bp[0] += a; bp[1] += a * u; bp[2] += a * s3;
     }
@@ -318,16 +321,20 @@ __device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
 
 /* philim (philim.f:4-65): limiter value for wave strengths a (= |w|^2) and
  * b (= projection of the upwind wave). */
+template <bool FAST>
 __device__ __forceinline__ double gf_philim(double a, double b, int meth)
 {
-    if (a == 0.0) return 0.0;
+    if (d_eqz<FAST>(a)) return 0.0;
     const double r = b / a;
     switch (meth) {
-    case 2: return fmax(fmax(0.0, fmin(1.0, 2.0 * r)), fmin(2.0, r));
+    case 2: return d_max<FAST>(d_max<FAST>(0.0, d_min<FAST>(1.0, 2.0 * r)), d_min<FAST>(2.0, r));
     case 3: return (r + fabs(r)) / (1.0 + fabs(r));
-    case 4: { const double c = (1.0 + r) * 0.5; return fmax(0.0, fmin(fmin(c, 2.0), 2.0 * r)); }
+    case 4: {
+        const double c = (1.0 + r) * 0.5;
+        return d_max<FAST>(0.0, d_min<FAST>(d_min<FAST>(c, 2.0), 2.0 * r));
+    }
     case 5: return r;
-    default: return fmax(0.0, fmin(1.0, r));
+    default: return d_max<FAST>(0.0, d_min<FAST>(1.0, r));
     }
 }
 
