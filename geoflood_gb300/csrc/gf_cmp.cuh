@@ -77,4 +77,26 @@ template <bool F> __device__ __forceinline__ double d_max_nn(double a, double b)
     return fmax(a, b);
 }
 
+/* 1/y from the hardware's approximate FP64 reciprocal refined by two
+ * Newton-Raphson steps r <- r + r (1 - y r) (quadratic convergence: about
+ * 2^-84 relative before the last rounding, i.e. within an ulp of the
+ * correctly rounded quotient). For normal, non-zero y only: the inputs
+ * here are depths, speeds and their differences away from zero. */
+__device__ __forceinline__ double gf_rcp(double y)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(y));
+    double e = fma(-y, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-y, r, 1.0);
+    return fma(r, e, r);
+}
+
+/* x / y: the IEEE quotient, or x * gf_rcp(y) in the production build */
+template <bool F> __device__ __forceinline__ double d_div(double x, double y)
+{
+    if (F) return x * gf_rcp(y);
+    return x / y;
+}
+
 #endif

@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(NT, MINB)
             double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
             if (w) {
                 if (FAST) {
-                    rh = 1.0 / h;
+                    rh = gf_rcp(h);
                     u = sm[L::OFF_HU + k] * rh;
                     v = sm[L::OFF_HV + k] * rh;
                     const double gh = g * h;

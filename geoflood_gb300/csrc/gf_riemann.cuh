@@ -97,9 +97,9 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
         }
         const double F0 = delu + (h0 - hL) * gL + (h0 - hR) * gR;
         const double slope = 2.0 * sh0 * dfdh;
-        const double t = sh0 - F0 / slope;
+        const double t = sh0 - d_div<FAST>(F0, slope);
         hm = t * t;
-        const double rm = 1.0 / hm;
+        const double rm = d_div<FAST>(1.0, hm);
         const double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (rm + rL));
         const double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (rm + rR));
         const double cm = sqrt(g * hm);
@@ -109,7 +109,7 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
                 The first F0 has (h0 - h_min) = 0, so F0 = F_min exactly. */
         const double F0 = F_min;
         if (FAST) {
-            hm = h_min - F0 * ((h_max - h_min) / (F_max - F0));
+            hm = h_min - F0 * d_div<FAST>(h_max - h_min, F_max - F0);
         } else {
             const double slope = (F_max - F0) / (h_max - h_min);
             hm = h_min - F0 / slope;
@@ -180,7 +180,7 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     /* Einfeldt / Roe speeds (rpn2_geoclaw.f:257-266). */
     const double sL = uL - cL;
     const double sR = uR + cR;
-    const double uhat = (cL * uL + cR * uR) / (cR + cL);
+    const double uhat = d_div<FAST>(cL * uL + cR * uR, cR + cL);
     const double chat = sqrt(g * 0.5 * (hR + hL));
     double sE1 = d_min<FAST>(sL, uhat - chat);
     double sE2 = d_max<FAST>(sR, uhat + chat);
@@ -201,7 +201,7 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     sE2 = l3;
     /* One reciprocal serves h*_HLL and Cramer's rule in the contracted
      * build: sE2 - sE1 = l3 - l1 = -(l1 - l3). */
-    const double rdet = FAST ? 1.0 / (l1 - l3) : 0.0;
+    const double rdet = FAST ? gf_rcp(l1 - l3) : 0.0;
     const double hstarHLL = FAST ? d_max<FAST>((huL - huR + sE2 * hR - sE1 * hL) * -rdet, 0.0)
                                  : fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
     const double l2 = 0.5 * (l1 + l3);
@@ -222,17 +222,18 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     else if (d_ltz<FAST>((uL - cL) * (uR - cR))) sonic = true;
     else sonic = false;
 
-    const double rs12 = (FAST && !sonic) ? 1.0 / s1s2bar : 0.0;
+    const double rs12 = (FAST && !sonic) ? gf_rcp(s1s2bar) : 0.0;
     double deldelh = sonic ? -delb : (FAST ? delb * g * hbar * rs12 : delb * g * hbar / s1s2bar);
+    const double hsd = hstarHLL * (sE2 - sE1);
     if (d_lt<FAST>(sE1, -crit) && d_gt<FAST>(sE2, crit)) {
-        deldelh = d_min<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE2);
-        deldelh = d_max<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = d_min<FAST>(deldelh, d_div<FAST>(hsd, sE2));
+        deldelh = d_max<FAST>(deldelh, d_div<FAST>(hsd, sE1));
     } else if (d_ge<FAST>(sE1, crit)) {
-        deldelh = d_min<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE1);
+        deldelh = d_min<FAST>(deldelh, d_div<FAST>(hsd, sE1));
         deldelh = d_max<FAST>(deldelh, -hL);
     } else if (d_le<FAST>(sE2, -crit)) {
         deldelh = d_min<FAST>(deldelh, hR);
-        deldelh = d_max<FAST>(deldelh, hstarHLL * (sE2 - sE1) / sE2);
+        deldelh = d_max<FAST>(deldelh, d_div<FAST>(hsd, sE2));
     }
     double deldelphi = sonic ? -g * hbar * delb
                              : (FAST ? -delb * g * hbar * s1s2tilde * rs12
@@ -325,7 +326,7 @@ template <bool FAST>
 __device__ __forceinline__ double gf_philim(double a, double b, int meth)
 {
     if (d_eqz<FAST>(a)) return 0.0;
-    const double r = b / a;
+    const double r = d_div<FAST>(b, a);
     switch (meth) {
     case 2: return d_max<FAST>(d_max<FAST>(0.0, d_min<FAST>(1.0, 2.0 * r)), d_min<FAST>(2.0, r));
     case 3: return (r + fabs(r)) / (1.0 + fabs(r));
