@@ -320,7 +320,10 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                     dt0 += fr[9] + fl[15]; dt1 += fr[10] + fl[16]; dt2 += fr[11] + fl[17];
                 }
                 ACCN[a] += dn0; ACCN[a + MM] += dn1; ACCN[a + 2 * MM] += dn2;
-                ACCT[a] += dt0; ACCT[a + MM] += dt1; ACCT[a + 2 * MM] += dt2;
+                /* transverse parts enter unscaled; 0.5 dt/dn applied here once */
+                ACCT[a] += half_dtdn * dt0;
+                ACCT[a + MM] += half_dtdn * dt1;
+                ACCT[a + 2 * MM] += half_dtdn * dt2;
             }
         }
     };
@@ -421,9 +424,16 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                         }
                     }
                     const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
-                    cq[0] += fac * (lim * fa[0]);
-                    cq[1] += fac * (lim * fa[1]);
-                    cq[2] += fac * (lim * fa[2]);
+                    if (FAST) {
+                        const double fl = fac * lim;
+                        cq[0] += fl * fa[0];
+                        cq[1] += fl * fa[1];
+                        cq[2] += fl * fa[2];
+                    } else {
+                        cq[0] += fac * (lim * fa[0]);
+                        cq[1] += fac * (lim * fa[1]);
+                        cq[2] += fac * (lim * fa[2]);
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -446,14 +456,21 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                     gf_rpt2_face<FAST>(cl, sm[L::OFF_B + cidx(n - 1, t - 1)],
                                        sm[L::OFF_B + cidx(n - 1, t + 1)], drytol, amdq, bm, bp);
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) { A[c] = half_dtdn * bm[c]; B[c] = half_dtdn * bp[c]; }
+                    for (int c = 0; c < 3; ++c) {
+                        /* the contracted build scales the transverse sums once per cell */
+                        A[c] = FAST ? bm[c] : half_dtdn * bm[c];
+                        B[c] = FAST ? bp[c] : half_dtdn * bp[c];
+                    }
                 }
                 if (wet[kr]) { /* rpt2 imp=2: right-going part into cell n */
                     const gf_cell cr = load_cell<DIR, EXACT, L>(sm, wet, kr);
                     gf_rpt2_face<FAST>(cr, sm[L::OFF_B + cidx(n, t - 1)],
                                        sm[L::OFF_B + cidx(n, t + 1)], drytol, apdq, bm, bp);
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) { Cc[c] = half_dtdn * bm[c]; D[c] = half_dtdn * bp[c]; }
+                    for (int c = 0; c < 3; ++c) {
+                        Cc[c] = FAST ? bm[c] : half_dtdn * bm[c];
+                        D[c] = FAST ? bp[c] : half_dtdn * bp[c];
+                    }
                 }
             }
             /* write in global component order (h, hu, hv) */

@@ -261,7 +261,15 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     if (d_lez<FAST>(huL + f11)) f31 = f31 + corr;
     else f33 = f33 + corr;
 
-    /* Wall masking (rpn2_geoclaw.f:303-309). */
+    /* Wall masking (rpn2_geoclaw.f:303-309). Without a wall every mask is 1
+     * and the products are the values themselves. */
+    if (FAST && Lc.wet && Rc.wet) {
+        s[0] = l1; s[1] = l2; s[2] = l3;
+        fw[0][0] = f11; fw[0][1] = f21; fw[0][2] = f31;
+        fw[1][0] = 0.0; fw[1][1] = beta2; fw[1][2] = 0.0;
+        fw[2][0] = f13; fw[2][1] = f23; fw[2][2] = f33;
+        return;
+    }
     s[0] = l1 * wall0; s[1] = l2 * wall1; s[2] = l3 * wall2;
     fw[0][0] = f11 * wall0; fw[0][1] = f21 * wall0; fw[0][2] = f31 * wall0;
     fw[1][0] = 0.0 * wall1; fw[1][1] = beta2 * wall1; fw[1][2] = 0.0 * wall1;
