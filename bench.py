@@ -166,6 +166,30 @@ def plain_per_patch_rate(ctx, q, aux, npatch=256):
     return npatch * M * M / el, f"{npatch} patches of 32x32, one gf_patch_update call each"
 
 
+def reduce_over_ranks(dist, values: dict, ops: dict) -> dict:
+    """Combine per-rank results on every rank: ops[k] is "max", "min" or
+    "sum". Replicas share no data; this only aggregates their timings and
+    counts (CPU tensors, so it runs on gloo as well as on NCCL)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return dict(values)
+    import torch
+
+    red = {"max": dist.ReduceOp.MAX, "min": dist.ReduceOp.MIN, "sum": dist.ReduceOp.SUM}
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    out = {}
+    for k, v in values.items():
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=red[ops[k]])
+        out[k] = float(t.item())
+    return out
+
+
+def shard(n: int, rank: int, world: int) -> list:
+    """Items of rank `rank` when n independent items (scenarios, forests)
+    are dealt round-robin to `world` replicas."""
+    return list(range(rank, n, world))
+
+
 SERVED_SEED = 4242
 
 
@@ -475,10 +499,7 @@ def run_gpu(args):
     lev.sync()
     kernel_ms = k0.elapsed_time(k1) / nk
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_over_ranks(dist, {"ms": ms}, {"ms": "max"})["ms"]
 
     # e2e through the C ABI with host buffers (pinned, Fortran layout); the
     # host array carries the filled ghost cells, as ForestClaw's storage does
@@ -500,6 +521,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_wall = (time.perf_counter() - t0) / ne
     e2e_ms = max(h0.elapsed_time(h1) / ne, 1e3 * e2e_wall)
+    e2e_ms = reduce_over_ranks(dist, {"ms": e2e_ms}, {"ms": "max"})["ms"]
     qbytes = q.size * 8
 
     plain_v, plain_sample = plain_per_patch_rate(ctx, q, aux)
