@@ -169,7 +169,7 @@ def plain_per_patch_rate(ctx, q, aux, npatch=256):
 def reduce_over_ranks(dist, values: dict, ops: dict) -> dict:
     """Combine per-rank results on every rank: ops[k] is "max", "min" or
     "sum". Replicas share no data; this only aggregates their timings and
-    counts (CPU tensors, so it runs on gloo as well as on NCCL)."""
+    counts (device tensors under NCCL, CPU tensors under gloo)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
         return dict(values)
     import torch
@@ -563,6 +563,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_forest:
         result["forest"] = forest_leg(args, local)
         result["batched"] = batched_leg(args, local)
+    if rank == 0 and not args.no_large:
+        result["large"] = large_leg(args, local)
     if rank == 0:
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
@@ -713,6 +715,48 @@ def batched_leg(args, dev=0):
     }
 
 
+def large_leg(args, dev=0):
+    """Large single scenario (config 5) as one forest: 2 x 2 brick, mx 32,
+    levels 3..7 (2 m finest cells, 8192^2 equivalent), fractal DEM with a
+    dendritic channel network, two-class Manning field (variable friction),
+    inundated start (~17k finest patches), inflow on two sides, regrid every
+    4 steps; a bounded number of step attempts of the 6 h run."""
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+
+    t0 = time.perf_counter()
+    sp = synth.large_scenario()
+    t_gen = time.perf_counter() - t0
+    ctx = gf.Context(dev)
+    ctx.set_phys(0, sp["phys"])
+    F = gf.Forest(ctx, sp["mx"], sp["nbx"], sp["nby"], sp["minlevel"], sp["maxlevel"], sp["dx0"],
+                  sp["dy0"], sp["aux"], sp["q"], mthbc=sp["mthbc"],
+                  regrid_interval=sp["regrid_interval"], refine=sp["refine"])
+    F.set_hydrograph(*sp["hydro"])
+    del sp
+    t0 = time.perf_counter()
+    F.init()
+    t_init = time.perf_counter() - t0
+    p0 = F.npatch
+    lv = F.patches()[:, 0]
+    t0 = time.perf_counter()
+    st = F.run(21600.0, 1, 1.0, 0.9, 1.0, max_steps=args.large_steps)
+    el = time.perf_counter() - t0
+    F.close()
+    ctx.close()
+    return {
+        "workload": "large scenario: 2x2 brick, mx 32, levels 3-7 (8192^2 at 2 m), fractal DEM "
+                    "Hurst 0.85 relief 50 m + dendritic channels, n 0.03/0.07 field, "
+                    f"inundated start, {args.large_steps} step attempts, regrid every 4",
+        "value": st["cell_updates"] / el, "unit": METRIC, "seconds": el,
+        "steps": st["steps"], "rejects": st["rejects"], "regrids": st["regrids"],
+        "simulated_s": st["t"], "patches_initial": int(p0), "patches_max": st["npatch_max"],
+        "finest_patches_initial": int((lv == lv.max()).sum()),
+        "cells_initial": int(p0) * 32 * 32,
+        "seconds_generate": t_gen, "seconds_init": t_init,
+    }
+
+
 def fp64_rates():
     """Measured FP64 pipe rates of this GPU (gf_measure_fp64_rates), ops/s."""
     import ctypes as C
@@ -742,6 +786,9 @@ def main():
     ap.add_argument("--batch-forests", type=int, default=64)
     ap.add_argument("--batch-time", type=float, default=10.0)
     ap.add_argument("--batched-only", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--large-only", action="store_true")
+    ap.add_argument("--large-steps", type=int, default=24)
     ap.add_argument("--served-scenarios", type=int, default=512)
     ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
     ap.add_argument("--served-reserve-sms", type=int, default=None)
@@ -750,6 +797,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.large_only:
+        print(json.dumps({"large": large_leg(args)}))
+        return 0
     if args.batched_only:
         print(json.dumps({"batched": batched_leg(args)}))
         return 0

@@ -340,3 +340,90 @@ def flood_forest(seed: int, target_patches: float, mx: int | None = None, minlev
                 aux=b, q=q, mthbc=(0, 1, 3, 3), regrid_interval=4,
                 refine=Refine(wave_tolerance=1e9, flowgrades=((0.01, 1, 1, maxlevel),)),
                 hydro=hydro, phys=Phys(manning_coefficient=(n,), manning_break=(1e10,)))
+
+
+def _carve(b: np.ndarray, pts: np.ndarray, dx: float, width: float, depth: float):
+    """Lower b by `depth` within width/2 of a polyline given by cell-centre
+    points (k, 2) in metres (a channel of the dendritic network)."""
+    ny, nx = b.shape
+    r = max(1, int(round(0.5 * width / dx)))
+    done = np.zeros_like(b, dtype=bool)
+    for x, y in pts:
+        i, j = int(x / dx), int(y / dx)
+        i0, i1, j0, j1 = max(i - r, 0), min(i + r + 1, nx), max(j - r, 0), min(j + r + 1, ny)
+        if i0 >= i1 or j0 >= j1:
+            continue
+        done[j0:j1, i0:i1] = True
+    b[done] -= depth
+
+
+def _walk(g, start, heading, length, step, wiggle, lx, ly):
+    """A seeded meandering polyline of `length` metres from `start`."""
+    pts = [np.array(start, float)]
+    ang = heading
+    for _ in range(int(length / step)):
+        ang += g.normal(0.0, wiggle)
+        ang = heading + np.clip(ang - heading, -0.6, 0.6)
+        p = pts[-1] + step * np.array([np.cos(ang), np.sin(ang)])
+        if not (0.0 <= p[0] < lx and 0.0 <= p[1] < ly):
+            break
+        pts.append(p)
+    return np.array(pts)
+
+
+def large_scenario(seed: int = 7, mx: int = 32, minlevel: int = 3, maxlevel: int = 7,
+                   wet_fraction: float = 0.25):
+    """The large single scenario: a 2 x 2 brick at 2 m finest cells (8192^2
+    at maxlevel 7, mx = 32), fractal DEM (Hurst 0.85, 50 m relief) draining
+    to the upper right, a dendritic channel network (two trunks from the
+    left and bottom inflow points, seeded tributaries), a Manning field of
+    two land-cover classes (0.03 / 0.07) used through variable friction
+    (aux field 2), and the inundated state of peak flooding: water up to the
+    bed's `wet_fraction` quantile plus full channels. One discharge
+    hydrograph (peak 800 m^3/s over 60 m windows) enters on the left and
+    bottom sides, the reference's single hydrograph applied on two flagged
+    sides. Refinement: depth > 0.01 m to maxlevel. Returns the Forest
+    keyword arguments plus 'hydro' and 'phys'."""
+    from . import Phys, Refine
+    g = rng(seed)
+    nb = 2
+    n = nb * mx << maxlevel
+    dxf = 2.0
+    L = n * dxf
+    lv = int(np.ceil(np.log2(n)))
+    lat = diamond_square(lv, 0.85, seed)
+    b = 0.25 * (lat[:-1, :-1] + lat[1:, :-1] + lat[:-1, 1:] + lat[1:, 1:])[:n, :n]
+    del lat
+    b -= b.min()
+    b *= 50.0 / max(b.max(), 1e-300)
+    x = (np.arange(n) + 0.5) * dxf
+    b += 0.001 * (L - x)[None, :] + 0.001 * (L - x)[:, None]
+    # dendritic network: two trunks and tributaries joining them
+    trunks = [_walk(g, (0.0, 0.5 * L), 0.25, 2 * L, 4.0, 0.05, L, L),
+              _walk(g, (0.5 * L, 0.0), 1.3, 2 * L, 4.0, 0.05, L, L)]
+    for tr in trunks:
+        _carve(b, tr, dxf, 60.0, 5.0)
+        for _ in range(6):
+            k = int(g.integers(len(tr) // 8, max(len(tr) - 1, len(tr) // 8 + 1)))
+            head = float(g.uniform(-2.5, 2.5))
+            trib = _walk(g, tr[k], head, float(g.uniform(0.1, 0.3)) * L, 4.0, 0.08, L, L)
+            _carve(b, trib, dxf, 20.0, 2.0)
+    # land cover: two classes from a coarse seeded fractal, nearest-cell upsampled
+    cover = diamond_square(8, 0.8, seed + 11)[:256, :256]
+    rep = n // 256
+    nman = np.where(np.kron(cover > 0.0, np.ones((rep, rep), bool)), 0.03, 0.07)
+    level = float(np.quantile(b[::8, ::8], wet_fraction))
+    q = np.zeros((n, n, 3))
+    q[..., 0] = np.maximum(level - b, 0.0)
+    aux = np.stack([b, nman])
+    peak = 800.0
+    width = 60.0
+    hydro = ([0.0, 1800.0, 7200.0], [0.1 * peak / width, peak / width, 0.1 * peak / width],
+             [1, 0, 1, 0], width, 0.5 * L, 0.5 * L)
+    phys = Phys(manning_coefficient=(0.035,), manning_break=(1e10,), variable_friction=True,
+                friction_index=2)
+    return dict(mx=mx, nbx=nb, nby=nb, minlevel=minlevel, maxlevel=maxlevel,
+                dx0=dxf * (1 << maxlevel), dy0=dxf * (1 << maxlevel), aux=aux, q=q,
+                mthbc=(0, 1, 0, 1), regrid_interval=4,
+                refine=Refine(wave_tolerance=1e9, flowgrades=((0.01, 1, 1, maxlevel),)),
+                hydro=hydro, phys=phys)
