@@ -452,6 +452,8 @@ def run_gpu(args):
     q, aux, py, px = workload()
     ncell = NPX * NPY * M * M
     ctx = gf.Context(local, gf.Phys())
+    # tile shapes per patch size, measured on this device (process-wide choice)
+    tiles = ctx.autotune(reps=3) if not args.no_autotune else None
     lev = gf.Level(ctx, q.shape[0], M, 1)
     lev.set_geometry(DX, DX)
     lev.upload(q, aux)
@@ -555,6 +557,7 @@ def run_gpu(args):
                      "note": "FP64-issue bound, not HBM bound: see fp64"},
         "fp64": fp64,
         "clocks": clk,
+        "tiles": tiles,
         "plain_per_patch": {"value": plain_v, "unit": METRIC, "sample": plain_sample,
                             "note": "single_step_update-style drop-in, host buffers per patch"},
     }
@@ -787,6 +790,7 @@ def main():
     ap.add_argument("--batch-time", type=float, default=10.0)
     ap.add_argument("--batched-only", action="store_true")
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--large-only", action="store_true")
     ap.add_argument("--large-steps", type=int, default=24)
     ap.add_argument("--served-scenarios", type=int, default=512)

@@ -160,6 +160,32 @@ class Context:
         p = phys.to_c()
         _check(self.h, self._lib.gf_ctx_set_phys(self.h, int(slot), C.byref(p)))
 
+    def autotune(self, reps: int = 5) -> list:
+        """Time every tile shape of the patch kernel per patch size on this
+        device and install the fastest (gf_autotune); returns per-mx results."""
+        res = (_lib.gf_tile_result * 3)()
+        _check(self.h, self._lib.gf_autotune(self.h, int(reps), res))
+        out = []
+        for r in res:
+            n = r.nvariant
+            out.append({"mx": r.mx,
+                        "tiles": [(r.threads[v], r.band[v]) for v in range(n)],
+                        "throughput": [r.throughput[v] for v in range(n)],
+                        "latency_us": [r.latency_us[v] for v in range(n)],
+                        "best_throughput": r.best_throughput, "best_latency": r.best_latency})
+        return out
+
+    @staticmethod
+    def tile(mx: int, goal: int = 0) -> int:
+        """Selected tile variant for patch size mx (goal 0 throughput, 1 latency)."""
+        return int(_lib.load().gf_tile_get(int(mx), int(goal)))
+
+    @staticmethod
+    def set_tile(mx: int, goal: int, variant: int):
+        rc = _lib.load().gf_tile_set(int(mx), int(goal), int(variant))
+        if rc != 0:
+            raise GeoFloodError(rc, "no such tile variant")
+
     def set_fp_contract(self, allow: bool):
         """False: run the contraction-free build (bit-level parity mode)."""
         _check(self.h, self._lib.gf_ctx_set_fp_contract(self.h, int(bool(allow))))

@@ -123,6 +123,16 @@ class gf_forest_batch_stats(C.Structure):
                 ("s_rounds", C.c_double), ("s_regrid", C.c_double), ("s_epoch", C.c_double)]
 
 
+GF_MAX_TILES = 4
+
+
+class gf_tile_result(C.Structure):
+    _fields_ = [("mx", C.c_int), ("nvariant", C.c_int), ("threads", C.c_int * GF_MAX_TILES),
+                ("band", C.c_int * GF_MAX_TILES), ("throughput", C.c_double * GF_MAX_TILES),
+                ("latency_us", C.c_double * GF_MAX_TILES), ("best_throughput", C.c_int),
+                ("best_latency", C.c_int)]
+
+
 XFER_AVG_FACE, XFER_AVG_CORNER, XFER_INTERP_FACE = 0, 1, 2
 XFER_INTERP_CORNER, XFER_INTERP2FINE, XFER_AVG2COARSE = 3, 4, 5
 
@@ -193,6 +203,9 @@ SIGNATURES = [
     ("gf_forest_upload", C.c_int, [_vp, _dp]),
     ("gf_forest_batch_run", C.c_int, [C.POINTER(_vp), C.c_int, C.c_double, C.c_int, C.c_double,
                                       C.c_double, C.c_double, C.POINTER(gf_forest_batch_stats)]),
+    ("gf_autotune", C.c_int, [_vp, C.c_int, C.POINTER(gf_tile_result)]),
+    ("gf_tile_get", C.c_int, [C.c_int, C.c_int]),
+    ("gf_tile_set", C.c_int, [C.c_int, C.c_int, C.c_int]),
     ("gf_server_opts_default", None, [C.POINTER(gf_server_opts)]),
     ("gf_server_create", C.c_int, [C.c_int, C.POINTER(gf_server_opts), C.POINTER(_vp)]),
     ("gf_server_destroy", None, [_vp]),

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -893,3 +894,106 @@ int ctx_check_phys(gf_ctx* c, int slot) { return check_phys_slot(c, slot); }
 int ctx_fail(gf_ctx* c, int code, const char* msg) { return fail(c, code, msg); }
 int ctx_cuda_fail(gf_ctx* c, cudaError_t e, const char* what) { return cuda_fail(c, e, what); }
 } // namespace gf
+
+/* ------------------------------------------------------------ tiling */
+extern "C" int gf_tile_get(int mx, int goal)
+{
+    if (!(mx == 8 || mx == 16 || mx == 32)) return GF_ERR_ARG;
+    return gf::tile_get(mx, goal);
+}
+
+extern "C" int gf_tile_set(int mx, int goal, int variant)
+{
+    if (!(mx == 8 || mx == 16 || mx == 32)) return GF_ERR_ARG;
+    return gf::tile_set(mx, goal, variant) ? GF_ERR_ARG : GF_OK;
+}
+
+extern "C" int gf_autotune(gf_ctx* c, int reps, gf_tile_result* out)
+{
+    if (!c || !out || reps < 1) return GF_ERR_ARG;
+    int rc = check_phys_slot(c, 0);
+    if (rc) return rc;
+    GF_CK(c, cudaSetDevice(c->device));
+    static const int ms[3] = {8, 16, 32};
+    const long target_cells = 4L << 20;
+    const int nsmall = 8;
+    cudaEvent_t e0, e1;
+    GF_CK(c, cudaEventCreate(&e0));
+    GF_CK(c, cudaEventCreate(&e1));
+    int result = GF_OK;
+    for (int k = 0; k < 3 && result == GF_OK; ++k) {
+        const int m = ms[k];
+        const long S = cells_of(m, m);
+        const int np = (int)(target_cells / ((long)m * m));
+        gf_tile_result& R = out[k];
+        std::memset(&R, 0, sizeof R);
+        R.mx = m;
+        R.nvariant = std::min(gf::tile_count(m), GF_MAX_TILES);
+        /* synthetic wet state, planes per patch: h, hu, hv then b */
+        std::vector<double> hq((size_t)np * 3 * S), hb((size_t)np * S);
+        for (int p = 0; p < np; ++p)
+            for (long e = 0; e < S; ++e) {
+                const int i = (int)(e % (m + 4)), j = (int)(e / (m + 4));
+                const double h = 1.5 + 0.5 * std::sin(0.37 * i + 0.11 * p) * std::cos(0.23 * j);
+                double* q = &hq[(size_t)p * 3 * S];
+                q[e] = h;
+                q[S + e] = 0.4 * h * std::sin(0.17 * j + p);
+                q[2 * S + e] = 0.3 * h * std::cos(0.19 * i);
+                hb[(size_t)p * S + e] = 0.2 * std::sin(0.05 * (i + j));
+            }
+        double *dq = nullptr, *db = nullptr, *dcfl = nullptr;
+        gf_patch_work* dw = nullptr;
+        cudaError_t e = cudaMalloc(&dq, hq.size() * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&db, hb.size() * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&dw, (size_t)np * sizeof(gf_patch_work));
+        if (e == cudaSuccess) e = cudaMalloc(&dcfl, (size_t)np * sizeof(double));
+        std::vector<gf_patch_work> w(np, gf_patch_work{});
+        for (int p = 0; p < np; ++p) {
+            w[p].q = dq + (size_t)p * 3 * S;
+            w[p].aux = db + (size_t)p * S;
+            w[p].dx = w[p].dy = 1.0;
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(dq, hq.data(), hq.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(db, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dw, w.data(), w.size() * sizeof(gf_patch_work), cudaMemcpyHostToDevice);
+        double best_t = -1.0, best_l = 1e300;
+        for (int v = 0; v < R.nvariant && e == cudaSuccess; ++v) {
+            gf::tile_shape(m, v, &R.threads[v], &R.band[v]);
+            for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+                const int n = pass == 0 ? np : nsmall;
+                e = gf::launch_patch_update_tile(m, v, dw, n, c->d_phys, 0.02, nullptr, nullptr, 1, dcfl,
+                                                 &c->d_status->gmax, &c->d_status->err, c->stream, 0);
+                if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+                for (int r = 0; r < reps && e == cudaSuccess; ++r)
+                    e = gf::launch_patch_update_tile(m, v, dw, n, c->d_phys, 0.02, nullptr, nullptr, 1,
+                                                     dcfl, &c->d_status->gmax, &c->d_status->err,
+                                                     c->stream, 0);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float msf = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&msf, e0, e1);
+                const double ms1 = (double)msf / reps;
+                if (pass == 0) R.throughput[v] = (double)np * m * m / (ms1 * 1e-3);
+                else R.latency_us[v] = ms1 * 1e3;
+            }
+            if (e == cudaSuccess) {
+                if (R.throughput[v] > best_t) { best_t = R.throughput[v]; R.best_throughput = v; }
+                if (R.latency_us[v] < best_l) { best_l = R.latency_us[v]; R.best_latency = v; }
+            }
+        }
+        if (dq) cudaFree(dq);
+        if (db) cudaFree(db);
+        if (dw) cudaFree(dw);
+        if (dcfl) cudaFree(dcfl);
+        if (e != cudaSuccess) {
+            result = cuda_fail(c, e, "autotune");
+            break;
+        }
+        gf::tile_set(m, 0, R.best_throughput);
+        gf::tile_set(m, 1, R.best_latency);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return result;
+}
+

@@ -16,9 +16,21 @@ namespace gf {
 cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, const gf_phys* phys,
                                 double dt, const double* gdt, const int* gpar, int maux, double* cfl,
                                 unsigned long long* gmax, int* err, cudaStream_t st,
-                                int max_ctas = 0);
+                                int max_ctas = 0, int goal = 0);
 size_t patch_update_smem_bytes(int m);
-int patch_update_occupancy(int m); /* resident CTAs per SM */
+int patch_update_occupancy(int m); /* resident CTAs per SM (throughput tile) */
+
+/* Tile shapes of the production patch kernel: variants per patch size, the
+ * selection per goal (0 throughput, 1 latency) used by launch_patch_update. */
+int tile_count(int m);
+int tile_shape(int m, int v, int* nt, int* rb);
+int tile_get(int m, int goal);
+int tile_set(int m, int goal, int v);
+cudaError_t launch_patch_update_tile(int m, int v, const gf_patch_work* work, int nwork,
+                                     const gf_phys* phys, double dt, const double* gdt,
+                                     const int* gpar, int maux, double* cfl,
+                                     unsigned long long* gmax, int* err, cudaStream_t st,
+                                     int max_ctas);
 cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwork,
                                       const gf_phys* phys, double dt, const double* gdt,
                                       const int* gpar, int maux, double* cfl,

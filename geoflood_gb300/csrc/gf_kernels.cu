@@ -35,17 +35,13 @@ static cudaError_t launch_update(const gf_patch_work* work, int nwork, const gf_
     return cudaGetLastError();
 }
 
-cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, const gf_phys* phys,
-                                double dt, const double* gdt, const int* gpar, int maux, double* cfl,
-                                unsigned long long* gmax, int* err, cudaStream_t st, int max_ctas)
-{
-    switch (m) {
-    case 32: return launch_update<32, 256, 7, 1>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
-    case 16: return launch_update<16, 128, 6, 1>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
-    case 8: return launch_update<8, 64, 5, 1>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
-    default: return cudaErrorInvalidValue;
-    }
-}
+/* ---- tile shapes (threads per patch x slices per band) per patch size ----
+ * Variant 0 of each size is the default; gf_autotune measures them all and
+ * installs the fastest for throughput (whole levels) and for latency (a
+ * lone small scenario, where one patch's critical path is the step time). */
+using UpdateFn = cudaError_t (*)(const gf_patch_work*, int, const gf_phys*, double, const double*,
+                                 const int*, int, double*, unsigned long long*, int*, int, cudaStream_t);
+using OccFn = int (*)();
 
 template <int M, int NT, int RB>
 static int occupancy_of()
@@ -60,14 +56,87 @@ static int occupancy_of()
     return n;
 }
 
-int patch_update_occupancy(int m)
+struct Tile {
+    int nt, rb;
+    UpdateFn fn;
+    OccFn occ;
+};
+
+#define GF_TILE(M, NT, RB) {NT, RB, &launch_update<M, NT, RB, 1>, &occupancy_of<M, NT, RB>}
+static const Tile kTiles8[] = {GF_TILE(8, 64, 5), GF_TILE(8, 128, 10), GF_TILE(8, 128, 5)};
+static const Tile kTiles16[] = {GF_TILE(16, 128, 6), GF_TILE(16, 256, 13), GF_TILE(16, 256, 9)};
+static const Tile kTiles32[] = {GF_TILE(32, 256, 7), GF_TILE(32, 256, 5)};
+#undef GF_TILE
+
+static const Tile* tiles_of(int m, int* n)
 {
     switch (m) {
-    case 32: return occupancy_of<32, 256, 7>();
-    case 16: return occupancy_of<16, 128, 6>();
-    case 8: return occupancy_of<8, 64, 5>();
-    default: return 0;
+    case 8: *n = (int)(sizeof kTiles8 / sizeof kTiles8[0]); return kTiles8;
+    case 16: *n = (int)(sizeof kTiles16 / sizeof kTiles16[0]); return kTiles16;
+    case 32: *n = (int)(sizeof kTiles32 / sizeof kTiles32[0]); return kTiles32;
+    default: *n = 0; return nullptr;
     }
+}
+
+/* selected variant per goal (0 throughput, 1 latency) and patch size */
+static int g_tile[2][3] = {{0, 0, 0}, {0, 0, 0}};
+static inline int mcls(int m) { return m == 8 ? 0 : m == 16 ? 1 : 2; }
+
+int tile_count(int m)
+{
+    int n = 0;
+    tiles_of(m, &n);
+    return n;
+}
+
+int tile_shape(int m, int v, int* nt, int* rb)
+{
+    int n = 0;
+    const Tile* t = tiles_of(m, &n);
+    if (!t || v < 0 || v >= n) return -1;
+    *nt = t[v].nt;
+    *rb = t[v].rb;
+    return 0;
+}
+
+int tile_get(int m, int goal) { return g_tile[goal != 0][mcls(m)]; }
+
+int tile_set(int m, int goal, int v)
+{
+    int n = 0;
+    tiles_of(m, &n);
+    if (v < 0 || v >= n) return -1;
+    g_tile[goal != 0][mcls(m)] = v;
+    return 0;
+}
+
+cudaError_t launch_patch_update_tile(int m, int v, const gf_patch_work* work, int nwork,
+                                     const gf_phys* phys, double dt, const double* gdt,
+                                     const int* gpar, int maux, double* cfl,
+                                     unsigned long long* gmax, int* err, cudaStream_t st,
+                                     int max_ctas)
+{
+    int n = 0;
+    const Tile* t = tiles_of(m, &n);
+    if (!t || v < 0 || v >= n) return cudaErrorInvalidValue;
+    return t[v].fn(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err, max_ctas, st);
+}
+
+cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, const gf_phys* phys,
+                                double dt, const double* gdt, const int* gpar, int maux, double* cfl,
+                                unsigned long long* gmax, int* err, cudaStream_t st, int max_ctas,
+                                int goal)
+{
+    if (!(m == 8 || m == 16 || m == 32)) return cudaErrorInvalidValue;
+    return launch_patch_update_tile(m, g_tile[goal != 0][mcls(m)], work, nwork, phys, dt, gdt, gpar,
+                                    maux, cfl, gmax, err, st, max_ctas);
+}
+
+int patch_update_occupancy(int m)
+{
+    int n = 0;
+    const Tile* t = tiles_of(m, &n);
+    return t ? t[g_tile[0][mcls(m)]].occ() : 0;
 }
 
 size_t patch_update_smem_bytes(int m)

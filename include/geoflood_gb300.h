@@ -496,6 +496,28 @@ int gf_server_cancel(gf_server* s, long long id);
 int gf_server_stats_get(gf_server* s, gf_server_stats* st);
 double gf_server_clock(const gf_server* s);
 
+/* ------------------------------------------------------------ tiling */
+/* Tile shapes of the production patch kernel (threads per patch x slices
+ * per band) per patch size, measured on this device: the fastest for whole
+ * levels (throughput) and the fastest lone small batch (latency) become
+ * the process-wide choice; the served form's smallest lane uses the
+ * latency choice, everything else the throughput choice. Synthetic
+ * all-wet patches, physics slot 0 of the context, `reps` timed launches
+ * per variant. No reference counterpart (tuning support). */
+#define GF_MAX_TILES 4
+typedef struct gf_tile_result {
+    int mx;
+    int nvariant;
+    int threads[GF_MAX_TILES], band[GF_MAX_TILES];
+    double throughput[GF_MAX_TILES]; /* cell-updates/s, ~4M-cell level     */
+    double latency_us[GF_MAX_TILES]; /* one launch over 8 patches           */
+    int best_throughput, best_latency;
+} gf_tile_result;
+int gf_autotune(gf_ctx* ctx, int reps, gf_tile_result* out /* [3]: mx 8, 16, 32 */);
+/* Current choice (goal 0 throughput, 1 latency) or a manual one. */
+int gf_tile_get(int mx, int goal);
+int gf_tile_set(int mx, int goal, int variant);
+
 /* ----------------------------------------------------------- probes */
 /* Measured FP64 pipe rates of `device` in operations per second:
  * rates[0] double fma, [1] double division, [2] double sqrt, [3] float fma.

@@ -1,0 +1,47 @@
+"""Tile shapes of the patch kernel (GPU required): every variant of every
+patch size meets the same parity bar against the oracle, and the autotuner
+measures them and installs a choice per goal."""
+import numpy as np
+import pytest
+
+import geoflood_gb300 as gf
+from geoflood_gb300 import synth
+
+from test_gpu_patch import compare, level_vs_oracle, random_state
+
+pytestmark = pytest.mark.gpu
+
+
+def variants(m):
+    return range({8: 3, 16: 3, 32: 2}[m])
+
+
+@pytest.mark.parametrize("m", [8, 16, 32])
+def test_every_tile_meets_the_parity_bar(ctx, m):
+    keep = gf.Context.tile(m, 0)
+    try:
+        for v in variants(m):
+            gf.Context.set_tile(m, 0, v)
+            q, aux = random_state(24, m, 40 + v)
+            out, ref, cg, cr, pg, pr = level_vs_oracle(ctx, q, aux, m, 2.0, 0.04, gf.Phys())
+            compare(q, out, ref, cg, cr, m, pcfl_gpu=pg, pcfl_ref=pr)
+            q, aux, _, _ = synth.uniform_dam_break_level(4, 4, m, 1.0, seed=v, x_dam=1.5 * m)
+            out, ref, cg, cr, pg, pr = level_vs_oracle(ctx, q, aux, m, 1.0, 0.05, gf.Phys())
+            compare(q, out, ref, cg, cr, m, pcfl_gpu=pg, pcfl_ref=pr)
+    finally:
+        gf.Context.set_tile(m, 0, keep)
+
+
+def test_autotune_measures_and_selects(ctx):
+    ctx.set_phys(0, gf.Phys())
+    res = ctx.autotune(reps=2)
+    assert [r["mx"] for r in res] == [8, 16, 32]
+    for r in res:
+        assert len(r["tiles"]) == len(variants(r["mx"]))
+        assert all(v > 0 for v in r["throughput"]) and all(v > 0 for v in r["latency_us"])
+        assert r["best_throughput"] == int(np.argmax(r["throughput"]))
+        assert r["best_latency"] == int(np.argmin(r["latency_us"]))
+        assert gf.Context.tile(r["mx"], 0) == r["best_throughput"]
+        assert gf.Context.tile(r["mx"], 1) == r["best_latency"]
+    with pytest.raises(gf.GeoFloodError):
+        gf.Context.set_tile(8, 0, 9)
