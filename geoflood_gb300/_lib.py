@@ -203,6 +203,20 @@ SIGNATURES = [
     ("gf_forest_upload", C.c_int, [_vp, _dp]),
     ("gf_forest_batch_run", C.c_int, [C.POINTER(_vp), C.c_int, C.c_double, C.c_int, C.c_double,
                                       C.c_double, C.c_double, C.POINTER(gf_forest_batch_stats)]),
+    ("gf_write_ascii_frame", C.c_int, [C.c_char_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                       _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int), _dp, _dp, _dp, _dp]),
+    ("gf_sample_gauge", C.c_int, [C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, C.c_double, C.c_double, C.c_double, _dp]),
+    ("gf_write_gauge_header", C.c_int, [C.c_char_p, C.c_int, C.c_double, C.c_double]),
+    ("gf_write_gauge_rows", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_int), _dp, _dp]),
+    ("gf_read_gauges_data", C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      _dp, _dp, _dp, _dp, _dp]),
+    ("gf_forest_write_ascii", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("gf_forest_set_output", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("gf_forest_set_gauges", C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), _dp, _dp, _dp, _dp, _dp]),
+    ("gf_forest_sample_gauges", C.c_int, [_vp, C.c_double]),
+    ("gf_forest_flush_gauges", C.c_int, [_vp]),
     ("gf_autotune", C.c_int, [_vp, C.c_int, C.POINTER(gf_tile_result)]),
     ("gf_tile_get", C.c_int, [C.c_int, C.c_int]),
     ("gf_tile_set", C.c_int, [C.c_int, C.c_int, C.c_int]),

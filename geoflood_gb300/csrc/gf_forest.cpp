@@ -133,6 +133,18 @@ struct gf_forest {
     std::vector<std::vector<gf_xfer_task>> h_itp; /* per level */
     std::vector<std::vector<int>> h_refresh;      /* slots per level */
     gf_group_state gst{};                         /* controller during a batched run */
+    /* output: frames and gauges */
+    std::string out_dir;
+    int out_frames = 0, next_frame = 0;
+    bool out_started = false; /* frame 0 and the initial gauge records done */
+    std::vector<gf_gauge_task> gauges; /* window per gauge; placement rebuilt */
+    std::vector<int> gauge_id;
+    std::vector<double> gauge_x, gauge_y;
+    bool gauges_placed = false, gauge_ghosts = false;
+    DArr<gf_gauge_task> d_gtask;
+    DArr<double> d_glast;
+    DArr<double> d_grec;
+    int grec_rows = 0, grec_cap = 0;
 };
 
 namespace {
@@ -196,6 +208,7 @@ void reindex(gf_forest* f)
         f->cells += (long long)f->M * f->M;
     }
     f->dirty = true;
+    f->gauges_placed = false;
 }
 
 int alloc_slot(gf_forest* f)
@@ -871,6 +884,106 @@ int init_forest(gf_forest* f)
     return build_tables(f);
 }
 
+/* ---- gauges ---------------------------------------------------------
+ * Each gauge lives in the leaf holding it: the finest-level patch index of
+ * the point (half-open cells, the domain's upper edges closed) selects the
+ * leaf through the level grids. Inside the leaf the cell and the offsets
+ * follow fc2d_geoclaw_update_gauge (fortran_source/geoclaw_gauges_fort.f90:
+ * 19-25); rounding at a patch edge is clamped to the cells the stencil can
+ * reach. The placement is rebuilt whenever the leaves change. */
+int place_gauges(gf_forest* f)
+{
+    const gf_forest_opts& o = f->o;
+    const int L = o.maxlevel, M = f->M;
+    const int nxL = npx_at(f, L), nyL = npy_at(f, L);
+    const double pxL = M * dx_at(f, L), pyL = M * dy_at(f, L);
+    f->gauge_ghosts = false;
+    for (size_t g = 0; g < f->gauges.size(); ++g) {
+        gf_gauge_task& T = f->gauges[g];
+        T.slot = -1;
+        const double x = f->gauge_x[g], y = f->gauge_y[g];
+        const double ux = (x - o.x0) / pxL, uy = (y - o.y0) / pyL;
+        if (!(ux >= 0.0) || !(uy >= 0.0) || ux > nxL || uy > nyL) continue;
+        const int IF = std::min((int)std::floor(ux), nxL - 1), JF = std::min((int)std::floor(uy), nyL - 1);
+        const int p = containing(f, L, IF, JF);
+        if (p < 0) continue;
+        const Leaf& lf = f->leaves[p];
+        const double dx = dx_at(f, lf.level), dy = dy_at(f, lf.level);
+        const double xl = o.x0 + lf.I * M * dx, yl = o.y0 + lf.J * M * dy;
+        const int ii = std::min(std::max((int)((x - xl) / dx) + 1, 1), M + 1);
+        const int jj = std::min(std::max((int)((y - yl) / dy) + 1, 1), M + 1);
+        T.xoff = (x - (xl + (ii - .5) * dx)) / dx;
+        T.yoff = (y - (yl + (jj - .5) * dy)) / dy;
+        T.slot = lf.slot;
+        T.level = lf.level;
+        T.ii = ii;
+        T.jj = jj;
+        if (ii >= M || jj >= M) f->gauge_ghosts = true;
+    }
+    FK(f, f->d_gtask.reserve(f->gauges.size()));
+    FK(f, cudaMemcpy(f->d_gtask.p, f->gauges.data(), f->gauges.size() * sizeof(gf_gauge_task),
+                     cudaMemcpyHostToDevice));
+    f->gauges_placed = true;
+    return GF_OK;
+}
+
+/* buffered records -> gaugeXXXXX.txt rows, each gauge's rows in time order */
+int flush_gauges(gf_forest* f)
+{
+    const int n = (int)f->gauges.size();
+    if (n == 0 || f->grec_rows == 0) return GF_OK;
+    std::vector<double> rec((size_t)f->grec_rows * n * 6);
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    FK(f, cudaMemcpyAsync(rec.data(), f->d_grec.p, rec.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FK(f, cudaStreamSynchronize(st));
+    std::vector<int> lev;
+    std::vector<double> tt, qv;
+    for (int g = 0; g < n; ++g) {
+        lev.clear();
+        tt.clear();
+        qv.clear();
+        for (int r = 0; r < f->grec_rows; ++r) {
+            const double* x = &rec[((size_t)r * n + g) * 6];
+            if (x[0] < 0) continue;
+            lev.push_back((int)x[0]);
+            tt.push_back(x[1]);
+            qv.insert(qv.end(), x + 2, x + 6);
+        }
+        if (lev.empty()) continue;
+        int rc = gf_write_gauge_rows(f->out_dir.c_str(), f->gauge_id[g], (int)lev.size(), lev.data(), tt.data(),
+                                     qv.data());
+        if (rc) return ffail(f, rc, "cannot append to a gauge file");
+    }
+    f->grec_rows = 0;
+    return GF_OK;
+}
+
+/* one record per gauge at time t from the current state */
+int sample_gauges(gf_forest* f, double t)
+{
+    const int n = (int)f->gauges.size();
+    if (n == 0) return GF_OK;
+    int rc;
+    if (f->dirty && (rc = build_tables(f))) return rc;
+    if (!f->gauges_placed && (rc = place_gauges(f))) return rc;
+    if (f->gauge_ghosts) {
+        /* a stencil reaches ghost cells: exchange them at t first (the
+         * exchange leaves the interiors unchanged) */
+        bool any = false;
+        for (const gf_gauge_task& T : f->gauges) any |= T.slot >= 0 && t >= T.t1 && t <= T.t2;
+        if (any && (rc = ghost_fill(f, t))) return rc;
+    }
+    if (f->grec_rows == f->grec_cap && (rc = flush_gauges(f))) return rc;
+    const double drytol2 = 0.1 * gf::ctx_host_phys(f->ctx, f->o.phys_slot)->dry_tolerance;
+    FK(f, gf::launch_gauge_sample(f->d_gtask.p, n, f->qbuf[f->par], f->aux, f->M, f->o.maux, drytol2, t,
+                                  f->d_glast.p, f->d_grec.p + (size_t)f->grec_rows * n * 6,
+                                  gf::ctx_stream(f->ctx)));
+    f->grec_rows++;
+    return GF_OK;
+}
+
+int write_frame(gf_forest* f, const char* dir, int iframe);
+
 /* ForestClaw outstyle 1 (fc2d_geoclaw_run.c:190-395) with variable dt,
  * reduce_cfl, advance-one-step (the step is the minlevel dt over
  * 2^(maxlevel - minlevel)) and no subcycling. */
@@ -883,6 +996,13 @@ int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, dou
     double t_curr = f->st.t;
     double dt_minlevel = initial_dt;
     long long taken = 0;
+    int rc;
+    if (!f->out_started) {
+        /* frame 0 and the initial gauge records (fc2d_geoclaw_run.c:195-210) */
+        if (f->out_frames && (rc = write_frame(f, f->out_dir.c_str(), f->next_frame++))) return rc;
+        if ((rc = sample_gauges(f, t_curr))) return rc;
+        f->out_started = true;
+    }
     for (int n = 0; n < nout; ++n) {
         const double tend = t_curr + dt_outer;
         while (t_curr < tend) {
@@ -896,8 +1016,7 @@ int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, dou
                 if (small_step < 0) took_small = true;
             }
             double cfl = 0.0;
-            int rc = step(f, t_curr, dt_step, &cfl);
-            if (rc) return rc;
+            if ((rc = step(f, t_curr, dt_step, &cfl))) return rc;
             ++taken;
             f->st.max_cfl_seen = std::max(f->st.max_cfl_seen, cfl);
             if (cfl > max_cfl) {
@@ -913,16 +1032,23 @@ int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, dou
             if (!took_small) dt_minlevel = dt_new;
             f->st.t = t_curr;
             f->st.dt = dt_minlevel;
+            /* gauges after every step, before a regrid (fc2d_geoclaw_run.c:380-393) */
+            if ((rc = sample_gauges(f, t_curr))) return rc;
             if (o.regrid_interval > 0 && f->st.steps % o.regrid_interval == 0) {
                 bool changed = false;
                 if ((rc = regrid(f, t_curr, &changed))) return rc;
             }
         }
+        /* a frame at every output time (fc2d_geoclaw_run.c:396-401) */
+        if (f->out_frames) {
+            if ((rc = flush_gauges(f))) return rc;
+            if ((rc = write_frame(f, f->out_dir.c_str(), f->next_frame++))) return rc;
+        }
     }
 out:
     f->st.t = t_curr;
     f->st.dt = dt_minlevel;
-    return GF_OK;
+    return flush_gauges(f);
 }
 
 } // namespace
@@ -978,6 +1104,9 @@ void gf_forest_destroy(gf_forest* f)
     f->d_refine.release();
     f->d_rgx.release();
     f->d_fill.release();
+    f->d_gtask.release();
+    f->d_glast.release();
+    f->d_grec.release();
     if (f->h_rb) cudaFreeHost(f->h_rb);
     delete f;
 }
@@ -1172,9 +1301,163 @@ int move_leaves(gf_forest* f, double* host, int nfield, bool to_host, bool aux)
     return GF_OK;
 }
 
+/* p4est numbers the trees of an mi x mj brick along the Morton curve of
+ * the smallest power-of-two box holding it (x bit first at each rank, a
+ * direction with no bits left skipped), leaving out positions outside the
+ * brick (p4est_connectivity_new_brick; p4est is not part of the reference
+ * tree). id[by * mi + bx] = tree number. */
+std::vector<int> brick_tree_ids(int mi, int mj)
+{
+    auto bits = [](int m) {
+        int b = 0;
+        while ((1 << b) < m) ++b;
+        return b;
+    };
+    const int lx = bits(mi), ly = bits(mj), rank = std::max(lx, ly);
+    std::vector<int> id((size_t)mi * mj, -1);
+    int next = 0;
+    for (long ti = 0; ti < (1L << (lx + ly)); ++ti) {
+        int x = 0, y = 0, c = 0;
+        for (int i = 0; i < rank; ++i) {
+            if (i < lx) x |= (int)((ti >> c++) & 1) << i;
+            if (i < ly) y |= (int)((ti >> c++) & 1) << i;
+        }
+        if (x < mi && y < mj) id[(size_t)y * mi + x] = next++;
+    }
+    return id;
+}
+
+inline uint64_t morton2(uint32_t x, uint32_t y)
+{
+    uint64_t k = 0;
+    for (int b = 0; b < 32; ++b)
+        k |= (uint64_t)((x >> b) & 1) << (2 * b) | (uint64_t)((y >> b) & 1) << (2 * b + 1);
+    return k;
+}
+
+/* the leaves in p4est order: tree, then the Morton index of the leaf's
+ * lower-left corner at maxlevel within the tree */
+std::vector<size_t> p4est_order(const gf_forest* f, std::vector<int>* block)
+{
+    const std::vector<int> tid = brick_tree_ids(f->o.nbx, f->o.nby);
+    const size_t n = f->leaves.size();
+    std::vector<std::pair<uint64_t, size_t>> key(n);
+    block->assign(n, 0);
+    for (size_t k = 0; k < n; ++k) {
+        const Leaf& L = f->leaves[k];
+        const int bx = L.I >> L.level, by = L.J >> L.level;
+        const uint32_t sx = (uint32_t)(L.I - (bx << L.level)) << (f->o.maxlevel - L.level);
+        const uint32_t sy = (uint32_t)(L.J - (by << L.level)) << (f->o.maxlevel - L.level);
+        const int t = tid[(size_t)by * f->o.nbx + bx];
+        (*block)[k] = t;
+        key[k] = {((uint64_t)t << 44) | morton2(sx, sy), k};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<size_t> ord(n);
+    for (size_t r = 0; r < n; ++r) ord[r] = key[r].second;
+    return ord;
+}
+
+int write_frame(gf_forest* f, const char* dir, int iframe)
+{
+    const size_t n = f->leaves.size();
+    const int M = f->M, maux = f->o.maux;
+    const size_t qper = 3 * (size_t)f->S, aper = (size_t)maux * f->S;
+    std::vector<double> q(n * qper), a(n * aper);
+    int rc = move_leaves(f, q.data(), 3, true, false);
+    if (!rc) rc = move_leaves(f, a.data(), maux, true, true);
+    if (rc) return rc;
+    std::vector<int> block;
+    const std::vector<size_t> ord = p4est_order(f, &block);
+    std::vector<double> qo(n * qper), ao(n * aper), xl(n), yl(n), dxv(n), dyv(n);
+    std::vector<int> gn(n), lv(n), bk(n);
+    for (size_t r = 0; r < n; ++r) {
+        const size_t k = ord[r];
+        const Leaf& L = f->leaves[k];
+        std::copy(q.begin() + k * qper, q.begin() + (k + 1) * qper, qo.begin() + r * qper);
+        std::copy(a.begin() + k * aper, a.begin() + (k + 1) * aper, ao.begin() + r * aper);
+        gn[r] = (int)r;
+        lv[r] = L.level;
+        bk[r] = block[k];
+        dxv[r] = dx_at(f, L.level);
+        dyv[r] = dy_at(f, L.level);
+        xl[r] = f->o.x0 + L.I * M * dxv[r];
+        yl[r] = f->o.y0 + L.J * M * dyv[r];
+    }
+    rc = gf_write_ascii_frame(dir, iframe, f->st.t, (int)n, M, maux, qo.data(), ao.data(), gn.data(), lv.data(),
+                              bk.data(), xl.data(), yl.data(), dxv.data(), dyv.data());
+    if (rc) return ffail(f, rc, "cannot write the frame files");
+    return GF_OK;
+}
+
 } // namespace
 
 extern "C" {
+
+int gf_forest_write_ascii(gf_forest* f, const char* dir, int iframe)
+{
+    if (!f || iframe < 0) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return write_frame(f, dir, iframe);
+}
+
+int gf_forest_set_output(gf_forest* f, const char* dir, int frames)
+{
+    if (!f) return GF_ERR_ARG;
+    f->out_dir = dir ? dir : "";
+    f->out_frames = frames != 0;
+    return GF_OK;
+}
+
+int gf_forest_set_gauges(gf_forest* f, int n, const int* id, const double* xc, const double* yc,
+                         const double* t1, const double* t2, const double* min_time_increment)
+{
+    if (!f || n < 0 || (n > 0 && (!id || !xc || !yc || !t1 || !t2 || !min_time_increment))) return GF_ERR_ARG;
+    for (int g = 0; g < n; ++g)
+        if (id[g] < 0 || id[g] > 99999 || !std::isfinite(xc[g]) || !std::isfinite(yc[g]) || !(min_time_increment[g] >= 0))
+            return ffail(f, GF_ERR_ARG, "gauge ids must be 0..99999 with finite positions and increments >= 0");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    int rc = flush_gauges(f);
+    if (rc) return rc;
+    f->gauges.assign(n, gf_gauge_task{});
+    f->gauge_id.assign(id, id + n);
+    f->gauge_x.assign(xc, xc + n);
+    f->gauge_y.assign(yc, yc + n);
+    for (int g = 0; g < n; ++g) {
+        f->gauges[g].slot = -1;
+        f->gauges[g].t1 = t1[g];
+        f->gauges[g].t2 = t2[g];
+        f->gauges[g].incr = min_time_increment[g];
+        if ((rc = gf_write_gauge_header(f->out_dir.c_str(), id[g], xc[g], yc[g])))
+            return ffail(f, rc, "cannot create a gauge file");
+    }
+    f->gauges_placed = false;
+    f->grec_rows = 0;
+    f->grec_cap = n > 0 ? std::max(1, std::min(4096, (1 << 21) / (6 * n))) : 0;
+    if (n > 0) {
+        FK(f, f->d_glast.reserve(n));
+        FK(f, f->d_grec.reserve((size_t)f->grec_cap * n * 6));
+        const std::vector<double> never(n, -INFINITY);
+        FK(f, cudaMemcpy(f->d_glast.p, never.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return GF_OK;
+}
+
+int gf_forest_sample_gauges(gf_forest* f, double t)
+{
+    if (!f) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return sample_gauges(f, t);
+}
+
+int gf_forest_flush_gauges(gf_forest* f)
+{
+    if (!f) return GF_ERR_ARG;
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    return flush_gauges(f);
+}
 
 int gf_forest_download(gf_forest* f, double* q)
 {

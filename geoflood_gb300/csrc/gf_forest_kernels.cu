@@ -1,5 +1,5 @@
 /*
- * Raster pyramid and patch fill for multi-level forests.
+ * Raster pyramid, patch fill and gauge sampling for multi-level forests.
  *
  * A forest's static fields (bathymetry, optional extra aux fields) and its
  * initial state are given as rasters at the finest level. Level l of the
@@ -84,6 +84,56 @@ __global__ void __launch_bounds__(128) patch_fill_kernel(const gf_fill_task* __r
     }
 }
 
+/* one thread per gauge: the gauge's value after an accepted step, as
+ * fc2d_geoclaw_update_gauge computes it (fortran_source/
+ * geoclaw_gauges_fort.f90:19-75): if any of the cell holding the gauge and
+ * its +x, +y, +xy neighbours is drier than 0.1 * dry_tolerance, that cell's
+ * h, hu, hv and bathymetry; else the bilinear blend of the four, evaluated
+ * in the Fortran expression's order (no contraction in this file). Values
+ * of h, hu, hv below 1e-99 in magnitude become 0. A gauge outside its
+ * window [t1, t2], sampled less than incr ago or already sampled at t
+ * writes level -1. Record: level, t, h, hu, hv, bathymetry. */
+__global__ void gauge_sample_kernel(const gf_gauge_task* __restrict__ tasks, int n,
+                                    const double* __restrict__ qbase,
+                                    const double* __restrict__ auxbase, long S, int n4, int maux,
+                                    double drytol2, double t, double* __restrict__ last,
+                                    double* __restrict__ rec)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const gf_gauge_task T = tasks[g];
+    double* r = rec + (long)g * 6;
+    const double lt = last[g];
+    if (T.slot < 0 || !(t >= T.t1 && t <= T.t2 && t >= lt + T.incr && t > lt)) {
+        r[0] = -1.0;
+        return;
+    }
+    const double* q = qbase + (long)T.slot * 3 * S;
+    const double* b = auxbase + (long)T.slot * maux * S;
+    /* Fortran cell (i, j), 1-based with mbc ghost cells, at plane offset */
+    const long c00 = (long)(T.jj + H - 1) * n4 + (T.ii + H - 1);
+    const long c10 = c00 + 1, c01 = c00 + n4, c11 = c00 + n4 + 1;
+    double v[4];
+    if (q[c00] < drytol2 || q[c10] < drytol2 || q[c01] < drytol2 || q[c11] < drytol2) {
+        for (int m = 0; m < 3; ++m) v[m] = q[m * S + c00];
+        v[3] = b[c00];
+    } else {
+        const double xo = T.xoff, yo = T.yoff;
+        for (int m = 0; m < 3; ++m) {
+            const double* p = q + m * S;
+            v[m] = (1.0 - xo) * (1.0 - yo) * p[c00] + xo * (1.0 - yo) * p[c10] +
+                   (1.0 - xo) * yo * p[c01] + xo * yo * p[c11];
+        }
+        v[3] = (1.0 - xo) * (1.0 - yo) * b[c00] + xo * (1.0 - yo) * b[c10] + (1.0 - xo) * yo * b[c01] +
+               xo * yo * b[c11];
+    }
+    r[0] = (double)T.level;
+    r[1] = t;
+    for (int m = 0; m < 3; ++m) r[2 + m] = fabs(v[m]) < 1e-99 ? 0.0 : v[m];
+    r[5] = v[3];
+    last[g] = t;
+}
+
 int grid_for(long total)
 {
     long b = (total + 255) / 256;
@@ -122,6 +172,17 @@ cudaError_t launch_patch_fill(int m, const gf_fill_task* tasks, int ntask, cudaS
     case 8: patch_fill_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask); break;
     default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gauge_sample(const gf_gauge_task* tasks, int n, const double* qbase,
+                                const double* auxbase, int m, int maux, double drytol2, double t,
+                                double* last, double* rec, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const int n4 = m + 2 * H;
+    gauge_sample_kernel<<<(n + 127) / 128, 128, 0, st>>>(tasks, n, qbase, auxbase, (long)n4 * n4, n4,
+                                                         maux, drytol2, t, last, rec);
     return cudaGetLastError();
 }
 

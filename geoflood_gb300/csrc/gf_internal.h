@@ -80,6 +80,10 @@ cudaError_t launch_pyramid_top(const double* src, double* dst, int nx, int ny, c
 cudaError_t launch_pyramid_down(const double* fine, double* coarse, int nxc, int nyc,
                                 cudaStream_t st);
 cudaError_t launch_patch_fill(int m, const gf_fill_task* tasks, int ntask, cudaStream_t st);
+/* one record of 6 doubles per gauge at rec (level -1: not recorded) */
+cudaError_t launch_gauge_sample(const gf_gauge_task* tasks, int n, const double* qbase,
+                                const double* auxbase, int m, int maux, double drytol2, double t,
+                                double* last, double* rec, cudaStream_t st);
 
 } // namespace gf
 

@@ -130,4 +130,14 @@ typedef struct gf_tag_task {
     int maxlevel, init_flag;
 } gf_tag_task;
 
+/* One gauge of a forest (gf_forest_kernels.cu): the slot of the leaf
+ * holding it (-1: outside the domain), the Fortran index (ii, jj) of the
+ * cell containing it, its offsets from that cell's centre in cells, and its
+ * recording window. */
+typedef struct gf_gauge_task {
+    int slot, level, ii, jj;
+    double xoff, yoff;
+    double t1, t2, incr;
+} gf_gauge_task;
+
 #endif

@@ -10,6 +10,7 @@ cell averages.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -145,6 +146,30 @@ class Forest:
         if q.shape != (self.npatch, self.mx + 4, self.mx + 4, 3):
             raise GeoFloodError(-1, "q must match the current leaves")
         _check(self.ctx.h, self._lib.gf_forest_upload(self.h, dptr(q)))
+
+    # ---- output in the reference's file formats --------------------------
+    def set_output(self, out_dir: str = "", frames: bool = True):
+        """Frames fort.tXXXX / fort.qXXXX (frame 0 before the first step, one
+        per output time) and gauge files go to out_dir during run()."""
+        _check(self.ctx.h, self._lib.gf_forest_set_output(self.h, os.fsencode(out_dir), int(frames)))
+
+    def set_gauges(self, gauges):
+        """gauges: [(id, x, y, t1, t2, min_time_increment)], e.g. from
+        output.read_gauges_data; creates the gauge files in the output dir."""
+        g = list(gauges)
+        ids = np.array([int(r[0]) for r in g], np.int32)
+        cols = [np.ascontiguousarray(np.array([r[k] for r in g], np.float64)) for k in range(1, 6)]
+        _check(self.ctx.h, self._lib.gf_forest_set_gauges(
+            self.h, len(g), ids.ctypes.data_as(C.POINTER(C.c_int)), *(dptr(c) for c in cols)))
+
+    def write_frame(self, iframe: int, out_dir: str = ""):
+        _check(self.ctx.h, self._lib.gf_forest_write_ascii(self.h, os.fsencode(out_dir), iframe))
+
+    def sample_gauges(self, t: float):
+        _check(self.ctx.h, self._lib.gf_forest_sample_gauges(self.h, t))
+
+    def flush_gauges(self):
+        _check(self.ctx.h, self._lib.gf_forest_flush_gauges(self.h))
 
 
 def batch_run(forests, t_final: float, nout: int = 1, initial_dt: float = 1.0,

@@ -397,6 +397,64 @@ typedef struct gf_forest_batch_stats {
 int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout, double initial_dt,
                         double desired_cfl, double max_cfl, gf_forest_batch_stats* st);
 
+/* ------------------------------------------------------------- output */
+/* ASCII frame fort.tXXXX + fort.qXXXX in directory dir (NULL or "": the
+ * working directory), as fc2d_geoclaw_output_ascii
+ * (src/fc2d_geoclaw/fc2d_geoclaw_output_ascii.c:38-109) and the Fortran
+ * writers fc2d_geoclaw_fort_write_header / _write_file
+ * (fclaw2d_source/fc2d_geoclaw_output_ascii_fort.f:1-117) write it: time
+ * as e30.20, the patch headers as i5 / e24.16, one 5E26.16 line of h, hu,
+ * hv, eta = h + aux(1) per interior cell (values below 1e-99 in magnitude
+ * written as 0), a blank record after each row. The npatch patches (Fortran
+ * layout, ghosts included) are written in the order given; grid_number and
+ * block may be NULL (0..npatch-1 and 0). iframe is taken modulo 10000. */
+int gf_write_ascii_frame(const char* dir, int iframe, double time, int npatch, int mx, int maux,
+                         const double* q, const double* aux, const int* grid_number,
+                         const int* level, const int* block, const double* xlower,
+                         const double* ylower, const double* dx, const double* dy);
+/* Gauge value at (xc, yc) in one patch (Fortran layout, ghosts included):
+ * out = h, hu, hv, bathymetry, bilinear between the cell holding the gauge
+ * and its +x / +y neighbours unless one of the four is drier than
+ * 0.1 * dry_tolerance (fc2d_geoclaw_update_gauge,
+ * fortran_source/geoclaw_gauges_fort.f90:1-77). */
+int gf_sample_gauge(int mx, int maux, const double* q, const double* aux, double xlower,
+                    double ylower, double dx, double dy, double dry_tolerance, double xc,
+                    double yc, double* out);
+/* gaugeXXXXX.txt: the header (geoclaw_create_gauge_files_default,
+ * src/fc2d_geoclaw/fc2d_geoclaw_gauges_default.c:172-200) and appended rows
+ * "level t h hu hv eta" (geoclaw_print_gauges_default, :275-305); qv holds
+ * nrow x (h, hu, hv, bathymetry). */
+int gf_write_gauge_header(const char* dir, int id, double xc, double yc);
+int gf_write_gauge_rows(const char* dir, int id, int nrow, const int* level, const double* t,
+                        const double* qv);
+/* gauges.data as geoclaw_read_gauges_data_default reads it
+ * (fc2d_geoclaw_gauges_default.c:56-167): *n = number of gauges; the arrays
+ * are filled when cap >= *n. */
+int gf_read_gauges_data(const char* path, int cap, int* n, int* id, double* xc, double* yc,
+                        double* t1, double* t2, double* min_time_increment);
+
+/* Forest output. Frames list the leaves in p4est order: blocks (trees of
+ * the nbx x nby brick) along the brick's Morton curve, leaves of a block
+ * along the Morton curve of their lower-left corners; grid_number is the
+ * position in that order, block the tree number. */
+int gf_forest_write_ascii(gf_forest* f, const char* dir, int iframe);
+/* With dir set, gf_forest_run writes frame 0 before its first step (once
+ * per forest) and the next frame after each output interval (frames != 0),
+ * and appends gauge rows there. */
+int gf_forest_set_output(gf_forest* f, const char* dir, int frames);
+/* Gauges sampled by gf_forest_run at the start of the first run and after
+ * every accepted step, before any regrid: gauge k records at time t when
+ * t1[k] <= t <= t2[k] and t >= (its last record) + min_time_increment[k],
+ * from the leaf holding (xc, yc), with ghost cells exchanged at t. Writes
+ * the gauge file headers in the output directory. n = 0 removes them. */
+int gf_forest_set_gauges(gf_forest* f, int n, const int* id, const double* xc, const double* yc,
+                         const double* t1, const double* t2, const double* min_time_increment);
+/* Record the gauges at time t from the current state (for host-driven
+ * loops over gf_forest_step / gf_forest_accept); rows are buffered on the
+ * device until gf_forest_flush_gauges appends them to the files. */
+int gf_forest_sample_gauges(gf_forest* f, double t);
+int gf_forest_flush_gauges(gf_forest* f);
+
 /* ------------------------------------------------- served scenarios */
 /* A request loop over flood scenarios (continuous batching). Each admitted
  * scenario keeps its state resident on the device; every batching round

@@ -15,11 +15,14 @@ follows; its agreement with ForestClaw is unpinned.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from . import (MBC, average2coarse, average_ghost, interpolate2fine, interpolate_ghost,
-               level_ghost_fill, level_update, refine as c_refine, tag4coarsening,
+               level_ghost_fill, level_update, params, refine as c_refine, tag4coarsening,
                tag4refinement)
+from . import output as fout
 
 FACES = ((-1, 0), (1, 0), (0, -1), (0, 1))          # left, right, bottom, top
 CORNERS = ((-1, -1), (1, -1), (-1, 1), (1, 1))       # ll, lr, ul, ur
@@ -61,6 +64,8 @@ class Forest:
         self.t = 0.0
         self.dt = 0.0
         self.max_cfl_seen = 0.0
+        self.out_dir, self.frames, self.next_frame, self.out_started = "", False, 0, False
+        self.gauges = []            # dicts: id, x, y, t1, t2, incr, last, rows
 
     # ---- geometry -------------------------------------------------------
     def npx(self, l):
@@ -322,11 +327,18 @@ class Forest:
         dt_minlevel = initial_dt
         taken = 0
         dts = []
+        if not self.out_started:
+            if self.frames:
+                self.write_frame(self.out_dir, self.next_frame)
+                self.next_frame += 1
+            self.sample_gauges(t_curr)
+            self.out_started = True
         for _ in range(nout):
             tend = t_curr + dt_outer
             while t_curr < tend:
                 if max_steps and taken >= max_steps:
                     self.t, self.dt = t_curr, dt_minlevel
+                    self.flush_gauges()
                     return dts
                 dt_step = dt_minlevel / level_factor
                 tol = 1e-2 * dt_step
@@ -352,10 +364,85 @@ class Forest:
                 dt_new = dt_minlevel * desired_cfl / cfl if cfl > 0.0 else float("inf")
                 if not took_small:
                     dt_minlevel = dt_new
+                self.t = t_curr
+                self.sample_gauges(t_curr)
                 if self.regrid_interval > 0 and self.steps % self.regrid_interval == 0:
                     self.regrid(t_curr)
+            if self.frames:
+                self.flush_gauges()
+                self.write_frame(self.out_dir, self.next_frame)
+                self.next_frame += 1
         self.t, self.dt = t_curr, dt_minlevel
+        self.flush_gauges()
         return dts
+
+    # ---- output -----------------------------------------------------------
+    def set_output(self, out_dir, frames=True):
+        self.out_dir, self.frames = out_dir, bool(frames)
+
+    def set_gauges(self, gauges):
+        """gauges: [(id, x, y, t1, t2, min_time_increment)]; writes the headers."""
+        self.gauges = []
+        for gid, x, y, t1, t2, incr in gauges:
+            self.gauges.append(dict(id=gid, x=x, y=y, t1=t1, t2=t2, incr=incr, last=-np.inf,
+                                    rows=[]))
+            with open(os.path.join(self.out_dir, "gauge%05d.txt" % gid), "w") as f:
+                f.write(fout.gauge_header(gid, x, y))
+
+    def frame_arrays(self):
+        keys = self.canonical()
+        order, trees = fout.p4est_order(keys, self.nbx, self.nby, self.lmax)
+        ks = [keys[n] for n in order]
+        q = np.stack([self.leaves[k][0] for k in ks])
+        aux = np.stack([self.leaves[k][1] for k in ks])
+        org = [self.origin(*k) for k in ks]
+        return (q, aux, [k[0] for k in ks], [trees[n] for n in order], [o[0] for o in org],
+                [o[1] for o in org], [self.dx(k[0]) for k in ks], [self.dy(k[0]) for k in ks])
+
+    def write_frame(self, out_dir, iframe):
+        fout.write_frame(out_dir, iframe, self.t, *self.frame_arrays())
+
+    def _gauge_leaf(self, g):
+        """(key, ii, jj, xoff, yoff) of the leaf holding gauge g, or None."""
+        L, m = self.lmax, self.m
+        ux = (g["x"] - self.x0) / (m * self.dx(L))
+        uy = (g["y"] - self.y0) / (m * self.dy(L))
+        if not (ux >= 0.0 and uy >= 0.0) or ux > self.npx(L) or uy > self.npy(L):
+            return None
+        IF = min(int(np.floor(ux)), self.npx(L) - 1)
+        JF = min(int(np.floor(uy)), self.npy(L) - 1)
+        key = self.containing(L, IF, JF)
+        if key is None:
+            return None
+        xl, yl = self.origin(*key)
+        return (key,) + fout.gauge_cell(m, xl, yl, self.dx(key[0]), self.dy(key[0]), g["x"], g["y"])
+
+    def sample_gauges(self, t):
+        """One record per gauge whose window holds t, after exchanging ghost
+        cells at t when a stencil reaches them."""
+        if not self.gauges:
+            return
+        place = [self._gauge_leaf(g) for g in self.gauges]
+        if any(p is not None and (p[1] >= self.m or p[2] >= self.m)
+               for p in place) and any(p is not None and g["t1"] <= t <= g["t2"]
+                                       for p, g in zip(place, self.gauges)):
+            self.ghost_fill(t)
+        drytol = params(self.phys).dry_tolerance
+        for p, g in zip(place, self.gauges):
+            if p is None or not (g["t1"] <= t <= g["t2"] and t >= g["last"] + g["incr"]
+                                 and t > g["last"]):
+                continue
+            key, ii, jj, xo, yo = p
+            q, aux = self.leaves[key]
+            g["rows"].append((key[0], t) + fout.sample_gauge(q, aux, ii, jj, xo, yo, drytol))
+            g["last"] = t
+
+    def flush_gauges(self):
+        for g in self.gauges:
+            if g["rows"]:
+                with open(os.path.join(self.out_dir, "gauge%05d.txt" % g["id"]), "a") as f:
+                    f.write(fout.gauge_rows(g["rows"]))
+                g["rows"] = []
 
     def patches(self):
         return np.array(self.canonical(), np.int32).reshape(-1, 3)
