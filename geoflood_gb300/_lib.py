@@ -203,6 +203,20 @@ SIGNATURES = [
     ("gf_forest_upload", C.c_int, [_vp, _dp]),
     ("gf_forest_batch_run", C.c_int, [C.POINTER(_vp), C.c_int, C.c_double, C.c_int, C.c_double,
                                       C.c_double, C.c_double, C.POINTER(gf_forest_batch_stats)]),
+    ("gf_topo_create", C.c_int, [C.POINTER(_vp)]),
+    ("gf_topo_destroy", None, [_vp]),
+    ("gf_topo_set_missing", C.c_int, [_vp, C.c_double]),
+    ("gf_topo_read_file", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("gf_topo_read_data", C.c_int, [_vp, C.c_char_p]),
+    ("gf_topo_add_grid", C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, _dp]),
+    ("gf_topo_count", C.c_int, [_vp]),
+    ("gf_topo_grid_info", C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp, _dp,
+                                    _dp, _dp, _dp, _dp, _dp]),
+    ("gf_topo_covered_area", C.c_int, [_vp, C.c_double, C.c_double, C.c_double, C.c_double, _dp]),
+    ("gf_topo_raster", C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                 C.c_double, C.c_double, C.c_double, C.c_double, _dp]),
+    ("gf_forest_set_topo", C.c_int, [_vp, _vp, C.c_int]),
     ("gf_write_ascii_frame", C.c_int, [C.c_char_p, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
                                        _dp, _dp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int), _dp, _dp, _dp, _dp]),

@@ -44,7 +44,8 @@ PER_FILE = {"gf_kernels_exact.cu": ["-fmad=false"],
             # must match the oracle bit for bit: no contraction
             "gf_amr.cu": ["-fmad=false"],
             "gf_served.cu": ["-fmad=false"],
-            "gf_forest_kernels.cu": ["-fmad=false"]}
+            "gf_forest_kernels.cu": ["-fmad=false"],
+            "gf_topo_kernels.cu": ["-fmad=false"]}
 
 
 def _compile(src: Path, extra: list[str]) -> Path:

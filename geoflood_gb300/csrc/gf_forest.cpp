@@ -231,6 +231,16 @@ int build_pyramid(gf_forest* f, const double* fields)
             const size_t n = (size_t)(nx_at(f, l) + 2 * GF_MBC) * (ny_at(f, l) + 2 * GF_MBC);
             FK(f, cudaMalloc(&f->pyr[(size_t)(l - o.minlevel) * f->nf + k], n * sizeof(double)));
         }
+    if (!fields) {
+        /* zero rasters: the caller fills them (gf_forest_set_topo) */
+        for (size_t k = 0; k < f->pyr.size(); ++k) {
+            const int l = o.minlevel + (int)(k / f->nf);
+            const size_t n = (size_t)(nx_at(f, l) + 2 * GF_MBC) * (ny_at(f, l) + 2 * GF_MBC);
+            FK(f, cudaMemsetAsync(f->pyr[k], 0, n * sizeof(double), st));
+        }
+        FK(f, cudaStreamSynchronize(st));
+        return GF_OK;
+    }
     const int nx = nx_at(f, o.maxlevel), ny = ny_at(f, o.maxlevel);
     double* stage = nullptr;
     FK(f, cudaMalloc(&stage, (size_t)nx * ny * sizeof(double)));
@@ -1113,7 +1123,7 @@ void gf_forest_destroy(gf_forest* f)
 
 int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, gf_forest** out)
 {
-    if (!c || !o || !fields || !out) return GF_ERR_ARG;
+    if (!c || !o || !out) return GF_ERR_ARG;
     *out = nullptr;
     if (!(o->mx == 8 || o->mx == 16 || o->mx == 32)) return gf::ctx_fail(c, GF_ERR_ARG, "mx must be 8, 16 or 32");
     if (o->maux < 1 || o->maux > 3) return gf::ctx_fail(c, GF_ERR_ARG, "maux must be 1..3");
@@ -1180,6 +1190,29 @@ int gf_forest_set_hydrograph(gf_forest* f, int n, const double* time, const doub
     f->bc.width = width;
     f->bc.x0 = x0;
     f->bc.y0 = y0;
+    return GF_OK;
+}
+
+int gf_forest_set_topo(gf_forest* f, gf_topo* t, int qinit)
+{
+    if (!f || !t) return GF_ERR_ARG;
+    if (!f->leaves.empty()) return ffail(f, GF_ERR_STATE, "set the topography before gf_forest_init");
+    FK(f, cudaSetDevice(gf::ctx_device(f->ctx)));
+    const gf_forest_opts& o = f->o;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const double xupper = o.x0 + (o.nbx * f->M) * o.dx0, yupper = o.y0 + (o.nby * f->M) * o.dy0;
+    const double sea_level = gf::ctx_host_phys(f->ctx, o.phys_slot)->sea_level;
+    for (int l = o.minlevel; l <= o.maxlevel; ++l) {
+        double* const* lv = &f->pyr[(size_t)(l - o.minlevel) * f->nf];
+        int rc = gf::topo_raster_device(f->ctx, t, nx_at(f, l), ny_at(f, l), GF_MBC, o.x0, o.y0, dx_at(f, l),
+                                        dy_at(f, l), xupper, yupper, lv[0], st);
+        if (rc) return rc;
+        if (qinit) {
+            const long cells = (long)(nx_at(f, l) + 2 * GF_MBC) * (ny_at(f, l) + 2 * GF_MBC);
+            FK(f, gf::launch_qinit_sea_level(lv[0], lv[o.maux], lv[o.maux + 1], lv[o.maux + 2], cells, sea_level, st));
+        }
+    }
+    FK(f, cudaStreamSynchronize(st));
     return GF_OK;
 }
 

@@ -1,5 +1,6 @@
 /*
- * Raster pyramid, patch fill and gauge sampling for multi-level forests.
+ * Raster pyramid, patch fill, sea-level initial state and gauge sampling
+ * for multi-level forests.
  *
  * A forest's static fields (bathymetry, optional extra aux fields) and its
  * initial state are given as rasters at the finest level. Level l of the
@@ -134,6 +135,19 @@ __global__ void gauge_sample_kernel(const gf_gauge_task* __restrict__ tasks, int
     last[g] = t;
 }
 
+/* fc2d_geoclaw_qinit without qinit files (fortran_source/
+ * geoclaw_qinit_fort.f90:24-27): h = max(0, sea_level - b), hu = hv = 0 */
+__global__ void qinit_sea_level_kernel(const double* __restrict__ b, double* __restrict__ h,
+                                       double* __restrict__ hu, double* __restrict__ hv, long cells,
+                                       double sea_level)
+{
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < cells; e += (long)gridDim.x * blockDim.x) {
+        h[e] = fmax(0.0, sea_level - b[e]);
+        hu[e] = 0.0;
+        hv[e] = 0.0;
+    }
+}
+
 int grid_for(long total)
 {
     long b = (total + 255) / 256;
@@ -172,6 +186,13 @@ cudaError_t launch_patch_fill(int m, const gf_fill_task* tasks, int ntask, cudaS
     case 8: patch_fill_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask); break;
     default: return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_qinit_sea_level(const double* b, double* h, double* hu, double* hv, long cells,
+                                   double sea_level, cudaStream_t st)
+{
+    qinit_sea_level_kernel<<<grid_for(cells), 256, 0, st>>>(b, h, hu, hv, cells, sea_level);
     return cudaGetLastError();
 }
 

@@ -80,6 +80,18 @@ cudaError_t launch_pyramid_top(const double* src, double* dst, int nx, int ny, c
 cudaError_t launch_pyramid_down(const double* fine, double* coarse, int nxc, int nyc,
                                 cudaStream_t st);
 cudaError_t launch_patch_fill(int m, const gf_fill_task* tasks, int ntask, cudaStream_t st);
+/* cell averages of topo grids over a raster (interior cells inside the
+ * domain, then the cells outside copy the nearest inside); *err = 1 when a
+ * cell overlaps no grid */
+cudaError_t launch_topo_raster(const gf_topo_grid* grids, const int* order, int n, int nx, int ny,
+                               int halo, double xlower, double ylower, double dx, double dy,
+                               double xupper, double yupper, double* out, int* err,
+                               cudaStream_t st);
+int topo_raster_device(gf_ctx* c, gf_topo* t, int nx, int ny, int halo, double xlower,
+                       double ylower, double dx, double dy, double xupper, double yupper,
+                       double* out, cudaStream_t st);
+cudaError_t launch_qinit_sea_level(const double* b, double* h, double* hu, double* hv, long cells,
+                                   double sea_level, cudaStream_t st);
 /* one record of 6 doubles per gauge at rec (level -1: not recorded) */
 cudaError_t launch_gauge_sample(const gf_gauge_task* tasks, int n, const double* qbase,
                                 const double* auxbase, int m, int maux, double drytol2, double t,

@@ -130,6 +130,14 @@ typedef struct gf_tag_task {
     int maxlevel, init_flag;
 } gf_tag_task;
 
+/* One topo grid on the device (gf_topo_kernels.cu): node values in file order
+ * (rows north to south, x fastest), node extent and spacing. */
+typedef struct gf_topo_grid {
+    const double* z;
+    int mx, my;
+    double xlow, ylow, xhi, yhi, dx, dy;
+} gf_topo_grid;
+
 /* One gauge of a forest (gf_forest_kernels.cu): the slot of the leaf
  * holding it (-1: outside the domain), the Fortran index (ii, jj) of the
  * cell containing it, its offsets from that cell's centre in cells, and its

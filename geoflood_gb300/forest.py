@@ -24,24 +24,30 @@ def _stats_dict(s: _lib.gf_forest_stats) -> dict:
 
 class Forest:
     """aux: (ny, nx) bathymetry or (maux, ny, nx); q: (ny, nx, 3) with h, hu,
-    hv; both at the finest level: nx = nbx*mx*2^maxlevel, ny = nby*mx*2^maxlevel."""
+    hv; both at the finest level: nx = nbx*mx*2^maxlevel, ny = nby*mx*2^maxlevel.
+    With aux = q = None the rasters start at zero and set_topo() fills them
+    from DEM files (maux then gives the number of aux fields)."""
 
     def __init__(self, ctx, mx: int, nbx: int, nby: int, minlevel: int, maxlevel: int,
-                 dx0: float, dy0: float, aux: np.ndarray, q: np.ndarray, x0: float = 0.0,
-                 y0: float = 0.0, phys_slot: int = 0, mthbc=(1, 1, 1, 1),
-                 regrid_interval: int = 0, max_patches: int = 0, refine: Refine | None = None):
+                 dx0: float, dy0: float, aux: np.ndarray | None, q: np.ndarray | None,
+                 x0: float = 0.0, y0: float = 0.0, phys_slot: int = 0, mthbc=(1, 1, 1, 1),
+                 regrid_interval: int = 0, max_patches: int = 0, refine: Refine | None = None,
+                 maux: int = 1):
         self.ctx = ctx
         self._lib = _lib.load()
-        aux = np.asarray(aux, np.float64)
-        if aux.ndim == 2:
-            aux = aux[None]
-        maux = aux.shape[0]
         nx, ny = nbx * mx << maxlevel, nby * mx << maxlevel
-        if aux.shape[1:] != (ny, nx) or q.shape != (ny, nx, 3):
-            raise ValueError(f"rasters must be ({ny}, {nx}) at the finest level")
-        planes = np.empty((maux + 3, ny, nx))
-        planes[:maux] = aux
-        planes[maux:] = np.moveaxis(np.asarray(q, np.float64), 2, 0)
+        if aux is None and q is None:
+            planes = None
+        else:
+            aux = np.asarray(aux, np.float64)
+            if aux.ndim == 2:
+                aux = aux[None]
+            maux = aux.shape[0]
+            if aux.shape[1:] != (ny, nx) or q.shape != (ny, nx, 3):
+                raise ValueError(f"rasters must be ({ny}, {nx}) at the finest level")
+            planes = np.empty((maux + 3, ny, nx))
+            planes[:maux] = aux
+            planes[maux:] = np.moveaxis(np.asarray(q, np.float64), 2, 0)
         o = _lib.gf_forest_opts()
         self._lib.gf_forest_opts_default(C.byref(o))
         o.mx, o.maux, o.nbx, o.nby = mx, maux, nbx, nby
@@ -84,6 +90,11 @@ class Forest:
         _check(self.ctx.h, self._lib.gf_forest_set_hydrograph(
             self.h, len(tm), dptr(tm), dptr(hv), sd.ctypes.data_as(C.POINTER(C.c_int)),
             width, x0, y0))
+
+    def set_topo(self, topo, qinit: bool = True):
+        """Bathymetry of every level from a Topo set (setaux per level); with
+        qinit, h = max(0, sea_level - b) and zero momentum. Before init()."""
+        _check(self.ctx.h, self._lib.gf_forest_set_topo(self.h, topo.h, int(qinit)))
 
     def init(self):
         _check(self.ctx.h, self._lib.gf_forest_init(self.h))

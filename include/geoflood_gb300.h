@@ -397,6 +397,56 @@ typedef struct gf_forest_batch_stats {
 int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout, double initial_dt,
                         double desired_cfl, double max_cfl, gf_forest_batch_stats* st);
 
+/* ----------------------------------------------------------- topography */
+/* A set of topo grids (DEMs) and the cell-averaged bathymetry setaux makes
+ * of them. Replaces topo_module's readers and ranking
+ * (geolib_source/topo_module.f90:160-402, 491-1059) and setaux's
+ * bathymetry (fortran_source/geoclaw_setaux_fort.f90:107-215 with
+ * cellgridintegrate2.f, topointegral.f, bilinearintegral.f): the bathymetry
+ * of a cell is the integral over the cell of the piecewise-bilinear surface
+ * through the nodes of the finest grid covering each part of it, divided by
+ * the cell area; cells outside the domain copy the nearest cell inside.
+ * Reading is host-only (no device needed); the integrals run on the device
+ * of the context or forest that uses the set. */
+typedef struct gf_topo gf_topo;
+#define GF_TOPO_MAX_FILES 16
+
+int gf_topo_create(gf_topo** out);
+void gf_topo_destroy(gf_topo* t);
+/* Value stored for no-data nodes of later files (default 99999, which the
+ * reference refuses when a file has missing data: so do these readers). */
+int gf_topo_set_missing(gf_topo* t, double topo_missing);
+/* Append a topo file of type +-1, +-2 or +-3 (negative: z is negated). */
+int gf_topo_read_file(gf_topo* t, const char* path, int topo_type);
+/* Append every file that a topo.data (test_topography = 0) lists; relative
+ * names are taken relative to the directory of topo.data. */
+int gf_topo_read_data(gf_topo* t, const char* topo_data_path);
+/* Append a grid from memory: mx x my nodes, lower-left node (xll, yll),
+ * spacing dx, dy, z in file order (rows north to south, x fastest). */
+int gf_topo_add_grid(gf_topo* t, int mx, int my, double xll, double yll, double dx, double dy,
+                     const double* z);
+int gf_topo_count(const gf_topo* t);
+/* Header of grid k (any pointer may be NULL) and its nodes (z may be NULL). */
+int gf_topo_grid_info(const gf_topo* t, int k, int* mx, int* my, double* xlow, double* ylow,
+                      double* xhi, double* yhi, double* dx, double* dy, double* z);
+/* Area of the rectangle covered by the grids (topoarea): the reference
+ * stops when it is below 99 % of the domain. */
+int gf_topo_covered_area(const gf_topo* t, double x1, double x2, double y1, double y2, double* area);
+/* Cell averages of a uniform raster: nx x ny cells of dx x dy from
+ * (xlower, ylower) plus `halo` cells each side, out (ny + 2 halo) x
+ * (nx + 2 halo) host doubles, row pitch nx + 2 halo; (xupper, yupper) is
+ * the domain's upper corner (cells beyond it copy the nearest cell inside).
+ * Computed on the context's device. */
+int gf_topo_raster(gf_ctx* c, gf_topo* t, int nx, int ny, int halo, double xlower, double ylower,
+                   double dx, double dy, double xupper, double yupper, double* out);
+/* Replace a forest's bathymetry (aux field 1) at every level by the cell
+ * averages of t -- setaux at each level -- before gf_forest_init; with
+ * qinit != 0 also set its initial state as fc2d_geoclaw_qinit does without
+ * qinit files (fortran_source/geoclaw_qinit_fort.f90:24-27):
+ * h = max(0, sea_level - b), hu = hv = 0, sea_level of the forest's
+ * physics. gf_forest_create accepts fields = NULL for this use. */
+int gf_forest_set_topo(gf_forest* f, gf_topo* t, int qinit);
+
 /* ------------------------------------------------------------- output */
 /* ASCII frame fort.tXXXX + fort.qXXXX in directory dir (NULL or "": the
  * working directory), as fc2d_geoclaw_output_ascii

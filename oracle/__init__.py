@@ -37,7 +37,8 @@ class orc_params(C.Structure):
 
 
 def build(force: bool = False) -> Path:
-    srcs = [HERE / "geoclaw_oracle.c", HERE / "geoclaw_oracle_ghost.c", HERE / "geoclaw_oracle_amr.c"]
+    srcs = [HERE / "geoclaw_oracle.c", HERE / "geoclaw_oracle_ghost.c", HERE / "geoclaw_oracle_amr.c",
+            HERE / "geoclaw_oracle_topo.c"]
     deps = srcs + [HERE / "geoclaw_oracle.h"]
     if not force and LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB

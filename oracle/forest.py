@@ -67,6 +67,23 @@ class Forest:
         self.out_dir, self.frames, self.next_frame, self.out_started = "", False, 0, False
         self.gauges = []            # dicts: id, x, y, t1, t2, incr, last, rows
 
+    def set_topo(self, topo_set, qinit=True):
+        """Bathymetry of every level from topo grids (setaux per level, see
+        oracle/topo.py) and, with qinit, h = max(0, sea_level - b), hu = hv = 0
+        (fortran_source/geoclaw_qinit_fort.f90:24-27)."""
+        xu = self.x0 + (self.nbx * self.m) * self.dx0
+        yu = self.y0 + (self.nby * self.m) * self.dy0
+        sea = params(self.phys).sea_level
+        for l in range(self.lmin, self.lmax + 1):
+            nx, ny = self.npx(l) * self.m, self.npy(l) * self.m
+            b = topo_set.raster(nx, ny, MBC, self.x0, self.y0, self.dx(l), self.dy(l), xu, yu)
+            p = self.pyr[l]
+            p[0] = b
+            if qinit:
+                p[self.maux] = np.maximum(0.0, sea - b)
+                p[self.maux + 1] = 0.0
+                p[self.maux + 2] = 0.0
+
     # ---- geometry -------------------------------------------------------
     def npx(self, l):
         return self.nbx << l

@@ -204,6 +204,25 @@ int orc_tag4coarsening(const orc_params* p, const orc_refine* rf, int mbc, int m
                        int maux, const double* const* q, const double* const* aux,
                        const double* xlower, const double* ylower, double dx, double dy, double t,
                        int level, int maxlevel, int init_flag);
+
+/* Topo grids (geoclaw_oracle_topo.c): node values z in file order (rows
+ * north to south, x fastest), node extent [xlow, xhi] x [ylow, yhi]. */
+typedef struct orc_topo_grid {
+    const double* z;
+    int mx, my;
+    double xlow, ylow, xhi, yhi, dx, dy;
+} orc_topo_grid;
+void orc_topo_rank(const orc_topo_grid* g, int n, int* order);
+double orc_topointegral(double xim, double xip, double yjm, double yjp, const orc_topo_grid* g);
+int orc_cellgridintegrate(double* out, double xim, double xip, double yjm, double yjp,
+                          const orc_topo_grid* g, const int* order, int n);
+double orc_topo_area(double x1, double x2, double y1, double y2, const orc_topo_grid* g,
+                     const int* order, int n);
+/* Cell averages of a uniform raster of nx x ny cells plus a halo (row
+ * pitch nx + 2 halo), as setaux sets aux(1) on the cells of a patch. */
+int orc_setaux_raster(const orc_topo_grid* g, const int* order, int n, int nx, int ny, int halo,
+                      double xlower, double ylower, double dx, double dy, double xupper,
+                      double yupper, double* out);
 #ifdef __cplusplus
 }
 #endif
