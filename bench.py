@@ -579,6 +579,8 @@ def run_gpu(args):
         result["batched"] = batched_leg(args, local)
     if rank == 0 and not args.no_large:
         result["large"] = large_leg(args, local)
+    if rank == 0 and not args.no_dem:
+        result["dem"] = dem_leg(args, local)
     if rank == 0:
         if not args.no_cpu_baseline:
             v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
@@ -633,6 +635,13 @@ def forest_leg(args, dev=0):
     st = F.run(1e9, 1, 5.0, 0.9, 1.0, max_steps=steps)
     gpu_s = time.perf_counter() - t0
     gpu_patches = F.patches()
+    # one frame of the final leaves in the reference's ASCII format
+    with tempfile.TemporaryDirectory() as td:
+        t0 = time.perf_counter()
+        F.write_frame(1, td)
+        frame_s = time.perf_counter() - t0
+        frame_bytes = sum(os.path.getsize(os.path.join(td, n)) for n in os.listdir(td))
+    frame_cells = int(len(gpu_patches)) * c["mx"] * c["mx"]
     F.close()
     ctx.close()
     oracle.load()
@@ -653,7 +662,80 @@ def forest_leg(args, dev=0):
                        "cores": 1, "kind": "port",
                        "note": "oracle forest driver (Python tree + C kernels, one thread)"},
         "patch_lists_equal_to_oracle": bool(np.array_equal(gpu_patches, O.patches())),
+        "ascii_frame": {"cells": frame_cells, "bytes": frame_bytes, "seconds": frame_s,
+                        "cells_per_s": frame_cells / frame_s, "MB_per_s": frame_bytes / frame_s / 1e6,
+                        "note": "gf_forest_write_ascii: leaf download + fort.t/fort.q text"},
     }
+
+
+def dem_leg(args, dev=0):
+    """DEM ingestion: a 2049 x 2049-node fractal DEM at 2 m over 4096 m x
+    4096 m and a 1025 x 1025-node inset at 0.5 m, both read from type-3
+    files, cell-averaged (setaux) at every level 0-5 of a 4 x 4 brick of
+    32 x 32 patches (cells 32 m .. 1 m, 22.4 M cells plus halos), against the
+    oracle's C restatement of the same integrals on one host thread."""
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+    from geoflood_gb300.topo import Topo
+    from oracle import topo as ot
+
+    A = np.round(synth.diamond_square(11, 0.8, SEED + 11) * 6.0 + 20.0, 3)
+    B = np.round(synth.diamond_square(10, 0.8, SEED + 12) * 2.0 + 20.0, 3)
+    grids = [(A, 0.0, 0.0, 2.0), (B, 1024.0, 1024.0, 0.5)]
+    mx, nb, lmax, dx0 = 32, 4, 5, 32.0
+    out = {"workload": "DEM 2049^2 nodes at 2 m + 1025^2 inset at 0.5 m (type-3 files), "
+                       "setaux at levels 0-5 of 4x4 blocks of mx 32 (cells 32 m..1 m)"}
+    with tempfile.TemporaryDirectory() as td:
+        paths = []
+        for k, (z, x0, y0, d) in enumerate(grids):
+            p = os.path.join(td, "dem%d.tt3" % k)
+            with open(p, "w") as f:
+                f.write("%d ncols\n%d nrows\n%r xlower\n%r ylower\n%r cellsize\n-9999 nodata\n"
+                        % (z.shape[1], z.shape[0], x0, y0, d))
+                np.savetxt(f, z[::-1], fmt="%.3f")
+            paths.append(p)
+        fbytes = sum(os.path.getsize(p) for p in paths)
+        t0 = time.perf_counter()
+        topo = Topo()
+        for p in paths:
+            topo.read_file(p, 3)
+        read_s = time.perf_counter() - t0
+    # the oracle integrates the same nodes (the readers are pinned by the tests)
+    ts = ot.TopoSet([topo.grid(k) for k in range(len(topo))])
+    ctx = gf.Context(dev)
+    ctx.set_phys(0, gf.Phys(sea_level=20.0))
+    cells = sum((nb * mx << l) ** 2 for l in range(lmax + 1))
+    F = gf.Forest(ctx, mx, nb, nb, 0, lmax, dx0, dx0, None, None)
+    t0 = time.perf_counter()
+    F.set_topo(topo)                      # first call: DEM upload + all levels
+    first_s = time.perf_counter() - t0
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        F.set_topo(topo)
+    dev_s = (time.perf_counter() - t0) / reps
+    F.close()
+    # parity on one level, and the oracle over every level
+    n2, d2, ext = nb * mx << 2, dx0 / 4, nb * mx * dx0
+    gpu_l2 = topo.raster(ctx, n2, n2, 2, 0.0, 0.0, d2, d2, ext, ext)
+    ctx.close()
+    equal = False
+    t0 = time.perf_counter()
+    for l in range(lmax + 1):
+        n = nb * mx << l
+        r = ts.raster(n, n, 2, 0.0, 0.0, dx0 / (1 << l), dx0 / (1 << l), ext, ext)
+        if l == 2:
+            equal = bool(np.array_equal(r, gpu_l2))
+    cpu_s = time.perf_counter() - t0
+    out.update({
+        "value": cells / dev_s, "unit": "cell-averages/s", "cells": cells, "seconds": dev_s,
+        "first_call_seconds": first_s,
+        "read": {"bytes": fbytes, "seconds": read_s, "MB_per_s": fbytes / read_s / 1e6},
+        "level2_equal_to_oracle": equal,
+        "cpu_oracle": {"value": cells / cpu_s, "unit": "cell-averages/s", "seconds": cpu_s,
+                       "cores": 1, "kind": "port", "sample": "all six levels"},
+    })
+    return out
 
 
 def batched_leg(args, dev=0):
@@ -804,6 +886,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--large-only", action="store_true")
     ap.add_argument("--large-steps", type=int, default=24)
+    ap.add_argument("--no-dem", action="store_true")
+    ap.add_argument("--dem-only", action="store_true")
     ap.add_argument("--served-scenarios", type=int, default=512)
     ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
     ap.add_argument("--served-reserve-sms", type=int, default=None)
@@ -814,6 +898,9 @@ def main():
         return run_reference(args)
     if args.large_only:
         print(json.dumps({"large": large_leg(args)}))
+        return 0
+    if args.dem_only:
+        print(json.dumps({"dem": dem_leg(args)}))
         return 0
     if args.batched_only:
         print(json.dumps({"batched": batched_leg(args)}))
