@@ -107,7 +107,7 @@ class gf_forest_opts(C.Structure):
                 ("minlevel", C.c_int), ("maxlevel", C.c_int), ("x0", C.c_double),
                 ("y0", C.c_double), ("dx0", C.c_double), ("dy0", C.c_double),
                 ("phys_slot", C.c_int), ("mthbc", C.c_int * 4), ("regrid_interval", C.c_int),
-                ("max_patches", C.c_int), ("refine", gf_refine)]
+                ("max_patches", C.c_int), ("refine", gf_refine), ("subcycle", C.c_int)]
 
 
 class gf_forest_stats(C.Structure):

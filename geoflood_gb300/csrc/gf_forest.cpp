@@ -145,6 +145,21 @@ struct gf_forest {
     DArr<double> d_glast;
     DArr<double> d_grec;
     int grec_rows = 0, grec_cap = 0;
+    /* subcycling: time-interpolated coarse patches and the step's start state */
+    double* qi = nullptr;
+    double* qsave = nullptr;
+    bool sub_dirty = true;
+    int sub_lo = 0, sub_hi = 0;                 /* levels present            */
+    std::vector<int> lev_off, lev_n;             /* canonical range per level */
+    std::vector<int> sx_avg_off, sx_avg_n;       /* [l * 6 + bc * 2 + bf]     */
+    std::vector<int> sx_itp_off;                 /* [l * 6 + bc * 2 + bf]     */
+    DArr<gf_xfer_task> d_sx;
+    std::vector<int> ss_ti_off;                  /* [l * 2 + p_old]           */
+    int ss_copy_off[3][2] = {{0, 0}, {0, 0}, {0, 0}}; /* save, restore, unify per par */
+    int ss_copy_n[3] = {0, 0, 0};
+    DArr<gf_slot_task> d_ss;
+    DArr<double> d_sub_dt;
+    DArr<int> d_par01;
 };
 
 namespace {
@@ -208,6 +223,7 @@ void reindex(gf_forest* f)
         f->cells += (long long)f->M * f->M;
     }
     f->dirty = true;
+    f->sub_dirty = true;
     f->gauges_placed = false;
 }
 
@@ -994,9 +1010,244 @@ int sample_gauges(gf_forest* f, double t)
 
 int write_frame(gf_forest* f, const char* dir, int iframe);
 
-/* ForestClaw outstyle 1 (fc2d_geoclaw_run.c:190-395) with variable dt,
- * reduce_cfl, advance-one-step (the step is the minlevel dt over
- * 2^(maxlevel - minlevel)) and no subcycling. */
+/* ---- subcycling -----------------------------------------------------
+ * ForestClaw's fclaw2d_advance_all_levels with subcycle = T (an external
+ * library; the schedule below is this project's statement of it): over one
+ * coarse step dt, level l takes 2^(l - lo) steps of dt / 2^(l - lo), coarse
+ * before fine (Berger-Oliger order). Before the first of its two sub-steps
+ * inside a parent step, a level's ghost cells come from the parent's state
+ * at the parent's start time; before the second, from the parent time-
+ * interpolated to the midpoint (fc2d_geoclaw_fort_timeinterp, alpha =
+ * 1/2) in a separate buffer whose own ghost cells are exchanged at that
+ * time. Each level keeps its own parity in the two state buffers; the
+ * step's start state is saved for a retake, and on acceptance the coarsest
+ * level (one step, odd parity) is copied back so all levels share one
+ * buffer again. Buffers: 0, 1 = state, 2 = time-interpolated patches. */
+inline double* qslot_b(gf_forest* f, int b, int slot)
+{
+    double* base = b < 2 ? f->qbuf[b] : f->qi;
+    return base + (size_t)slot * 3 * f->S;
+}
+
+int build_sub_tables(gf_forest* f)
+{
+    int rc = build_tables(f);
+    if (rc) return rc;
+    if (!f->sub_dirty) return GF_OK;
+    const size_t pool = (size_t)f->cap * 3 * f->S * sizeof(double);
+    if (!f->qi) FK(f, cudaMalloc(&f->qi, pool));
+    if (!f->qsave) FK(f, cudaMalloc(&f->qsave, pool));
+    const int nlev = f->o.maxlevel + 1;
+    f->lev_off.assign(nlev + 1, 0);
+    f->lev_n.assign(nlev + 1, 0);
+    f->sub_lo = nlev;
+    f->sub_hi = -1;
+    for (size_t k = 0; k < f->leaves.size(); ++k) {
+        const int l = f->leaves[k].level;
+        if (f->lev_n[l]++ == 0) f->lev_off[l] = (int)k;
+        f->sub_lo = std::min(f->sub_lo, l);
+        f->sub_hi = std::max(f->sub_hi, l);
+    }
+    std::vector<int> slot_level(f->cap, -1);
+    for (const Leaf& L : f->leaves) slot_level[L.slot] = L.level;
+    const size_t per = 3 * (size_t)f->S;
+    auto slot_of = [&](const double* q) { return (int)((q - f->qbuf[0]) / (long)per); };
+    /* transfer lists by level and buffer pair (coarse bc in 0..2, fine bf in 0..1) */
+    std::vector<gf_xfer_task> x;
+    f->sx_avg_off.assign((size_t)nlev * 6, 0);
+    f->sx_avg_n.assign(nlev, 0);
+    f->sx_itp_off.assign((size_t)nlev * 6, 0);
+    std::vector<std::vector<gf_xfer_task>> avg_l(nlev);
+    for (const gf_xfer_task& t : f->h_avg) avg_l[slot_level[slot_of(t.qc)]].push_back(t);
+    for (int l = 0; l < nlev; ++l) {
+        f->sx_avg_n[l] = (int)avg_l[l].size();
+        for (int bc = 0; bc < 3; ++bc)
+            for (int bf = 0; bf < 2; ++bf) {
+                f->sx_avg_off[(size_t)l * 6 + bc * 2 + bf] = (int)x.size();
+                for (gf_xfer_task t : avg_l[l]) {
+                    t.qc = qslot_b(f, bc, slot_of(t.qc));
+                    t.qf = qslot_b(f, bf, slot_of(t.qf));
+                    x.push_back(t);
+                }
+                f->sx_itp_off[(size_t)l * 6 + bc * 2 + bf] = (int)x.size();
+                for (gf_xfer_task t : f->h_itp[l]) {
+                    t.qc = qslot_b(f, bc, slot_of(t.qc));
+                    t.qf = qslot_b(f, bf, slot_of(t.qf));
+                    x.push_back(t);
+                }
+            }
+    }
+    /* time interpolation per level and old parity; save / restore / unify per parity */
+    std::vector<gf_slot_task> sl;
+    f->ss_ti_off.assign((size_t)nlev * 2, 0);
+    for (int l = 0; l < nlev; ++l)
+        for (int po = 0; po < 2; ++po) {
+            f->ss_ti_off[(size_t)l * 2 + po] = (int)sl.size();
+            for (int k = 0; k < f->lev_n[l]; ++k) {
+                const int s = f->leaves[f->lev_off[l] + k].slot;
+                sl.push_back(gf_slot_task{qslot(f, po, s), qslot(f, po ^ 1, s), f->qi + (size_t)s * per});
+            }
+        }
+    for (int kind = 0; kind < 3; ++kind)
+        for (int par = 0; par < 2; ++par) {
+            f->ss_copy_off[kind][par] = (int)sl.size();
+            int n = 0;
+            for (const Leaf& L : f->leaves) {
+                const bool fine = L.level > f->sub_lo;
+                const double* save = f->qsave + (size_t)L.slot * per;
+                if (kind == 0 && fine) sl.push_back(gf_slot_task{qslot(f, par, L.slot), nullptr, const_cast<double*>(save)});
+                else if (kind == 1 && fine) sl.push_back(gf_slot_task{save, nullptr, qslot(f, par, L.slot)});
+                else if (kind == 2 && !fine)
+                    sl.push_back(gf_slot_task{qslot(f, par ^ 1, L.slot), nullptr, qslot(f, par, L.slot)});
+                else continue;
+                ++n;
+            }
+            f->ss_copy_n[kind] = n;
+        }
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    FK(f, f->d_sx.reserve(x.size() + 1));
+    FK(f, f->d_ss.reserve(sl.size() + 1));
+    if (!x.empty())
+        FK(f, cudaMemcpyAsync(f->d_sx.p, x.data(), x.size() * sizeof(gf_xfer_task), cudaMemcpyHostToDevice, st));
+    if (!sl.empty())
+        FK(f, cudaMemcpyAsync(f->d_ss.p, sl.data(), sl.size() * sizeof(gf_slot_task), cudaMemcpyHostToDevice, st));
+    FK(f, f->d_sub_dt.reserve(nlev));
+    FK(f, f->d_par01.reserve(2));
+    const int p01[2] = {0, 1};
+    FK(f, cudaMemcpyAsync(f->d_par01.p, p01, sizeof p01, cudaMemcpyHostToDevice, st));
+    f->sub_dirty = false;
+    return GF_OK;
+}
+
+/* same-level copies and physical sides of level l's leaves in buffer b at t */
+int sub_ghost(gf_forest* f, int l, int b, double t, const gf_ghost_ref* refs, int n)
+{
+    if (n <= 0) return GF_OK;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    gf_ghost_block blk{};
+    blk.q = b < 2 ? f->qbuf[b] : f->qi;
+    blk.aux = f->aux;
+    blk.nbr = f->d_nbr.p;
+    blk.geom = f->d_geom.p;
+    blk.phys_of = nullptr;
+    blk.bc = f->bc;
+    blk.bc.q0hu = hydro_at(f, t);
+    blk.phys = f->o.phys_slot;
+    blk.maux = f->o.maux;
+    blk.skip = 0;
+    (void)l;
+    FK(f, f->d_block.reserve(1));
+    /* pageable source, stream-ordered: staged before the call returns */
+    FK(f, cudaMemcpyAsync(f->d_block.p, &blk, sizeof blk, cudaMemcpyHostToDevice, st));
+    FK(f, gf::launch_ghost_fill(f->M, f->d_block.p, refs, n, gf::ctx_device_phys(f->ctx), st));
+    return GF_OK;
+}
+
+/* ghost cells of level l at t: averages from level l + 1, copies and
+ * physical sides, then (cbuf >= 0) interpolation from level l - 1's
+ * patches in buffer cbuf and the physical sides again */
+int sub_fill_level(gf_forest* f, int l, double t, const int* p, int cbuf)
+{
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const gf_phys* phys = gf::ctx_device_phys(f->ctx);
+    int rc;
+    if (l < f->sub_hi && f->sx_avg_n[l])
+        FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_avg_off[(size_t)l * 6 + p[l] * 2 + p[l + 1]],
+                                  f->sx_avg_n[l], phys, st));
+    if ((rc = sub_ghost(f, l, p[l], t, f->d_refs_all.p + f->lev_off[l], f->lev_n[l]))) return rc;
+    if (cbuf >= 0 && f->itp_n[l]) {
+        FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_itp_off[(size_t)l * 6 + cbuf * 2 + p[l]], f->itp_n[l],
+                                  phys, st));
+        if ((rc = sub_ghost(f, l, p[l], t, f->d_refs_lv.p + f->ref_off[l], f->ref_n[l]))) return rc;
+    }
+    return GF_OK;
+}
+
+int sub_update(gf_forest* f, int l, int* p)
+{
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const gf_phys* phys = gf::ctx_device_phys(f->ctx);
+    int* err = reinterpret_cast<int*>(f->d_rb.p);
+    const gf_patch_work* w = f->d_work.p + f->lev_off[l];
+    if (gf::ctx_exact(f->ctx))
+        FK(f, gf::launch_patch_update_exact(f->M, w, f->lev_n[l], phys, 0.0, f->d_sub_dt.p + l, f->d_par01.p + p[l],
+                                            f->o.maux, nullptr, f->d_rb.p + 1, err, st));
+    else
+        FK(f, gf::launch_patch_update(f->M, w, f->lev_n[l], phys, 0.0, f->d_sub_dt.p + l, f->d_par01.p + p[l],
+                                      f->o.maux, nullptr, f->d_rb.p + 1, err, st));
+    p[l] ^= 1;
+    return GF_OK;
+}
+
+int sub_level(gf_forest* f, int l, double tl, double dtl, int* p)
+{
+    int rc;
+    if ((rc = sub_update(f, l, p))) return rc;
+    if (l >= f->sub_hi) return GF_OK;
+    const int po = p[l] ^ 1; /* level l's state at tl */
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const gf_phys* phys = gf::ctx_device_phys(f->ctx);
+    for (int k = 0; k < 2; ++k) {
+        const double tf = k ? tl + dtl * 0.5 : tl;
+        int cbuf = po;
+        if (k == 1) {
+            /* level l at the midpoint, with its ghost cells exchanged there */
+            FK(f, gf::launch_tinterp_strip(f->M, f->d_ss.p + f->ss_ti_off[(size_t)l * 2 + po], f->lev_n[l], 0.5, st));
+            if (f->sx_avg_n[l])
+                FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_avg_off[(size_t)l * 6 + 2 * 2 + p[l + 1]],
+                                          f->sx_avg_n[l], phys, st));
+            if ((rc = sub_ghost(f, l, 2, tf, f->d_refs_all.p + f->lev_off[l], f->lev_n[l]))) return rc;
+            cbuf = 2;
+        }
+        if ((rc = sub_fill_level(f, l + 1, tf, p, cbuf))) return rc;
+        if ((rc = sub_level(f, l + 1, tf, dtl * 0.5, p))) return rc;
+    }
+    return GF_OK;
+}
+
+/* one subcycled coarse step; the result is pending until sub_finish */
+int sub_step(gf_forest* f, double t, double dt, double* cfl, long long* updates)
+{
+    int rc = build_sub_tables(f);
+    if (rc) return rc;
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const int nlev = f->o.maxlevel + 1;
+    std::vector<double> dts(nlev, 0.0);
+    long long cu = 0;
+    double d = dt;
+    for (int l = f->sub_lo; l <= f->sub_hi; ++l, d *= 0.5) {
+        dts[l] = d;
+        cu += (long long)f->lev_n[l] * f->M * f->M << (l - f->sub_lo);
+    }
+    FK(f, cudaMemcpyAsync(f->d_sub_dt.p, dts.data(), nlev * sizeof(double), cudaMemcpyHostToDevice, st));
+    FK(f, f->d_rb.reserve(2));
+    FK(f, cudaMemsetAsync(f->d_rb.p, 0, 2 * sizeof(unsigned long long), st));
+    FK(f, gf::launch_slot_copy(f->M, f->d_ss.p + f->ss_copy_off[0][f->par], f->ss_copy_n[0], st));
+    std::vector<int> p(nlev + 1, f->par);
+    if ((rc = sub_fill_level(f, f->sub_lo, t, p.data(), -1))) return rc;
+    if ((rc = sub_level(f, f->sub_lo, t, dt, p.data()))) return rc;
+    FK(f, cudaMemcpyAsync(f->h_rb, f->d_rb.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    FK(f, cudaStreamSynchronize(st));
+    if ((int)f->h_rb[0]) return ffail(f, GF_ERR_DEVICE, "a patch-update copy wait timed out");
+    std::memcpy(cfl, &f->h_rb[1], sizeof *cfl);
+    *updates = cu;
+    return GF_OK;
+}
+
+/* accept: the coarsest level back into the shared buffer; retake: the
+ * finer levels' start state back */
+int sub_finish(gf_forest* f, bool accept)
+{
+    cudaStream_t st = gf::ctx_stream(f->ctx);
+    const int kind = accept ? 2 : 1;
+    FK(f, gf::launch_slot_copy(f->M, f->d_ss.p + f->ss_copy_off[kind][f->par], f->ss_copy_n[kind], st));
+    return GF_OK;
+}
+
+/* ForestClaw outstyle 1 (fc2d_geoclaw_run.c:190-395) with variable dt and
+ * reduce_cfl: with advance-one-step (subcycle = 0) every level takes the
+ * minlevel dt over 2^(maxlevel - minlevel); with subcycle = 1 the step is
+ * the minlevel dt and the levels subcycle (sub_step). */
 int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
                   double max_cfl, int max_steps)
 {
@@ -1017,7 +1268,7 @@ int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, dou
         const double tend = t_curr + dt_outer;
         while (t_curr < tend) {
             if (max_steps > 0 && taken >= max_steps) goto out;
-            double dt_step = dt_minlevel / level_factor;
+            double dt_step = o.subcycle ? dt_minlevel : dt_minlevel / level_factor;
             const double tol = 1e-2 * dt_step;
             bool took_small = false;
             const double small_step = tend - (t_curr + dt_step);
@@ -1026,17 +1277,25 @@ int run_outstyle1(gf_forest* f, double t_final, int nout, double initial_dt, dou
                 if (small_step < 0) took_small = true;
             }
             double cfl = 0.0;
-            if ((rc = step(f, t_curr, dt_step, &cfl))) return rc;
+            long long updates = f->cells;
+            if (o.subcycle) rc = sub_step(f, t_curr, dt_step, &cfl, &updates);
+            else rc = step(f, t_curr, dt_step, &cfl);
+            if (rc) return rc;
             ++taken;
             f->st.max_cfl_seen = std::max(f->st.max_cfl_seen, cfl);
             if (cfl > max_cfl) {
+                if (o.subcycle && (rc = sub_finish(f, false))) return rc;
                 dt_minlevel = dt_minlevel * desired_cfl / cfl;
                 f->st.rejects++;
                 continue;
             }
-            f->par ^= 1;
+            if (o.subcycle) {
+                if ((rc = sub_finish(f, true))) return rc;
+            } else {
+                f->par ^= 1;
+            }
             f->st.steps++;
-            f->st.cell_updates += f->cells;
+            f->st.cell_updates += updates;
             t_curr += dt_step;
             const double dt_new = dt_minlevel * desired_cfl / cfl;
             if (!took_small) dt_minlevel = dt_new;
@@ -1117,6 +1376,12 @@ void gf_forest_destroy(gf_forest* f)
     f->d_gtask.release();
     f->d_glast.release();
     f->d_grec.release();
+    if (f->qi) cudaFree(f->qi);
+    if (f->qsave) cudaFree(f->qsave);
+    f->d_sx.release();
+    f->d_ss.release();
+    f->d_sub_dt.release();
+    f->d_par01.release();
     if (f->h_rb) cudaFreeHost(f->h_rb);
     delete f;
 }
@@ -1775,6 +2040,8 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
         if (!forests[k] || forests[k]->ctx != ctx) return GF_ERR_ARG;
         if (forests[k]->leaves.empty()) return ffail(forests[k], GF_ERR_STATE, "forest not initialised");
         if (forests[k]->o.maxlevel >= kBatchLevels) return ffail(forests[k], GF_ERR_ARG, "maxlevel too deep");
+        if (forests[k]->o.subcycle)
+            return ffail(forests[k], GF_ERR_UNSUPPORTED, "batched runs take every level's step together (subcycle = 0)");
         for (int j = 0; j < k; ++j)
             if (forests[j] == forests[k]) return ffail(forests[k], GF_ERR_ARG, "a forest appears twice");
     }

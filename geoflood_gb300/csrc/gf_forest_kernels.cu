@@ -1,6 +1,7 @@
 /*
- * Raster pyramid, patch fill, sea-level initial state and gauge sampling
- * for multi-level forests.
+ * Raster pyramid, patch fill, sea-level initial state, gauge sampling and
+ * the subcycling helpers (time interpolation, patch copies) for
+ * multi-level forests.
  *
  * A forest's static fields (bathymetry, optional extra aux fields) and its
  * initial state are given as rasters at the finest level. Level l of the
@@ -148,6 +149,40 @@ __global__ void qinit_sea_level_kernel(const double* __restrict__ b, double* __r
     }
 }
 
+/* Time interpolation of one coarse patch for the ghost cells of finer
+ * patches at an intermediate time, as fc2d_geoclaw_fort_timeinterp
+ * (fclaw2d_source/fc2d_geoclaw_timeinterp_fort.f:16-58) computes it: the
+ * interior cells within two layers of a face take qold + alpha (qnew -
+ * qold); the ghost ring takes qold's (exchanged at the old time), so that
+ * cells the exchange at the new time does not reach stay defined. */
+template <int M>
+__global__ void __launch_bounds__(128) tinterp_strip_kernel(const gf_slot_task* __restrict__ tasks, int ntask,
+                                                            double alpha)
+{
+    constexpr int N = M + 2 * H, S = N * N;
+    if ((int)blockIdx.x >= ntask) return;
+    const gf_slot_task T = tasks[blockIdx.x];
+    for (int k = threadIdx.x; k < 3 * S; k += blockDim.x) {
+        const int c = k % S, i = c % N - H + 1, j = c / N - H + 1; /* Fortran indices */
+        if (i < 1 || i > M || j < 1 || j > M) {
+            T.c[k] = T.a[k];
+            continue;
+        }
+        const int d = min(min(i - 1, j - 1), min(M - i, M - j));
+        if (d < 2) T.c[k] = T.a[k] + alpha * (T.b[k] - T.a[k]);
+    }
+}
+
+/* whole-patch copies (3 planes) */
+template <int M>
+__global__ void __launch_bounds__(128) slot_copy_kernel(const gf_slot_task* __restrict__ tasks, int ntask)
+{
+    constexpr int N = M + 2 * H, S = N * N;
+    if ((int)blockIdx.x >= ntask) return;
+    const gf_slot_task T = tasks[blockIdx.x];
+    for (int k = threadIdx.x; k < 3 * S; k += blockDim.x) T.c[k] = T.a[k];
+}
+
 int grid_for(long total)
 {
     long b = (total + 255) / 256;
@@ -184,6 +219,30 @@ cudaError_t launch_patch_fill(int m, const gf_fill_task* tasks, int ntask, cudaS
     case 32: patch_fill_kernel<32><<<ntask, 128, 0, st>>>(tasks, ntask); break;
     case 16: patch_fill_kernel<16><<<ntask, 128, 0, st>>>(tasks, ntask); break;
     case 8: patch_fill_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tinterp_strip(int m, const gf_slot_task* tasks, int ntask, double alpha, cudaStream_t st)
+{
+    if (ntask <= 0) return cudaSuccess;
+    switch (m) {
+    case 32: tinterp_strip_kernel<32><<<ntask, 128, 0, st>>>(tasks, ntask, alpha); break;
+    case 16: tinterp_strip_kernel<16><<<ntask, 128, 0, st>>>(tasks, ntask, alpha); break;
+    case 8: tinterp_strip_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask, alpha); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_slot_copy(int m, const gf_slot_task* tasks, int ntask, cudaStream_t st)
+{
+    if (ntask <= 0) return cudaSuccess;
+    switch (m) {
+    case 32: slot_copy_kernel<32><<<ntask, 128, 0, st>>>(tasks, ntask); break;
+    case 16: slot_copy_kernel<16><<<ntask, 128, 0, st>>>(tasks, ntask); break;
+    case 8: slot_copy_kernel<8><<<ntask, 128, 0, st>>>(tasks, ntask); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -90,6 +90,9 @@ cudaError_t launch_topo_raster(const gf_topo_grid* grids, const int* order, int 
 int topo_raster_device(gf_ctx* c, gf_topo* t, int nx, int ny, int halo, double xlower,
                        double ylower, double dx, double dy, double xupper, double yupper,
                        double* out, cudaStream_t st);
+cudaError_t launch_tinterp_strip(int m, const gf_slot_task* tasks, int ntask, double alpha,
+                                 cudaStream_t st);
+cudaError_t launch_slot_copy(int m, const gf_slot_task* tasks, int ntask, cudaStream_t st);
 cudaError_t launch_qinit_sea_level(const double* b, double* h, double* hu, double* hv, long cells,
                                    double sea_level, cudaStream_t st);
 /* one record of 6 doubles per gauge at rec (level -1: not recorded) */

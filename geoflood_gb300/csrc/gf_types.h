@@ -130,6 +130,15 @@ typedef struct gf_tag_task {
     int maxlevel, init_flag;
 } gf_tag_task;
 
+/* Subcycling (gf_forest_kernels.cu): one patch's time interpolation
+ * (qi = qold + alpha (qnew - qold) on the two cell layers along each face,
+ * qold's ghost ring copied) or one patch copy (src -> dst, all planes). */
+typedef struct gf_slot_task {
+    const double* a;  /* qold / src */
+    const double* b;  /* qnew       */
+    double* c;        /* qi / dst   */
+} gf_slot_task;
+
 /* One topo grid on the device (gf_topo_kernels.cu): node values in file order
  * (rows north to south, x fastest), node extent and spacing. */
 typedef struct gf_topo_grid {

@@ -32,7 +32,7 @@ class Forest:
                  dx0: float, dy0: float, aux: np.ndarray | None, q: np.ndarray | None,
                  x0: float = 0.0, y0: float = 0.0, phys_slot: int = 0, mthbc=(1, 1, 1, 1),
                  regrid_interval: int = 0, max_patches: int = 0, refine: Refine | None = None,
-                 maux: int = 1):
+                 maux: int = 1, subcycle: bool = False):
         self.ctx = ctx
         self._lib = _lib.load()
         nx, ny = nbx * mx << maxlevel, nby * mx << maxlevel
@@ -59,6 +59,7 @@ class Forest:
         o.regrid_interval = regrid_interval
         o.max_patches = max_patches
         o.refine = (refine or Refine()).to_c()
+        o.subcycle = int(bool(subcycle))
         self.mx, self.maux = mx, maux
         self.minlevel, self.maxlevel = minlevel, maxlevel
         h = C.c_void_p()

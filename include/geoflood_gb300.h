@@ -335,6 +335,9 @@ typedef struct gf_forest_opts {
     int regrid_interval;   /* accepted steps between regrids (0: never)      */
     int max_patches;       /* slot capacity (0: nbx*nby*4^maxlevel)          */
     gf_refine refine;      /* refinement criteria                            */
+    int subcycle;          /* 1: level l takes 2^(l - lmin) steps of dt / 2^(l - lmin)
+                              per coarse step (ForestClaw subcycle = T); 0: every
+                              level takes the finest level's step             */
 } gf_forest_opts;
 
 typedef struct gf_forest_stats {

@@ -44,7 +44,9 @@ def pyramid(fields: np.ndarray, levels: int) -> list:
 
 class Forest:
     def __init__(self, mx, nbx, nby, minlevel, maxlevel, dx0, dy0, aux, q, x0=0.0, y0=0.0,
-                 phys=None, mthbc=(1, 1, 1, 1), regrid_interval=0, rf=None, hy=None):
+                 phys=None, mthbc=(1, 1, 1, 1), regrid_interval=0, rf=None, hy=None,
+                 subcycle=False):
+        self.subcycle = bool(subcycle)
         self.m, self.nbx, self.nby = mx, nbx, nby
         self.lmin, self.lmax = minlevel, maxlevel
         self.dx0, self.dy0, self.x0, self.y0 = dx0, dy0, x0, y0
@@ -126,7 +128,9 @@ class Forest:
         return [q, aux]
 
     # ---- ghost exchange -------------------------------------------------
-    def _level_fill(self, l, t):
+    def _level_fill(self, l, t, arrays=None):
+        """Same-level copies and physical sides of level l; arrays (key -> q)
+        replaces the leaves' own states when given."""
         keys = [k for k in self.canonical() if k[0] == l]
         if not keys:
             return
@@ -138,14 +142,15 @@ class Forest:
                     nbr[n, s] = -1
                 else:
                     nbr[n, s] = pos.get((l, I + di, J + dj), -2)
-        q = np.stack([self.leaves[k][0] for k in keys])
+        qof = (lambda k: arrays[k]) if arrays is not None else (lambda k: self.leaves[k][0])
+        q = np.stack([qof(k) for k in keys])
         aux = np.stack([self.leaves[k][1] for k in keys])
         xl = np.array([self.origin(*k)[0] for k in keys])
         yl = np.array([self.origin(*k)[1] for k in keys])
         level_ghost_fill(q, aux, nbr, xl, yl, self.dx(l), self.dy(l), t, self.mthbc, self.phys,
                          self.hy)
         for n, k in enumerate(keys):
-            self.leaves[k][0][...] = q[n]
+            qof(k)[...] = q[n]
             self.leaves[k][1][...] = aux[n]
 
     def ghost_fill(self, t):
@@ -206,6 +211,129 @@ class Forest:
                         interpolate_ghost(qc, ac, qf, af, 1, 3 - cc, m * (2 * ck[1] - I),
                                           m * (2 * ck[2] - J), self.phys)
             self._level_fill(l, t)
+
+    # ---- subcycling ---------------------------------------------------------
+    # The level-by-level schedule the device forest follows with subcycle = 1
+    # (ForestClaw's fclaw2d_advance_all_levels, an external library: this is
+    # the project's statement of it): coarse before fine; a level's two
+    # sub-steps inside its parent's step take their coarse ghost values from
+    # the parent's start state and from the parent time-interpolated to the
+    # midpoint (fc2d_geoclaw_fort_timeinterp on the two layers along each
+    # face, the old ghost ring kept, ghost cells exchanged at the midpoint).
+    def _avg_level(self, l, qc_of):
+        """fine (level l + 1) -> coarse averages into level-l ghost cells;
+        qc_of(key) gives the coarse array to write."""
+        m = self.m
+        for (lv, I, J) in self.canonical():
+            if lv != l:
+                continue
+            qc, ac = qc_of((lv, I, J)), self.leaves[(lv, I, J)][1]
+            for fc, (di, dj) in enumerate(FACES):
+                NI, NJ = I + di, J + dj
+                if not self.inside(l, NI, NJ) or (l, NI, NJ) in self.leaves:
+                    continue
+                if l > self.lmin and (l - 1, NI >> 1, NJ >> 1) in self.leaves:
+                    continue
+                for c in range(2):
+                    if fc < 2:
+                        FI, FJ = 2 * NI + (1 if di < 0 else 0), 2 * J + c
+                    else:
+                        FI, FJ = 2 * I + c, 2 * NJ + (1 if dj < 0 else 0)
+                    qf, af = self.leaves[(l + 1, FI, FJ)]
+                    average_ghost(qc, ac, qf, af, 0, fc, m * (2 * I - FI), m * (2 * J - FJ),
+                                  self.phys)
+            for cc, (di, dj) in enumerate(CORNERS):
+                DI, DJ = I + di, J + dj
+                if not self.inside(l, DI, DJ) or (l, DI, DJ) in self.leaves:
+                    continue
+                if self.containing(l, DI, DJ) is not None:
+                    continue
+                FI, FJ = 2 * DI + (1 if di < 0 else 0), 2 * DJ + (1 if dj < 0 else 0)
+                qf, af = self.leaves[(l + 1, FI, FJ)]
+                average_ghost(qc, ac, qf, af, 1, cc, m * (2 * I - FI), m * (2 * J - FJ), self.phys)
+
+    def _interp_level(self, l, qc_of):
+        """coarse (level l - 1, arrays from qc_of) -> fine ghost cells of level l."""
+        m = self.m
+        for (lp, I, J), (qf, af) in self.leaves.items():
+            if lp != l:
+                continue
+            for fc, (di, dj) in enumerate(FACES):
+                NI, NJ = I + di, J + dj
+                if not self.inside(l, NI, NJ) or (l, NI, NJ) in self.leaves:
+                    continue
+                ck = (l - 1, NI >> 1, NJ >> 1)
+                if ck in self.leaves:
+                    interpolate_ghost(qc_of(ck), self.leaves[ck][1], qf, af, 0, fc ^ 1,
+                                      m * (2 * ck[1] - I), m * (2 * ck[2] - J), self.phys)
+            for cc, (di, dj) in enumerate(CORNERS):
+                DI, DJ = I + di, J + dj
+                if not self.inside(l, DI, DJ) or (l, DI, DJ) in self.leaves:
+                    continue
+                ck = (l - 1, DI >> 1, DJ >> 1)
+                if ck not in self.leaves:
+                    continue
+                xok = 2 * ck[1] == DI if di > 0 else 2 * ck[1] + 1 == DI
+                yok = 2 * ck[2] == DJ if dj > 0 else 2 * ck[2] + 1 == DJ
+                if xok and yok:
+                    interpolate_ghost(qc_of(ck), self.leaves[ck][1], qf, af, 1, 3 - cc,
+                                      m * (2 * ck[1] - I), m * (2 * ck[2] - J), self.phys)
+
+    def _fill_level_sub(self, l, t, csrc, hi):
+        own = lambda k: self.leaves[k][0]  # noqa: E731
+        if l < hi:
+            self._avg_level(l, own)
+        self._level_fill(l, t)
+        if csrc is not None:
+            self._interp_level(l, csrc.__getitem__)
+            self._level_fill(l, t)
+
+    def _update_level(self, l, dt):
+        keys = [k for k in self.canonical() if k[0] == l]
+        q = np.stack([self.leaves[k][0] for k in keys])
+        aux = np.stack([self.leaves[k][1] for k in keys])
+        dx = np.array([self.dx(l)] * len(keys))
+        dy = np.array([self.dy(l)] * len(keys))
+        cfl = level_update(q, aux, dx, dy, 0.0, dt, self.phys)
+        for n, k in enumerate(keys):
+            self.leaves[k][0][...] = q[n]
+        return cfl
+
+    def _sub_level(self, l, tl, dtl, hi):
+        keys = [k for k in self.canonical() if k[0] == l]
+        old = {k: self.leaves[k][0].copy() for k in keys}
+        cfl = self._update_level(l, dtl)
+        if l >= hi:
+            return cfl
+        m = self.m
+        i = np.arange(m + 4) - 1                      # Fortran index of each array column
+        d = np.minimum(np.minimum(i[None, :] - 1, i[:, None] - 1), np.minimum(m - i[None, :], m - i[:, None]))
+        strip = (d < 2) & (i[None, :] >= 1) & (i[None, :] <= m) & (i[:, None] >= 1) & (i[:, None] <= m)
+        for k in (0, 1):
+            tf = tl + dtl * 0.5 if k else tl
+            src = old
+            if k == 1:
+                qi = {}
+                for key in keys:
+                    a, b = old[key], self.leaves[key][0]
+                    qi[key] = a.copy()
+                    qi[key][strip] = a[strip] + 0.5 * (b[strip] - a[strip])
+                self._avg_level(l, qi.__getitem__)
+                self._level_fill(l, tf, arrays=qi)
+                src = qi
+            self._fill_level_sub(l + 1, tf, src, hi)
+            cfl = max(cfl, self._sub_level(l + 1, tf, dtl * 0.5, hi))
+        return cfl
+
+    def step_subcycled(self, t, dt):
+        """One coarse step dt with subcycling; returns the max CFL of all
+        sub-steps and the number of cell-updates."""
+        levels = sorted({k[0] for k in self.leaves})
+        lo, hi = levels[0], levels[-1]
+        self._fill_level_sub(lo, t, None, hi)
+        cfl = self._sub_level(lo, t, dt, hi)
+        cu = sum(self.m * self.m << (k[0] - lo) for k in self.leaves)
+        return cfl, cu
 
     # ---- tags, balance, regrid ------------------------------------------
     def _tags(self, t, init_flag):
@@ -357,7 +485,7 @@ class Forest:
                     self.t, self.dt = t_curr, dt_minlevel
                     self.flush_gauges()
                     return dts
-                dt_step = dt_minlevel / level_factor
+                dt_step = dt_minlevel if self.subcycle else dt_minlevel / level_factor
                 tol = 1e-2 * dt_step
                 took_small = False
                 small_step = tend - (t_curr + dt_step)
@@ -366,7 +494,10 @@ class Forest:
                     if small_step < 0:
                         took_small = True
                 snap = self.snapshot()
-                cfl = self.step(t_curr, dt_step)
+                if self.subcycle:
+                    cfl, cu = self.step_subcycled(t_curr, dt_step)
+                else:
+                    cfl, cu = self.step(t_curr, dt_step), len(self.leaves) * self.m * self.m
                 taken += 1
                 self.max_cfl_seen = max(self.max_cfl_seen, cfl)
                 if cfl > max_cfl:
@@ -375,7 +506,7 @@ class Forest:
                     self.rejects += 1
                     continue
                 self.steps += 1
-                self.cell_updates += len(self.leaves) * self.m * self.m
+                self.cell_updates += cu
                 t_curr += dt_step
                 dts.append(dt_step)
                 dt_new = dt_minlevel * desired_cfl / cfl if cfl > 0.0 else float("inf")
