@@ -643,6 +643,20 @@ def forest_leg(args, dev=0):
         frame_bytes = sum(os.path.getsize(os.path.join(td, n)) for n in os.listdir(td))
     frame_cells = int(len(gpu_patches)) * c["mx"] * c["mx"]
     F.close()
+    # the same dam break to a 60 s horizon with and without subcycling
+    horizon = {}
+    for sub in (False, True):
+        G = gf.Forest(ctx, c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"],
+                      c["b"], c["q"], mthbc=c["mthbc"], regrid_interval=c["regrid"], refine=c["rf"],
+                      subcycle=sub)
+        G.init()
+        t0 = time.perf_counter()
+        hs = G.run(60.0, 1, 5.0, 0.9, 1.0)
+        sec = time.perf_counter() - t0
+        G.close()
+        horizon["subcycled" if sub else "advance_one_step"] = {
+            "seconds": sec, "coarse_or_global_steps": hs["steps"], "rejects": hs["rejects"],
+            "cell_updates": hs["cell_updates"], "value": hs["cell_updates"] / sec, "unit": METRIC}
     ctx.close()
     oracle.load()
     O = of.Forest(c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"], c["b"],
@@ -662,6 +676,7 @@ def forest_leg(args, dev=0):
                        "cores": 1, "kind": "port",
                        "note": "oracle forest driver (Python tree + C kernels, one thread)"},
         "patch_lists_equal_to_oracle": bool(np.array_equal(gpu_patches, O.patches())),
+        "to_60s": horizon,
         "ascii_frame": {"cells": frame_cells, "bytes": frame_bytes, "seconds": frame_s,
                         "cells_per_s": frame_cells / frame_s, "MB_per_s": frame_bytes / frame_s / 1e6,
                         "note": "gf_forest_write_ascii: leaf download + fort.t/fort.q text"},

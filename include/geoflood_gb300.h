@@ -314,7 +314,10 @@ int gf_patch_update_noalloc(int device, const gf_phys* phys, int npatch,
  * interpolate2fine / average2coarse for the new patches; time stepping by
  * outstyle 1 (fc2d_geoclaw_run.c:190-395) with all levels advanced by the
  * same step (subcycle = F, advance-one-step = T, as the reference's
- * examples set them) and a regrid every regrid_interval accepted steps.
+ * examples set them) or, with opts.subcycle = 1, level by level with
+ * time-interpolated coarse ghost cells (ForestClaw's subcycle = T,
+ * fclaw2d_advance_all_levels; fclaw2d_source/fc2d_geoclaw_timeinterp_fort.f
+ * for the interpolation), and a regrid every regrid_interval accepted steps.
  *
  * Static fields and the initial state come as rasters at the finest level
  * (maxlevel): maux aux fields then h, hu, hv, each ny x nx doubles with x
