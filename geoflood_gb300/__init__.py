@@ -304,6 +304,10 @@ class Level:
         _check(self.ctx.h, self._lib.gf_level_step_host(self.h, dptr(q), t, dt, C.byref(mc)))
         return mc.value
 
+    def set_pipeline(self, nchunks: int = 0):
+        """Chunks of step_host (0 auto, 1 no overlap); results do not depend on it."""
+        _check(self.ctx.h, self._lib.gf_level_set_pipeline(self.h, int(nchunks)))
+
     def set_layout(self, nbr: np.ndarray, xlower=None, ylower=None):
         nb = np.ascontiguousarray(nbr, dtype=np.int32).reshape(self.npatch, 8)
         xl = None if xlower is None else np.ascontiguousarray(xlower, dtype=np.float64)

@@ -159,6 +159,7 @@ SIGNATURES = [
     ("gf_level_download_aux", C.c_int, [_vp, _dp]),
     ("gf_level_step", C.c_int, [_vp, C.c_double, C.c_double, _dp]),
     ("gf_level_step_host", C.c_int, [_vp, _dp, C.c_double, C.c_double, _dp]),
+    ("gf_level_set_pipeline", C.c_int, [_vp, C.c_int]),
     ("gf_level_step_async", C.c_int, [_vp, C.c_double, C.c_double]),
     ("gf_level_sync", C.c_int, [_vp, _dp]),
     ("gf_ctx_stream", C.c_int, [_vp, C.POINTER(_vp)]),

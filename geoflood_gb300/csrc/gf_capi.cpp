@@ -124,6 +124,17 @@ struct gf_level {
     gf_bc_spec bc{};
     gf_ghost_block* d_ghost = nullptr; /* one block, rewritten per fill */
     std::vector<double> hy_time, hy_hu;
+    std::vector<int> h_nbr;            /* host copy of the neighbour table */
+    /* host-buffer step pipeline: patches in chunks [off[k], off[k+1]) whose
+     * copies run on a second stream beside the other chunks' work */
+    int pipe_request = 0;              /* 0 auto, else the number of chunks */
+    bool pipe_ready = false;
+    cudaStream_t cs = nullptr;         /* copies                            */
+    cudaStream_t cs2 = nullptr;        /* odd chunks' transposes and updates */
+    cudaStream_t cs3 = nullptr;        /* ghost fills and transposes back    */
+    std::vector<cudaEvent_t> ev;       /* start, end2, end3, then up[k], upd[k], dn[k] */
+    std::vector<int> off, dlo, dhi;    /* chunk j's ghost cells read chunks dlo[j]..dhi[j] */
+    gf_ghost_ref* d_refs = nullptr;
 };
 
 namespace {
@@ -433,6 +444,11 @@ void gf_level_destroy(gf_level* L)
     if (L->d_geom) cudaFree(L->d_geom);
     if (L->d_phys_of) cudaFree(L->d_phys_of);
     if (L->d_ghost) cudaFree(L->d_ghost);
+    if (L->d_refs) cudaFree(L->d_refs);
+    for (cudaEvent_t e : L->ev) cudaEventDestroy(e);
+    if (L->cs) cudaStreamDestroy(L->cs);
+    if (L->cs2) cudaStreamDestroy(L->cs2);
+    if (L->cs3) cudaStreamDestroy(L->cs3);
     delete L;
 }
 
@@ -467,8 +483,10 @@ int gf_level_set_layout(gf_level* L, const int* nbr, const double* xlower, const
     GF_CK(c, cudaMemcpyAsync(L->d_nbr, nbr, (size_t)L->npatch * 8 * sizeof(int),
                              cudaMemcpyHostToDevice, c->stream));
     GF_CK(c, cudaStreamSynchronize(c->stream));
+    L->h_nbr.assign(nbr, nbr + 8L * L->npatch);
     L->layout_set = true;
     L->geom_dirty = true;
+    L->pipe_ready = false;
     return GF_OK;
 }
 
@@ -515,12 +533,10 @@ static double hydro_interp(const gf_level* L, double t)
     return 0.0;
 }
 
-int gf_level_ghost_fill_async(gf_level* L, double t)
+/* geometry (if changed) and the ghost block for time t, on the context's stream */
+static int level_ghost_prepare(gf_level* L, double t)
 {
-    if (!L) return GF_ERR_ARG;
     gf_ctx* c = L->ctx;
-    if (!L->layout_set) return fail(c, GF_ERR_STATE, "level layout (neighbour table) not set");
-    GF_CK(c, cudaSetDevice(c->device));
     if (L->geom_dirty) {
         std::vector<gf_patch_geom> g(L->npatch);
         for (int k = 0; k < L->npatch; ++k) g[k] = {L->xlower[k], L->ylower[k], L->dx[k], L->dy[k]};
@@ -542,6 +558,17 @@ int gf_level_ghost_fill_async(gf_level* L, double t)
     blk.maux = L->maux;
     /* pageable source: the copy is staged before the call returns */
     GF_CK(c, cudaMemcpyAsync(L->d_ghost, &blk, sizeof blk, cudaMemcpyHostToDevice, c->stream));
+    return GF_OK;
+}
+
+int gf_level_ghost_fill_async(gf_level* L, double t)
+{
+    if (!L) return GF_ERR_ARG;
+    gf_ctx* c = L->ctx;
+    if (!L->layout_set) return fail(c, GF_ERR_STATE, "level layout (neighbour table) not set");
+    GF_CK(c, cudaSetDevice(c->device));
+    int rc = level_ghost_prepare(L, t);
+    if (rc) return rc;
     GF_CK(c, gf::launch_ghost_fill(L->mx, L->d_ghost, nullptr, L->npatch, c->d_phys, c->stream));
     return GF_OK;
 }
@@ -654,6 +681,65 @@ int gf_level_step(gf_level* L, double t, double dt, double* maxcfl)
 
 int gf_level_ghost_fill_async(gf_level* L, double t);
 
+/* Chunks for the host-buffer step: equal whole waves of the update kernel
+ * (its resident CTAs on all SMs), about two waves or more each, at most 8. */
+static int level_pipe_setup(gf_level* L)
+{
+    if (L->pipe_ready) return GF_OK;
+    gf_ctx* c = L->ctx;
+    int sms = 0;
+    GF_CK(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    const int wave = std::max(1, gf::patch_update_occupancy(L->mx) * sms);
+    int k = L->pipe_request > 0 ? L->pipe_request : std::max(1, std::min(8, L->npatch / (2 * wave)));
+    k = std::min(k, L->npatch);
+    int chunk = (L->npatch + k - 1) / k;
+    if (L->pipe_request <= 0 && k > 1) chunk = (chunk + wave - 1) / wave * wave;
+    L->off.clear();
+    for (int p = 0; p < L->npatch; p += chunk) L->off.push_back(p);
+    L->off.push_back(L->npatch);
+    const int nc = (int)L->off.size() - 1;
+    L->dlo.assign(nc, 0);
+    L->dhi.assign(nc, 0);
+    for (int j = 0; j < nc; ++j) {
+        int lo = j, hi = j;
+        if (L->layout_set)
+            for (int p = L->off[j]; p < L->off[j + 1]; ++p)
+                for (int s = 0; s < 8; ++s) {
+                    const int nb = L->h_nbr[8L * p + s];
+                    if (nb >= 0) {
+                        lo = std::min(lo, nb / chunk);
+                        hi = std::max(hi, nb / chunk);
+                    }
+                }
+        L->dlo[j] = lo;
+        L->dhi[j] = hi;
+    }
+    if (!L->cs) GF_CK(c, cudaStreamCreateWithFlags(&L->cs, cudaStreamNonBlocking));
+    if (!L->cs2) GF_CK(c, cudaStreamCreateWithFlags(&L->cs2, cudaStreamNonBlocking));
+    if (!L->cs3) GF_CK(c, cudaStreamCreateWithFlags(&L->cs3, cudaStreamNonBlocking));
+    while ((int)L->ev.size() < 3 * nc + 3) {
+        cudaEvent_t e;
+        GF_CK(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        L->ev.push_back(e);
+    }
+    if (!L->d_refs) {
+        std::vector<gf_ghost_ref> r(L->npatch);
+        for (int p = 0; p < L->npatch; ++p) r[p] = gf_ghost_ref{0, p};
+        GF_CK(c, cudaMalloc(&L->d_refs, r.size() * sizeof(gf_ghost_ref)));
+        GF_CK(c, cudaMemcpy(L->d_refs, r.data(), r.size() * sizeof(gf_ghost_ref), cudaMemcpyHostToDevice));
+    }
+    L->pipe_ready = true;
+    return GF_OK;
+}
+
+/* One step from host buffers, pipelined over chunks of patches: chunk k's
+ * upload runs on a copy stream; its transpose and update run on one of two
+ * compute streams (alternating, so one launch's last patches overlap the
+ * next launch's first); once every chunk a chunk's ghost cells read is
+ * updated, that chunk's ghost fill and transpose back follow on a third
+ * stream (so they never hold up an update) and its download on the copy
+ * stream. The kernels and data are those of one whole-level pass: the
+ * result is identical. */
 int gf_level_step_host(gf_level* L, double* q, double t, double dt, double* maxcfl)
 {
     if (!L || !q) return GF_ERR_ARG;
@@ -661,15 +747,73 @@ int gf_level_step_host(gf_level* L, double* q, double t, double dt, double* maxc
     GF_CK(c, cudaSetDevice(c->device));
     int rc = level_prepare(L);
     if (rc) return rc;
-    if ((rc = level_upload_q_async(L, q))) return rc;
+    if ((rc = level_pipe_setup(L))) return rc;
+    if (L->layout_set && (rc = level_ghost_prepare(L, t + dt))) return rc;
+    const int nc = (int)L->off.size() - 1;
+    cudaEvent_t* up = L->ev.data() + 3;
+    cudaEvent_t* upd = up + nc;
+    cudaEvent_t* dn = upd + nc;
+    const size_t per = 3 * (size_t)L->S;
+    cudaStream_t cst[2] = {c->stream, L->cs2};
+    GF_CK(c, cudaMemsetAsync(L->d_status, 0, sizeof(DevStatus), c->stream));
+    GF_CK(c, cudaEventRecord(L->ev[0], c->stream));
+    GF_CK(c, cudaStreamWaitEvent(L->cs, L->ev[0], 0));
+    GF_CK(c, cudaStreamWaitEvent(L->cs2, L->ev[0], 0));
+    GF_CK(c, cudaStreamWaitEvent(L->cs3, L->ev[0], 0));
+    for (int k = 0; k < nc; ++k) {
+        const size_t o = L->off[k] * per, n = (size_t)(L->off[k + 1] - L->off[k]) * per;
+        GF_CK(c, cudaMemcpyAsync(L->d_stage + o, q + o, n * sizeof(double), cudaMemcpyHostToDevice, L->cs));
+        GF_CK(c, cudaEventRecord(up[k], L->cs));
+    }
+    std::vector<char> done(nc, 0);
+    auto finish_chunk = [&](int j) -> int {
+        const int p0 = L->off[j], np = L->off[j + 1] - p0;
+        cudaStream_t sj = L->cs3;
+        for (int i = L->dlo[j]; i <= L->dhi[j]; ++i) GF_CK(c, cudaStreamWaitEvent(sj, upd[i], 0));
+        if (L->layout_set)
+            GF_CK(c, gf::launch_ghost_fill(L->mx, L->d_ghost, L->d_refs + p0, np, c->d_phys, sj));
+        GF_CK(c, gf::launch_soa_to_aos(L->d_q + p0 * per, L->d_stage + p0 * per, np, (int)L->S, 3, per, per, sj));
+        GF_CK(c, cudaEventRecord(dn[j], sj));
+        GF_CK(c, cudaStreamWaitEvent(L->cs, dn[j], 0));
+        GF_CK(c, cudaMemcpyAsync(q + p0 * per, L->d_stage + p0 * per, np * per * sizeof(double),
+                                 cudaMemcpyDeviceToHost, L->cs));
+        done[j] = 1;
+        return GF_OK;
+    };
+    for (int k = 0; k < nc; ++k) {
+        const int p0 = L->off[k], np = L->off[k + 1] - p0;
+        cudaStream_t sk = cst[k & 1];
+        GF_CK(c, cudaStreamWaitEvent(sk, up[k], 0));
+        GF_CK(c, gf::launch_aos_to_soa(L->d_stage + p0 * per, L->d_q + p0 * per, np, (int)L->S, 3, per, per, sk));
+        if (c->exact)
+            GF_CK(c, gf::launch_patch_update_exact(L->mx, L->d_work + p0, np, c->d_phys, dt, nullptr, nullptr,
+                                                   L->maux, L->d_cfl + p0, &L->d_status->gmax,
+                                                   &L->d_status->err, sk));
+        else
+            GF_CK(c, gf::launch_patch_update(L->mx, L->d_work + p0, np, c->d_phys, dt, nullptr, nullptr, L->maux,
+                                             L->d_cfl + p0, &L->d_status->gmax, &L->d_status->err, sk));
+        GF_CK(c, cudaEventRecord(upd[k], sk));
+        /* chunks whose neighbours are all updated now */
+        for (int j = 0; j < nc; ++j)
+            if (!done[j] && L->dhi[j] <= k && (rc = finish_chunk(j))) return rc;
+    }
+    GF_CK(c, cudaEventRecord(L->ev[1], L->cs2));
+    GF_CK(c, cudaEventRecord(L->ev[2], L->cs3));
+    GF_CK(c, cudaStreamWaitEvent(c->stream, L->ev[1], 0));
+    GF_CK(c, cudaStreamWaitEvent(c->stream, L->ev[2], 0));
     double mc = 0.0;
-    if ((rc = enqueue_batch(c, L->mx, L->d_work, L->npatch, L->maux, dt, L->d_cfl, L->d_status)))
-        return rc;
-    if (L->layout_set && (rc = gf_level_ghost_fill_async(L, t + dt))) return rc;
-    if ((rc = finish_batch(c, L->d_status, &mc))) return rc;
-    if ((rc = level_download_q_async(L, q))) return rc;
-    GF_CK(c, cudaStreamSynchronize(c->stream));
+    rc = finish_batch(c, L->d_status, &mc);
+    GF_CK(c, cudaStreamSynchronize(L->cs));
+    if (rc) return rc;
     if (maxcfl) *maxcfl = mc;
+    return GF_OK;
+}
+
+int gf_level_set_pipeline(gf_level* L, int nchunks)
+{
+    if (!L || nchunks < 0) return GF_ERR_ARG;
+    L->pipe_request = nchunks;
+    L->pipe_ready = false;
     return GF_OK;
 }
 

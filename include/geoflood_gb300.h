@@ -169,9 +169,15 @@ int gf_level_step(gf_level* lev, double t, double dt, double* maxcfl);
 
 /* The same step end to end from host buffers: upload q (Fortran layout),
  * step, fill ghost cells at t + dt if a layout is set, download q. aux stays
- * resident. */
+ * resident. The patches go in chunks: one chunk's copies (on a second
+ * stream) run beside other chunks' transposes, updates and ghost fills, so
+ * with pinned q most of the traffic hides behind the update. */
 int gf_level_step_host(gf_level* lev, double* q, double t, double dt,
                        double* maxcfl);
+/* Chunks of gf_level_step_host: 0 (default) picks whole waves of the update
+ * kernel, at most 8 chunks; 1 runs one chunk (no overlap); n > 1 n equal
+ * chunks. The result does not depend on it. */
+int gf_level_set_pipeline(gf_level* lev, int nchunks);
 
 /* Asynchronous form of gf_level_step: enqueue the step on the context
  * stream and return; gf_level_sync waits and reports the max CFL of the

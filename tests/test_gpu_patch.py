@@ -269,3 +269,41 @@ def test_exact_build_beam_warming(exact_ctx):
     out, ref, cg, cr, pg, pr = level_vs_oracle(exact_ctx, q, aux, m, 2.0, 0.04, phys, slot=7)
     s = slice(MBC, MBC + m)
     assert np.array_equal(out[:, s, s], ref[:, s, s])
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_step_host_pipeline_chunks_give_identical_results(ctx, shuffle):
+    """gf_level_step_host in 1, 3 or 7 chunks, and the automatic choice, on a
+    12 x 10 brick with a layout (ghost fill in the pipeline), patches either
+    row-major or shuffled so that a chunk's ghost cells read far chunks: q
+    (ghost cells included) and the CFL equal the resident step's bit for bit.
+    A first ghost fill makes the aux ghost cells consistent (a fill rewrites
+    them), so every step below sees the same bathymetry."""
+    m, py, px = 16, 10, 12
+    n = py * px
+    q, aux = random_state(n, m, 59)
+    nbr, xl, yl = synth.brick_layout(py, px, m, 2.0)
+    if shuffle:
+        perm = np.random.default_rng(5).permutation(n)     # new index -> old index
+        inv = np.empty(n, np.int64)
+        inv[perm] = np.arange(n)
+        q, aux, xl, yl = q[perm], aux[perm], xl[perm], yl[perm]
+        nb = nbr[perm]
+        nbr = np.where(nb >= 0, inv[np.maximum(nb, 0)], -1).astype(np.int32)
+    ctx.set_phys(0, gf.Phys())
+    lev = gf.Level(ctx, n, m)
+    lev.set_geometry(2.0, 2.0)
+    lev.set_layout(nbr, xl, yl)
+    lev.upload(q, aux)
+    lev.ghost_fill(0.0)
+    q0 = lev.download()
+    c_ref = lev.step(0.0, 0.04)
+    lev.ghost_fill(0.04)
+    ref = lev.download()
+    for chunks in (1, 3, 7, 0):
+        lev.set_pipeline(chunks)
+        qh = q0.copy()
+        c = lev.step_host(qh, 0.0, 0.04)
+        assert c == c_ref, chunks
+        assert np.array_equal(qh, ref), chunks
+    lev.close()
