@@ -1406,8 +1406,11 @@ int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, g
         return gf::ctx_fail(c, GF_ERR_ARG, "refinement parameter counts out of range");
     int rc = gf::ctx_check_phys(c, o->phys_slot);
     if (rc) return rc;
+    /* a regrid holds the new patches and the ones they replace at once: at
+     * most full refinement plus the parents being split (a quarter of it) */
     const long long full = (long long)o->nbx * o->nby << (2 * o->maxlevel);
-    long long cap = o->max_patches > 0 ? std::min<long long>(o->max_patches, full) : full;
+    const long long peak = full + (full + 3) / 4;
+    long long cap = o->max_patches > 0 ? std::min<long long>(o->max_patches, peak) : peak;
     if (cap > (1LL << 22)) return gf::ctx_fail(c, GF_ERR_ARG, "set max_patches (full refinement is too large)");
     gf_forest* f = new gf_forest;
     f->ctx = c;

@@ -342,7 +342,8 @@ typedef struct gf_forest_opts {
     int phys_slot;         /* physics set in the context's table             */
     int mthbc[4];          /* left, right, bottom, top: 0 inflow, 1 extrap, 3 wall */
     int regrid_interval;   /* accepted steps between regrids (0: never)      */
-    int max_patches;       /* slot capacity (0: nbx*nby*4^maxlevel)          */
+    int max_patches;       /* slot capacity (0: 5/4 of nbx*nby*4^maxlevel, the
+                              most a regrid can hold at once)                */
     gf_refine refine;      /* refinement criteria                            */
     int subcycle;          /* 1: level l takes 2^(l - lmin) steps of dt / 2^(l - lmin)
                               per coarse step (ForestClaw subcycle = T); 0: every

@@ -98,3 +98,18 @@ def test_production_build_per_step_with_inflow(ctx):
             O.regrid(t)
             assert np.array_equal(G.patches(), O.patches()), k
     G.close()
+
+
+def test_regrid_to_full_refinement_fits_default_pool(ctx):
+    """A forest that refines everywhere: the regrid holds the new children
+    and their parents at once, which the default slot pool must allow."""
+    b, q = rasters("lake")
+    ctx.set_phys(SLOT, gf.Phys())
+    everywhere = gf.Refine(wave_tolerance=1e9, regions=((0.0, 2000.0, 0.0, 1000.0, 0.0, 1e9, 3, 3),))
+    G = gf.Forest(ctx, M, NBX, NBY, LMIN, LMAX, DX0, DX0, b, q, mthbc=(3, 3, 3, 3),
+                  regrid_interval=1, refine=everywhere, phys_slot=SLOT)
+    G.init()
+    G.run(20.0, 1, 5.0, 0.9, 1.0, max_steps=3)
+    P = G.patches()
+    assert len(P) == NBX * NBY * 4 ** LMAX and set(P[:, 0]) == {LMAX}
+    G.close()
