@@ -807,6 +807,21 @@ def batched_leg(args, dev=0):
     for F in B:
         F.close()
     ctx.close()
+    # the oracle's forest driver (Python tree, C kernels on all host cores)
+    # on a bounded sample: two forests of the batch, 4 step attempts each
+    import oracle
+    from oracle import forest as of
+    cu_o, s_o, picks = 0, 0.0, [int(np.argsort(patches0)[n // 4]), int(np.argsort(patches0)[n // 2])]
+    for k in picks:
+        sp = specs[k]
+        O = of.Forest(sp["mx"], sp["nbx"], sp["nby"], sp["minlevel"], sp["maxlevel"], sp["dx0"], sp["dy0"],
+                      sp["aux"], sp["q"], phys=sp["phys"], mthbc=sp["mthbc"],
+                      regrid_interval=sp["regrid_interval"], rf=sp["refine"], hy=oracle.hydro(*sp["hydro"]))
+        O.init()
+        t0 = time.perf_counter()
+        O.run(T, 1, 1.6, 0.9, 1.0, max_steps=4)
+        s_o += time.perf_counter() - t0
+        cu_o += O.cell_updates
     mxs = [sp["mx"] for sp in specs]
     return {
         "workload": f"{n} forests, mx in {{8,16,32}} ({mxs.count(8)}/{mxs.count(16)}/"
@@ -823,6 +838,10 @@ def batched_leg(args, dev=0):
         "launches": bst["launches"], "cell_updates": work,
         "host_seconds": {"rounds": bst["s_rounds"], "regrid": bst["s_regrid"],
                          "epoch": bst["s_epoch"]},
+        "cpu_oracle": {"value": cu_o / s_o, "unit": METRIC, "seconds": s_o, "cores": os.cpu_count(),
+                       "kind": "port",
+                       "sample": f"forests {picks} (quartile and median size), 4 step attempts each; "
+                                 "per cell-update, not the whole batch"},
     }
 
 
@@ -844,7 +863,6 @@ def large_leg(args, dev=0):
                   sp["dy0"], sp["aux"], sp["q"], mthbc=sp["mthbc"],
                   regrid_interval=sp["regrid_interval"], refine=sp["refine"])
     F.set_hydrograph(*sp["hydro"])
-    del sp
     t0 = time.perf_counter()
     F.init()
     t_init = time.perf_counter() - t0
@@ -855,6 +873,20 @@ def large_leg(args, dev=0):
     el = time.perf_counter() - t0
     F.close()
     ctx.close()
+    # the oracle's forest driver on the same scenario, 2 step attempts (no
+    # regrid falls inside them)
+    import oracle
+    from oracle import forest as of
+    O = of.Forest(sp["mx"], sp["nbx"], sp["nby"], sp["minlevel"], sp["maxlevel"], sp["dx0"], sp["dy0"],
+                  sp["aux"], sp["q"], phys=sp["phys"], mthbc=sp["mthbc"], regrid_interval=0,
+                  rf=sp["refine"], hy=oracle.hydro(*sp["hydro"]))
+    del sp
+    O.init()
+    t0 = time.perf_counter()
+    O.run(21600.0, 1, 1.0, 0.9, 1.0, max_steps=2)
+    s_o = time.perf_counter() - t0
+    cu_o = O.cell_updates
+    del O
     return {
         "workload": "large scenario: 2x2 brick, mx 32, levels 3-7 (8192^2 at 2 m), fractal DEM "
                     "Hurst 0.85 relief 50 m + dendritic channels, n 0.03/0.07 field, "
@@ -865,6 +897,8 @@ def large_leg(args, dev=0):
         "finest_patches_initial": int((lv == lv.max()).sum()),
         "cells_initial": int(p0) * 32 * 32,
         "seconds_generate": t_gen, "seconds_init": t_init,
+        "cpu_oracle": {"value": cu_o / s_o, "unit": METRIC, "seconds": s_o, "cores": os.cpu_count(),
+                       "kind": "port", "sample": "2 step attempts of the same scenario (per cell-update)"},
     }
 
 
