@@ -158,8 +158,20 @@ struct gf_forest {
     int ss_copy_off[3][2] = {{0, 0}, {0, 0}, {0, 0}}; /* save, restore, unify per par */
     int ss_copy_n[3] = {0, 0, 0};
     DArr<gf_slot_task> d_ss;
-    DArr<double> d_sub_dt;
     DArr<int> d_par01;
+    /* a subcycled step as a CUDA graph: a host-only plan pass writes the
+     * step's level dts and ghost blocks (their boundary times) to pinned
+     * staging; the graph's first node copies them to the device */
+    bool sub_plan = false;
+    int sub_nblk = 0;
+    std::vector<gf_ghost_block> sub_blocks;
+    char* h_sub = nullptr;
+    size_t h_sub_cap = 0;
+    DArr<char> d_sub_stage;
+    cudaGraphExec_t sub_exec = nullptr;
+    bool sub_graph_ok = false;
+    int sub_graph_par = -1, sub_graph_nblk = -1;
+    bool sub_graph_exact = false;
 };
 
 namespace {
@@ -1034,6 +1046,7 @@ int build_sub_tables(gf_forest* f)
     int rc = build_tables(f);
     if (rc) return rc;
     if (!f->sub_dirty) return GF_OK;
+    f->sub_graph_ok = false;
     const size_t pool = (size_t)f->cap * 3 * f->S * sizeof(double);
     if (!f->qi) FK(f, cudaMalloc(&f->qi, pool));
     if (!f->qsave) FK(f, cudaMalloc(&f->qsave, pool));
@@ -1111,7 +1124,6 @@ int build_sub_tables(gf_forest* f)
         FK(f, cudaMemcpyAsync(f->d_sx.p, x.data(), x.size() * sizeof(gf_xfer_task), cudaMemcpyHostToDevice, st));
     if (!sl.empty())
         FK(f, cudaMemcpyAsync(f->d_ss.p, sl.data(), sl.size() * sizeof(gf_slot_task), cudaMemcpyHostToDevice, st));
-    FK(f, f->d_sub_dt.reserve(nlev));
     FK(f, f->d_par01.reserve(2));
     const int p01[2] = {0, 1};
     FK(f, cudaMemcpyAsync(f->d_par01.p, p01, sizeof p01, cudaMemcpyHostToDevice, st));
@@ -1119,27 +1131,34 @@ int build_sub_tables(gf_forest* f)
     return GF_OK;
 }
 
-/* same-level copies and physical sides of level l's leaves in buffer b at t */
+/* same-level copies and physical sides of level l's leaves in buffer b at
+ * t. Ghost block i of the step: the plan pass writes it, the launch pass
+ * points the fill at its device copy. */
+constexpr size_t kSubBlkOff = 256 * sizeof(double); /* staging: dts, then blocks */
+
 int sub_ghost(gf_forest* f, int l, int b, double t, const gf_ghost_ref* refs, int n)
 {
-    if (n <= 0) return GF_OK;
-    cudaStream_t st = gf::ctx_stream(f->ctx);
-    gf_ghost_block blk{};
-    blk.q = b < 2 ? f->qbuf[b] : f->qi;
-    blk.aux = f->aux;
-    blk.nbr = f->d_nbr.p;
-    blk.geom = f->d_geom.p;
-    blk.phys_of = nullptr;
-    blk.bc = f->bc;
-    blk.bc.q0hu = hydro_at(f, t);
-    blk.phys = f->o.phys_slot;
-    blk.maux = f->o.maux;
-    blk.skip = 0;
     (void)l;
-    FK(f, f->d_block.reserve(1));
-    /* pageable source, stream-ordered: staged before the call returns */
-    FK(f, cudaMemcpyAsync(f->d_block.p, &blk, sizeof blk, cudaMemcpyHostToDevice, st));
-    FK(f, gf::launch_ghost_fill(f->M, f->d_block.p, refs, n, gf::ctx_device_phys(f->ctx), st));
+    if (n <= 0) return GF_OK;
+    const int i = f->sub_nblk++;
+    if (f->sub_plan) {
+        gf_ghost_block blk{};
+        blk.q = b < 2 ? f->qbuf[b] : f->qi;
+        blk.aux = f->aux;
+        blk.nbr = f->d_nbr.p;
+        blk.geom = f->d_geom.p;
+        blk.phys_of = nullptr;
+        blk.bc = f->bc;
+        blk.bc.q0hu = hydro_at(f, t);
+        blk.phys = f->o.phys_slot;
+        blk.maux = f->o.maux;
+        blk.skip = 0;
+        if ((int)f->sub_blocks.size() <= i) f->sub_blocks.resize(i + 1);
+        f->sub_blocks[i] = blk;
+        return GF_OK;
+    }
+    const gf_ghost_block* d_blk = reinterpret_cast<const gf_ghost_block*>(f->d_sub_stage.p + kSubBlkOff) + i;
+    FK(f, gf::launch_ghost_fill(f->M, d_blk, refs, n, gf::ctx_device_phys(f->ctx), gf::ctx_stream(f->ctx)));
     return GF_OK;
 }
 
@@ -1151,13 +1170,15 @@ int sub_fill_level(gf_forest* f, int l, double t, const int* p, int cbuf)
     cudaStream_t st = gf::ctx_stream(f->ctx);
     const gf_phys* phys = gf::ctx_device_phys(f->ctx);
     int rc;
-    if (l < f->sub_hi && f->sx_avg_n[l])
+    const bool go = !f->sub_plan;
+    if (go && l < f->sub_hi && f->sx_avg_n[l])
         FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_avg_off[(size_t)l * 6 + p[l] * 2 + p[l + 1]],
                                   f->sx_avg_n[l], phys, st));
     if ((rc = sub_ghost(f, l, p[l], t, f->d_refs_all.p + f->lev_off[l], f->lev_n[l]))) return rc;
     if (cbuf >= 0 && f->itp_n[l]) {
-        FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_itp_off[(size_t)l * 6 + cbuf * 2 + p[l]], f->itp_n[l],
-                                  phys, st));
+        if (go)
+            FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_itp_off[(size_t)l * 6 + cbuf * 2 + p[l]],
+                                      f->itp_n[l], phys, st));
         if ((rc = sub_ghost(f, l, p[l], t, f->d_refs_lv.p + f->ref_off[l], f->ref_n[l]))) return rc;
     }
     return GF_OK;
@@ -1169,11 +1190,14 @@ int sub_update(gf_forest* f, int l, int* p)
     const gf_phys* phys = gf::ctx_device_phys(f->ctx);
     int* err = reinterpret_cast<int*>(f->d_rb.p);
     const gf_patch_work* w = f->d_work.p + f->lev_off[l];
-    if (gf::ctx_exact(f->ctx))
-        FK(f, gf::launch_patch_update_exact(f->M, w, f->lev_n[l], phys, 0.0, f->d_sub_dt.p + l, f->d_par01.p + p[l],
+    const double* dts = reinterpret_cast<const double*>(f->d_sub_stage.p);
+    if (f->sub_plan) {
+        /* the plan pass only tracks the parities */
+    } else if (gf::ctx_exact(f->ctx))
+        FK(f, gf::launch_patch_update_exact(f->M, w, f->lev_n[l], phys, 0.0, dts + l, f->d_par01.p + p[l],
                                             f->o.maux, nullptr, f->d_rb.p + 1, err, st));
     else
-        FK(f, gf::launch_patch_update(f->M, w, f->lev_n[l], phys, 0.0, f->d_sub_dt.p + l, f->d_par01.p + p[l],
+        FK(f, gf::launch_patch_update(f->M, w, f->lev_n[l], phys, 0.0, dts + l, f->d_par01.p + p[l],
                                       f->o.maux, nullptr, f->d_rb.p + 1, err, st));
     p[l] ^= 1;
     return GF_OK;
@@ -1192,10 +1216,13 @@ int sub_level(gf_forest* f, int l, double tl, double dtl, int* p)
         int cbuf = po;
         if (k == 1) {
             /* level l at the midpoint, with its ghost cells exchanged there */
-            FK(f, gf::launch_tinterp_strip(f->M, f->d_ss.p + f->ss_ti_off[(size_t)l * 2 + po], f->lev_n[l], 0.5, st));
-            if (f->sx_avg_n[l])
-                FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_avg_off[(size_t)l * 6 + 2 * 2 + p[l + 1]],
-                                          f->sx_avg_n[l], phys, st));
+            if (!f->sub_plan) {
+                FK(f, gf::launch_tinterp_strip(f->M, f->d_ss.p + f->ss_ti_off[(size_t)l * 2 + po], f->lev_n[l],
+                                               0.5, st));
+                if (f->sx_avg_n[l])
+                    FK(f, gf::launch_transfer(f->M, f->d_sx.p + f->sx_avg_off[(size_t)l * 6 + 2 * 2 + p[l + 1]],
+                                              f->sx_avg_n[l], phys, st));
+            }
             if ((rc = sub_ghost(f, l, 2, tf, f->d_refs_all.p + f->lev_off[l], f->lev_n[l]))) return rc;
             cbuf = 2;
         }
@@ -1205,27 +1232,86 @@ int sub_level(gf_forest* f, int l, double tl, double dtl, int* p)
     return GF_OK;
 }
 
-/* one subcycled coarse step; the result is pending until sub_finish */
+/* one subcycled coarse step; the result is pending until sub_finish.
+ * The step's launches (a few per level and sub-step) run as one CUDA graph:
+ * captured on the first step after the leaves change, replayed after a
+ * host-only plan pass has written this step's level dts and ghost blocks
+ * (whose boundary times move with t and dt) to the pinned staging the
+ * graph's first node copies. */
 int sub_step(gf_forest* f, double t, double dt, double* cfl, long long* updates)
 {
     int rc = build_sub_tables(f);
     if (rc) return rc;
     cudaStream_t st = gf::ctx_stream(f->ctx);
     const int nlev = f->o.maxlevel + 1;
-    std::vector<double> dts(nlev, 0.0);
     long long cu = 0;
-    double d = dt;
-    for (int l = f->sub_lo; l <= f->sub_hi; ++l, d *= 0.5) {
-        dts[l] = d;
-        cu += (long long)f->lev_n[l] * f->M * f->M << (l - f->sub_lo);
-    }
-    FK(f, cudaMemcpyAsync(f->d_sub_dt.p, dts.data(), nlev * sizeof(double), cudaMemcpyHostToDevice, st));
-    FK(f, f->d_rb.reserve(2));
-    FK(f, cudaMemsetAsync(f->d_rb.p, 0, 2 * sizeof(unsigned long long), st));
-    FK(f, gf::launch_slot_copy(f->M, f->d_ss.p + f->ss_copy_off[0][f->par], f->ss_copy_n[0], st));
+    for (int l = f->sub_lo; l <= f->sub_hi; ++l) cu += (long long)f->lev_n[l] * f->M * f->M << (l - f->sub_lo);
+    /* plan pass */
     std::vector<int> p(nlev + 1, f->par);
-    if ((rc = sub_fill_level(f, f->sub_lo, t, p.data(), -1))) return rc;
-    if ((rc = sub_level(f, f->sub_lo, t, dt, p.data()))) return rc;
+    f->sub_plan = true;
+    f->sub_nblk = 0;
+    rc = sub_fill_level(f, f->sub_lo, t, p.data(), -1);
+    if (!rc) rc = sub_level(f, f->sub_lo, t, dt, p.data());
+    f->sub_plan = false;
+    if (rc) return rc;
+    const int nblk = f->sub_nblk;
+    const size_t bytes = kSubBlkOff + (size_t)nblk * sizeof(gf_ghost_block);
+    if (bytes > f->h_sub_cap) {
+        if (f->h_sub) cudaFreeHost(f->h_sub);
+        f->h_sub = nullptr;
+        f->h_sub_cap = 0;
+        FK(f, cudaMallocHost(reinterpret_cast<void**>(&f->h_sub), bytes + bytes / 2));
+        f->h_sub_cap = bytes + bytes / 2;
+        f->sub_graph_ok = false;
+    }
+    double* hdt = reinterpret_cast<double*>(f->h_sub);
+    double d = dt;
+    for (int l = 0; l < nlev; ++l) hdt[l] = 0.0;
+    for (int l = f->sub_lo; l <= f->sub_hi; ++l, d *= 0.5) hdt[l] = d;
+    std::memcpy(f->h_sub + kSubBlkOff, f->sub_blocks.data(), (size_t)nblk * sizeof(gf_ghost_block));
+    const bool exact = gf::ctx_exact(f->ctx);
+    if (!f->sub_graph_ok || f->sub_graph_par != f->par || f->sub_graph_nblk != nblk || f->sub_graph_exact != exact) {
+        f->sub_graph_ok = false;
+        FK(f, f->d_sub_stage.reserve(bytes));
+        FK(f, f->d_rb.reserve(2));
+        FK(f, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int crc = GF_OK;
+        auto cap = [&](cudaError_t e) { if (e != cudaSuccess && crc == GF_OK) crc = gf::ctx_cuda_fail(f->ctx, e, "subcycled step capture"); };
+        cap(cudaMemcpyAsync(f->d_sub_stage.p, f->h_sub, bytes, cudaMemcpyHostToDevice, st));
+        cap(cudaMemsetAsync(f->d_rb.p, 0, 2 * sizeof(unsigned long long), st));
+        cap(gf::launch_slot_copy(f->M, f->d_ss.p + f->ss_copy_off[0][f->par], f->ss_copy_n[0], st));
+        std::vector<int> q(nlev + 1, f->par);
+        f->sub_nblk = 0;
+        if (crc == GF_OK) crc = sub_fill_level(f, f->sub_lo, t, q.data(), -1);
+        if (crc == GF_OK) crc = sub_level(f, f->sub_lo, t, dt, q.data());
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+        if (crc) {
+            if (graph) cudaGraphDestroy(graph);
+            return crc;
+        }
+        FK(f, ee);
+        /* same shape as the last capture (the usual regrid): update in place */
+        bool updated = false;
+        if (f->sub_exec) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(f->sub_exec, graph, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(f->sub_exec);
+                f->sub_exec = nullptr;
+            }
+        }
+        cudaError_t ei = cudaSuccess;
+        if (!updated) ei = cudaGraphInstantiate(&f->sub_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        FK(f, ei);
+        f->sub_graph_ok = true;
+        f->sub_graph_par = f->par;
+        f->sub_graph_nblk = nblk;
+        f->sub_graph_exact = exact;
+    }
+    FK(f, cudaGraphLaunch(f->sub_exec, st));
     FK(f, cudaMemcpyAsync(f->h_rb, f->d_rb.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     FK(f, cudaStreamSynchronize(st));
     if ((int)f->h_rb[0]) return ffail(f, GF_ERR_DEVICE, "a patch-update copy wait timed out");
@@ -1380,8 +1466,10 @@ void gf_forest_destroy(gf_forest* f)
     if (f->qsave) cudaFree(f->qsave);
     f->d_sx.release();
     f->d_ss.release();
-    f->d_sub_dt.release();
     f->d_par01.release();
+    if (f->sub_exec) cudaGraphExecDestroy(f->sub_exec);
+    f->d_sub_stage.release();
+    if (f->h_sub) cudaFreeHost(f->h_sub);
     if (f->h_rb) cudaFreeHost(f->h_rb);
     delete f;
 }
