@@ -577,6 +577,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_forest:
         result["forest"] = forest_leg(args, local)
         result["batched"] = batched_leg(args, local)
+        result["served_amr"] = fserved_leg(args, local)
     if rank == 0 and not args.no_large:
         result["large"] = large_leg(args, local)
     if rank == 0 and not args.no_dem:
@@ -845,6 +846,145 @@ def batched_leg(args, dev=0):
     }
 
 
+def fserved_leg(args, dev=0):
+    """Served AMR forests (config 3 as a request stream): forests as in the
+    batched leg (mx drawn from {8, 16, 32}, levels 2..5, target patches
+    log-uniform [50, 2000], reservoir + inflow hydrograph, regrid every 4
+    steps, a bounded simulated time) arrive as a Poisson stream at 80 % of
+    the capacity measured in a saturated calibration pass, into the forest
+    server running its request loop on its own thread. Reports throughput,
+    p50/p99 latency (submit to done), the slowdown of a sample against its
+    isolated latency, and that the sample's results equal the isolated runs
+    bit for bit; the sample also runs through Forest.run one by one."""
+    import geoflood_gb300 as gf
+    from geoflood_gb300 import synth
+    from geoflood_gb300.serve import ForestRequest, ForestServer, Hydrograph
+
+    n = args.fserved_forests
+    T = args.batch_time
+    g = np.random.default_rng(SEED + 5)
+    targets = np.exp(g.uniform(np.log(50), np.log(2000), n))
+    specs = [synth.flood_forest(SEED + 300 + k, float(targets[k])) for k in range(n)]
+
+    def req(sp):
+        h = sp["hydro"]
+        return ForestRequest(mx=sp["mx"], nbx=sp["nbx"], nby=sp["nby"], minlevel=sp["minlevel"],
+                             maxlevel=sp["maxlevel"], dx0=sp["dx0"], dy0=sp["dy0"], t_final=T,
+                             aux=sp["aux"], q=sp["q"], mthbc=sp["mthbc"],
+                             regrid_interval=sp["regrid_interval"], refine=sp["refine"],
+                             phys=sp["phys"], nout=1, initial_dt=1.6,
+                             hydro=Hydrograph(np.array(h[0]), np.array(h[1]), tuple(h[2]), h[3],
+                                              h[4], h[5]))
+
+    srv = ForestServer(device=dev)
+    srv.start()
+    # -- calibration: a saturated batch, throughput until half of it is done
+    ncal = min(16, n)
+    st_a = srv.stats()
+    t0 = srv.clock()
+    cal = [srv.submit(req(specs[k])) for k in range(ncal)]
+    samples = []
+    while True:
+        st = srv.stats()
+        samples.append((srv.clock(), st["cell_updates"] - st_a["cell_updates"], st["active"] + st["queued"]))
+        if st["active"] + st["queued"] == 0:
+            break
+        time.sleep(0.002)
+    half = next((t, w) for t, w, left in samples if left <= ncal // 2)
+    cap = half[1] / max(half[0] - t0, 1e-9)
+    cal_info = [srv.wait(i, timeout=600) for i in cal]
+    for i in cal:
+        srv.release(i)
+    est_work = float(np.mean([i["cell_updates"] for i in cal_info]))
+    rate = 0.8 * cap / est_work
+    gaps = np.random.default_rng(SEED + 6).exponential(1.0 / rate, n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    order = np.argsort(targets)
+    sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 6)})
+    reqs = [req(sp).prepare() for sp in specs]   # raster blocks built before the stream
+    st0 = srv.stats()
+    t_start = srv.clock()
+    ids, infos, outs, late = {}, {}, {}, 0
+    for k in range(n):
+        t_arr = t_start + arrivals[k]
+        while srv.clock() < t_arr:
+            time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
+        late += srv.clock() - t_arr > 0.01
+        ids[k] = srv.submit(reqs[k])
+        for j in list(ids):
+            if j not in infos:
+                i = srv.poll(ids[j])
+                if i["state"] in ("done", "failed", "cancelled"):
+                    infos[j] = i
+    for k in range(n):
+        if k not in infos:
+            infos[k] = srv.wait(ids[k], timeout=3600)
+    for k in range(n):
+        if k in sample and infos[k]["state"] == "done":
+            outs[k] = srv.download(ids[k])
+        srv.release(ids[k])
+    st1 = srv.stats()
+    t_end = max(i["t_done"] for i in infos.values())
+    failed = sum(1 for i in infos.values() if i["state"] != "done")
+    lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
+    work = sum(i["cell_updates"] for i in infos.values())
+    # -- isolated re-runs of the sample: latency alone, same bits
+    slow, same, detail = [], True, []
+    for k in sample:
+        sid = srv.submit(reqs[k])
+        ik = srv.wait(sid, timeout=600)
+        p, q, _ = srv.download(sid)
+        srv.release(sid)
+        t_iso = ik["t_done"] - ik["t_submit"]
+        t_mix = infos[k]["t_done"] - infos[k]["t_submit"]
+        slow.append(t_mix / t_iso)
+        same &= (k in outs and np.array_equal(p, outs[k][0]) and np.array_equal(q, outs[k][1])
+                 and ik["steps"] == infos[k]["steps"])
+        detail.append({"mx": specs[k]["mx"], "npatch_max": ik["npatch_max"], "steps": ik["steps"],
+                       "isolated_s": t_iso, "mixed_s": t_mix,
+                       "queued_s": infos[k]["t_admit"] - infos[k]["t_submit"]})
+    srv.stop()
+    srv.close()
+    # -- the sample through Forest.run, one after another
+    ctx = gf.Context(dev)
+    w1, s1 = 0, 0.0
+    for k in sample:
+        sp = specs[k]
+        ctx.set_phys(1, sp["phys"])
+        F = gf.Forest(ctx, sp["mx"], sp["nbx"], sp["nby"], sp["minlevel"], sp["maxlevel"], sp["dx0"],
+                      sp["dy0"], sp["aux"], sp["q"], mthbc=sp["mthbc"],
+                      regrid_interval=sp["regrid_interval"], refine=sp["refine"], phys_slot=1)
+        F.set_hydrograph(*sp["hydro"])
+        tp = time.perf_counter()
+        F.init()
+        w1 += F.run(T, 1, 1.6, 0.9, 1.0)["cell_updates"]
+        s1 += time.perf_counter() - tp
+        F.close()
+    ctx.close()
+    mxs = [sp["mx"] for sp in specs]
+    served_rate = work / (t_end - t_start)
+    return {
+        "workload": f"{n} forests, mx in {{8,16,32}} ({mxs.count(8)}/{mxs.count(16)}/{mxs.count(32)}), "
+                    f"levels 2-5, target patches log-uniform [50, 2000], {T:g} s simulated, regrid "
+                    "every 4 steps; Poisson arrivals at 80 % of the calibrated capacity",
+        "value": served_rate, "unit": METRIC, "forests": n, "failed": failed,
+        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+        "slowdown_vs_isolated": {"p50": float(np.percentile(slow, 50)), "p99": float(np.percentile(slow, 99)),
+                                 "max": float(max(slow)), "sample": len(sample), "detail": detail},
+        "alone_equals_mix": bool(same),
+        "one_by_one": {"value": w1 / s1, "unit": METRIC, "seconds": s1,
+                       "note": "the sample through Forest.run (init included), one after another"},
+        "vs_one_by_one": served_rate / (w1 / s1),
+        "capacity": {"value": cap, "unit": METRIC, "forests": ncal, "window_s": half[0] - t0},
+        "arrival_rate_per_s": rate, "late_submissions": int(late), "stream_seconds": t_end - t_start,
+        "cell_updates": work, "iterations": st1["iterations"] - st0["iterations"],
+        "epochs": st1["epochs"] - st0["epochs"], "rounds": st1["rounds"] - st0["rounds"],
+        "launches": st1["launches"] - st0["launches"], "regrids": st1["regrids"] - st0["regrids"],
+        "host_seconds": {k: st1[k] - st0[k] for k in ("s_admit", "s_epoch", "s_rounds", "s_regrid")},
+        "peak_device_bytes": st1["bytes_peak"],
+    }
+
+
 def large_leg(args, dev=0):
     """Large single scenario (config 5) as one forest: 2 x 2 brick, mx 32,
     levels 3..7 (2 m finest cells, 8192^2 equivalent), fractal DEM with a
@@ -931,6 +1071,8 @@ def main():
     ap.add_argument("--batch-forests", type=int, default=64)
     ap.add_argument("--batch-time", type=float, default=10.0)
     ap.add_argument("--batched-only", action="store_true")
+    ap.add_argument("--fserved-forests", type=int, default=32)
+    ap.add_argument("--fserved-only", action="store_true")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--large-only", action="store_true")
@@ -950,6 +1092,9 @@ def main():
         return 0
     if args.dem_only:
         print(json.dumps({"dem": dem_leg(args)}))
+        return 0
+    if args.fserved_only:
+        print(json.dumps({"served_amr": fserved_leg(args)}))
         return 0
     if args.batched_only:
         print(json.dumps({"batched": batched_leg(args)}))

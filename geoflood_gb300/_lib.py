@@ -123,6 +123,37 @@ class gf_forest_batch_stats(C.Structure):
                 ("s_rounds", C.c_double), ("s_regrid", C.c_double), ("s_epoch", C.c_double)]
 
 
+class gf_forest_request(C.Structure):
+    _fields_ = [("opts", gf_forest_opts), ("phys", gf_phys), ("fields", C.c_void_p),
+                ("topo", C.c_void_p), ("qinit", C.c_int), ("nhydro", C.c_int),
+                ("hydro_time", C.c_void_p), ("hydro_hu", C.c_void_p), ("hydro_side", C.c_int * 4),
+                ("hydro_width", C.c_double), ("hydro_x0", C.c_double), ("hydro_y0", C.c_double),
+                ("t_final", C.c_double), ("nout", C.c_int), ("initial_dt", C.c_double),
+                ("desired_cfl", C.c_double), ("max_cfl", C.c_double)]
+
+
+class gf_fserver_opts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("backfill", C.c_int)]
+
+
+class gf_forest_request_info(C.Structure):
+    _fields_ = [("state", C.c_int), ("steps", C.c_longlong), ("rejects", C.c_longlong),
+                ("regrids", C.c_longlong), ("cell_updates", C.c_longlong), ("t", C.c_double),
+                ("dt", C.c_double), ("max_cfl_seen", C.c_double), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("npatch", C.c_int),
+                ("npatch_max", C.c_int), ("footprint", C.c_size_t), ("device_bytes", C.c_size_t)]
+
+
+class gf_fserver_stats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("done", C.c_longlong),
+                ("failed", C.c_longlong), ("iterations", C.c_longlong), ("epochs", C.c_longlong),
+                ("rounds", C.c_longlong), ("launches", C.c_longlong), ("regrids", C.c_longlong),
+                ("cell_updates", C.c_longlong), ("s_admit", C.c_double), ("s_epoch", C.c_double),
+                ("s_rounds", C.c_double), ("s_regrid", C.c_double), ("bytes_in_use", C.c_size_t),
+                ("bytes_peak", C.c_size_t), ("active", C.c_int), ("queued", C.c_int),
+                ("held", C.c_int)]
+
+
 GF_MAX_TILES = 4
 
 
@@ -249,6 +280,25 @@ SIGNATURES = [
     ("gf_server_cancel", C.c_int, [_vp, C.c_longlong]),
     ("gf_server_stats_get", C.c_int, [_vp, C.POINTER(gf_server_stats)]),
     ("gf_server_clock", C.c_double, [_vp]),
+    ("gf_forest_footprint", C.c_size_t, [C.POINTER(gf_forest_opts)]),
+    ("gf_fserver_opts_default", None, [C.POINTER(gf_fserver_opts)]),
+    ("gf_fserver_create", C.c_int, [C.c_int, C.POINTER(gf_fserver_opts), C.POINTER(_vp)]),
+    ("gf_fserver_destroy", None, [_vp]),
+    ("gf_fserver_last_error", C.c_char_p, [_vp]),
+    ("gf_fserver_ctx", _vp, [_vp]),
+    ("gf_fserver_submit", C.c_int, [_vp, C.POINTER(gf_forest_request), C.POINTER(C.c_longlong)]),
+    ("gf_fserver_pump", C.c_int, [_vp, C.POINTER(C.c_int)]),
+    ("gf_fserver_start", C.c_int, [_vp]),
+    ("gf_fserver_stop", C.c_int, [_vp]),
+    ("gf_fserver_wait", C.c_int, [_vp, C.c_longlong, C.c_double]),
+    ("gf_fserver_poll", C.c_int, [_vp, C.c_longlong, C.POINTER(gf_forest_request_info)]),
+    ("gf_fserver_cancel", C.c_int, [_vp, C.c_longlong]),
+    ("gf_fserver_forest", C.c_int, [_vp, C.c_longlong, C.POINTER(_vp)]),
+    ("gf_fserver_download", C.c_int, [_vp, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int), _dp, _dp]),
+    ("gf_fserver_release", C.c_int, [_vp, C.c_longlong]),
+    ("gf_fserver_stats_get", C.c_int, [_vp, C.POINTER(gf_fserver_stats)]),
+    ("gf_fserver_clock", C.c_double, [_vp]),
 ]
 
 _lib = None

@@ -1534,6 +1534,32 @@ int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, g
     return GF_OK;
 }
 
+size_t gf_forest_footprint(const gf_forest_opts* o)
+{
+    if (!o || !(o->mx == 8 || o->mx == 16 || o->mx == 32) || o->maux < 1 || o->maux > 3 || o->nbx < 1 ||
+        o->nby < 1 || o->minlevel < 0 || o->maxlevel < o->minlevel || o->maxlevel > 10)
+        return 0;
+    const long long full = (long long)o->nbx * o->nby << (2 * o->maxlevel);
+    const long long peak = full + (full + 3) / 4;
+    const long long cap = o->max_patches > 0 ? std::min<long long>(o->max_patches, peak) : peak;
+    if (cap > (1LL << 22)) return 0;
+    const size_t S = (size_t)(o->mx + 2 * GF_MBC) * (o->mx + 2 * GF_MBC);
+    const int nf = o->maux + 3;
+    size_t n = 0;
+    for (int l = o->minlevel; l <= o->maxlevel; ++l)
+        n += (size_t)nf * ((size_t)(o->nbx * o->mx << l) + 2 * GF_MBC) * ((size_t)(o->nby * o->mx << l) + 2 * GF_MBC) *
+             sizeof(double);
+    n += (size_t)(o->nbx * o->mx << o->maxlevel) * (size_t)(o->nby * o->mx << o->maxlevel) * sizeof(double);
+    n += (size_t)cap * (6 + o->maux) * S * sizeof(double);
+    /* leaf tables (grown by half again when they grow): neighbours, geometry,
+     * work item, ghost references, coarse/fine transfers of both parities,
+     * tagging and regrid transfers */
+    const size_t per_slot = 8 * sizeof(int) + sizeof(gf_patch_geom) + sizeof(gf_patch_work) + 2 * sizeof(gf_ghost_ref) +
+                            20 * sizeof(gf_xfer_task) + sizeof(gf_tag_task) + sizeof(int) + sizeof(gf_fill_task);
+    n += (size_t)cap * per_slot * 3 / 2;
+    return n + ((size_t)1 << 20);
+}
+
 int gf_forest_set_hydrograph(gf_forest* f, int n, const double* time, const double* hu,
                              const int* side, double width, double x0, double y0)
 {
@@ -2119,25 +2145,23 @@ int build_epoch(Batch& B)
 
 } // namespace
 
-extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout,
-                                   double initial_dt, double desired_cfl, double max_cfl,
-                                   gf_forest_batch_stats* bst)
-{
-    if (!forests || n < 1 || !(t_final > 0) || nout < 1 || !(initial_dt > 0) || !(desired_cfl > 0) ||
-        !(max_cfl > 0))
-        return GF_ERR_ARG;
-    gf_ctx* ctx = forests[0]->ctx;
-    for (int k = 0; k < n; ++k) {
-        if (!forests[k] || forests[k]->ctx != ctx) return GF_ERR_ARG;
-        if (forests[k]->leaves.empty()) return ffail(forests[k], GF_ERR_STATE, "forest not initialised");
-        if (forests[k]->o.maxlevel >= kBatchLevels) return ffail(forests[k], GF_ERR_ARG, "maxlevel too deep");
-        if (forests[k]->o.subcycle)
-            return ffail(forests[k], GF_ERR_UNSUPPORTED, "batched runs take every level's step together (subcycle = 0)");
-        for (int j = 0; j < k; ++j)
-            if (forests[j] == forests[k]) return ffail(forests[k], GF_ERR_ARG, "a forest appears twice");
-    }
-    if (cudaSetDevice(gf::ctx_device(ctx)) != cudaSuccess) return GF_ERR_CUDA;
+namespace {
+
+/* A batched run in progress: the members' rounds, their regrids and the
+ * epoch rebuilds, one iteration at a time (gf_forest_batch_run drives it to
+ * the end; the forest server adds and retires members between iterations). */
+struct BatchRun {
     Batch B;
+    gf_forest_batch_stats S{};
+    double round_ms = 0.05;
+    int rounds_paused = 0;
+    bool rebuild = true;
+};
+
+int batch_begin(BatchRun& R, gf_ctx* ctx)
+{
+    Batch& B = R.B;
+    if (cudaSetDevice(gf::ctx_device(ctx)) != cudaSuccess) return GF_ERR_CUDA;
     B.ctx = ctx;
     B.st = gf::ctx_stream(ctx);
     BK(B, cudaEventCreate(&B.ev0));
@@ -2149,125 +2173,232 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
         gf::launch_patch_update_exact(kCls[c], nullptr, 0, nullptr, 0.0, nullptr, nullptr, 0, nullptr,
                                       nullptr, nullptr, B.st);
     }
-    gf_forest_batch_stats S{};
-    /* controllers at the start (fc2d_geoclaw_run.c:197-225) */
-    for (int k = 0; k < n; ++k) {
-        gf_forest* f = forests[k];
-        gf_group_state& g = f->gst;
-        std::memset(&g, 0, sizeof g);
-        g.qb[0] = f->qbuf[0];
-        g.qb[1] = f->qbuf[1];
-        g.dt_outer = t_final / nout;
-        g.t_curr = f->st.t;
-        g.tend = g.t_curr + g.dt_outer;
-        g.dt_minlevel = initial_dt;
-        g.desired_cfl = desired_cfl;
-        g.max_cfl = max_cfl;
-        g.max_cfl_seen = f->st.max_cfl_seen;
-        g.level_factor = (double)(1 << (f->o.maxlevel - f->o.minlevel));
-        g.steps = f->st.steps;
-        g.rejects = f->st.rejects;
-        g.nout = nout;
-        g.active = 1;
-        g.cur = f->par;
-        g.regrid_interval = f->o.regrid_interval;
-        g.since_regrid = f->o.regrid_interval > 0 ? (int)(f->st.steps % f->o.regrid_interval) : 0;
-        B.fs.push_back(f);
-    }
-    double round_ms = 0.05;
-    int rounds_paused = 0;
-    bool rebuild = true;
-    while (true) {
-        /* drop finished forests; stop when none is left */
-        std::vector<gf_forest*> live;
-        for (gf_forest* f : B.fs)
-            if (f->gst.active) live.push_back(f);
-        if (live.empty()) break;
-        if (live.size() != B.fs.size()) {
-            B.fs.swap(live);
-            rebuild = true;
-        }
-        using clk = std::chrono::steady_clock;
-        auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
-        if (rebuild) {
-            const auto te = clk::now();
-            int rc = build_epoch(B);
-            S.s_epoch += secs(te);
-            if (rc) return rc;
-            S.epochs++;
-            rebuild = false;
-            rounds_paused = 0;
-        }
-        const int ng = (int)B.fs.size();
-        int rounds = (int)std::ceil(0.5 / std::max(round_ms, 1e-3));
-        rounds = std::max(1, std::min(64, rounds));
-        const auto tr = clk::now();
-        BK(B, cudaEventRecord(B.ev0, B.st));
-        for (int r = 0; r < rounds; ++r) BK(B, cudaGraphLaunch(B.exec, B.st));
-        BK(B, cudaMemcpyAsync(B.h_rb, B.d + B.off_rb, 8, cudaMemcpyDeviceToHost, B.st));
-        BK(B, cudaMemcpyAsync(B.h_rb + 8, B.d + B.off_gs, ng * sizeof(gf_group_state),
-                              cudaMemcpyDeviceToHost, B.st));
-        BK(B, cudaEventRecord(B.ev1, B.st));
-        BK(B, cudaStreamSynchronize(B.st));
-        S.s_rounds += secs(tr);
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) round_ms = std::max(1e-3, (double)ms / rounds);
-        S.rounds += rounds;
-        S.launches += (long long)rounds * B.launches_per_round;
-        int err;
-        std::memcpy(&err, B.h_rb, sizeof err);
-        if (err) return ffail(B.fs[0], GF_ERR_DEVICE, "a patch-update copy wait timed out");
-        const gf_group_state* gs = reinterpret_cast<const gf_group_state*>(B.h_rb + 8);
-        int npaused = 0, nactive = 0;
-        for (int g = 0; g < ng; ++g) {
-            gf_forest* f = B.fs[g];
-            const long long before = f->gst.steps;
-            const int hoff = f->gst.hydro_off;
-            f->gst = gs[g];
-            f->gst.hydro_off = hoff;
-            f->par = f->gst.cur;
-            f->st.cell_updates += (f->gst.steps - before) * f->cells;
-            S.cell_updates += (f->gst.steps - before) * f->cells;
-            f->st.steps = f->gst.steps;
-            f->st.rejects = f->gst.rejects;
-            f->st.t = f->gst.t_curr;
-            f->st.dt = f->gst.dt_minlevel;
-            f->st.max_cfl_seen = f->gst.max_cfl_seen;
-            if (f->gst.active) {
-                ++nactive;
-                npaused += f->gst.paused != 0;
-            }
-        }
-        if (npaused) rounds_paused += rounds;
-        /* regrid the waiting forests together once all live ones wait, or
-         * after a while (the others keep stepping meanwhile) */
-        if (npaused && (npaused == nactive || rounds_paused >= 16)) {
-            std::vector<gf_forest*> due;
-            std::vector<double> ts;
-            for (gf_forest* f : B.fs)
-                if (f->gst.active && f->gst.paused) {
-                    due.push_back(f);
-                    ts.push_back(f->gst.t_curr);
-                }
-            const auto tg = clk::now();
-            int rc = regrid_many(ctx, due, ts);
-            S.s_regrid += secs(tg);
-            if (rc) return rc;
-            for (gf_forest* f : due) {
-                f->gst.paused = 0;
-                f->gst.since_regrid = 0;
-                S.regrids++;
-            }
-            rebuild = true;
-        } else if (nactive < ng) {
-            rebuild = true; /* finished forests leave the epoch */
-        }
-    }
-    for (int k = 0; k < n; ++k) {
-        gf_forest* f = forests[k];
-        f->st.npatch = (int)f->leaves.size();
-        f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
-    }
-    if (bst) *bst = S;
     return GF_OK;
+}
+
+/* controller at the start of a member's run (fc2d_geoclaw_run.c:197-225) */
+void batch_add(BatchRun& R, gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
+               double max_cfl)
+{
+    gf_group_state& g = f->gst;
+    std::memset(&g, 0, sizeof g);
+    g.qb[0] = f->qbuf[0];
+    g.qb[1] = f->qbuf[1];
+    g.dt_outer = t_final / nout;
+    g.t_curr = f->st.t;
+    g.tend = g.t_curr + g.dt_outer;
+    g.dt_minlevel = initial_dt;
+    g.desired_cfl = desired_cfl;
+    g.max_cfl = max_cfl;
+    g.max_cfl_seen = f->st.max_cfl_seen;
+    g.level_factor = (double)(1 << (f->o.maxlevel - f->o.minlevel));
+    g.steps = f->st.steps;
+    g.rejects = f->st.rejects;
+    g.nout = nout;
+    g.active = 1;
+    g.cur = f->par;
+    g.regrid_interval = f->o.regrid_interval;
+    g.since_regrid = f->o.regrid_interval > 0 ? (int)(f->st.steps % f->o.regrid_interval) : 0;
+    R.B.fs.push_back(f);
+    R.rebuild = true;
+}
+
+/* one iteration: drop finished members, rebuild the epoch if needed, run
+ * ~0.5 ms of rounds, read the controllers back, regrid the waiting
+ * members. *live = members still running (0: nothing was run). */
+int batch_iterate(BatchRun& R, int* live_out)
+{
+    Batch& B = R.B;
+    gf_forest_batch_stats& S = R.S;
+    std::vector<gf_forest*> live;
+    for (gf_forest* f : B.fs)
+        if (f->gst.active) live.push_back(f);
+    if (live.size() != B.fs.size()) {
+        B.fs.swap(live);
+        R.rebuild = true;
+    }
+    *live_out = (int)B.fs.size();
+    if (B.fs.empty()) return GF_OK;
+    using clk = std::chrono::steady_clock;
+    auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    if (R.rebuild) {
+        const auto te = clk::now();
+        int rc = build_epoch(B);
+        S.s_epoch += secs(te);
+        if (rc) return rc;
+        S.epochs++;
+        R.rebuild = false;
+        R.rounds_paused = 0;
+    }
+    const int ng = (int)B.fs.size();
+    int rounds = (int)std::ceil(0.5 / std::max(R.round_ms, 1e-3));
+    rounds = std::max(1, std::min(64, rounds));
+    const auto tr = clk::now();
+    BK(B, cudaEventRecord(B.ev0, B.st));
+    for (int r = 0; r < rounds; ++r) BK(B, cudaGraphLaunch(B.exec, B.st));
+    BK(B, cudaMemcpyAsync(B.h_rb, B.d + B.off_rb, 8, cudaMemcpyDeviceToHost, B.st));
+    BK(B, cudaMemcpyAsync(B.h_rb + 8, B.d + B.off_gs, ng * sizeof(gf_group_state), cudaMemcpyDeviceToHost,
+                          B.st));
+    BK(B, cudaEventRecord(B.ev1, B.st));
+    BK(B, cudaStreamSynchronize(B.st));
+    S.s_rounds += secs(tr);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) R.round_ms = std::max(1e-3, (double)ms / rounds);
+    S.rounds += rounds;
+    S.launches += (long long)rounds * B.launches_per_round;
+    int err;
+    std::memcpy(&err, B.h_rb, sizeof err);
+    if (err) return ffail(B.fs[0], GF_ERR_DEVICE, "a patch-update copy wait timed out");
+    const gf_group_state* gs = reinterpret_cast<const gf_group_state*>(B.h_rb + 8);
+    int npaused = 0, nactive = 0;
+    for (int g = 0; g < ng; ++g) {
+        gf_forest* f = B.fs[g];
+        const long long before = f->gst.steps;
+        const int hoff = f->gst.hydro_off;
+        f->gst = gs[g];
+        f->gst.hydro_off = hoff;
+        f->par = f->gst.cur;
+        f->st.cell_updates += (f->gst.steps - before) * f->cells;
+        S.cell_updates += (f->gst.steps - before) * f->cells;
+        f->st.steps = f->gst.steps;
+        f->st.rejects = f->gst.rejects;
+        f->st.t = f->gst.t_curr;
+        f->st.dt = f->gst.dt_minlevel;
+        f->st.max_cfl_seen = f->gst.max_cfl_seen;
+        if (f->gst.active) {
+            ++nactive;
+            npaused += f->gst.paused != 0;
+        } else {
+            f->st.npatch = (int)f->leaves.size();
+            f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+        }
+    }
+    if (npaused) R.rounds_paused += rounds;
+    /* regrid the waiting members together once all live ones wait, or
+     * after a while (the others keep stepping meanwhile) */
+    if (npaused && (npaused == nactive || R.rounds_paused >= 16)) {
+        std::vector<gf_forest*> due;
+        std::vector<double> ts;
+        for (gf_forest* f : B.fs)
+            if (f->gst.active && f->gst.paused) {
+                due.push_back(f);
+                ts.push_back(f->gst.t_curr);
+            }
+        const auto tg = clk::now();
+        int rc = regrid_many(B.ctx, due, ts);
+        S.s_regrid += secs(tg);
+        if (rc) return rc;
+        for (gf_forest* f : due) {
+            f->gst.paused = 0;
+            f->gst.since_regrid = 0;
+            f->st.npatch_max = std::max(f->st.npatch_max, (int)f->leaves.size());
+            S.regrids++;
+        }
+        R.rebuild = true;
+    } else if (nactive < ng) {
+        R.rebuild = true; /* finished members leave the epoch */
+    }
+    return GF_OK;
+}
+
+int batch_check(gf_forest* f, gf_ctx* ctx)
+{
+    if (!f || f->ctx != ctx) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    if (f->o.maxlevel >= kBatchLevels) return ffail(f, GF_ERR_ARG, "maxlevel too deep");
+    if (f->o.subcycle)
+        return ffail(f, GF_ERR_UNSUPPORTED, "batched runs take every level's step together (subcycle = 0)");
+    return GF_OK;
+}
+
+} // namespace
+
+extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout,
+                                   double initial_dt, double desired_cfl, double max_cfl,
+                                   gf_forest_batch_stats* bst)
+{
+    if (!forests || n < 1 || !(t_final > 0) || nout < 1 || !(initial_dt > 0) || !(desired_cfl > 0) ||
+        !(max_cfl > 0))
+        return GF_ERR_ARG;
+    gf_ctx* ctx = forests[0] ? forests[0]->ctx : nullptr;
+    for (int k = 0; k < n; ++k) {
+        int rc = batch_check(forests[k], ctx);
+        if (rc) return rc;
+        for (int j = 0; j < k; ++j)
+            if (forests[j] == forests[k]) return ffail(forests[k], GF_ERR_ARG, "a forest appears twice");
+    }
+    BatchRun R;
+    int rc = batch_begin(R, ctx);
+    if (rc) return rc;
+    for (int k = 0; k < n; ++k) batch_add(R, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl);
+    int live = 1;
+    while (live) {
+        if ((rc = batch_iterate(R, &live))) return rc;
+    }
+    if (bst) *bst = R.S;
+    return GF_OK;
+}
+
+struct gf::ForestBatch {
+    BatchRun R;
+};
+
+int gf::forest_batch_create(gf_ctx* c, ForestBatch** out)
+{
+    if (!c || !out) return GF_ERR_ARG;
+    ForestBatch* b = new ForestBatch;
+    int rc = batch_begin(b->R, c);
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GF_OK;
+}
+
+void gf::forest_batch_destroy(ForestBatch* b) { delete b; }
+
+int gf::forest_batch_add(ForestBatch* b, gf_forest* f, double t_final, int nout, double initial_dt,
+                         double desired_cfl, double max_cfl)
+{
+    if (!b || !(t_final > 0) || nout < 1 || !(initial_dt > 0) || !(desired_cfl > 0) || !(max_cfl > 0))
+        return GF_ERR_ARG;
+    int rc = batch_check(f, b->R.B.ctx);
+    if (rc) return rc;
+    for (gf_forest* g : b->R.B.fs)
+        if (g == f) return ffail(f, GF_ERR_ARG, "the forest is already a member");
+    batch_add(b->R, f, t_final, nout, initial_dt, desired_cfl, max_cfl);
+    return GF_OK;
+}
+
+int gf::forest_batch_iterate(ForestBatch* b, int* live) { return batch_iterate(b->R, live); }
+
+void gf::forest_batch_remove(ForestBatch* b, gf_forest* f)
+{
+    std::vector<gf_forest*>& fs = b->R.B.fs;
+    auto it = std::find(fs.begin(), fs.end(), f);
+    if (it == fs.end()) return;
+    fs.erase(it);
+    f->gst.active = 0;
+    b->R.rebuild = true;
+}
+
+bool gf::forest_batch_running(const gf_forest* f) { return f->gst.active != 0; }
+
+void gf::forest_batch_get_stats(const ForestBatch* b, gf_forest_batch_stats* st) { *st = b->R.S; }
+
+size_t gf::forest_device_bytes(const gf_forest* f)
+{
+    size_t n = 0;
+    for (int l = f->o.minlevel; l <= f->o.maxlevel; ++l)
+        n += (size_t)f->nf * (nx_at(f, l) + 2 * GF_MBC) * (ny_at(f, l) + 2 * GF_MBC) * sizeof(double);
+    n += (size_t)f->cap * (6 + f->o.maux) * f->S * sizeof(double);
+    n += f->d_nbr.n * sizeof(int) + f->d_geom.n * sizeof(gf_patch_geom) + f->d_work.n * sizeof(gf_patch_work) +
+         (f->d_refs_all.n + f->d_refs_lv.n) * sizeof(gf_ghost_ref) + f->d_block.n * sizeof(gf_ghost_block) +
+         f->d_gdt.n * sizeof(double) + f->d_gpar.n * sizeof(int) + f->d_rb.n * 8 +
+         f->d_tagt.n * sizeof(gf_tag_task) + f->d_tags.n * sizeof(int) + f->d_refine.n * sizeof(gf_refine) +
+         f->d_rgx.n * sizeof(gf_xfer_task) + f->d_fill.n * sizeof(gf_fill_task) +
+         f->d_gtask.n * sizeof(gf_gauge_task) + (f->d_glast.n + f->d_grec.n) * sizeof(double);
+    for (int b = 0; b < 2; ++b) n += (f->d_avg[b].n + f->d_itp[b].n) * sizeof(gf_xfer_task);
+    return n;
 }

@@ -100,6 +100,23 @@ cudaError_t launch_gauge_sample(const gf_gauge_task* tasks, int n, const double*
                                 const double* auxbase, int m, int maux, double drytol2, double t,
                                 double* last, double* rec, cudaStream_t st);
 
+/* A batched forest run driven one iteration at a time (gf_forest.cpp):
+ * members join between iterations and leave when their run ends (or when
+ * dropped); each iteration runs about half a millisecond of rounds, then
+ * regrids the members that wait for it. */
+struct ForestBatch;
+int forest_batch_create(gf_ctx* c, ForestBatch** out);
+void forest_batch_destroy(ForestBatch* b);
+/* checks the forest and starts its outstyle-1 run at its current time */
+int forest_batch_add(ForestBatch* b, gf_forest* f, double t_final, int nout, double initial_dt,
+                     double desired_cfl, double max_cfl);
+int forest_batch_iterate(ForestBatch* b, int* live);
+/* the forest leaves now (its run ended, or it is cancelled) */
+void forest_batch_remove(ForestBatch* b, gf_forest* f);
+bool forest_batch_running(const gf_forest* f);
+void forest_batch_get_stats(const ForestBatch* b, gf_forest_batch_stats* st);
+size_t forest_device_bytes(const gf_forest* f);
+
 } // namespace gf
 
 #endif

@@ -22,6 +22,47 @@ def _stats_dict(s: _lib.gf_forest_stats) -> dict:
     return {k: getattr(s, k) for k, _ in _lib.gf_forest_stats._fields_}
 
 
+def forest_planes(aux, q, nx: int, ny: int, maux: int = 1):
+    """(planes, maux): the (maux + 3, ny, nx) raster block gf_forest_create
+    takes (aux fields, then h, hu, hv), or None for zero rasters."""
+    if aux is None and q is None:
+        return None, maux
+    aux = np.asarray(aux, np.float64)
+    if aux.ndim == 2:
+        aux = aux[None]
+    maux = aux.shape[0]
+    if aux.shape[1:] != (ny, nx) or q.shape != (ny, nx, 3):
+        raise ValueError(f"rasters must be ({ny}, {nx}) at the finest level")
+    planes = np.empty((maux + 3, ny, nx))
+    planes[:maux] = aux
+    planes[maux:] = np.moveaxis(np.asarray(q, np.float64), 2, 0)
+    return planes, maux
+
+
+def forest_opts(mx: int, nbx: int, nby: int, minlevel: int, maxlevel: int, dx0: float,
+                dy0: float, maux: int = 1, x0: float = 0.0, y0: float = 0.0, phys_slot: int = 0,
+                mthbc=(1, 1, 1, 1), regrid_interval: int = 0, max_patches: int = 0,
+                refine: Refine | None = None, subcycle: bool = False) -> _lib.gf_forest_opts:
+    o = _lib.gf_forest_opts()
+    _lib.load().gf_forest_opts_default(C.byref(o))
+    o.mx, o.maux, o.nbx, o.nby = mx, maux, nbx, nby
+    o.minlevel, o.maxlevel = minlevel, maxlevel
+    o.x0, o.y0, o.dx0, o.dy0 = x0, y0, dx0, dy0
+    o.phys_slot = phys_slot
+    for k in range(4):
+        o.mthbc[k] = int(mthbc[k])
+    o.regrid_interval = regrid_interval
+    o.max_patches = max_patches
+    o.refine = (refine or Refine()).to_c()
+    o.subcycle = int(bool(subcycle))
+    return o
+
+
+def footprint(o: _lib.gf_forest_opts) -> int:
+    """Device bytes a forest with these options may hold at most (0: invalid)."""
+    return int(_lib.load().gf_forest_footprint(C.byref(o)))
+
+
 class Forest:
     """aux: (ny, nx) bathymetry or (maux, ny, nx); q: (ny, nx, 3) with h, hu,
     hv; both at the finest level: nx = nbx*mx*2^maxlevel, ny = nby*mx*2^maxlevel.
@@ -36,30 +77,9 @@ class Forest:
         self.ctx = ctx
         self._lib = _lib.load()
         nx, ny = nbx * mx << maxlevel, nby * mx << maxlevel
-        if aux is None and q is None:
-            planes = None
-        else:
-            aux = np.asarray(aux, np.float64)
-            if aux.ndim == 2:
-                aux = aux[None]
-            maux = aux.shape[0]
-            if aux.shape[1:] != (ny, nx) or q.shape != (ny, nx, 3):
-                raise ValueError(f"rasters must be ({ny}, {nx}) at the finest level")
-            planes = np.empty((maux + 3, ny, nx))
-            planes[:maux] = aux
-            planes[maux:] = np.moveaxis(np.asarray(q, np.float64), 2, 0)
-        o = _lib.gf_forest_opts()
-        self._lib.gf_forest_opts_default(C.byref(o))
-        o.mx, o.maux, o.nbx, o.nby = mx, maux, nbx, nby
-        o.minlevel, o.maxlevel = minlevel, maxlevel
-        o.x0, o.y0, o.dx0, o.dy0 = x0, y0, dx0, dy0
-        o.phys_slot = phys_slot
-        for k in range(4):
-            o.mthbc[k] = int(mthbc[k])
-        o.regrid_interval = regrid_interval
-        o.max_patches = max_patches
-        o.refine = (refine or Refine()).to_c()
-        o.subcycle = int(bool(subcycle))
+        planes, maux = forest_planes(aux, q, nx, ny, maux)
+        o = forest_opts(mx, nbx, nby, minlevel, maxlevel, dx0, dy0, maux, x0, y0, phys_slot, mthbc,
+                        regrid_interval, max_patches, refine, subcycle)
         self.mx, self.maux = mx, maux
         self.minlevel, self.maxlevel = minlevel, maxlevel
         h = C.c_void_p()

@@ -212,3 +212,206 @@ class Server:
 
     def clock(self) -> float:
         return float(self._lib.gf_server_clock(self.h))
+
+
+# ------------------------------------------------------------ AMR forests
+
+@dataclass
+class ForestRequest:
+    """An adaptive scenario for the forest server: the options of a Forest
+    (rasters at the finest level, or zero rasters plus a Topo set) and its
+    outstyle-1 run. aux: (ny, nx) or (maux, ny, nx); q: (ny, nx, 3)."""
+    mx: int
+    nbx: int
+    nby: int
+    minlevel: int
+    maxlevel: int
+    dx0: float
+    dy0: float
+    t_final: float
+    aux: np.ndarray | None = None
+    q: np.ndarray | None = None
+    topo: object | None = None
+    qinit: bool = True
+    maux: int = 1
+    x0: float = 0.0
+    y0: float = 0.0
+    mthbc: tuple = (1, 1, 1, 1)
+    regrid_interval: int = 0
+    max_patches: int = 0
+    refine: object | None = None
+    phys: Phys = field(default_factory=Phys)
+    hydro: Hydrograph | None = None
+    nout: int = 1
+    initial_dt: float = 1.0
+    desired_cfl: float = 0.9
+    max_cfl: float = 1.0
+
+    def opts(self, maux: int | None = None):
+        from .forest import forest_opts
+        return forest_opts(self.mx, self.nbx, self.nby, self.minlevel, self.maxlevel, self.dx0,
+                           self.dy0, self.maux if maux is None else maux, self.x0, self.y0, 0,
+                           self.mthbc, self.regrid_interval, self.max_patches, self.refine)
+
+    def prepare(self) -> "ForestRequest":
+        """Build the C request (and its raster block) now, so that a later
+        submit only queues it; change no field after this."""
+        self._prepared = None
+        self._prepared = self.to_c()
+        return self
+
+    def to_c(self) -> tuple[_lib.gf_forest_request, tuple]:
+        if getattr(self, "_prepared", None) is not None:
+            return self._prepared
+        from .forest import forest_planes
+        nx, ny = self.nbx * self.mx << self.maxlevel, self.nby * self.mx << self.maxlevel
+        planes, maux = forest_planes(self.aux, self.q, nx, ny, self.maux)
+        r = _lib.gf_forest_request()
+        r.opts = self.opts(maux)
+        r.phys = self.phys.to_c()
+        r.fields = planes.ctypes.data if planes is not None else None
+        r.topo = self.topo.h if self.topo is not None else None
+        r.qinit = int(bool(self.qinit))
+        keep = (planes, self.topo)
+        if self.hydro is not None:
+            tm = np.ascontiguousarray(self.hydro.time, np.float64)
+            hu = np.ascontiguousarray(self.hydro.hu, np.float64)
+            r.nhydro = len(tm)
+            r.hydro_time = tm.ctypes.data
+            r.hydro_hu = hu.ctypes.data
+            for k in range(4):
+                r.hydro_side[k] = int(self.hydro.side[k])
+            r.hydro_width, r.hydro_x0, r.hydro_y0 = self.hydro.width, self.hydro.x0, self.hydro.y0
+            keep = keep + (tm, hu)
+        r.t_final, r.nout = self.t_final, self.nout
+        r.initial_dt, r.desired_cfl, r.max_cfl = self.initial_dt, self.desired_cfl, self.max_cfl
+        return r, keep
+
+
+class ForestServer:
+    """Request loop over adaptive scenarios on one GPU (gf_fserver): every
+    admitted forest steps in the batched forest engine's shared rounds; a
+    finished forest stays on the device until release()."""
+
+    def __init__(self, device: int = 0, hbm_budget: int | None = None, max_active: int = 256,
+                 backfill: bool = True, exact: bool | None = None):
+        self._lib = _lib.load()
+        o = _lib.gf_fserver_opts()
+        self._lib.gf_fserver_opts_default(C.byref(o))
+        if hbm_budget is not None:
+            o.hbm_budget = int(hbm_budget)
+        o.max_active = int(max_active)
+        o.backfill = int(bool(backfill))
+        h = C.c_void_p()
+        rc = self._lib.gf_fserver_create(int(device), C.byref(o), C.byref(h))
+        if rc != 0:
+            raise GeoFloodError(rc, f"gf_fserver_create failed ({STATUS_NAMES.get(rc, rc)})")
+        self.h = h
+        self.ctx_h = C.c_void_p(self._lib.gf_fserver_ctx(h))
+        if exact is not None:
+            self._check(self._lib.gf_ctx_set_fp_contract(self.ctx_h, int(not exact)))
+        self._keep: dict[int, tuple] = {}
+        self._req: dict[int, ForestRequest] = {}
+
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self._lib.gf_fserver_last_error(self.h)
+            raise GeoFloodError(rc, f"{STATUS_NAMES.get(rc, rc)}: "
+                                    f"{msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.gf_fserver_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def footprint(req: ForestRequest) -> int:
+        from .forest import footprint
+        r, _ = req.to_c()
+        return footprint(r.opts)
+
+    def submit(self, req: ForestRequest) -> int:
+        r, keep = req.to_c()
+        sid = C.c_longlong()
+        self._check(self._lib.gf_fserver_submit(self.h, C.byref(r), C.byref(sid)))
+        self._keep[sid.value] = keep
+        self._req[sid.value] = req
+        return sid.value
+
+    def pump(self) -> bool:
+        busy = C.c_int()
+        self._check(self._lib.gf_fserver_pump(self.h, C.byref(busy)))
+        return bool(busy.value)
+
+    def run_until_idle(self, timeout: float = 600.0):
+        t_end = self.clock() + timeout
+        while self.pump():
+            if self.clock() > t_end:
+                raise GeoFloodError(-5, "forest server did not go idle")
+
+    def start(self):
+        self._check(self._lib.gf_fserver_start(self.h))
+
+    def stop(self):
+        self._check(self._lib.gf_fserver_stop(self.h))
+
+    def wait(self, sid: int, timeout: float = 600.0) -> dict:
+        self._check(self._lib.gf_fserver_wait(self.h, int(sid), float(timeout)))
+        return self.poll(sid)
+
+    def poll(self, sid: int) -> dict:
+        i = _lib.gf_forest_request_info()
+        self._check(self._lib.gf_fserver_poll(self.h, int(sid), C.byref(i)))
+        d = {k: getattr(i, k) for k, _ in _lib.gf_forest_request_info._fields_}
+        d["state"] = _lib.SCEN_STATE_NAMES.get(i.state, str(i.state))
+        if d["state"] != "queued":
+            self._keep.pop(sid, None)   # the server no longer reads the rasters
+        return d
+
+    def download(self, sid: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(patches (n, 3) of level, I, J; q; aux) of a done request, in the
+        canonical leaf order."""
+        n = C.c_int()
+        self._check(self._lib.gf_fserver_download(self.h, int(sid), C.byref(n), None, None, None,
+                                                  None, None))
+        req = self._req[sid]
+        maux = req.aux.shape[0] if req.aux is not None and np.ndim(req.aux) == 3 else (
+            1 if req.aux is not None else req.maux)
+        n4 = req.mx + 4
+        lv, ii, jj = (np.zeros(n.value, np.int32) for _ in range(3))
+        q = np.empty((n.value, n4, n4, 3))
+        aux = np.empty((n.value, n4, n4, maux))
+        ip = C.POINTER(C.c_int)
+        self._check(self._lib.gf_fserver_download(
+            self.h, int(sid), None, lv.ctypes.data_as(ip), ii.ctypes.data_as(ip),
+            jj.ctypes.data_as(ip), _lib.dptr(q), _lib.dptr(aux)))
+        return np.stack([lv, ii, jj], axis=1), q, aux
+
+    def release(self, sid: int):
+        self._check(self._lib.gf_fserver_release(self.h, int(sid)))
+        self._keep.pop(sid, None)
+        self._req.pop(sid, None)
+
+    def cancel(self, sid: int):
+        self._check(self._lib.gf_fserver_cancel(self.h, int(sid)))
+
+    def stats(self) -> dict:
+        st = _lib.gf_fserver_stats()
+        self._check(self._lib.gf_fserver_stats_get(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.gf_fserver_stats._fields_}
+
+    def clock(self) -> float:
+        return float(self._lib.gf_fserver_clock(self.h))

@@ -617,6 +617,96 @@ int gf_server_cancel(gf_server* s, long long id);
 int gf_server_stats_get(gf_server* s, gf_server_stats* st);
 double gf_server_clock(const gf_server* s);
 
+/* ---------------------------------------------------- served AMR forests */
+/* A request loop over adaptive flood scenarios: each request is a forest
+ * (gf_forest_create / set_hydrograph / set_topo / init on admission) that
+ * then runs its outstyle-1 loop (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395,
+ * regrids every regrid_interval steps) inside the batched engine of
+ * gf_forest_batch_run, with every other admitted forest of any mx in the
+ * same replayed rounds. Members join between iterations (about half a
+ * millisecond of rounds each) and leave when their run ends; each
+ * membership change re-captures the round's graph. A request's result
+ * equals its own gf_forest_run bit for bit.
+ *
+ * Admission is by device footprint (gf_forest_footprint) against the
+ * budget, first come first served (backfill: later requests that fit pass
+ * a head that does not). A finished forest stays resident, counted against
+ * the budget, until gf_fserver_release; read it meanwhile through
+ * gf_fserver_forest (or gf_fserver_download while the loop thread runs).
+ * The caller keeps fields and topo alive until the request leaves QUEUED.
+ * Subcycled forests (opts.subcycle = 1) are refused: batched rounds step
+ * every level together. */
+typedef struct gf_fserver gf_fserver;
+
+typedef struct gf_forest_request {
+    gf_forest_opts opts;   /* phys_slot is ignored: the server assigns one      */
+    gf_phys phys;
+    const double* fields;  /* rasters as gf_forest_create (NULL: zero rasters)  */
+    gf_topo* topo;         /* nullable: bathymetry from DEMs (gf_forest_set_topo) */
+    int qinit;             /* with topo: still water at phys.sea_level          */
+    int nhydro;            /* hydrograph samples (0 = none), copied on submit    */
+    const double* hydro_time;
+    const double* hydro_hu;
+    int hydro_side[4];
+    double hydro_width, hydro_x0, hydro_y0;
+    double t_final;
+    int nout;
+    double initial_dt, desired_cfl, max_cfl;
+} gf_forest_request;
+
+typedef struct gf_fserver_opts {
+    size_t hbm_budget;     /* device bytes admitted and unreleased forests may hold */
+    int max_active;        /* forests running at once (1..GF_MAX_PHYS)          */
+    int backfill;
+} gf_fserver_opts;
+
+typedef struct gf_forest_request_info {
+    int state;             /* gf_scenario_state                                 */
+    long long steps, rejects, regrids, cell_updates;
+    double t, dt, max_cfl_seen;
+    double t_submit, t_admit, t_done; /* seconds on the server clock (-1: not yet) */
+    int npatch, npatch_max;
+    size_t footprint;      /* bytes reserved at admission                       */
+    size_t device_bytes;   /* bytes the forest holds (0 before admission)       */
+} gf_forest_request_info;
+
+typedef struct gf_fserver_stats {
+    long long submitted, admitted, done, failed;
+    long long iterations, epochs, rounds, launches, regrids, cell_updates;
+    double s_admit, s_epoch, s_rounds, s_regrid; /* host seconds per phase      */
+    size_t bytes_in_use, bytes_peak;
+    int active, queued, held;
+} gf_fserver_stats;
+
+/* Device bytes a forest with these options may hold at most (0: invalid). */
+size_t gf_forest_footprint(const gf_forest_opts* o);
+void gf_fserver_opts_default(gf_fserver_opts* o);
+int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out);
+void gf_fserver_destroy(gf_fserver* s);
+const char* gf_fserver_last_error(const gf_fserver* s);
+/* The server's context (fp-contract mode, topo rasters); owned by the server. */
+gf_ctx* gf_fserver_ctx(gf_fserver* s);
+/* Queue a request (validated here; GF_ERR_NOMEM if it can never fit). */
+int gf_fserver_submit(gf_fserver* s, const gf_forest_request* r, long long* id);
+/* One pass of the loop: admit, run one iteration of the batch, retire the
+ * finished. *busy = 1 while requests are queued or running. */
+int gf_fserver_pump(gf_fserver* s, int* busy);
+int gf_fserver_start(gf_fserver* s);
+int gf_fserver_stop(gf_fserver* s);
+int gf_fserver_wait(gf_fserver* s, long long id, double timeout_s);
+int gf_fserver_poll(gf_fserver* s, long long id, gf_forest_request_info* info);
+int gf_fserver_cancel(gf_fserver* s, long long id);
+/* A DONE request's forest (borrowed; valid until gf_fserver_release). */
+int gf_fserver_forest(gf_fserver* s, long long id, gf_forest** f);
+/* npatch and the leaves' state / aux of a DONE request, canonical order
+ * (as gf_forest_patches / gf_forest_download); any argument may be NULL. */
+int gf_fserver_download(gf_fserver* s, long long id, int* npatch, int* level, int* I, int* J,
+                        double* q, double* aux);
+/* Destroy a finished request's forest and return its bytes to the budget. */
+int gf_fserver_release(gf_fserver* s, long long id);
+int gf_fserver_stats_get(gf_fserver* s, gf_fserver_stats* st);
+double gf_fserver_clock(const gf_fserver* s);
+
 /* ------------------------------------------------------------ tiling */
 /* Tile shapes of the production patch kernel (threads per patch x slices
  * per band) per patch size, measured on this device: the fastest for whole
