@@ -190,6 +190,11 @@ class Context:
         """False: run the contraction-free build (bit-level parity mode)."""
         _check(self.h, self._lib.gf_ctx_set_fp_contract(self.h, int(bool(allow))))
 
+    def set_mixed_update(self, on: bool):
+        """Batched forest rounds: one persistent update launch for all patch
+        sizes (True, the default) or one launch per size."""
+        _check(self.h, self._lib.gf_ctx_set_mixed_update(self.h, int(bool(on))))
+
     @property
     def stream(self) -> int:
         """cudaStream_t of this context as an integer handle."""

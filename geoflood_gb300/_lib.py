@@ -195,6 +195,7 @@ SIGNATURES = [
     ("gf_level_sync", C.c_int, [_vp, _dp]),
     ("gf_ctx_stream", C.c_int, [_vp, C.POINTER(_vp)]),
     ("gf_ctx_set_fp_contract", C.c_int, [_vp, C.c_int]),
+    ("gf_ctx_set_mixed_update", C.c_int, [_vp, C.c_int]),
     ("gf_level_patch_cfl", C.c_int, [_vp, _dp]),
     ("gf_level_set_layout", C.c_int, [_vp, C.POINTER(C.c_int), _dp, _dp]),
     ("gf_level_set_bc", C.c_int, [_vp, C.POINTER(C.c_int)]),

@@ -87,6 +87,7 @@ struct gf_ctx {
     double* h_gdt = nullptr; /* pinned */
     std::string last_error;
     bool exact = false; /* run the contraction-free build */
+    bool mixed = true;  /* batched forms: one persistent launch for all patch sizes */
     /* scratch for the host-buffer drop-in paths */
     DevBuf<double> q_aos, q_soa, aux_aos, aux_soa, cfl;
     DevBuf<gf_patch_work> work;
@@ -843,6 +844,13 @@ int gf_ctx_set_fp_contract(gf_ctx* c, int allow)
     return GF_OK;
 }
 
+int gf_ctx_set_mixed_update(gf_ctx* c, int on)
+{
+    if (!c) return GF_ERR_ARG;
+    c->mixed = (on != 0);
+    return GF_OK;
+}
+
 int gf_ctx_stream(gf_ctx* c, void** stream)
 {
     if (!c || !stream) return GF_ERR_ARG;
@@ -1032,6 +1040,7 @@ namespace gf {
 cudaStream_t ctx_stream(gf_ctx* c) { return c->stream; }
 int ctx_device(gf_ctx* c) { return c->device; }
 bool ctx_exact(gf_ctx* c) { return c->exact; }
+bool ctx_mixed(gf_ctx* c) { return c->mixed; }
 const gf_phys* ctx_device_phys(gf_ctx* c) { return c->d_phys; }
 const gf_phys* ctx_host_phys(gf_ctx* c, int slot) { return &c->h_phys[slot]; }
 int ctx_check_phys(gf_ctx* c, int slot) { return check_phys_slot(c, slot); }

@@ -1917,7 +1917,7 @@ struct Batch {
     char* d = nullptr;
     size_t cap = 0;
     size_t off_blk = 0, off_gs = 0, off_dt = 0, off_par = 0, off_dl = 0, off_rb = 0, off_hyt = 0,
-           off_hyu = 0;
+           off_hyu = 0, off_sched = 0;
     size_t off_refs[3] = {}, off_avg[3] = {}, off_work[3] = {};
     size_t off_itp[3][kBatchLevels] = {}, off_ref[3][kBatchLevels] = {};
     int n_refs[3] = {}, n_avg[3] = {}, n_work[3] = {};
@@ -1989,7 +1989,22 @@ int enqueue_batch_round(Batch& B)
         }
     }
     const bool exact = gf::ctx_exact(B.ctx);
-    for (int c = 0; c < 3; ++c) {
+    if (gf::ctx_mixed(B.ctx)) {
+        /* one persistent launch: the work lists lie contiguous, mx 32 first */
+        const int nw[3] = {B.n_work[2], B.n_work[1], B.n_work[0]};
+        const gf_patch_work* w = reinterpret_cast<gf_patch_work*>(d + B.off_work[2]);
+        unsigned int* sched = reinterpret_cast<unsigned int*>(d + B.off_sched);
+        if (nw[0] + nw[1] + nw[2]) {
+            if (exact)
+                BK(B, gf::launch_patch_update_mixed_exact(w, nw, phys, 0.0, gdt, gpar, 3, nullptr, rb + 1, err,
+                                                          sched, B.st));
+            else
+                BK(B, gf::launch_patch_update_mixed(w, nw, phys, 0.0, gdt, gpar, 3, nullptr, rb + 1, err, sched,
+                                                    B.st));
+            ++n;
+        }
+    }
+    for (int c = 0; c < 3 && !gf::ctx_mixed(B.ctx); ++c) {
         if (!B.n_work[c]) continue;
         const gf_patch_work* w = reinterpret_cast<gf_patch_work*>(d + B.off_work[c]);
         if (exact)
@@ -2046,10 +2061,14 @@ int build_epoch(Batch& B)
     B.off_rb = take((ng + 1) * sizeof(unsigned long long));
     B.off_hyt = take(std::max<size_t>(nhy, 1) * sizeof(double));
     B.off_hyu = take(std::max<size_t>(nhy, 1) * sizeof(double));
+    /* work items of all sizes contiguous, mx 32 first (the mixed launch's list) */
+    B.off_work[2] = take((size_t)(B.n_work[0] + B.n_work[1] + B.n_work[2]) * sizeof(gf_patch_work));
+    B.off_work[1] = B.off_work[2] + (size_t)B.n_work[2] * sizeof(gf_patch_work);
+    B.off_work[0] = B.off_work[1] + (size_t)B.n_work[1] * sizeof(gf_patch_work);
+    B.off_sched = take(2 * sizeof(unsigned int));
     for (int c = 0; c < 3; ++c) {
         B.off_refs[c] = take(B.n_refs[c] * sizeof(gf_ghost_ref));
         B.off_avg[c] = take(B.n_avg[c] * sizeof(gf_xfer_task));
-        B.off_work[c] = take(B.n_work[c] * sizeof(gf_patch_work));
         for (int l = 0; l < kBatchLevels; ++l) {
             B.off_itp[c][l] = take(B.n_itp[c][l] * sizeof(gf_xfer_task));
             B.off_ref[c][l] = take(B.n_ref[c][l] * sizeof(gf_ghost_ref));
@@ -2173,6 +2192,11 @@ int batch_begin(BatchRun& R, gf_ctx* ctx)
         gf::launch_patch_update_exact(kCls[c], nullptr, 0, nullptr, 0.0, nullptr, nullptr, 0, nullptr,
                                       nullptr, nullptr, B.st);
     }
+    const int none[3] = {0, 0, 0};
+    gf::launch_patch_update_mixed(nullptr, none, nullptr, 0.0, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
+                                  nullptr, B.st);
+    gf::launch_patch_update_mixed_exact(nullptr, none, nullptr, 0.0, nullptr, nullptr, 0, nullptr, nullptr,
+                                        nullptr, nullptr, B.st);
     return GF_OK;
 }
 

@@ -36,6 +36,22 @@ cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwor
                                       const int* gpar, int maux, double* cfl,
                                       unsigned long long* gmax, int* err, cudaStream_t st);
 
+/* All patch sizes in one persistent launch. work holds n[0] items of mx =
+ * 32, then n[1] of mx = 16, then n[2] of mx = 8; sched is a pair of counters
+ * owned by the call site, zero before the first launch and reset by each
+ * launch on exit (so launches sharing a pair must not overlap). The grid is
+ * one CTA per SM, capped by max_ctas > 0. */
+cudaError_t launch_patch_update_mixed(const gf_patch_work* work, const int n[3], const gf_phys* phys,
+                                      double dt, const double* gdt, const int* gpar, int maux,
+                                      double* cfl, unsigned long long* gmax, int* err,
+                                      unsigned int* sched, cudaStream_t st, int max_ctas = 0);
+cudaError_t launch_patch_update_mixed_exact(const gf_patch_work* work, const int n[3],
+                                            const gf_phys* phys, double dt, const double* gdt,
+                                            const int* gpar, int maux, double* cfl,
+                                            unsigned long long* gmax, int* err, unsigned int* sched,
+                                            cudaStream_t st, int max_ctas = 0);
+int sm_count(); /* of the current device */
+
 cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int ncell, int nf,
                               long src_stride, long dst_stride, cudaStream_t st);
 cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int ncell, int nf,
@@ -69,6 +85,7 @@ cudaError_t launch_tags(int m, const gf_tag_task* tasks, int ntask, const gf_ref
 cudaStream_t ctx_stream(gf_ctx* c);
 int ctx_device(gf_ctx* c);
 bool ctx_exact(gf_ctx* c); /* contraction-free update build selected */
+bool ctx_mixed(gf_ctx* c); /* batched forms: one launch for all patch sizes */
 const gf_phys* ctx_device_phys(gf_ctx* c);
 const gf_phys* ctx_host_phys(gf_ctx* c, int slot);
 int ctx_check_phys(gf_ctx* c, int slot);

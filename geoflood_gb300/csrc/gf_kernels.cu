@@ -132,6 +132,46 @@ cudaError_t launch_patch_update(int m, const gf_patch_work* work, int nwork, con
                                     maux, cfl, gmax, err, st, max_ctas);
 }
 
+int sm_count()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!cache[dev]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 1;
+    }
+    return cache[dev];
+}
+
+/* mixed tile: 256 threads for every size; mx = 8 takes a whole patch per
+ * band, mx = 16 its 256-thread variant, mx = 32 the default */
+constexpr int kMixNT = 256, kMixRB8 = 10, kMixRB16 = 13, kMixRB32 = 7;
+
+cudaError_t launch_patch_update_mixed(const gf_patch_work* work, const int n[3], const gf_phys* phys,
+                                      double dt, const double* gdt, const int* gpar, int maux,
+                                      double* cfl, unsigned long long* gmax, int* err,
+                                      unsigned int* sched, cudaStream_t st, int max_ctas)
+{
+    using X = MixedSmem<kMixRB8, kMixRB16, kMixRB32, false>;
+    auto kern = patch_update_mixed_kernel<kMixNT, kMixRB8, kMixRB16, kMixRB32, false>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X::BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const int nwork = n[0] + n[1] + n[2];
+    if (nwork <= 0) return cudaSuccess;
+    int grid = sm_count();
+    if (max_ctas > 0 && max_ctas < grid) grid = max_ctas;
+    if (grid > nwork) grid = nwork;
+    kern<<<grid, kMixNT, X::BYTES, st>>>(work, n[0], n[1], n[2], phys, dt, gdt, gpar, maux, cfl, gmax, err,
+                                         sched);
+    return cudaGetLastError();
+}
+
 int patch_update_occupancy(int m)
 {
     int n = 0;

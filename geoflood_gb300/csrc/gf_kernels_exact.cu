@@ -47,4 +47,28 @@ cudaError_t launch_patch_update_exact(int m, const gf_patch_work* work, int nwor
     }
 }
 
+cudaError_t launch_patch_update_mixed_exact(const gf_patch_work* work, const int n[3],
+                                            const gf_phys* phys, double dt, const double* gdt,
+                                            const int* gpar, int maux, double* cfl,
+                                            unsigned long long* gmax, int* err, unsigned int* sched,
+                                            cudaStream_t st, int max_ctas)
+{
+    /* the per-size exact tiles at 256 threads: mx = 32 keeps 4 slices per band */
+    using X = gf_exact::MixedSmem<10, 13, 4, true>;
+    auto kern = gf_exact::patch_update_mixed_kernel<256, 10, 13, 4, true>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X::BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const int nwork = n[0] + n[1] + n[2];
+    if (nwork <= 0) return cudaSuccess;
+    int grid = sm_count();
+    if (max_ctas > 0 && max_ctas < grid) grid = max_ctas;
+    if (grid > nwork) grid = nwork;
+    kern<<<grid, 256, X::BYTES, st>>>(work, n[0], n[1], n[2], phys, dt, gdt, gpar, maux, cfl, gmax, err, sched);
+    return cudaGetLastError();
+}
+
 } // namespace gf

@@ -300,30 +300,33 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                     for (int c = 0; c < 3; ++c) TM[a + c * MM] += (0.0 - fr[6 + c]) - fl[12 + c];
                 }
             } else {
-                double dn0 = 0.0, dn1 = 0.0, dn2 = 0.0, dt0 = 0.0, dt1 = 0.0, dt2 = 0.0;
+                /* each slice's part enters the accumulators on its own, slices in
+                 * increasing order, so the sums do not depend on where the band
+                 * boundaries fall: every tile shape gives the same bits */
+                if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
+                    const double* fr = O + ((t - 1 - t0) * G::FB + n) * L::O_STRIDE;
+                    const double* fl = O + ((t - 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    ACCT[a] += half_dtdn * (fr[9] + fl[15]);
+                    ACCT[a + MM] += half_dtdn * (fr[10] + fl[16]);
+                    ACCT[a + 2 * MM] += half_dtdn * (fr[11] + fl[17]);
+                }
                 if (t >= t0 && t <= t1) {
                     const double* fr = O + ((t - t0) * G::FB + n) * L::O_STRIDE;       /* face n+1 */
                     const double* fl = O + ((t - t0) * G::FB + (n - 1)) * L::O_STRIDE; /* face n   */
-                    dn0 = fr[0] - fl[3]; dn1 = fr[1] - fl[4]; dn2 = fr[2] - fl[5];
-                    dt0 = (fr[6] - fr[9]) + (fl[12] - fl[15]);
-                    dt1 = (fr[7] - fr[10]) + (fl[13] - fl[16]);
-                    dt2 = (fr[8] - fr[11]) + (fl[14] - fl[17]);
+                    ACCN[a] += fr[0] - fl[3];
+                    ACCN[a + MM] += fr[1] - fl[4];
+                    ACCN[a + 2 * MM] += fr[2] - fl[5];
+                    ACCT[a] += half_dtdn * ((fr[6] - fr[9]) + (fl[12] - fl[15]));
+                    ACCT[a + MM] += half_dtdn * ((fr[7] - fr[10]) + (fl[13] - fl[16]));
+                    ACCT[a + 2 * MM] += half_dtdn * ((fr[8] - fr[11]) + (fl[14] - fl[17]));
                 }
                 if (t + 1 >= t0 && t + 1 <= t1) { /* slice above: down-going parts */
                     const double* fr = O + ((t + 1 - t0) * G::FB + n) * L::O_STRIDE;
                     const double* fl = O + ((t + 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
-                    dt0 += -fr[6] - fl[12]; dt1 += -fr[7] - fl[13]; dt2 += -fr[8] - fl[14];
+                    ACCT[a] -= half_dtdn * (fr[6] + fl[12]);
+                    ACCT[a + MM] -= half_dtdn * (fr[7] + fl[13]);
+                    ACCT[a + 2 * MM] -= half_dtdn * (fr[8] + fl[14]);
                 }
-                if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
-                    const double* fr = O + ((t - 1 - t0) * G::FB + n) * L::O_STRIDE;
-                    const double* fl = O + ((t - 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
-                    dt0 += fr[9] + fl[15]; dt1 += fr[10] + fl[16]; dt2 += fr[11] + fl[17];
-                }
-                ACCN[a] += dn0; ACCN[a + MM] += dn1; ACCN[a + 2 * MM] += dn2;
-                /* transverse parts enter unscaled; 0.5 dt/dn applied here once */
-                ACCT[a] += half_dtdn * dt0;
-                ACCT[a + MM] += half_dtdn * dt1;
-                ACCT[a + 2 * MM] += half_dtdn * dt2;
             }
         }
     };
@@ -526,7 +529,174 @@ __device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double ba
     }
 }
 
-/* The fused kernel. One CTA per work item. */
+/* One work item of the fused update: stage the patch, b4step2, both face
+ * sweeps, flux differencing + src2, CFL. All threads of the CTA take part;
+ * returns false (on every thread) when the staging copy's wait timed out,
+ * after the error flag is set and the copy has landed or been waited for. */
+template <int M, int NT, int RB, bool EXACT>
+__device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& phase, gf_patch_work wk,
+                                           int wi, const gf_phys* __restrict__ phys_table,
+                                           double dt_uniform, const double* __restrict__ group_dt,
+                                           const int* __restrict__ group_par, int maux,
+                                           double* __restrict__ cfl_out,
+                                           unsigned long long* __restrict__ group_max, int* __restrict__ err)
+{
+    using G = Geo<M>;
+    using L = Smem<M, RB, EXACT>;
+    constexpr int N = G::N;
+    constexpr int S = G::S;
+    constexpr bool FAST = !EXACT;
+    int* cnt = reinterpret_cast<int*>(sm + L::OFF_INT);
+    uint16_t* la = reinterpret_cast<uint16_t*>(cnt + L::CNT_INTS);
+    uint16_t* lb = la + L::LIST_A;
+    unsigned char* wet = reinterpret_cast<unsigned char*>(sm) + L::OFF_WET_BYTES;
+    double* red = sm + L::OFF_RED;
+
+    const double dt = group_dt ? group_dt[wk.group] : dt_uniform;
+    /* a group with no step this round (dt <= 0) is skipped as a whole */
+    if (group_dt && !(dt > 0.0)) return true;
+    if (group_par && group_par[wk.group]) {
+        /* the group's state lives in the second buffer: read there, write back */
+        double* t = wk.q;
+        wk.q = wk.qout;
+        wk.qout = t;
+    }
+    const gf_phys P = phys_table[wk.phys];
+    const double g = P.grav, drytol = P.dry_tolerance;
+
+    /* ---- stage the patch (h, hu, hv planes and b) with bulk copies ---- */
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(bar, (uint32_t)(4 * S * sizeof(double)));
+        bulk_g2s(sm + L::OFF_H, wk.q, (uint32_t)(3 * S * sizeof(double)), bar);
+        bulk_g2s(sm + L::OFF_B, wk.aux, (uint32_t)(S * sizeof(double)), bar);
+    }
+    const uint32_t ph = phase;
+    phase ^= 1u;
+    if (!__syncthreads_and(mbar_wait(bar, ph, 1u << 22))) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        mbar_wait(bar, ph, 1u << 22); /* let any copy in flight land */
+        return false;
+    }
+
+    /* ---- b4step2 on all cells + per-cell quotients ---- */
+    int any_wet = 0;
+    for (int k = threadIdx.x; k < S; k += NT) {
+        double h = sm[L::OFF_H + k];
+        if (d_lt<FAST>(h, drytol)) {
+            h = d_max<FAST>(h, 0.0);
+            sm[L::OFF_H + k] = h;
+            sm[L::OFF_HU + k] = 0.0;
+            sm[L::OFF_HV + k] = 0.0;
+        }
+        const bool w = d_gt<FAST>(h, drytol);
+        wet[k] = w ? 1 : 0;
+        any_wet |= w;
+        double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
+        if (w) {
+            if (FAST) {
+                rh = gf_rcp(h);
+                u = sm[L::OFF_HU + k] * rh;
+                v = sm[L::OFF_HV + k] * rh;
+                const double gh = g * h;
+                rc = rsqrt(gh);
+                c = gh * rc;
+            } else {
+                u = sm[L::OFF_HU + k] / h;
+                v = sm[L::OFF_HV + k] / h;
+                c = sqrt(g * h);
+            }
+        }
+        sm[L::OFF_U + k] = u;
+        sm[L::OFF_V + k] = v;
+        sm[L::OFF_C + k] = c;
+        if (FAST) {
+            sm[L::OFF_RH + k] = rh;
+            sm[L::OFF_RC + k] = rc;
+        }
+    }
+    for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
+    any_wet = __syncthreads_or(any_wet);
+
+    const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
+    double smax_x = 0.0, smax_y = 0.0;
+    if (any_wet) {
+        const double c16g = 1.0 / (16.0 * g);
+        const double rsg = rsqrt(g);
+        const double crit = fmax(drytol * g, 1e-6);
+        const double crit2 = sqrt(crit);
+        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2);
+        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2);
+    }
+
+    /* ---- flux-difference update, src2, write interior ---- */
+    double* gq = wk.qout ? wk.qout : wk.q;
+    const double* gaux = wk.aux;
+    const int fidx = P.friction_index - 1;
+    for (int e = threadIdx.x; e < M * M; e += NT) {
+        const int i = 1 + e % M, j = 1 + e / M;
+        const int k = (j + 1) * N + (i + 1);
+        double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
+        if (EXACT) {
+            /* q - dtdx*(fm(i+1,j) - fp(i,j)) - dtdy*(gm(i,j+1) - gp(i,j)) */
+            const double* FM = sm + L::OFF_ACC;
+            const double* FP = FM + 3 * M * M;
+            const double* GM = FP + 3 * M * M;
+            const double* GP = GM + 3 * M * M;
+            h = h - dtdx * (FM[e] - FP[e]) - dtdy * (GM[e] - GP[e]);
+            hu = hu - dtdx * (FM[e + M * M] - FP[e + M * M]) - dtdy * (GM[e + M * M] - GP[e + M * M]);
+            hv = hv - dtdx * (FM[e + 2 * M * M] - FP[e + 2 * M * M]) -
+                 dtdy * (GM[e + 2 * M * M] - GP[e + 2 * M * M]);
+        } else {
+            const double* DX = sm + L::OFF_ACC;
+            const double* DY = sm + L::OFF_ACC + 3 * M * M;
+            h = h - dtdx * DX[e] - dtdy * DY[e];
+            hu = hu - dtdx * DX[e + M * M] - dtdy * DY[e + M * M];
+            hv = hv - dtdx * DX[e + 2 * M * M] - dtdy * DY[e + 2 * M * M];
+        }
+        if (P.src_term > 0) {
+            const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
+                                    ? gaux[(size_t)fidx * S + k]
+                                    : 0.0;
+            src2_cell<FAST>(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
+        }
+        gq[k] = h;
+        gq[S + k] = hu;
+        gq[2 * S + k] = hv;
+    }
+
+    /* ---- CFL: warp-shuffle max, then across warps ---- */
+    double cx = smax_x, cy = smax_y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
+        cy = fmax(cy, __shfl_xor_sync(0xffffffffu, cy, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[warp] = cx;
+        red[32 + warp] = cy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = 0.0, my = 0.0;
+        for (int w2 = 0; w2 < NT / 32; ++w2) {
+            mx = fmax(mx, red[w2]);
+            my = fmax(my, red[32 + w2]);
+        }
+        double cfl = fmax(dtdx * mx, dtdy * my);
+        if (cfl > P.maxcfl_cap) cfl = 0.0;
+        if (cfl_out) cfl_out[wi] = cfl;
+        if (group_max) atomicMax(group_max + wk.group, dkey(cfl));
+    }
+    /* shared memory is restaged by the bulk (async-proxy) copies of the next
+     * work item: order this item's generic-proxy accesses before them */
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    return true;
+}
+
+/* The fused kernel for one patch size: one CTA per work item, or a
+ * persistent grid striding over the work list. */
 template <int M, int NT, int RB, int MINB, bool EXACT>
 __global__ void __launch_bounds__(NT, MINB)
     patch_update_kernel(const gf_patch_work* __restrict__ work, int nwork,
@@ -535,166 +705,78 @@ __global__ void __launch_bounds__(NT, MINB)
                         int maux, double* __restrict__ cfl_out,
                         unsigned long long* __restrict__ group_max, int* __restrict__ err)
 {
-    using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
-    constexpr int N = G::N;
-    constexpr int S = G::S;
-    constexpr bool FAST = !EXACT;
     extern __shared__ __align__(128) double sm[];
-    int* cnt = reinterpret_cast<int*>(sm + L::OFF_INT);
-    uint16_t* la = reinterpret_cast<uint16_t*>(cnt + L::CNT_INTS);
-    uint16_t* lb = la + L::LIST_A;
-    unsigned char* wet = reinterpret_cast<unsigned char*>(sm) + L::OFF_WET_BYTES;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::OFF_BAR);
-    double* red = sm + L::OFF_RED;
-
     if (threadIdx.x == 0) mbar_init(bar, 1);
     __syncthreads();
     uint32_t phase = 0;
-    /* persistent over the work list: one patch at a time per CTA */
-    for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
-        gf_patch_work wk = work[wi];
-        const double dt = group_dt ? group_dt[wk.group] : dt_uniform;
-        /* a group with no step this round (dt <= 0) is skipped as a whole */
-        if (group_dt && !(dt > 0.0)) continue;
-        if (group_par && group_par[wk.group]) {
-            /* the group's state lives in the second buffer: read there, write back */
-            double* t = wk.q;
-            wk.q = wk.qout;
-            wk.qout = t;
-        }
-        const gf_phys P = phys_table[wk.phys];
-        const double g = P.grav, drytol = P.dry_tolerance;
-
-        /* ---- stage the patch (h, hu, hv planes and b) with bulk copies ---- */
-        if (threadIdx.x == 0) {
-            mbar_expect_tx(bar, (uint32_t)(4 * S * sizeof(double)));
-            bulk_g2s(sm + L::OFF_H, wk.q, (uint32_t)(3 * S * sizeof(double)), bar);
-            bulk_g2s(sm + L::OFF_B, wk.aux, (uint32_t)(S * sizeof(double)), bar);
-        }
-        const uint32_t ph = phase;
-        phase ^= 1u;
-        if (!__syncthreads_and(mbar_wait(bar, ph, 1u << 22))) {
-            if (threadIdx.x == 0) atomicExch(err, 1);
-            mbar_wait(bar, ph, 1u << 22); /* let any copy in flight land */
+    for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x)
+        if (!patch_item<M, NT, RB, EXACT>(sm, bar, phase, work[wi], wi, phys_table, dt_uniform, group_dt,
+                                          group_par, maux, cfl_out, group_max, err))
             return;
-        }
+}
 
-        /* ---- b4step2 on all cells + per-cell quotients ---- */
-        int any_wet = 0;
-        for (int k = threadIdx.x; k < S; k += NT) {
-            double h = sm[L::OFF_H + k];
-            if (d_lt<FAST>(h, drytol)) {
-                h = d_max<FAST>(h, 0.0);
-                sm[L::OFF_H + k] = h;
-                sm[L::OFF_HU + k] = 0.0;
-                sm[L::OFF_HV + k] = 0.0;
-            }
-            const bool w = d_gt<FAST>(h, drytol);
-            wet[k] = w ? 1 : 0;
-            any_wet |= w;
-            double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
-            if (w) {
-                if (FAST) {
-                    rh = gf_rcp(h);
-                    u = sm[L::OFF_HU + k] * rh;
-                    v = sm[L::OFF_HV + k] * rh;
-                    const double gh = g * h;
-                    rc = rsqrt(gh);
-                    c = gh * rc;
-                } else {
-                    u = sm[L::OFF_HU + k] / h;
-                    v = sm[L::OFF_HV + k] / h;
-                    c = sqrt(g * h);
-                }
-            }
-            sm[L::OFF_U + k] = u;
-            sm[L::OFF_V + k] = v;
-            sm[L::OFF_C + k] = c;
-            if (FAST) {
-                sm[L::OFF_RH + k] = rh;
-                sm[L::OFF_RC + k] = rc;
-            }
-        }
-        for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
-        any_wet = __syncthreads_or(any_wet);
+/* Shared-memory bytes of the mixed kernel: the largest class layout, then
+ * the mbarrier and the two work-cursor slots. */
+template <int RB8, int RB16, int RB32, bool EXACT>
+struct MixedSmem {
+    static constexpr size_t B8 = Smem<8, RB8, EXACT>::BYTES, B16 = Smem<16, RB16, EXACT>::BYTES,
+                            B32 = Smem<32, RB32, EXACT>::BYTES;
+    static constexpr size_t MAXB = B8 > B16 ? (B8 > B32 ? B8 : B32) : (B16 > B32 ? B16 : B32);
+    static constexpr size_t OFF_CTL = (MAXB + 15) / 16 * 16;
+    static constexpr size_t BYTES = OFF_CTL + 32;
+};
 
-        const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
-        double smax_x = 0.0, smax_y = 0.0;
-        if (any_wet) {
-            const double c16g = 1.0 / (16.0 * g);
-            const double rsg = rsqrt(g);
-            const double crit = fmax(drytol * g, 1e-6);
-            const double crit2 = sqrt(crit);
-            smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2);
-            smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2);
-        }
-
-        /* ---- flux-difference update, src2, write interior ---- */
-        double* gq = wk.qout ? wk.qout : wk.q;
-        const double* gaux = wk.aux;
-        const int fidx = P.friction_index - 1;
-        for (int e = threadIdx.x; e < M * M; e += NT) {
-            const int i = 1 + e % M, j = 1 + e / M;
-            const int k = (j + 1) * N + (i + 1);
-            double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
-            if (EXACT) {
-                /* q - dtdx*(fm(i+1,j) - fp(i,j)) - dtdy*(gm(i,j+1) - gp(i,j)) */
-                const double* FM = sm + L::OFF_ACC;
-                const double* FP = FM + 3 * M * M;
-                const double* GM = FP + 3 * M * M;
-                const double* GP = GM + 3 * M * M;
-                h = h - dtdx * (FM[e] - FP[e]) - dtdy * (GM[e] - GP[e]);
-                hu = hu - dtdx * (FM[e + M * M] - FP[e + M * M]) - dtdy * (GM[e + M * M] - GP[e + M * M]);
-                hv = hv - dtdx * (FM[e + 2 * M * M] - FP[e + 2 * M * M]) -
-                     dtdy * (GM[e + 2 * M * M] - GP[e + 2 * M * M]);
-            } else {
-                const double* DX = sm + L::OFF_ACC;
-                const double* DY = sm + L::OFF_ACC + 3 * M * M;
-                h = h - dtdx * DX[e] - dtdy * DY[e];
-                hu = hu - dtdx * DX[e + M * M] - dtdy * DY[e + M * M];
-                hv = hv - dtdx * DX[e + 2 * M * M] - dtdy * DY[e + 2 * M * M];
-            }
-            if (P.src_term > 0) {
-                const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
-                                        ? gaux[(size_t)fidx * S + k]
-                                        : 0.0;
-                src2_cell<FAST>(P, dt, sm[L::OFF_B + k], nvar, h, hu, hv);
-            }
-            gq[k] = h;
-            gq[S + k] = hu;
-            gq[2 * S + k] = hv;
-        }
-
-        /* ---- CFL: warp-shuffle max, then across warps ---- */
-        double cx = smax_x, cy = smax_y;
-    #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            cx = fmax(cx, __shfl_xor_sync(0xffffffffu, cx, o));
-            cy = fmax(cy, __shfl_xor_sync(0xffffffffu, cy, o));
-        }
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (lane == 0) {
-            red[warp] = cx;
-            red[32 + warp] = cy;
-        }
+/* All patch sizes in one persistent launch. The work list holds the mx = 32
+ * items, then the mx = 16 items, then the mx = 8 items; CTAs take items in
+ * that order from a device cursor (sched[0]) so that the long items start
+ * first and the short ones fill the tail. sched[1] counts CTAs that found
+ * the list empty; the last of them resets both counters for the next launch
+ * (both start at zero). */
+template <int NT, int RB8, int RB16, int RB32, bool EXACT>
+__global__ void __launch_bounds__(NT, 1)
+    patch_update_mixed_kernel(const gf_patch_work* __restrict__ work, int n32, int n16, int n8,
+                              const gf_phys* __restrict__ phys_table, double dt_uniform,
+                              const double* __restrict__ group_dt, const int* __restrict__ group_par,
+                              int maux, double* __restrict__ cfl_out,
+                              unsigned long long* __restrict__ group_max, int* __restrict__ err,
+                              unsigned int* __restrict__ sched)
+{
+    using X = MixedSmem<RB8, RB16, RB32, EXACT>;
+    extern __shared__ __align__(128) double sm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(sm) + X::OFF_CTL);
+    volatile int* slot = reinterpret_cast<volatile int*>(reinterpret_cast<char*>(sm) + X::OFF_CTL + 8);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    const int nwork = n32 + n16 + n8;
+    uint32_t phase = 0;
+    /* the cursor value goes through one of two slots by iteration parity: a
+     * skipped item has no barrier after its read, and the next write goes to
+     * the other slot */
+    for (int it = 0;; ++it) {
+        if (threadIdx.x == 0) slot[it & 1] = (int)atomicAdd(sched, 1u);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double mx = 0.0, my = 0.0;
-            for (int w2 = 0; w2 < NT / 32; ++w2) {
-                mx = fmax(mx, red[w2]);
-                my = fmax(my, red[32 + w2]);
-            }
-            double cfl = fmax(dtdx * mx, dtdy * my);
-            if (cfl > P.maxcfl_cap) cfl = 0.0;
-            if (cfl_out) cfl_out[wi] = cfl;
-            if (group_max) atomicMax(group_max + wk.group, dkey(cfl));
+        const int wi = slot[it & 1];
+        if (wi >= nwork) break;
+        bool ok;
+        if (wi < n32)
+            ok = patch_item<32, NT, RB32, EXACT>(sm, bar, phase, work[wi], wi, phys_table, dt_uniform, group_dt,
+                                                 group_par, maux, cfl_out, group_max, err);
+        else if (wi < n32 + n16)
+            ok = patch_item<16, NT, RB16, EXACT>(sm, bar, phase, work[wi], wi, phys_table, dt_uniform, group_dt,
+                                                 group_par, maux, cfl_out, group_max, err);
+        else
+            ok = patch_item<8, NT, RB8, EXACT>(sm, bar, phase, work[wi], wi, phys_table, dt_uniform, group_dt,
+                                               group_par, maux, cfl_out, group_max, err);
+        if (!ok) break;
+    }
+    if (threadIdx.x == 0) {
+        if (atomicAdd(sched + 1, 1u) == gridDim.x - 1) {
+            atomicExch(sched, 0u);
+            atomicExch(sched + 1, 0u);
         }
-        /* shared memory is restaged by the bulk (async-proxy) copies of the next
-         * work item: order this item's generic-proxy accesses before them */
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-    } /* work list */
+    }
 }
 
 } // namespace GF_KNS

@@ -82,6 +82,11 @@ int gf_ctx_stream(gf_ctx* ctx, void** stream);
  * order, so each FP64 operation rounds as the Fortran expression is written
  * (fortran_source/geoclaw_step2_wrap_fort.f:97-115 for the final sum). */
 int gf_ctx_set_fp_contract(gf_ctx* ctx, int allow);
+/* Batched forest rounds (gf_forest_batch_run, the forest server) update
+ * the patches of every size in one persistent launch over one work list
+ * (on = 1, the default) or launch once per patch size (on = 0). Results
+ * are the same either way. */
+int gf_ctx_set_mixed_update(gf_ctx* ctx, int on);
 
 /* Store physics set `slot` (0 <= slot < GF_MAX_PHYS). Replaces the
  * module set-up fc2d_geoclaw_module_setup (fc2d_geoclaw.cpp, calling

@@ -81,3 +81,27 @@ def test_batch_matches_oracle_forests_bitwise(ctx):
             F.close()
     finally:
         ctx.set_fp_contract(True)
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_mixed_and_per_size_updates_agree(ctx, exact):
+    """The one-launch update over all patch sizes (a device cursor over the
+    concatenated work list) and the per-size launches give the same bits."""
+    ctx.set_phys(SLOT, PHYS)
+    ctx.set_fp_contract(not exact)
+    outs = []
+    try:
+        for mixed in (True, False):
+            ctx.set_mixed_update(mixed)
+            fs = [make(ctx, m=8, seed=4, regrid=3), make(ctx, m=16, seed=5, regrid=2),
+                  make(ctx, m=32, seed=6, regrid=4), make(ctx, m=8, seed=7, regrid=2)]
+            batch_run(fs, 25.0, 1, 5.0, 0.9, 1.0)
+            outs.append([(F.patches(), F.download(), F.stats()) for F in fs])
+            for F in fs:
+                F.close()
+    finally:
+        ctx.set_mixed_update(True)
+        ctx.set_fp_contract(True)
+    for (pa, qa, sa), (pb, qb, sb) in zip(*outs):
+        assert np.array_equal(pa, pb) and np.array_equal(qa[S], qb[S])
+        assert sa["steps"] == sb["steps"] and sa["regrids"] == sb["regrids"]

@@ -32,6 +32,25 @@ def test_every_tile_meets_the_parity_bar(ctx, m):
         gf.Context.set_tile(m, 0, keep)
 
 
+@pytest.mark.parametrize("m", [8, 16, 32])
+def test_tile_shapes_give_the_same_bits(ctx, m):
+    """Threads per patch and slices per band change the work split, not the
+    sums: every variant's step equals variant 0's bit for bit."""
+    keep = gf.Context.tile(m, 0)
+    outs = []
+    try:
+        for v in variants(m):
+            gf.Context.set_tile(m, 0, v)
+            q, aux, _, _ = synth.uniform_dam_break_level(4, 4, m, 1.0, seed=7, x_dam=1.5 * m)
+            out, _, cg, _, pg, _ = level_vs_oracle(ctx, q, aux, m, 1.0, 0.05, gf.Phys())
+            outs.append((out, cg, pg))
+    finally:
+        gf.Context.set_tile(m, 0, keep)
+    for out, cg, pg in outs[1:]:
+        assert np.array_equal(out, outs[0][0]) and cg == outs[0][1]
+        assert np.array_equal(pg, outs[0][2])
+
+
 def test_autotune_measures_and_selects(ctx):
     ctx.set_phys(0, gf.Phys())
     res = ctx.autotune(reps=2)
