@@ -876,7 +876,10 @@ def fserved_leg(args, dev=0):
                              hydro=Hydrograph(np.array(h[0]), np.array(h[1]), tuple(h[2]), h[3],
                                               h[4], h[5]))
 
-    srv = ForestServer(device=dev)
+    lanes = {} if args.fserved_lane_cells is None else {"lane_cells": args.fserved_lane_cells}
+    if args.fserved_reserve_sms is not None:
+        lanes["reserve_sms"] = args.fserved_reserve_sms
+    srv = ForestServer(device=dev, **lanes)
     srv.start()
     # -- calibration: a saturated batch, throughput until half of it is done
     ncal = min(16, n)
@@ -896,7 +899,7 @@ def fserved_leg(args, dev=0):
     for i in cal:
         srv.release(i)
     est_work = float(np.mean([i["cell_updates"] for i in cal_info]))
-    rate = 0.8 * cap / est_work
+    rate = args.fserved_rate or 0.8 * cap / est_work
     gaps = np.random.default_rng(SEED + 6).exponential(1.0 / rate, n)
     arrivals = np.cumsum(gaps) - gaps[0]
     order = np.argsort(targets)
@@ -1073,6 +1076,11 @@ def main():
     ap.add_argument("--batched-only", action="store_true")
     ap.add_argument("--fserved-forests", type=int, default=32)
     ap.add_argument("--fserved-only", action="store_true")
+    ap.add_argument("--fserved-lane-cells", type=int, default=None,
+                    help="forest server: small-lane threshold in cells (0: one lane)")
+    ap.add_argument("--fserved-reserve-sms", type=int, default=None)
+    ap.add_argument("--fserved-rate", type=float, default=None,
+                    help="forest arrivals per second (default: 80 %% of the calibrated capacity)")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--large-only", action="store_true")

@@ -133,7 +133,8 @@ class gf_forest_request(C.Structure):
 
 
 class gf_fserver_opts(C.Structure):
-    _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("backfill", C.c_int)]
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("backfill", C.c_int),
+                ("lane_cells", C.c_longlong), ("reserve_sms", C.c_int)]
 
 
 class gf_forest_request_info(C.Structure):
@@ -141,12 +142,14 @@ class gf_forest_request_info(C.Structure):
                 ("regrids", C.c_longlong), ("cell_updates", C.c_longlong), ("t", C.c_double),
                 ("dt", C.c_double), ("max_cfl_seen", C.c_double), ("t_submit", C.c_double),
                 ("t_admit", C.c_double), ("t_done", C.c_double), ("npatch", C.c_int),
-                ("npatch_max", C.c_int), ("footprint", C.c_size_t), ("device_bytes", C.c_size_t)]
+                ("npatch_max", C.c_int), ("footprint", C.c_size_t), ("device_bytes", C.c_size_t),
+                ("lane", C.c_int)]
 
 
 class gf_fserver_stats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("done", C.c_longlong),
-                ("failed", C.c_longlong), ("iterations", C.c_longlong), ("epochs", C.c_longlong),
+                ("failed", C.c_longlong), ("lane_admitted", C.c_longlong * 2),
+                ("iterations", C.c_longlong), ("epochs", C.c_longlong),
                 ("rounds", C.c_longlong), ("launches", C.c_longlong), ("regrids", C.c_longlong),
                 ("cell_updates", C.c_longlong), ("s_admit", C.c_double), ("s_epoch", C.c_double),
                 ("s_rounds", C.c_double), ("s_regrid", C.c_double), ("bytes_in_use", C.c_size_t),

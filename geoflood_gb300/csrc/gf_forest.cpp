@@ -1928,8 +1928,13 @@ struct Batch {
     cudaGraphExec_t exec = nullptr;
     int launches_per_round = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_ctx = nullptr; /* context-stream work (tables, regrids) before the rounds */
+    bool own_stream = false;
+    int max_ctas = 0;             /* grid cap of the mixed update (0: one CTA per SM) */
     ~Batch()
     {
+        if (ev_ctx) cudaEventDestroy(ev_ctx);
+        if (own_stream && st) cudaStreamDestroy(st);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (d) cudaFree(d);
@@ -1997,10 +2002,10 @@ int enqueue_batch_round(Batch& B)
         if (nw[0] + nw[1] + nw[2]) {
             if (exact)
                 BK(B, gf::launch_patch_update_mixed_exact(w, nw, phys, 0.0, gdt, gpar, 3, nullptr, rb + 1, err,
-                                                          sched, B.st));
+                                                          sched, B.st, B.max_ctas));
             else
                 BK(B, gf::launch_patch_update_mixed(w, nw, phys, 0.0, gdt, gpar, 3, nullptr, rb + 1, err, sched,
-                                                    B.st));
+                                                    B.st, B.max_ctas));
             ++n;
         }
     }
@@ -2175,14 +2180,28 @@ struct BatchRun {
     double round_ms = 0.05;
     int rounds_paused = 0;
     bool rebuild = true;
+    bool inflight = false; /* rounds and their readback enqueued, not yet taken in */
+    int rounds_inflight = 0;
+    std::chrono::steady_clock::time_point t_launch;
 };
 
-int batch_begin(BatchRun& R, gf_ctx* ctx)
+/* stream_priority: 0 runs the rounds on the context's stream; otherwise on
+ * a stream of their own with that priority (1 = the greatest the device
+ * offers, 2 = the least), so that batches can overlap on the device. */
+int batch_begin(BatchRun& R, gf_ctx* ctx, int stream_priority = 0, int max_ctas = 0)
 {
     Batch& B = R.B;
     if (cudaSetDevice(gf::ctx_device(ctx)) != cudaSuccess) return GF_ERR_CUDA;
     B.ctx = ctx;
     B.st = gf::ctx_stream(ctx);
+    B.max_ctas = max_ctas;
+    if (stream_priority) {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi); /* hi: the numerically lowest, greatest priority */
+        BK(B, cudaStreamCreateWithPriority(&B.st, cudaStreamNonBlocking, stream_priority == 1 ? hi : lo));
+        B.own_stream = true;
+    }
+    BK(B, cudaEventCreateWithFlags(&B.ev_ctx, cudaEventDisableTiming));
     BK(B, cudaEventCreate(&B.ev0));
     BK(B, cudaEventCreate(&B.ev1));
     /* kernel attributes are set outside stream capture */
@@ -2227,13 +2246,14 @@ void batch_add(BatchRun& R, gf_forest* f, double t_final, int nout, double initi
     R.rebuild = true;
 }
 
-/* one iteration: drop finished members, rebuild the epoch if needed, run
- * ~0.5 ms of rounds, read the controllers back, regrid the waiting
- * members. *live = members still running (0: nothing was run). */
-int batch_iterate(BatchRun& R, int* live_out)
+/* Launch one iteration: drop finished members, rebuild the epoch if needed,
+ * enqueue ~0.5 ms of rounds and the controllers' readback. *live = members
+ * (0: nothing was launched). */
+int batch_launch(BatchRun& R, int* live_out)
 {
     Batch& B = R.B;
     gf_forest_batch_stats& S = R.S;
+    if (R.inflight) return gf::ctx_fail(B.ctx, GF_ERR_STATE, "batch iteration already in flight");
     std::vector<gf_forest*> live;
     for (gf_forest* f : B.fs)
         if (f->gst.active) live.push_back(f);
@@ -2257,15 +2277,36 @@ int batch_iterate(BatchRun& R, int* live_out)
     const int ng = (int)B.fs.size();
     int rounds = (int)std::ceil(0.5 / std::max(R.round_ms, 1e-3));
     rounds = std::max(1, std::min(64, rounds));
-    const auto tr = clk::now();
+    R.t_launch = clk::now();
+    const cudaStream_t cst = gf::ctx_stream(B.ctx);
+    if (B.st != cst) {
+        /* tables and regrids of the members went to the context's stream */
+        BK(B, cudaEventRecord(B.ev_ctx, cst));
+        BK(B, cudaStreamWaitEvent(B.st, B.ev_ctx, 0));
+    }
     BK(B, cudaEventRecord(B.ev0, B.st));
     for (int r = 0; r < rounds; ++r) BK(B, cudaGraphLaunch(B.exec, B.st));
     BK(B, cudaMemcpyAsync(B.h_rb, B.d + B.off_rb, 8, cudaMemcpyDeviceToHost, B.st));
     BK(B, cudaMemcpyAsync(B.h_rb + 8, B.d + B.off_gs, ng * sizeof(gf_group_state), cudaMemcpyDeviceToHost,
                           B.st));
     BK(B, cudaEventRecord(B.ev1, B.st));
-    BK(B, cudaStreamSynchronize(B.st));
-    S.s_rounds += secs(tr);
+    R.inflight = true;
+    R.rounds_inflight = rounds;
+    return GF_OK;
+}
+
+/* Take in a finished iteration (its readback has landed): the members'
+ * controllers, then the regrids of the waiting members. */
+int batch_complete(BatchRun& R)
+{
+    Batch& B = R.B;
+    gf_forest_batch_stats& S = R.S;
+    using clk = std::chrono::steady_clock;
+    auto secs = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    R.inflight = false;
+    const int ng = (int)B.fs.size();
+    const int rounds = R.rounds_inflight;
+    S.s_rounds += secs(R.t_launch);
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess) R.round_ms = std::max(1e-3, (double)ms / rounds);
     S.rounds += rounds;
@@ -2325,6 +2366,15 @@ int batch_iterate(BatchRun& R, int* live_out)
     return GF_OK;
 }
 
+/* one iteration, waited for */
+int batch_iterate(BatchRun& R, int* live_out)
+{
+    int rc = batch_launch(R, live_out);
+    if (rc || !*live_out) return rc;
+    BK(R.B, cudaEventSynchronize(R.B.ev1));
+    return batch_complete(R);
+}
+
 int batch_check(gf_forest* f, gf_ctx* ctx)
 {
     if (!f || f->ctx != ctx) return GF_ERR_ARG;
@@ -2367,11 +2417,11 @@ struct gf::ForestBatch {
     BatchRun R;
 };
 
-int gf::forest_batch_create(gf_ctx* c, ForestBatch** out)
+int gf::forest_batch_create(gf_ctx* c, ForestBatch** out, int stream_priority, int max_ctas)
 {
     if (!c || !out) return GF_ERR_ARG;
     ForestBatch* b = new ForestBatch;
-    int rc = batch_begin(b->R, c);
+    int rc = batch_begin(b->R, c, stream_priority, max_ctas);
     if (rc) {
         delete b;
         return rc;
@@ -2389,6 +2439,7 @@ int gf::forest_batch_add(ForestBatch* b, gf_forest* f, double t_final, int nout,
         return GF_ERR_ARG;
     int rc = batch_check(f, b->R.B.ctx);
     if (rc) return rc;
+    if (b->R.inflight) return ffail(f, GF_ERR_STATE, "members join between iterations");
     for (gf_forest* g : b->R.B.fs)
         if (g == f) return ffail(f, GF_ERR_ARG, "the forest is already a member");
     batch_add(b->R, f, t_final, nout, initial_dt, desired_cfl, max_cfl);
@@ -2397,8 +2448,28 @@ int gf::forest_batch_add(ForestBatch* b, gf_forest* f, double t_final, int nout,
 
 int gf::forest_batch_iterate(ForestBatch* b, int* live) { return batch_iterate(b->R, live); }
 
+int gf::forest_batch_launch(ForestBatch* b, int* live) { return batch_launch(b->R, live); }
+
+int gf::forest_batch_test(ForestBatch* b, int wait, int* done)
+{
+    *done = 1;
+    if (!b->R.inflight) return GF_OK;
+    cudaError_t e = wait ? cudaEventSynchronize(b->R.B.ev1) : cudaEventQuery(b->R.B.ev1);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return GF_OK;
+    }
+    if (e != cudaSuccess) return gf::ctx_cuda_fail(b->R.B.ctx, e, "batch iteration");
+    return batch_complete(b->R);
+}
+
+bool gf::forest_batch_inflight(const ForestBatch* b) { return b->R.inflight; }
+
+int gf::forest_batch_members(const ForestBatch* b) { return (int)b->R.B.fs.size(); }
+
 void gf::forest_batch_remove(ForestBatch* b, gf_forest* f)
 {
+    /* callers remove members only between iterations */
     std::vector<gf_forest*>& fs = b->R.B.fs;
     auto it = std::find(fs.begin(), fs.end(), f);
     if (it == fs.end()) return;

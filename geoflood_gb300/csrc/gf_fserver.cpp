@@ -17,6 +17,13 @@
  * The admitted and finished-but-unreleased forests together stay within the
  * HBM budget, by the footprint bound of their options; each active forest
  * has its own physics slot of the server's context.
+ *
+ * With two lanes the loop keeps one batch per lane in flight at once: small
+ * forests (by cells after their initial refinement) on a high-priority
+ * stream, large ones on a low-priority stream whose update grid leaves
+ * reserve_sms SMs free. A pass takes in the iterations that have finished,
+ * lets members leave and join the idle lanes, admits, and launches the idle
+ * lanes again; it never waits on the device.
  */
 #include <cuda_runtime.h>
 
@@ -45,6 +52,7 @@ struct Req {
     gf_forest_request_info info{};
     gf_forest* f = nullptr;
     int slot = -1;
+    int lane = -1;
     size_t held = 0; /* bytes counted against the budget */
     bool cancel_req = false;
 };
@@ -55,7 +63,9 @@ struct gf_fserver {
     int device = 0;
     gf_fserver_opts o{};
     gf_ctx* ctx = nullptr;
-    gf::ForestBatch* batch = nullptr;
+    int nlanes = 1;
+    gf::ForestBatch* lanes[2] = {nullptr, nullptr};
+    std::vector<Req*> joining[2]; /* built forests waiting for their lane to be idle */
     Clock::time_point t0;
     std::mutex mu;
     std::condition_variable cv;
@@ -160,9 +170,6 @@ int admit(gf_fserver* s, Req* x)
                                       x->r.hydro_width, x->r.hydro_x0, x->r.hydro_y0);
     if (!rc && x->r.topo) rc = gf_forest_set_topo(x->f, x->r.topo, x->r.qinit);
     if (!rc) rc = gf_forest_init(x->f);
-    if (!rc)
-        rc = gf::forest_batch_add(s->batch, x->f, x->r.t_final, x->r.nout, x->r.initial_dt, x->r.desired_cfl,
-                                  x->r.max_cfl);
     x->r.fields = nullptr;
     x->r.topo = nullptr;
     if (rc) {
@@ -171,22 +178,102 @@ int admit(gf_fserver* s, Req* x)
         drop(s, x);
         return rc;
     }
-    s->active.push_back(x);
+    const long long cells = (long long)gf_forest_npatch(x->f) * x->r.opts.mx * x->r.opts.mx;
+    x->lane = (s->nlanes > 1 && cells >= s->o.lane_cells) ? 1 : 0;
+    x->info.lane = x->lane;
+    s->stats.lane_admitted[x->lane]++;
+    s->joining[x->lane].push_back(x);
     return GF_OK;
+}
+
+/* members join a lane between its iterations */
+void join(gf_fserver* s, int k)
+{
+    for (Req* x : s->joining[k]) {
+        if (x->cancel_req) {
+            finish(s, x, GF_SCEN_CANCELLED);
+            drop(s, x);
+            continue;
+        }
+        int rc = gf::forest_batch_add(s->lanes[k], x->f, x->r.t_final, x->r.nout, x->r.initial_dt,
+                                      x->r.desired_cfl, x->r.max_cfl);
+        if (rc) {
+            s->last_error = gf_ctx_last_error(s->ctx);
+            finish(s, x, GF_SCEN_FAILED);
+            drop(s, x);
+            continue;
+        }
+        s->active.push_back(x);
+    }
+    s->joining[k].clear();
+}
+
+int fail_all(gf_fserver* s, int rc)
+{
+    s->broken = true;
+    s->last_error = gf_ctx_last_error(s->ctx);
+    for (Req* x : s->active) finish(s, x, GF_SCEN_FAILED);
+    s->active.clear();
+    for (int k = 0; k < 2; ++k) {
+        for (Req* x : s->joining[k]) finish(s, x, GF_SCEN_FAILED);
+        s->joining[k].clear();
+    }
+    return rc;
 }
 
 bool fits(const gf_fserver* s, const Req* x)
 {
-    return (int)s->active.size() < s->o.max_active && !s->free_slots.empty() &&
+    const size_t running = s->active.size() + s->joining[0].size() + s->joining[1].size();
+    return (int)running < s->o.max_active && !s->free_slots.empty() &&
            s->bytes_in_use + x->info.footprint <= s->o.hbm_budget;
 }
 
-int pump_locked(gf_fserver* s, int* busy)
+/* One pass of the loop; never waits on the device. *progress = 1 when an
+ * iteration was taken in or launched, or a request changed state. */
+int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
 {
     if (s->broken) return sfail(s, GF_ERR_STATE, "the batch failed; destroy the server");
-    const auto ta = Clock::now();
+    int moved = 0;
+    /* take in the iterations that have finished */
+    for (int k = 0; k < s->nlanes; ++k) {
+        if (!gf::forest_batch_inflight(s->lanes[k])) continue;
+        int done = 0;
+        int rc = gf::forest_batch_test(s->lanes[k], 0, &done);
+        if (rc) return fail_all(s, rc);
+        if (done) {
+            s->stats.iterations++;
+            moved = 1;
+        }
+    }
+    /* idle lanes: cancelled and finished members leave (a finished forest
+     * stays resident for the caller; its physics slot is free again) */
+    std::vector<Req*> still;
+    for (Req* x : s->active) {
+        gf::ForestBatch* b = s->lanes[x->lane];
+        if (gf::forest_batch_inflight(b)) {
+            still.push_back(x);
+            continue;
+        }
+        if (x->cancel_req) {
+            gf::forest_batch_remove(b, x->f);
+            finish(s, x, GF_SCEN_CANCELLED);
+            drop(s, x);
+            moved = 1;
+        } else if (!gf::forest_batch_running(x->f)) {
+            gf::forest_batch_remove(b, x->f);
+            finish(s, x, GF_SCEN_DONE);
+            s->free_slots.push_back(x->slot);
+            x->slot = -1;
+            moved = 1;
+        } else {
+            still.push_back(x);
+        }
+    }
+    s->active.swap(still);
     /* admission, first come first served (backfill: later requests that
-     * fit may pass a head that does not) */
+     * fit may pass a head that does not); built forests join their lane
+     * when it is idle */
+    const auto ta = Clock::now();
     for (auto it = s->queue.begin(); it != s->queue.end();) {
         Req* x = *it;
         if (!fits(s, x)) {
@@ -196,69 +283,64 @@ int pump_locked(gf_fserver* s, int* busy)
         }
         it = s->queue.erase(it);
         admit(s, x); /* a failed build fails only this request */
+        moved = 1;
     }
     s->stats.s_admit += std::chrono::duration<double>(Clock::now() - ta).count();
-    std::vector<Req*> still;
-    for (Req* x : s->active) {
-        if (!x->cancel_req) {
-            still.push_back(x);
-            continue;
-        }
-        gf::forest_batch_remove(s->batch, x->f);
-        finish(s, x, GF_SCEN_CANCELLED);
-        drop(s, x);
+    for (int k = 0; k < s->nlanes; ++k) {
+        if (gf::forest_batch_inflight(s->lanes[k])) continue;
+        if (!s->joining[k].empty()) join(s, k);
+        if (!gf::forest_batch_members(s->lanes[k])) continue;
+        int live = 0;
+        int rc = gf::forest_batch_launch(s->lanes[k], &live);
+        if (rc) return fail_all(s, rc);
+        moved |= live > 0;
     }
-    s->active.swap(still);
-    int live = 0;
-    if (!s->active.empty()) {
-        int rc = gf::forest_batch_iterate(s->batch, &live);
-        s->stats.iterations++;
-        if (rc) {
-            s->broken = true;
-            s->last_error = gf_ctx_last_error(s->ctx);
-            for (Req* x : s->active) finish(s, x, GF_SCEN_FAILED);
-            s->active.clear();
-            return rc;
-        }
+    gf_forest_batch_stats sum{};
+    for (int k = 0; k < s->nlanes; ++k) {
+        gf_forest_batch_stats b;
+        gf::forest_batch_get_stats(s->lanes[k], &b);
+        sum.epochs += b.epochs;
+        sum.rounds += b.rounds;
+        sum.launches += b.launches;
+        sum.regrids += b.regrids;
+        sum.cell_updates += b.cell_updates;
+        sum.s_epoch += b.s_epoch;
+        sum.s_rounds += b.s_rounds;
+        sum.s_regrid += b.s_regrid;
     }
-    /* retire: a finished forest stays resident until released; its
-     * physics slot is free again */
-    still.clear();
-    for (Req* x : s->active) {
-        if (gf::forest_batch_running(x->f)) {
-            still.push_back(x);
-            continue;
-        }
-        gf::forest_batch_remove(s->batch, x->f);
-        finish(s, x, GF_SCEN_DONE);
-        s->free_slots.push_back(x->slot);
-        x->slot = -1;
-    }
-    s->active.swap(still);
-    gf_forest_batch_stats b;
-    gf::forest_batch_get_stats(s->batch, &b);
-    s->stats.epochs = b.epochs;
-    s->stats.rounds = b.rounds;
-    s->stats.launches = b.launches;
-    s->stats.regrids = b.regrids;
-    s->stats.cell_updates = b.cell_updates;
-    s->stats.s_epoch = b.s_epoch;
-    s->stats.s_rounds = b.s_rounds;
-    s->stats.s_regrid = b.s_regrid;
-    if (busy) *busy = !s->queue.empty() || !s->active.empty();
+    s->stats.epochs = sum.epochs;
+    s->stats.rounds = sum.rounds;
+    s->stats.launches = sum.launches;
+    s->stats.regrids = sum.regrids;
+    s->stats.cell_updates = sum.cell_updates;
+    s->stats.s_epoch = sum.s_epoch;
+    s->stats.s_rounds = sum.s_rounds;
+    s->stats.s_regrid = sum.s_regrid;
+    if (busy) *busy = !s->queue.empty() || !s->active.empty() || !s->joining[0].empty() || !s->joining[1].empty();
+    if (progress) *progress = moved;
     return GF_OK;
+}
+
+/* wait for every lane's iteration in flight (before forests are freed) */
+void drain(gf_fserver* s)
+{
+    for (int k = 0; k < s->nlanes; ++k) {
+        int done = 0;
+        if (s->lanes[k] && gf::forest_batch_inflight(s->lanes[k])) gf::forest_batch_test(s->lanes[k], 1, &done);
+    }
 }
 
 void loop_main(gf_fserver* s)
 {
     cudaSetDevice(s->device);
     while (s->running.load()) {
-        int busy = 0;
+        int busy = 0, moved = 0;
         {
             std::lock_guard<std::mutex> g(s->mu);
-            if (pump_locked(s, &busy)) busy = 0;
+            if (pump_locked(s, &busy, &moved)) busy = 0;
         }
         if (!busy) std::this_thread::sleep_for(std::chrono::microseconds(200));
+        else if (!moved) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
@@ -279,6 +361,8 @@ void gf_fserver_opts_default(gf_fserver_opts* o)
     o->hbm_budget = (size_t)64 << 30;
     o->max_active = 256;
     o->backfill = 1;
+    o->lane_cells = 1 << 18;
+    o->reserve_sms = 48;
 }
 
 int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out)
@@ -288,13 +372,26 @@ int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out)
     gf_fserver_opts o;
     if (opts) o = *opts;
     else gf_fserver_opts_default(&o);
-    if (o.max_active < 1 || o.max_active > GF_MAX_PHYS || o.hbm_budget == 0) return GF_ERR_ARG;
+    if (o.max_active < 1 || o.max_active > GF_MAX_PHYS || o.hbm_budget == 0 || o.lane_cells < 0 ||
+        o.reserve_sms < 0)
+        return GF_ERR_ARG;
     gf_fserver* s = new gf_fserver;
     s->device = device;
     s->o = o;
     s->t0 = Clock::now();
     int rc = gf_ctx_create(device, &s->ctx);
-    if (!rc) rc = gf::forest_batch_create(s->ctx, &s->batch);
+    if (!rc && o.lane_cells > 0) {
+        /* the small lane on the greatest stream priority; the large lane's
+         * update grid leaves reserve_sms SMs to it */
+        s->nlanes = 2;
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+        const int cap = (o.reserve_sms > 0 && nsm - o.reserve_sms > 0) ? nsm - o.reserve_sms : 0;
+        rc = gf::forest_batch_create(s->ctx, &s->lanes[0], 1, 0);
+        if (!rc) rc = gf::forest_batch_create(s->ctx, &s->lanes[1], 2, cap);
+    } else if (!rc) {
+        rc = gf::forest_batch_create(s->ctx, &s->lanes[0]);
+    }
     if (rc) {
         gf_fserver_destroy(s);
         return rc;
@@ -308,11 +405,13 @@ void gf_fserver_destroy(gf_fserver* s)
 {
     if (!s) return;
     gf_fserver_stop(s);
+    drain(s);
     for (auto& kv : s->all) {
         if (kv.second->f) gf_forest_destroy(kv.second->f);
         delete kv.second;
     }
-    if (s->batch) gf::forest_batch_destroy(s->batch);
+    for (int k = 0; k < 2; ++k)
+        if (s->lanes[k]) gf::forest_batch_destroy(s->lanes[k]);
     if (s->ctx) gf_ctx_destroy(s->ctx);
     delete s;
 }
@@ -341,6 +440,7 @@ int gf_fserver_submit(gf_fserver* s, const gf_forest_request* r, long long* id)
     x->info.t_done = -1;
     x->info.dt = r->initial_dt;
     x->info.footprint = bytes;
+    x->info.lane = -1;
     s->all[x->id] = x;
     s->queue.push_back(x);
     s->stats.submitted++;
@@ -385,9 +485,14 @@ int gf_fserver_wait(gf_fserver* s, long long id, double timeout_s)
         if (s->running.load()) {
             s->cv.wait_for(g, std::chrono::milliseconds(2));
         } else {
-            int busy = 0;
-            int rc = pump_locked(s, &busy);
+            int busy = 0, moved = 0;
+            int rc = pump_locked(s, &busy, &moved);
             if (rc) return rc;
+            if (!moved) {
+                g.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+                g.lock();
+            }
         }
     }
     return x->info.state == GF_SCEN_FAILED ? GF_ERR_STATE : GF_OK;
@@ -469,7 +574,7 @@ int gf_fserver_release(gf_fserver* s, long long id)
     if (!x) return sfail(s, GF_ERR_ARG, "unknown request id");
     if (x->info.state == GF_SCEN_QUEUED || x->info.state == GF_SCEN_ACTIVE)
         return sfail(s, GF_ERR_STATE, "the request is still running (cancel it first)");
-    drop(s, x);
+    drop(s, x); /* a finished forest is no member of any lane: nothing in flight reads it */
     return GF_OK;
 }
 

@@ -122,12 +122,20 @@ cudaError_t launch_gauge_sample(const gf_gauge_task* tasks, int n, const double*
  * dropped); each iteration runs about half a millisecond of rounds, then
  * regrids the members that wait for it. */
 struct ForestBatch;
-int forest_batch_create(gf_ctx* c, ForestBatch** out);
+/* stream_priority 0: the context's stream; 1 / 2: a stream of its own at the
+ * greatest / least priority. max_ctas > 0 caps the update grid. */
+int forest_batch_create(gf_ctx* c, ForestBatch** out, int stream_priority = 0, int max_ctas = 0);
 void forest_batch_destroy(ForestBatch* b);
 /* checks the forest and starts its outstyle-1 run at its current time */
 int forest_batch_add(ForestBatch* b, gf_forest* f, double t_final, int nout, double initial_dt,
                      double desired_cfl, double max_cfl);
 int forest_batch_iterate(ForestBatch* b, int* live);
+/* the same in two halves: launch (members and epoch fixed until the
+ * iteration is taken in), then test (wait = 1 blocks) and take it in */
+int forest_batch_launch(ForestBatch* b, int* live);
+int forest_batch_test(ForestBatch* b, int wait, int* done);
+bool forest_batch_inflight(const ForestBatch* b);
+int forest_batch_members(const ForestBatch* b);
 /* the forest leaves now (its run ended, or it is cancelled) */
 void forest_batch_remove(ForestBatch* b, gf_forest* f);
 bool forest_batch_running(const gf_forest* f);

@@ -294,7 +294,11 @@ class ForestServer:
     finished forest stays on the device until release()."""
 
     def __init__(self, device: int = 0, hbm_budget: int | None = None, max_active: int = 256,
-                 backfill: bool = True, exact: bool | None = None):
+                 backfill: bool = True, exact: bool | None = None, lane_cells: int | None = None,
+                 reserve_sms: int | None = None):
+        """lane_cells: forests with fewer cells after initial refinement batch
+        in the small lane (0: one lane); reserve_sms: SMs the large lane's
+        update leaves to the small lane."""
         self._lib = _lib.load()
         o = _lib.gf_fserver_opts()
         self._lib.gf_fserver_opts_default(C.byref(o))
@@ -302,6 +306,10 @@ class ForestServer:
             o.hbm_budget = int(hbm_budget)
         o.max_active = int(max_active)
         o.backfill = int(bool(backfill))
+        if lane_cells is not None:
+            o.lane_cells = int(lane_cells)
+        if reserve_sms is not None:
+            o.reserve_sms = int(reserve_sms)
         h = C.c_void_p()
         rc = self._lib.gf_fserver_create(int(device), C.byref(o), C.byref(h))
         if rc != 0:
@@ -411,7 +419,9 @@ class ForestServer:
     def stats(self) -> dict:
         st = _lib.gf_fserver_stats()
         self._check(self._lib.gf_fserver_stats_get(self.h, C.byref(st)))
-        return {k: getattr(st, k) for k, _ in _lib.gf_fserver_stats._fields_}
+        d = {k: getattr(st, k) for k, _ in _lib.gf_fserver_stats._fields_}
+        d["lane_admitted"] = list(st.lane_admitted)
+        return d
 
     def clock(self) -> float:
         return float(self._lib.gf_fserver_clock(self.h))

@@ -635,7 +635,10 @@ double gf_server_clock(const gf_server* s);
  *
  * Admission is by device footprint (gf_forest_footprint) against the
  * budget, first come first served (backfill: later requests that fit pass
- * a head that does not). A finished forest stays resident, counted against
+ * a head that does not). With two lanes, small and large forests batch
+ * separately on two streams: the small lane's short rounds run on the
+ * higher-priority stream and on SMs the large lane's update leaves free, so
+ * they are not held behind the large forests' updates. A finished forest stays resident, counted against
  * the budget, until gf_fserver_release; read it meanwhile through
  * gf_fserver_forest (or gf_fserver_download while the loop thread runs).
  * The caller keeps fields and topo alive until the request leaves QUEUED.
@@ -663,6 +666,10 @@ typedef struct gf_fserver_opts {
     size_t hbm_budget;     /* device bytes admitted and unreleased forests may hold */
     int max_active;        /* forests running at once (1..GF_MAX_PHYS)          */
     int backfill;
+    long long lane_cells;  /* > 0: forests with fewer cells after initial refinement
+                              run in a small lane (its own high-priority stream),
+                              the others in a large lane; 0: one lane            */
+    int reserve_sms;       /* the large lane's update leaves this many SMs free  */
 } gf_fserver_opts;
 
 typedef struct gf_forest_request_info {
@@ -673,10 +680,12 @@ typedef struct gf_forest_request_info {
     int npatch, npatch_max;
     size_t footprint;      /* bytes reserved at admission                       */
     size_t device_bytes;   /* bytes the forest holds (0 before admission)       */
+    int lane;              /* 0 small, 1 large (-1 before admission)            */
 } gf_forest_request_info;
 
 typedef struct gf_fserver_stats {
     long long submitted, admitted, done, failed;
+    long long lane_admitted[2];  /* per lane (small, large)                     */
     long long iterations, epochs, rounds, launches, regrids, cell_updates;
     double s_admit, s_epoch, s_rounds, s_regrid; /* host seconds per phase      */
     size_t bytes_in_use, bytes_peak;

@@ -50,6 +50,14 @@ def own_run(ctx, req: ForestRequest):
     return out
 
 
+def pump_until(srv, cond, timeout=60.0):
+    """pump() never waits on the device: pass until cond() holds."""
+    t_end = srv.clock() + timeout
+    while not cond():
+        srv.pump()
+        assert srv.clock() < t_end, "condition not reached"
+
+
 def check_same(srv, sid, want):
     P, q, st = want
     info = srv.poll(sid)
@@ -77,6 +85,26 @@ def test_mixed_requests_equal_their_own_runs(ctx):
         assert st["launches"] > 0 and st["epochs"] >= 2
 
 
+@pytest.mark.parametrize("lane_cells", [0, 4096])
+def test_lanes_give_the_same_results(ctx, lane_cells):
+    """One lane on the context's stream, or small and large forests in two
+    lanes that overlap on the device (the large lane's update on fewer
+    SMs): every result equals its own run."""
+    reqs = [request(**kw) for kw in MIX] + [request(m=8, seed=11, regrid=2)]
+    want = [own_run(ctx, r) for r in reqs]
+    with ForestServer(lane_cells=lane_cells, reserve_sms=24) as srv:
+        ids = [srv.submit(r) for r in reqs]
+        srv.run_until_idle()
+        for sid, w in zip(ids, want):
+            check_same(srv, sid, w)
+        lanes = [srv.poll(s)["lane"] for s in ids]
+        st = srv.stats()
+        if lane_cells:
+            assert set(lanes) == {0, 1} and st["lane_admitted"] == [lanes.count(0), lanes.count(1)]
+        else:
+            assert set(lanes) == {0} and st["lane_admitted"] == [len(ids), 0]
+
+
 def test_arrivals_join_a_running_batch(ctx):
     """Requests submitted while others run: joining mid-run (and the graph
     re-captures that follow) leaves every result unchanged."""
@@ -85,11 +113,10 @@ def test_arrivals_join_a_running_batch(ctx):
     want = [own_run(ctx, r) for r in reqs]
     with ForestServer() as srv:
         ids = [srv.submit(reqs[0])]
-        for _ in range(3):
-            srv.pump()
-        assert srv.poll(ids[0])["state"] == "active" and srv.poll(ids[0])["steps"] > 0
+        pump_until(srv, lambda: srv.poll(ids[0])["steps"] > 0)
+        assert srv.poll(ids[0])["state"] == "active"
         ids.append(srv.submit(reqs[1]))
-        srv.pump()
+        pump_until(srv, lambda: srv.poll(ids[1])["steps"] > 0)
         ids.append(srv.submit(reqs[2]))
         srv.run_until_idle()
         for sid, w in zip(ids, want):
@@ -137,10 +164,10 @@ def test_cancel_and_refusals(ctx):
         assert srv.poll(b)["state"] == "queued"   # max_active = 1
         srv.wait(a)
         check_same(srv, a, want)
-        srv.pump()
+        pump_until(srv, lambda: srv.poll(b)["steps"] > 0)
         assert srv.poll(b)["state"] == "active"
         srv.cancel(b)                          # running
-        srv.pump()
+        pump_until(srv, lambda: srv.poll(b)["state"] != "active")
         assert srv.poll(b)["state"] == "cancelled" and srv.poll(c)["state"] == "cancelled"
         assert srv.stats()["bytes_in_use"] == srv.poll(a)["footprint"]
         bad = request()
