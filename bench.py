@@ -855,7 +855,8 @@ def fserved_leg(args, dev=0):
     server running its request loop on its own thread. Reports throughput,
     p50/p99 latency (submit to done), the slowdown of a sample against its
     isolated latency, and that the sample's results equal the isolated runs
-    bit for bit; the sample also runs through Forest.run one by one."""
+    bit for bit; the calibration forests also run through Forest.run one by
+    one (the same work as the saturated pass)."""
     import geoflood_gb300 as gf
     from geoflood_gb300 import synth
     from geoflood_gb300.serve import ForestRequest, ForestServer, Hydrograph
@@ -899,59 +900,76 @@ def fserved_leg(args, dev=0):
     for i in cal:
         srv.release(i)
     est_work = float(np.mean([i["cell_updates"] for i in cal_info]))
-    rate = args.fserved_rate or 0.8 * cap / est_work
-    gaps = np.random.default_rng(SEED + 6).exponential(1.0 / rate, n)
-    arrivals = np.cumsum(gaps) - gaps[0]
+    sat_work = sum(i["cell_updates"] for i in cal_info)
+    sat_s = max(i["t_done"] for i in cal_info) - t0
     order = np.argsort(targets)
     sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 6)})
     reqs = [req(sp).prepare() for sp in specs]   # raster blocks built before the stream
-    st0 = srv.stats()
-    t_start = srv.clock()
-    ids, infos, outs, late = {}, {}, {}, 0
-    for k in range(n):
-        t_arr = t_start + arrivals[k]
-        while srv.clock() < t_arr:
-            time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
-        late += srv.clock() - t_arr > 0.01
-        ids[k] = srv.submit(reqs[k])
-        for j in list(ids):
-            if j not in infos:
-                i = srv.poll(ids[j])
-                if i["state"] in ("done", "failed", "cancelled"):
-                    infos[j] = i
-    for k in range(n):
-        if k not in infos:
-            infos[k] = srv.wait(ids[k], timeout=3600)
-    for k in range(n):
-        if k in sample and infos[k]["state"] == "done":
-            outs[k] = srv.download(ids[k])
-        srv.release(ids[k])
-    st1 = srv.stats()
-    t_end = max(i["t_done"] for i in infos.values())
-    failed = sum(1 for i in infos.values() if i["state"] != "done")
-    lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
-    work = sum(i["cell_updates"] for i in infos.values())
-    # -- isolated re-runs of the sample: latency alone, same bits
-    slow, same, detail = [], True, []
+
+    def stream(rate, seed):
+        """Poisson arrivals at `rate` forests/s; every forest waited for."""
+        gaps = np.random.default_rng(seed).exponential(1.0 / rate, n)
+        arrivals = np.cumsum(gaps) - gaps[0]
+        st0 = srv.stats()
+        t_start = srv.clock()
+        ids, late = {}, 0
+        for k in range(n):
+            t_arr = t_start + arrivals[k]
+            while srv.clock() < t_arr:
+                time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
+            late += srv.clock() - t_arr > 0.01
+            ids[k] = srv.submit(reqs[k])
+        infos = {k: srv.wait(ids[k], timeout=3600) for k in range(n)}
+        outs = {k: srv.download(ids[k]) for k in sample if infos[k]["state"] == "done"}
+        for k in range(n):
+            srv.release(ids[k])
+        st1 = srv.stats()
+        t_end = max(i["t_done"] for i in infos.values())
+        lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
+        work = sum(i["cell_updates"] for i in infos.values())
+        return {"infos": infos, "outs": outs, "late": late, "t_start": t_start, "t_end": t_end,
+                "lat": lat, "work": work, "st0": st0, "st1": st1, "rate": rate,
+                "failed": sum(1 for i in infos.values() if i["state"] != "done")}
+
+    rate = args.fserved_rate or 0.8 * cap / est_work
+    main_run = stream(rate, SEED + 6)
+    low_run = stream(0.5 * cap / est_work, SEED + 7)
+    # -- isolated re-runs of the sample: latency alone, same bits as in both streams
+    iso = {}
+    same = True
     for k in sample:
         sid = srv.submit(reqs[k])
         ik = srv.wait(sid, timeout=600)
         p, q, _ = srv.download(sid)
         srv.release(sid)
-        t_iso = ik["t_done"] - ik["t_submit"]
-        t_mix = infos[k]["t_done"] - infos[k]["t_submit"]
-        slow.append(t_mix / t_iso)
-        same &= (k in outs and np.array_equal(p, outs[k][0]) and np.array_equal(q, outs[k][1])
-                 and ik["steps"] == infos[k]["steps"])
-        detail.append({"mx": specs[k]["mx"], "npatch_max": ik["npatch_max"], "steps": ik["steps"],
-                       "isolated_s": t_iso, "mixed_s": t_mix,
-                       "queued_s": infos[k]["t_admit"] - infos[k]["t_submit"]})
+        iso[k] = ik
+        for run in (main_run, low_run):
+            o = run["outs"].get(k)
+            same &= (o is not None and np.array_equal(p, o[0]) and np.array_equal(q, o[1])
+                     and ik["steps"] == run["infos"][k]["steps"])
+
+    def slowdowns(run):
+        sl = [(run["infos"][k]["t_done"] - run["infos"][k]["t_submit"])
+              / (iso[k]["t_done"] - iso[k]["t_submit"]) for k in sample]
+        return {"p50": float(np.percentile(sl, 50)), "p99": float(np.percentile(sl, 99)),
+                "max": float(max(sl)), "sample": len(sample)}
+
+    detail = [{"mx": specs[k]["mx"], "npatch_max": iso[k]["npatch_max"], "steps": iso[k]["steps"],
+               "isolated_s": iso[k]["t_done"] - iso[k]["t_submit"],
+               "mixed_s": main_run["infos"][k]["t_done"] - main_run["infos"][k]["t_submit"],
+               "mixed_50pct_s": low_run["infos"][k]["t_done"] - low_run["infos"][k]["t_submit"],
+               "lane": iso[k]["lane"]} for k in sample]
+    infos, lat, work = main_run["infos"], main_run["lat"], main_run["work"]
+    t_start, t_end, late, failed = main_run["t_start"], main_run["t_end"], main_run["late"], main_run["failed"]
+    st0, st1 = main_run["st0"], main_run["st1"]
+    slow = slowdowns(main_run)
+    slow["detail"] = detail
     srv.stop()
     srv.close()
-    # -- the sample through Forest.run, one after another
+    # -- the calibration forests through Forest.run, one after another
     ctx = gf.Context(dev)
     w1, s1 = 0, 0.0
-    for k in sample:
+    for k in range(ncal):
         sp = specs[k]
         ctx.set_phys(1, sp["phys"])
         F = gf.Forest(ctx, sp["mx"], sp["nbx"], sp["nby"], sp["minlevel"], sp["maxlevel"], sp["dx0"],
@@ -972,13 +990,20 @@ def fserved_leg(args, dev=0):
                     "every 4 steps; Poisson arrivals at 80 % of the calibrated capacity",
         "value": served_rate, "unit": METRIC, "forests": n, "failed": failed,
         "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-        "slowdown_vs_isolated": {"p50": float(np.percentile(slow, 50)), "p99": float(np.percentile(slow, 99)),
-                                 "max": float(max(slow)), "sample": len(sample), "detail": detail},
+        "slowdown_vs_isolated": slow,
         "alone_equals_mix": bool(same),
+        "at_50pct_load": {"value": low_run["work"] / (low_run["t_end"] - low_run["t_start"]), "unit": METRIC,
+                          "arrival_rate_per_s": low_run["rate"],
+                          "p50_latency_s": float(np.percentile(low_run["lat"], 50)),
+                          "p99_latency_s": float(np.percentile(low_run["lat"], 99)),
+                          "slowdown_vs_isolated": slowdowns(low_run), "failed": low_run["failed"]},
+        "saturated": {"value": sat_work / sat_s, "unit": METRIC, "forests": ncal, "seconds": sat_s,
+                      "note": "the first forests of the stream submitted at once, until all are done"},
         "one_by_one": {"value": w1 / s1, "unit": METRIC, "seconds": s1,
-                       "note": "the sample through Forest.run (init included), one after another"},
-        "vs_one_by_one": served_rate / (w1 / s1),
-        "capacity": {"value": cap, "unit": METRIC, "forests": ncal, "window_s": half[0] - t0},
+                       "note": "the same forests through Forest.run (init included), one after another"},
+        "saturated_vs_one_by_one": (sat_work / sat_s) / (w1 / s1),
+        "capacity": {"value": cap, "unit": METRIC, "forests": ncal, "window_s": half[0] - t0,
+                     "note": "saturated, until half of the forests are done; sets the arrival rate"},
         "arrival_rate_per_s": rate, "late_submissions": int(late), "stream_seconds": t_end - t_start,
         "cell_updates": work, "iterations": st1["iterations"] - st0["iterations"],
         "epochs": st1["epochs"] - st0["epochs"], "rounds": st1["rounds"] - st0["rounds"],

@@ -2465,6 +2465,13 @@ int gf::forest_batch_test(ForestBatch* b, int wait, int* done)
 
 bool gf::forest_batch_inflight(const ForestBatch* b) { return b->R.inflight; }
 
+void gf::forest_batch_set_max_ctas(ForestBatch* b, int max_ctas)
+{
+    if (b->R.B.max_ctas == max_ctas) return;
+    b->R.B.max_ctas = max_ctas;
+    b->R.rebuild = true;
+}
+
 int gf::forest_batch_members(const ForestBatch* b) { return (int)b->R.B.fs.size(); }
 
 void gf::forest_batch_remove(ForestBatch* b, gf_forest* f)

@@ -64,6 +64,7 @@ struct gf_fserver {
     gf_fserver_opts o{};
     gf_ctx* ctx = nullptr;
     int nlanes = 1;
+    int cap_large = 0; /* the large lane's update grid while the small lane has members */
     gf::ForestBatch* lanes[2] = {nullptr, nullptr};
     std::vector<Req*> joining[2]; /* built forests waiting for their lane to be idle */
     Clock::time_point t0;
@@ -290,6 +291,11 @@ int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
         if (gf::forest_batch_inflight(s->lanes[k])) continue;
         if (!s->joining[k].empty()) join(s, k);
         if (!gf::forest_batch_members(s->lanes[k])) continue;
+        if (k == 1) {
+            /* the large lane leaves SMs free only while small forests run */
+            const bool small = gf::forest_batch_members(s->lanes[0]) > 0 || !s->joining[0].empty();
+            gf::forest_batch_set_max_ctas(s->lanes[1], small ? s->cap_large : 0);
+        }
         int live = 0;
         int rc = gf::forest_batch_launch(s->lanes[k], &live);
         if (rc) return fail_all(s, rc);
@@ -387,8 +393,9 @@ int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out)
         int nsm = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
         const int cap = (o.reserve_sms > 0 && nsm - o.reserve_sms > 0) ? nsm - o.reserve_sms : 0;
+        s->cap_large = cap;
         rc = gf::forest_batch_create(s->ctx, &s->lanes[0], 1, 0);
-        if (!rc) rc = gf::forest_batch_create(s->ctx, &s->lanes[1], 2, cap);
+        if (!rc) rc = gf::forest_batch_create(s->ctx, &s->lanes[1], 2, 0);
     } else if (!rc) {
         rc = gf::forest_batch_create(s->ctx, &s->lanes[0]);
     }

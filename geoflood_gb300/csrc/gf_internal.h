@@ -135,6 +135,8 @@ int forest_batch_iterate(ForestBatch* b, int* live);
 int forest_batch_launch(ForestBatch* b, int* live);
 int forest_batch_test(ForestBatch* b, int wait, int* done);
 bool forest_batch_inflight(const ForestBatch* b);
+/* between iterations: a new update grid cap (the epoch is captured again) */
+void forest_batch_set_max_ctas(ForestBatch* b, int max_ctas);
 int forest_batch_members(const ForestBatch* b);
 /* the forest leaves now (its run ended, or it is cancelled) */
 void forest_batch_remove(ForestBatch* b, gf_forest* f);
