@@ -260,83 +260,93 @@ def served_stream(args):
     rate = 0.8 * cap / est_work
     gaps = np.random.default_rng(SERVED_SEED + 7).exponential(1.0 / rate, n)
     arrivals = np.cumsum(gaps) - gaps[0]
-    order = np.argsort(cells)
-    sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 12)})
+    # size-stratified sample from the first half (which both loads run)
+    order = np.argsort(cells[: n // 2])
+    sample = sorted({int(order[int(round(f * (n // 2 - 1)))]) for f in np.linspace(0.0, 1.0, 12)})
 
-    # -- the stream: producer threads keep generated scenarios ahead of the
-    #    arrivals (numpy releases the GIL in the array work)
-    ready, cond, nxt, taken = {}, threading.Condition(), [0], [0]
-    ahead = 48
+    def run_stream(arrivals, count):
+        """The first `count` scenarios at the given arrival times: producer
+        threads keep generated scenarios ahead of the arrivals (numpy
+        releases the GIL in the array work)."""
+        ready, cond, nxt, taken = {}, threading.Condition(), [0], [0]
+        ahead = 48
 
-    def producer():
-        while True:
+        def producer():
+            while True:
+                with cond:
+                    while nxt[0] < count and nxt[0] >= taken[0] + ahead:
+                        cond.wait()
+                    if nxt[0] >= count:
+                        return
+                    k = nxt[0]
+                    nxt[0] += 1
+                item = make(k)
+                with cond:
+                    ready[k] = item
+                    cond.notify_all()
+
+        def take(k):
             with cond:
-                while nxt[0] < n and nxt[0] >= taken[0] + ahead:
+                while k not in ready:
                     cond.wait()
-                if nxt[0] >= n:
-                    return
-                k = nxt[0]
-                nxt[0] += 1
-            item = make(k)
-            with cond:
-                ready[k] = item
+                taken[0] = k + 1
                 cond.notify_all()
+                return ready.pop(k)
 
-    def take(k):
+        workers = [threading.Thread(target=producer, daemon=True)
+                   for _ in range(max(2, min(8, (os.cpu_count() or 4) // 2)))]
+        for w in workers:
+            w.start()
         with cond:
-            while k not in ready:
-                cond.wait()
-            taken[0] = k + 1
-            cond.notify_all()
-            return ready.pop(k)
+            while len(ready) < min(ahead, count) and any(w.is_alive() for w in workers):
+                cond.wait(0.05)
+        st0 = srv.stats()
+        t_start = srv.clock()
+        ids, pending, infos, outs, late, mx_of = {}, [], {}, {}, 0, {}
 
-    workers = [threading.Thread(target=producer, daemon=True)
-               for _ in range(max(2, min(8, (os.cpu_count() or 4) // 2)))]
-    for w in workers:
-        w.start()
-    with cond:
-        while len(ready) < min(ahead, n) and any(w.is_alive() for w in workers):
-            cond.wait(0.05)
-    st0 = srv.stats()
-    t_start = srv.clock()
-    ids, pending, infos, outs, late, mx_of = {}, [], {}, {}, 0, {}
+        def sweep(block=False):
+            for k in list(pending):
+                info = srv.wait(ids[k], timeout=3600) if block else srv.poll(ids[k])
+                if info["state"] in ("done", "failed", "cancelled"):
+                    infos[k] = info
+                    pending.remove(k)
+                    if k not in sample:
+                        srv.release(ids[k])
 
-    def sweep(block=False):
-        for k in list(pending):
-            info = srv.wait(ids[k], timeout=3600) if block else srv.poll(ids[k])
-            if info["state"] in ("done", "failed", "cancelled"):
-                infos[k] = info
-                pending.remove(k)
-                if k not in sample:
-                    srv.release(ids[k])
+        for k in range(count):
+            sc, qo = take(k)
+            t_arr = t_start + arrivals[k]
+            while srv.clock() < t_arr:
+                time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
+            if srv.clock() - t_arr > 0.01:
+                late += 1
+            ids[k] = srv.submit(sc, qo)
+            mx_of[k] = sc.mx
+            pending.append(k)
+            if k in sample:
+                outs[k] = qo
+            del sc, qo
+            sweep()
+        for w in workers:
+            w.join()
+        sweep(block=True)
+        for k in sample:
+            if k in ids:
+                srv.release(ids[k])
+        return infos, outs, late, mx_of, st0, srv.stats(), t_start, max(i["t_done"] for i in infos.values())
 
-    for i in range(n):
-        k = i
-        sc, qo = take(k)
-        t_arr = t_start + arrivals[i]
-        while srv.clock() < t_arr:
-            time.sleep(min(0.002, max(t_arr - srv.clock(), 0.0)))
-        if srv.clock() - t_arr > 0.01:
-            late += 1
-        ids[k] = srv.submit(sc, qo)
-        mx_of[k] = sc.mx
-        pending.append(k)
-        if k in sample:
-            outs[k] = qo
-        del sc, qo
-        sweep()
-    for w in workers:
-        w.join()
-    sweep(block=True)
-    t_end = max(i["t_done"] for i in infos.values())
-    st1 = srv.stats()
+    infos, outs, late, mx_of, st0, st1, t_start, t_end = run_stream(arrivals, n)
+    # the first half of the stream again at 50 % load (arrival gaps x 1.6)
+    n_low = n // 2
+    low = run_stream(arrivals[:n_low] * 1.6, n_low)
     failed = sum(1 for i in infos.values() if i["state"] != "done")
     lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
     work = sum(i["cell_updates"] for i in infos.values())
     served_rate = work / (t_end - t_start)
 
     # -- isolated re-runs of a size-stratified sample: latency alone, same bits
-    slow, same, detail = [], True, []
+    slow, slow_low, same, detail = [], [], True, []
+    infos_low, outs_low = low[0], low[1]
     for k in sample:
         sc, qo = make(k)
         sid = srv.submit(sc, qo)
@@ -345,12 +355,16 @@ def served_stream(args):
         t_mix = infos[k]["t_done"] - infos[k]["t_submit"]
         slow.append(t_mix / t_iso)
         same &= bool(np.array_equal(qo, outs[k])) and ik["steps"] == infos[k]["steps"]
+        if k in infos_low:
+            slow_low.append((infos_low[k]["t_done"] - infos_low[k]["t_submit"]) / t_iso)
+            same &= bool(np.array_equal(qo, outs_low[k]))
         detail.append({"cells": int(sc.cells), "mx": sc.mx, "lane": ik["lane"], "steps": ik["steps"],
                        "isolated_s": t_iso, "mixed_s": t_mix,
                        "queued_s": infos[k]["t_admit"] - infos[k]["t_submit"]})
         srv.release(sid)
     srv.stop()
     srv.close()
+    lat_low = np.array([i["t_done"] - i["t_submit"] for i in infos_low.values()])
 
     # -- the plain per-patch drop-in on the same work mix
     ctx = gf.Context(dev)
@@ -378,6 +392,13 @@ def served_stream(args):
                                  "p99": float(np.percentile(slow, 99)), "max": float(max(slow)),
                                  "sample": len(sample), "detail": detail},
         "alone_equals_mix": same,
+        "at_50pct_load": {"scenarios": n_low, "arrival_rate_per_s": rate / 1.6,
+                          "p50_latency_s": float(np.percentile(lat_low, 50)),
+                          "p99_latency_s": float(np.percentile(lat_low, 99)),
+                          "slowdown_vs_isolated": {"p50": float(np.percentile(slow_low, 50)),
+                                                   "p99": float(np.percentile(slow_low, 99)),
+                                                   "max": float(max(slow_low)), "sample": len(slow_low)},
+                          "note": "the first half of the stream, arrival gaps x 1.6"},
         "plain_per_patch": {"value": plain_rate, "unit": METRIC,
                             "per_mx": {str(k): v for k, v in rate_mx.items()},
                             "note": "gf_patch_update per patch with host buffers, weighted by "
