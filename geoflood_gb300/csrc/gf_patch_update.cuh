@@ -385,10 +385,24 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 s[mw] = wc[mw];
                 fw[mw][0] = wc[3 + 3 * mw]; fw[mw][1] = wc[4 + 3 * mw]; fw[mw][2] = wc[5 + 3 * mw];
             }
-            /* fluctuations from the unlimited f-waves (rpn2_geoclaw.f:359-376) */
+            /* fluctuations from the unlimited f-waves (rpn2_geoclaw.f:359-376).
+             * The middle f-wave is (0, beta2, 0) in local order: the contracted
+             * build skips its two zero components (adding +0.0 to a sum that
+             * starts at +0.0 changes no bits). */
             double amdq[3] = {0.0, 0.0, 0.0}, apdq[3] = {0.0, 0.0, 0.0};
 #pragma unroll
             for (int mw = 0; mw < 3; ++mw) {
+                if (FAST && mw == 1) {
+                    if (d_ltz<FAST>(s[1])) {
+                        amdq[1] += fw[1][1];
+                    } else if (d_gtz<FAST>(s[1])) {
+                        apdq[1] += fw[1][1];
+                    } else {
+                        amdq[1] += 0.5 * fw[1][1];
+                        apdq[1] += 0.5 * fw[1][1];
+                    }
+                    continue;
+                }
                 if (d_ltz<FAST>(s[mw])) {
                     amdq[0] += fw[mw][0]; amdq[1] += fw[mw][1]; amdq[2] += fw[mw][2];
                 } else if (d_gtz<FAST>(s[mw])) {
@@ -407,6 +421,23 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
 #pragma unroll
                 for (int mw = 0; mw < 3; ++mw) {
                     const double* fa = fw[mw];
+                    if (FAST && mw == 1) {
+                        /* the middle wave has one non-zero component: its norm
+                         * and projections are single products */
+                        double lim = 1.0;
+                        const double a = fa[1];
+                        if (P.mthlim[1] != 0) {
+                            const double wnorm2 = a * a;
+                            if (!d_eqz<FAST>(wnorm2)) {
+                                const double dotl = (wl + 3 + 3)[1] * a;
+                                const double dotr = a * (wr + 3 + 3)[1];
+                                lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[1]) ? dotl : dotr, P.mthlim[1]);
+                            }
+                        }
+                        const double fac = copysign(1.0, s[1]) * (1.0 - fabs(s[1]) * dtdn);
+                        cq[1] += (fac * lim) * a;
+                        continue;
+                    }
                     double lim = 1.0;
                     if (P.mthlim[mw] != 0) {
                         /* dot products in the global (h, hu, hv) order */
