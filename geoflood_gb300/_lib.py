@@ -285,6 +285,7 @@ SIGNATURES = [
     ("gf_server_stats_get", C.c_int, [_vp, C.POINTER(gf_server_stats)]),
     ("gf_server_clock", C.c_double, [_vp]),
     ("gf_forest_footprint", C.c_size_t, [C.POINTER(gf_forest_opts)]),
+    ("gf_probe_bounded_wait", C.c_int, [C.c_int, C.c_int, C.c_uint, C.POINTER(C.c_int), _dp]),
     ("gf_fserver_opts_default", None, [C.POINTER(gf_fserver_opts)]),
     ("gf_fserver_create", C.c_int, [C.c_int, C.POINTER(gf_fserver_opts), C.POINTER(_vp)]),
     ("gf_fserver_destroy", None, [_vp]),

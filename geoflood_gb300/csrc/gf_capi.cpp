@@ -251,6 +251,7 @@ int gf_ctx_create(int device, gf_ctx** out)
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMalloc(&c->d_gdt, sizeof(double) * 64);
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_gdt, sizeof(double) * 64);
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(DevStatus));
     if (e != cudaSuccess) {
         gf_ctx_destroy(c);
         return e == cudaErrorMemoryAllocation ? GF_ERR_NOMEM : GF_ERR_CUDA;
@@ -1114,7 +1115,10 @@ extern "C" int gf_autotune(gf_ctx* c, int reps, gf_tile_result* out)
             gf::tile_shape(m, v, &R.threads[v], &R.band[v]);
             for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
                 const int n = pass == 0 ? np : nsmall;
-                e = gf::launch_patch_update_tile(m, v, dw, n, c->d_phys, 0.02, nullptr, nullptr, 1, dcfl,
+                /* a set error flag makes the kernel skip its items */
+                e = cudaMemsetAsync(c->d_status, 0, sizeof(DevStatus), c->stream);
+                if (e == cudaSuccess)
+                    e = gf::launch_patch_update_tile(m, v, dw, n, c->d_phys, 0.02, nullptr, nullptr, 1, dcfl,
                                                  &c->d_status->gmax, &c->d_status->err, c->stream, 0);
                 if (e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
                 for (int r = 0; r < reps && e == cudaSuccess; ++r)

@@ -74,6 +74,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
+/* Polls of a wait before it gives up: a poll of a phase that does not
+ * complete suspends about 3.8 us on GB300 (gf_probe_bounded_wait), so the
+ * limit is about half a second, far above any staging copy. */
+constexpr uint32_t kWaitPolls = 1u << 17;
+
 /* Bounded wait on phase `parity`; returns false if the limit ran out. */
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_iter)
 {
@@ -595,6 +600,10 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
     const gf_phys P = phys_table[wk.phys];
     const double g = P.grav, drytol = P.dry_tolerance;
 
+    /* after a wait of this launch (or an earlier one of the same step) gave
+     * up, the step has failed: later items leave at once */
+    if (__syncthreads_or(threadIdx.x == 0 && err && *reinterpret_cast<volatile int*>(err) != 0)) return false;
+
     /* ---- stage the patch (h, hu, hv planes and b) with bulk copies ---- */
     if (threadIdx.x == 0) {
         mbar_expect_tx(bar, (uint32_t)(4 * S * sizeof(double)));
@@ -603,9 +612,9 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
     }
     const uint32_t ph = phase;
     phase ^= 1u;
-    if (!__syncthreads_and(mbar_wait(bar, ph, 1u << 22))) {
+    if (!__syncthreads_and(mbar_wait(bar, ph, kWaitPolls))) {
         if (threadIdx.x == 0) atomicExch(err, 1);
-        mbar_wait(bar, ph, 1u << 22); /* let any copy in flight land */
+        mbar_wait(bar, ph, kWaitPolls); /* let any copy in flight land */
         return false;
     }
 

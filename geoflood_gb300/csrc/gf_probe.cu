@@ -7,8 +7,22 @@
 #include <cuda_runtime.h>
 
 #include "geoflood_gb300.h"
+#include "gf_patch_update.cuh"
 
 namespace {
+
+/* One CTA waits, with the bounded try_wait loop of the patch kernels, on
+ * phase 0 of an mbarrier that expects one arrival: thread 0 arrives first
+ * (arrive = 1) or nothing ever arrives (arrive = 0). */
+__global__ void __launch_bounds__(32) bounded_wait_kernel(int arrive, uint32_t max_iter, int* status)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) gf::mbar_init(&bar, 1);
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) gf::mbar_expect_tx(&bar, 0);
+    const bool ok = __syncthreads_and(gf::mbar_wait(&bar, 0, max_iter));
+    if (threadIdx.x == 0) status[0] = ok ? 0 : 1;
+}
 
 constexpr int kIters = 2048;
 
@@ -86,4 +100,31 @@ extern "C" int gf_measure_fp64_rates(int device, double* rates)
     cudaFree(in);
     cudaFree(out);
     return e == cudaSuccess ? GF_OK : GF_ERR_CUDA;
+}
+
+extern "C" int gf_probe_bounded_wait(int device, int arrive, unsigned int max_iter, int* timed_out, double* ms)
+{
+    if (!timed_out || max_iter == 0) return GF_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return GF_ERR_CUDA;
+    int* d = nullptr;
+    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return GF_ERR_NOMEM;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int h = -1;
+    cudaMemset(d, 0xff, sizeof(int));
+    cudaEventRecord(e0);
+    bounded_wait_kernel<<<1, 32>>>(arrive, max_iter, d);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) return GF_ERR_CUDA;
+    *timed_out = h;
+    if (ms) *ms = t;
+    return GF_OK;
 }

@@ -749,6 +749,14 @@ int gf_tile_set(int mx, int goal, int variant);
  * The patch update is FP64-issue bound; this is its roofline denominator.
  * No reference counterpart (measurement support). */
 int gf_measure_fp64_rates(int device, double* rates);
+/* Failure detection of the device waits: every wait in this library's
+ * kernels (the patch staging copies' mbarrier) polls at most a fixed number
+ * of times, then records an error the host turns into GF_ERR_DEVICE, and
+ * the kernel returns. This runs that bounded wait in one CTA on a barrier
+ * phase that nothing completes (arrive = 0: *timed_out = 1) or that the CTA
+ * completes itself (arrive = 1: *timed_out = 0), for at most max_iter polls;
+ * *ms (nullable) is the kernel's duration. The context stays usable. */
+int gf_probe_bounded_wait(int device, int arrive, unsigned int max_iter, int* timed_out, double* ms);
 
 #ifdef __cplusplus
 }
