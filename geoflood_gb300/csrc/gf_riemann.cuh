@@ -225,7 +225,20 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double rs12 = (FAST && !sonic) ? gf_rcp(s1s2bar) : 0.0;
     double deldelh = sonic ? -delb : (FAST ? delb * g * hbar * rs12 : delb * g * hbar / s1s2bar);
     const double hsd = hstarHLL * (sE2 - sE1);
-    if (d_lt<FAST>(sE1, -crit) && d_gt<FAST>(sE2, crit)) {
+    if (FAST) {
+        /* The bounds hsd / sE clamp rarely: compare hsd with deldelh * sE (the
+         * sign of sE is known in each branch) and divide only to clamp. */
+        if (d_lt<FAST>(sE1, -crit) && d_gt<FAST>(sE2, crit)) {
+            if (d_lt<FAST>(hsd, deldelh * sE2)) deldelh = d_div<FAST>(hsd, sE2); /* min, sE2 > 0 */
+            if (d_lt<FAST>(hsd, deldelh * sE1)) deldelh = d_div<FAST>(hsd, sE1); /* max, sE1 < 0 */
+        } else if (d_ge<FAST>(sE1, crit)) {
+            if (d_lt<FAST>(hsd, deldelh * sE1)) deldelh = d_div<FAST>(hsd, sE1); /* min, sE1 > 0 */
+            deldelh = d_max<FAST>(deldelh, -hL);
+        } else if (d_le<FAST>(sE2, -crit)) {
+            deldelh = d_min<FAST>(deldelh, hR);
+            if (d_lt<FAST>(hsd, deldelh * sE2)) deldelh = d_div<FAST>(hsd, sE2); /* max, sE2 < 0 */
+        }
+    } else if (d_lt<FAST>(sE1, -crit) && d_gt<FAST>(sE2, crit)) {
         deldelh = d_min<FAST>(deldelh, d_div<FAST>(hsd, sE2));
         deldelh = d_max<FAST>(deldelh, d_div<FAST>(hsd, sE1));
     } else if (d_ge<FAST>(sE1, crit)) {
