@@ -138,12 +138,16 @@ struct Smem {
     static constexpr int OFF_BAR = OFF_RED + 64;                    /* 1 x u64     */
     /* integer region: class counts per band and face lists (u16) */
     static constexpr int OFF_INT = OFF_BAR + 2;
-    static constexpr int CNT_INTS = NBAND * 2 * 3 * 2;              /* [band][A|B][class][count|pos] */
+    static constexpr int NCLS = 5;                                  /* face classes, see build_lists */
+    static constexpr int CNT_INTS = NBAND * 2 * NCLS * 2;           /* [band][A|B][class][count|pos] */
     static constexpr int LIST_A = G::NSLICE * G::FA;
     static constexpr int LIST_B = G::NSLICE * G::FB;
     static constexpr size_t INT_BYTES = ((CNT_INTS * 4 + (LIST_A + LIST_B) * 2) + 15) / 16 * 16;
     static constexpr size_t OFF_WET_BYTES = (size_t)OFF_INT * 8 + INT_BYTES;
-    static constexpr size_t BYTES = OFF_WET_BYTES + ((G::S + 15) / 16) * 16;
+    /* class of each normal-solve face of the sweep (u8), kept between the
+     * count and place passes */
+    static constexpr size_t OFF_FCLS_BYTES = OFF_WET_BYTES + ((G::S + 15) / 16) * 16;
+    static constexpr size_t BYTES = OFF_FCLS_BYTES + ((LIST_A + 15) / 16) * 16;
 };
 
 /* Load the cell view for a face sweep in direction DIR (0 = x, 1 = y). */
@@ -173,56 +177,81 @@ __device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned ch
 }
 
 /* Build, for every band of one sweep direction, the normal-solve faces
- * (list A) and the limited faces (list B) ordered by class: both cells wet,
- * one wet, both dry. Two passes (count, then place) over all faces. */
+ * (list A) and the limited faces (list B) ordered by class, so that a warp
+ * runs one code path. Classes: 0..2 both cells wet, by the wave structure
+ * riemanntype will find (0 two rarefactions, 1 two shocks, 2 a shock and a
+ * rarefaction; list B puts all wet pairs in class 0); 3 one cell wet; 4 both
+ * dry. The wave structure is estimated without a square root (F_max <= 0 as
+ * delu <= 0 and delu^2 hmin hmax >= (hmax - hmin)^2 g (hmin + hmax) / 2); a
+ * borderline face in the neighbouring class only costs divergence, since
+ * every face's solve is the same computation wherever it is listed. Two
+ * passes (count, then place) over all faces. */
 template <int M, int NT, int RB, int DIR, bool EXACT>
-__device__ __forceinline__ void build_lists(const unsigned char* wet, int* cnt, uint16_t* la,
-                                            uint16_t* lb)
+__device__ __forceinline__ void build_lists(const double* sm, const unsigned char* wet, int* cnt, uint16_t* la,
+                                            uint16_t* lb, double g)
 {
     using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
     constexpr int N = G::N;
+    constexpr int NC = L::NCLS;
+    unsigned char* fcls = const_cast<unsigned char*>(reinterpret_cast<const unsigned char*>(sm)) + L::OFF_FCLS_BYTES;
     auto cidx = [](int n, int t) -> int {
         return DIR == 0 ? (t + 1) * N + (n + 1) : (n + 1) * N + (t + 1);
     };
-    /* cnt layout: [band][list 0|1][class 0..2][0 = count, 1 = position] */
+    /* cnt layout: [band][list 0|1][class 0..4][0 = count, 1 = position] */
     auto C = [&](int band, int list, int cls, int w) -> int& {
-        return cnt[((band * 2 + list) * 3 + cls) * 2 + w];
+        return cnt[((band * 2 + list) * NC + cls) * 2 + w];
     };
     for (int k = threadIdx.x; k < L::CNT_INTS; k += NT) cnt[k] = 0;
     __syncthreads();
     for (int f = threadIdx.x; f < G::NSLICE * G::FA; f += NT) {
         const int t = f / G::FA, n = f % G::FA;
-        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        const int kl = cidx(n - 1, t), kr = cidx(n, t);
+        const int nw = wet[kl] + wet[kr];
+        int cls = nw == 0 ? 4 : nw == 1 ? 3 : 0;
+        if (nw == 2) {
+            const double hL = sm[L::OFF_H + kl], hR = sm[L::OFF_H + kr];
+            const double uL = sm[(DIR == 0 ? L::OFF_U : L::OFF_V) + kl];
+            const double uR = sm[(DIR == 0 ? L::OFF_U : L::OFF_V) + kr];
+            const double cL = sm[L::OFF_C + kl], cR = sm[L::OFF_C + kr];
+            constexpr bool F = !EXACT; /* comparisons on the integer pipe */
+            const double delu = uR - uL;
+            const double hmin = d_min<F>(hL, hR), hmax = d_max<F>(hL, hR);
+            const double dh = hmax - hmin;
+            if (d_gtz<F>(delu + 2.0 * (d_min<F>(cL, cR) - d_max<F>(cL, cR)))) cls = 0;
+            else if (d_lez<F>(delu) && d_ge<F>(delu * delu * (hmin * hmax), dh * dh * (0.5 * g) * (hmin + hmax)))
+                cls = 1;
+            else cls = 2;
+        }
+        fcls[f] = (unsigned char)cls;
         atomicAdd(&C(t / RB, 0, cls, 0), 1);
     }
     for (int f = threadIdx.x; f < G::NSLICE * G::FB; f += NT) {
         const int t = f / G::FB, n = 1 + f % G::FB;
-        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
-        atomicAdd(&C(t / RB, 1, cls, 0), 1);
+        const int nw = wet[cidx(n - 1, t)] + wet[cidx(n, t)];
+        atomicAdd(&C(t / RB, 1, nw == 0 ? 4 : nw == 1 ? 3 : 0, 0), 1);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < L::NBAND * 2; e += NT) {
         const int band = e >> 1, list = e & 1;
         int acc = 0;
-        for (int cls = 0; cls < 3; ++cls) {
+        for (int cls = 0; cls < NC; ++cls) {
             C(band, list, cls, 1) = acc;
             acc += C(band, list, cls, 0);
         }
     }
     __syncthreads();
     for (int f = threadIdx.x; f < G::NSLICE * G::FA; f += NT) {
-        const int t = f / G::FA, n = f % G::FA;
-        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        const int t = f / G::FA;
         const int band = t / RB;
-        const int pos = atomicAdd(&C(band, 0, cls, 1), 1);
+        const int pos = atomicAdd(&C(band, 0, fcls[f], 1), 1);
         la[band * RB * G::FA + pos] = (uint16_t)(f - band * RB * G::FA);
     }
     for (int f = threadIdx.x; f < G::NSLICE * G::FB; f += NT) {
         const int t = f / G::FB, n = 1 + f % G::FB;
-        const int cls = 2 - (wet[cidx(n - 1, t)] + wet[cidx(n, t)]);
+        const int nw = wet[cidx(n - 1, t)] + wet[cidx(n, t)];
         const int band = t / RB;
-        const int pos = atomicAdd(&C(band, 1, cls, 1), 1);
+        const int pos = atomicAdd(&C(band, 1, nw == 0 ? 4 : nw == 1 ? 3 : 0, 1), 1);
         lb[band * RB * G::FB + pos] = (uint16_t)(f - band * RB * G::FB);
     }
     __syncthreads();
@@ -256,10 +285,10 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
         return DIR == 0 ? (n - 1) + M * (t - 1) : (t - 1) + M * (n - 1);
     };
     auto C = [&](int band, int list, int cls) -> int {
-        return cnt[((band * 2 + list) * 3 + cls) * 2 + 0];
+        return cnt[((band * 2 + list) * L::NCLS + cls) * 2 + 0];
     };
 
-    build_lists<M, NT, RB, DIR, EXACT>(wet, cnt, la, lb);
+    build_lists<M, NT, RB, DIR, EXACT>(sm, wet, cnt, la, lb, g);
 
     /* Contracted build: DX, DY. Exact build: fm(i+1,j), fp(i,j), gm(i,j+1),
      * gp(i,j) of the reference, in sweep coordinates N_M, N_P (normal) and
@@ -341,8 +370,10 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
         const int t1 = min(t0 + RB, G::NSLICE) - 1; /* last slice of band */
         const uint16_t* lA = la + band * RB * G::FA;
         const uint16_t* lB = lb + band * RB * G::FB;
-        const int a2 = C(band, 0, 0), a1 = C(band, 0, 1), a0 = C(band, 0, 2);
-        const int b2 = C(band, 1, 0), b1 = C(band, 1, 1), b0 = C(band, 1, 2);
+        /* a2 / b2 both cells wet (list A by wave structure), a1 / b1 one
+         * wet, a0 / b0 both dry */
+        const int a2 = C(band, 0, 0) + C(band, 0, 1) + C(band, 0, 2), a1 = C(band, 0, 3), a0 = C(band, 0, 4);
+        const int b2 = C(band, 1, 0), b1 = C(band, 1, 3), b0 = C(band, 1, 4);
 
         /* ---- stage A: normal Riemann solves, faces 0..M+2, by class ---- */
         for (int idx = threadIdx.x; idx < a2 + a1 + a0; idx += NT) {
