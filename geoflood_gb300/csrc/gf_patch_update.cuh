@@ -179,9 +179,10 @@ __device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned ch
 /* Build, for every band of one sweep direction, the normal-solve faces
  * (list A) and the limited faces (list B) ordered by class, so that a warp
  * runs one code path. Classes: 0..2 both cells wet, by the wave structure
- * riemanntype will find (0 two rarefactions, 1 two shocks, 2 a shock and a
- * rarefaction; list B puts all wet pairs in class 0); 3 one cell wet; 4 both
- * dry. The wave structure is estimated without a square root (F_max <= 0 as
+ * riemanntype will find (0 two shocks, the costly branch, first so that one
+ * class boundary at most splits its warps; 1 two rarefactions; 2 a shock
+ * and a rarefaction; list B puts all wet pairs in class 0); 3 one cell wet;
+ * 4 both dry. The wave structure is estimated without a square root (F_max <= 0 as
  * delu <= 0 and delu^2 hmin hmax >= (hmax - hmin)^2 g (hmin + hmax) / 2); a
  * borderline face in the neighbouring class only costs divergence, since
  * every face's solve is the same computation wherever it is listed. Two
@@ -218,9 +219,9 @@ __device__ __forceinline__ void build_lists(const double* sm, const unsigned cha
             const double delu = uR - uL;
             const double hmin = d_min<F>(hL, hR), hmax = d_max<F>(hL, hR);
             const double dh = hmax - hmin;
-            if (d_gtz<F>(delu + 2.0 * (d_min<F>(cL, cR) - d_max<F>(cL, cR)))) cls = 0;
+            if (d_gtz<F>(delu + 2.0 * (d_min<F>(cL, cR) - d_max<F>(cL, cR)))) cls = 1;
             else if (d_lez<F>(delu) && d_ge<F>(delu * delu * (hmin * hmax), dh * dh * (0.5 * g) * (hmin + hmax)))
-                cls = 1;
+                cls = 0;
             else cls = 2;
         }
         fcls[f] = (unsigned char)cls;
