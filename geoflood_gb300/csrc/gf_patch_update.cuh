@@ -120,8 +120,12 @@ struct Smem {
     using G = Geo<M>;
     static constexpr int NACC = EXACT ? 4 : 2;
     static constexpr int NBAND = (G::NSLICE + RB - 1) / RB;
-    static constexpr int W_STRIDE = 12; /* s[3] + fw[3][3]                   */
-    static constexpr int O_STRIDE = 18; /* faddm faddp A B C D, 3 comps each */
+    /* Odd strides (in doubles) spread a warp's accesses to face records and
+     * accumulator rows over the shared-memory banks. */
+    static constexpr int W_STRIDE = 13; /* s[3] + fw[3][3], 1 pad            */
+    static constexpr int O_STRIDE = 19; /* faddm faddp A B C D, 3 comps each, 1 pad */
+    static constexpr int MS = M + 1;    /* accumulator row stride            */
+    static constexpr int PLANE = M * MS; /* one accumulator component        */
     static constexpr int OFF_H = 0;
     static constexpr int OFF_HU = OFF_H + G::S;
     static constexpr int OFF_HV = OFF_HU + G::S;
@@ -132,7 +136,7 @@ struct Smem {
     static constexpr int OFF_RH = OFF_C + G::S;                     /* contracted only */
     static constexpr int OFF_RC = OFF_RH + (EXACT ? 0 : G::S);      /* contracted only */
     static constexpr int OFF_ACC = OFF_RC + (EXACT ? 0 : G::S);     /* NACC x [3][M*M] */
-    static constexpr int OFF_W = OFF_ACC + NACC * 3 * M * M;
+    static constexpr int OFF_W = OFF_ACC + NACC * 3 * PLANE;
     static constexpr int OFF_O = OFF_W + RB * G::FA * W_STRIDE;
     static constexpr int OFF_RED = OFF_O + RB * G::FB * O_STRIDE; /* 2*32 doubles */
     static constexpr int OFF_BAR = OFF_RED + 64;                    /* 1 x u64     */
@@ -276,14 +280,14 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
     /* local component l -> global component (h, hu, hv) */
     constexpr int G1 = (DIR == 0) ? 1 : 2; /* normal momentum     */
     constexpr int G2 = (DIR == 0) ? 2 : 1; /* transverse momentum */
-    constexpr int MM = M * M;
+    constexpr int MM = L::PLANE; /* component stride of the accumulators */
     double smax = 0.0;
 
     auto cidx = [](int n, int t) -> int {
         return DIR == 0 ? (t + 1) * N + (n + 1) : (n + 1) * N + (t + 1);
     };
     auto aidx = [](int n, int t) -> int {
-        return DIR == 0 ? (n - 1) + M * (t - 1) : (t - 1) + M * (n - 1);
+        return DIR == 0 ? (n - 1) + L::MS * (t - 1) : (t - 1) + L::MS * (n - 1);
     };
     auto C = [&](int band, int list, int cls) -> int {
         return cnt[((band * 2 + list) * L::NCLS + cls) * 2 + 0];
@@ -686,7 +690,7 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
             sm[L::OFF_RC + k] = rc;
         }
     }
-    for (int k = threadIdx.x; k < L::NACC * 3 * M * M; k += NT) sm[L::OFF_ACC + k] = 0.0;
+    for (int k = threadIdx.x; k < L::NACC * 3 * L::PLANE; k += NT) sm[L::OFF_ACC + k] = 0.0;
     any_wet = __syncthreads_or(any_wet);
 
     const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
@@ -708,22 +712,23 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
         const int i = 1 + e % M, j = 1 + e / M;
         const int k = (j + 1) * N + (i + 1);
         double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
+        constexpr int PL = L::PLANE;
+        const int a = (i - 1) + L::MS * (j - 1); /* accumulator index of the cell */
         if (EXACT) {
             /* q - dtdx*(fm(i+1,j) - fp(i,j)) - dtdy*(gm(i,j+1) - gp(i,j)) */
             const double* FM = sm + L::OFF_ACC;
-            const double* FP = FM + 3 * M * M;
-            const double* GM = FP + 3 * M * M;
-            const double* GP = GM + 3 * M * M;
-            h = h - dtdx * (FM[e] - FP[e]) - dtdy * (GM[e] - GP[e]);
-            hu = hu - dtdx * (FM[e + M * M] - FP[e + M * M]) - dtdy * (GM[e + M * M] - GP[e + M * M]);
-            hv = hv - dtdx * (FM[e + 2 * M * M] - FP[e + 2 * M * M]) -
-                 dtdy * (GM[e + 2 * M * M] - GP[e + 2 * M * M]);
+            const double* FP = FM + 3 * PL;
+            const double* GM = FP + 3 * PL;
+            const double* GP = GM + 3 * PL;
+            h = h - dtdx * (FM[a] - FP[a]) - dtdy * (GM[a] - GP[a]);
+            hu = hu - dtdx * (FM[a + PL] - FP[a + PL]) - dtdy * (GM[a + PL] - GP[a + PL]);
+            hv = hv - dtdx * (FM[a + 2 * PL] - FP[a + 2 * PL]) - dtdy * (GM[a + 2 * PL] - GP[a + 2 * PL]);
         } else {
             const double* DX = sm + L::OFF_ACC;
-            const double* DY = sm + L::OFF_ACC + 3 * M * M;
-            h = h - dtdx * DX[e] - dtdy * DY[e];
-            hu = hu - dtdx * DX[e + M * M] - dtdy * DY[e + M * M];
-            hv = hv - dtdx * DX[e + 2 * M * M] - dtdy * DY[e + 2 * M * M];
+            const double* DY = sm + L::OFF_ACC + 3 * PL;
+            h = h - dtdx * DX[a] - dtdy * DY[a];
+            hu = hu - dtdx * DX[a + PL] - dtdy * DY[a + PL];
+            hv = hv - dtdx * DX[a + 2 * PL] - dtdy * DY[a + 2 * PL];
         }
         if (P.src_term > 0) {
             const double nvar = (P.variable_friction && fidx >= 0 && fidx < maux)
