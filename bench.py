@@ -40,8 +40,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
-# 47.6 M FP64 warp instructions x 26.33 lanes / 4 194 304 cell-updates
-FP64_LANE_OPS_PER_CELL_UPDATE = 47.604012e6 * 26.33 / (4194304.0)
+# FP64 pipe issue slots per cell-update of this workload: 39.74 M FP64 warp
+# instructions (ncu sm__inst_executed_pipe_fp64.sum) x 32 lanes / 4 194 304
+# cell-updates
+FP64_LANE_OPS_PER_CELL_UPDATE = 39.736483e6 * 32 / 4194304.0
 M = 32
 NPX = NPY = 64
 DX = 1.0
@@ -562,10 +564,9 @@ def run_gpu(args):
                 "ffma_gops": rates["ffma"] / 1e9,
                 "kernel_cell_updates_per_s": ncell / (kernel_ms * 1e-3),
                 "peak_source": "measured live (gf_measure_fp64_rates)"}
-        # FP64 lane operations per cell-update of this workload, from the ncu
-        # capture of the same kernel (sm__inst_executed_pipe_fp64 x lanes per
-        # instruction / cells): the achieved FP64 rate follows from the live
-        # kernel time
+        # FP64 issue slots (warp instructions x 32 lanes) per cell-update of
+        # this workload, from the ncu capture of the same kernel: the achieved
+        # FP64 issue rate follows from the live kernel time
         ops = FP64_LANE_OPS_PER_CELL_UPDATE
         ach = ops * ncell / (kernel_ms * 1e-3) / 1e9
         fp64.update({"lane_ops_per_cell_update": ops, "achieved_gops": ach,
