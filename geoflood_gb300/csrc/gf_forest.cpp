@@ -172,6 +172,17 @@ struct gf_forest {
     bool sub_graph_ok = false;
     int sub_graph_par = -1, sub_graph_nblk = -1;
     bool sub_graph_exact = false;
+    long long sub_updates = 0; /* cell-updates of the step in flight */
+    /* a subcycled run driven step by step among others (concurrent runner):
+     * the outstyle-1 state between steps, the step in flight on `sst` */
+    struct SubRun {
+        double t_curr = 0, dt_minlevel = 0, dt_outer = 0, tend = 0, dt_step = 0;
+        double desired_cfl = 0, max_cfl = 0;
+        int nout = 0, nint = 0;
+        bool took_small = false, active = false, pending = false, cancel = false;
+    } sr;
+    cudaStream_t sst = nullptr;       /* owned by the runner */
+    cudaEvent_t sev_ctx = nullptr, sev_done = nullptr;
 };
 
 namespace {
@@ -1238,7 +1249,7 @@ int sub_level(gf_forest* f, int l, double tl, double dtl, int* p)
  * host-only plan pass has written this step's level dts and ghost blocks
  * (whose boundary times move with t and dt) to the pinned staging the
  * graph's first node copies. */
-int sub_step(gf_forest* f, double t, double dt, double* cfl, long long* updates)
+int sub_launch(gf_forest* f, double t, double dt, cudaStream_t ls)
 {
     int rc = build_sub_tables(f);
     if (rc) return rc;
@@ -1311,13 +1322,37 @@ int sub_step(gf_forest* f, double t, double dt, double* cfl, long long* updates)
         f->sub_graph_nblk = nblk;
         f->sub_graph_exact = exact;
     }
+    f->sub_updates = cu;
+    if (ls && ls != st) {
+        /* on the runner's stream, after this forest's tables, transfers and
+         * slot copies on the context's stream */
+        if (!f->sev_ctx) FK(f, cudaEventCreateWithFlags(&f->sev_ctx, cudaEventDisableTiming));
+        if (!f->sev_done) FK(f, cudaEventCreateWithFlags(&f->sev_done, cudaEventDisableTiming));
+        FK(f, cudaEventRecord(f->sev_ctx, st));
+        FK(f, cudaStreamWaitEvent(ls, f->sev_ctx, 0));
+        st = ls;
+    }
     FK(f, cudaGraphLaunch(f->sub_exec, st));
     FK(f, cudaMemcpyAsync(f->h_rb, f->d_rb.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    FK(f, cudaStreamSynchronize(st));
+    if (f->sev_done && st == ls) FK(f, cudaEventRecord(f->sev_done, st));
+    return GF_OK;
+}
+
+/* the launched step's CFL (its readback has landed) */
+int sub_collect(gf_forest* f, double* cfl, long long* updates)
+{
     if ((int)f->h_rb[0]) return ffail(f, GF_ERR_DEVICE, "a patch-update copy wait timed out");
     std::memcpy(cfl, &f->h_rb[1], sizeof *cfl);
-    *updates = cu;
+    *updates = f->sub_updates;
     return GF_OK;
+}
+
+int sub_step(gf_forest* f, double t, double dt, double* cfl, long long* updates)
+{
+    int rc = sub_launch(f, t, dt, nullptr);
+    if (rc) return rc;
+    FK(f, cudaStreamSynchronize(gf::ctx_stream(f->ctx)));
+    return sub_collect(f, cfl, updates);
 }
 
 /* accept: the coarsest level back into the shared buffer; retake: the
@@ -1471,6 +1506,8 @@ void gf_forest_destroy(gf_forest* f)
     f->d_sub_stage.release();
     if (f->h_sub) cudaFreeHost(f->h_sub);
     if (f->h_rb) cudaFreeHost(f->h_rb);
+    if (f->sev_ctx) cudaEventDestroy(f->sev_ctx);
+    if (f->sev_done) cudaEventDestroy(f->sev_done);
     delete f;
 }
 
@@ -2381,7 +2418,155 @@ int batch_check(gf_forest* f, gf_ctx* ctx)
     if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
     if (f->o.maxlevel >= kBatchLevels) return ffail(f, GF_ERR_ARG, "maxlevel too deep");
     if (f->o.subcycle)
-        return ffail(f, GF_ERR_UNSUPPORTED, "batched runs take every level's step together (subcycle = 0)");
+        return ffail(f, GF_ERR_UNSUPPORTED, "shared rounds take every level's step together (subcycle = 0)");
+    return GF_OK;
+}
+
+/* ---- subcycled forests side by side ----
+ * A subcycled coarse step is one captured graph per forest (sub_launch), so
+ * subcycled forests batch by running side by side: each forest's steps go
+ * to one of a pool of streams and the host drives every forest's outstyle-1
+ * loop (fc2d_geoclaw_run.c:190-395, as run_outstyle1 with subcycle = 1)
+ * without waiting on the device: a pass takes in the steps whose readback
+ * has landed (accept or retake, next dt, regrid when due) and launches each
+ * idle forest's next step. Each forest's launches keep their order, so its
+ * result equals its own gf_forest_run. */
+struct SubRunner {
+    gf_ctx* ctx = nullptr;
+    std::vector<cudaStream_t> streams;
+    std::vector<gf_forest*> fs;
+    size_t next = 0;
+    long long launched = 0, regrids = 0, cell_updates = 0;
+    ~SubRunner()
+    {
+        for (cudaStream_t st : streams) cudaStreamDestroy(st);
+    }
+};
+constexpr int kSubStreams = 16;
+
+int sub_run_add(SubRunner& R, gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
+                double max_cfl)
+{
+    if (!f || f->ctx != R.ctx) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    if (!f->o.subcycle) return ffail(f, GF_ERR_ARG, "not a subcycled forest");
+    if ((int)R.streams.size() < kSubStreams) {
+        cudaStream_t st;
+        FK(f, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        R.streams.push_back(st);
+    }
+    f->sst = R.streams[R.next++ % R.streams.size()];
+    gf_forest::SubRun& r = f->sr;
+    r = gf_forest::SubRun{};
+    r.t_curr = f->st.t;
+    r.dt_minlevel = initial_dt;
+    r.dt_outer = t_final / nout;
+    r.tend = r.t_curr + r.dt_outer;
+    r.nout = nout;
+    r.desired_cfl = desired_cfl;
+    r.max_cfl = max_cfl;
+    r.active = true;
+    R.fs.push_back(f);
+    return GF_OK;
+}
+
+/* the next step: the outstyle-1 dt clipping to the output time, then launch */
+int sub_run_launch(SubRunner& R, gf_forest* f)
+{
+    gf_forest::SubRun& r = f->sr;
+    while (!(r.t_curr < r.tend)) {
+        if (++r.nint >= r.nout) {
+            r.active = false;
+            f->st.t = r.t_curr;
+            f->st.dt = r.dt_minlevel;
+            f->st.npatch = (int)f->leaves.size();
+            f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+            return GF_OK;
+        }
+        r.tend = r.t_curr + r.dt_outer;
+    }
+    double dt_step = r.dt_minlevel;
+    const double tol = 1e-2 * dt_step;
+    r.took_small = false;
+    const double small_step = r.tend - (r.t_curr + dt_step);
+    if (small_step < tol) {
+        dt_step = r.tend - r.t_curr;
+        if (small_step < 0) r.took_small = true;
+    }
+    r.dt_step = dt_step;
+    int rc = sub_launch(f, r.t_curr, dt_step, f->sst);
+    if (rc) return rc;
+    r.pending = true;
+    R.launched++;
+    return GF_OK;
+}
+
+/* take in the step in flight: accept or retake, next dt, regrid when due */
+int sub_run_complete(SubRunner& R, gf_forest* f)
+{
+    gf_forest::SubRun& r = f->sr;
+    r.pending = false;
+    double cfl = 0.0;
+    long long updates = 0;
+    int rc = sub_collect(f, &cfl, &updates);
+    if (rc) return rc;
+    f->st.max_cfl_seen = std::max(f->st.max_cfl_seen, cfl);
+    if (cfl > r.max_cfl) {
+        if ((rc = sub_finish(f, false))) return rc;
+        r.dt_minlevel = r.dt_minlevel * r.desired_cfl / cfl;
+        f->st.rejects++;
+        return GF_OK;
+    }
+    if ((rc = sub_finish(f, true))) return rc;
+    f->st.steps++;
+    f->st.cell_updates += updates;
+    R.cell_updates += updates;
+    r.t_curr += r.dt_step;
+    const double dt_new = r.dt_minlevel * r.desired_cfl / cfl;
+    if (!r.took_small) r.dt_minlevel = dt_new;
+    f->st.t = r.t_curr;
+    f->st.dt = r.dt_minlevel;
+    if (f->o.regrid_interval > 0 && f->st.steps % f->o.regrid_interval == 0) {
+        bool changed = false;
+        if ((rc = regrid(f, r.t_curr, &changed))) return rc;
+        R.regrids++;
+        f->st.npatch_max = std::max(f->st.npatch_max, (int)f->leaves.size());
+    }
+    return GF_OK;
+}
+
+/* One pass; never waits on the device (wait = 1: block on one step in
+ * flight when nothing else could move). *live = forests still running. */
+int sub_run_pass(SubRunner& R, int wait, int* live, int* progress)
+{
+    int moved = 0;
+    for (gf_forest* f : R.fs) {
+        if (!f->sr.pending) continue;
+        const cudaError_t e = cudaEventQuery(f->sev_done);
+        if (e == cudaErrorNotReady) continue;
+        if (e != cudaSuccess) return gf::ctx_cuda_fail(R.ctx, e, "subcycled step");
+        int rc = sub_run_complete(R, f);
+        if (rc) return rc;
+        moved = 1;
+    }
+    for (gf_forest* f : R.fs) {
+        if (f->sr.pending || !f->sr.active || f->sr.cancel) continue;
+        int rc = sub_run_launch(R, f);
+        if (rc) return rc;
+        moved = 1;
+    }
+    int n = 0;
+    gf_forest* first = nullptr;
+    for (gf_forest* f : R.fs) {
+        n += f->sr.active || f->sr.pending;
+        if (!first && f->sr.pending) first = f;
+    }
+    if (wait && !moved && first) {
+        const cudaError_t e = cudaEventSynchronize(first->sev_done);
+        if (e != cudaSuccess) return gf::ctx_cuda_fail(R.ctx, e, "subcycled step");
+    }
+    *live = n;
+    if (progress) *progress = moved;
     return GF_OK;
 }
 
@@ -2396,20 +2581,42 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
         return GF_ERR_ARG;
     gf_ctx* ctx = forests[0] ? forests[0]->ctx : nullptr;
     for (int k = 0; k < n; ++k) {
-        int rc = batch_check(forests[k], ctx);
+        if (!forests[k] || forests[k]->ctx != ctx) return GF_ERR_ARG;
+        int rc = forests[k]->o.subcycle ? (forests[k]->leaves.empty()
+                                               ? ffail(forests[k], GF_ERR_STATE, "forest not initialised")
+                                               : GF_OK)
+                                        : batch_check(forests[k], ctx);
         if (rc) return rc;
         for (int j = 0; j < k; ++j)
             if (forests[j] == forests[k]) return ffail(forests[k], GF_ERR_ARG, "a forest appears twice");
     }
+    /* forests that take every level's step together share rounds;
+     * subcycled forests run side by side on their own streams */
     BatchRun R;
+    SubRunner U;
+    U.ctx = ctx;
     int rc = batch_begin(R, ctx);
     if (rc) return rc;
-    for (int k = 0; k < n; ++k) batch_add(R, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl);
-    int live = 1;
-    while (live) {
-        if ((rc = batch_iterate(R, &live))) return rc;
+    int nb = 0, ns = 0;
+    for (int k = 0; k < n; ++k) {
+        if (forests[k]->o.subcycle) {
+            if ((rc = sub_run_add(U, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl))) return rc;
+            ++ns;
+        } else {
+            batch_add(R, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl);
+            ++nb;
+        }
     }
-    if (bst) *bst = R.S;
+    int live_b = nb, live_s = ns;
+    while (live_b || live_s) {
+        if (live_s && (rc = sub_run_pass(U, live_b == 0, &live_s, nullptr))) return rc;
+        if (live_b && (rc = batch_iterate(R, &live_b))) return rc;
+    }
+    if (bst) {
+        *bst = R.S;
+        bst->regrids += U.regrids;
+        bst->cell_updates += U.cell_updates;
+    }
     return GF_OK;
 }
 

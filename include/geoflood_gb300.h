@@ -401,7 +401,11 @@ int gf_forest_upload(gf_forest* f, const double* q);
  * every forest, CFL reduction) is captured as a CUDA graph per epoch and
  * replayed; a forest whose regrid is due waits on the device until the
  * host regrids it, after which the epoch is rebuilt and captured again.
- * Each forest's result equals its own gf_forest_run. */
+ * Subcycled forests (subcycle = 1) run side by side instead: each coarse
+ * step is that forest's captured graph, launched on one of a pool of
+ * streams, and the host drives every forest's loop without waiting on the
+ * device, so many forests' steps overlap on the GPU. Each forest's result
+ * equals its own gf_forest_run. */
 typedef struct gf_forest_batch_stats {
     long long rounds;        /* graph replays                               */
     long long epochs;        /* captures (membership or tables changed)     */

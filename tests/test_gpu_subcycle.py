@@ -111,8 +111,39 @@ def test_subcycling_takes_fewer_coarse_steps(ctx):
     assert runs[True]["steps"] < runs[False]["steps"]
 
 
-def test_batched_runs_refuse_subcycled_forests(ctx):
-    G, _ = pair(ctx, gf.Phys(friction_forcing=False))
-    with pytest.raises(gf.GeoFloodError):
-        gf.forest.batch_run([G], 10.0)
-    G.close()
+def forest(ctx, m=M, seed=3, regrid=2, subcycle=True, mthbc=(3, 3, 3, 3), hydro=None):
+    b, q = rasters("dambreak", seed, m)
+    F = gf.Forest(ctx, m, NBX, NBY, LMIN, LMAX, 1000.0 / m, 1000.0 / m, b, q, mthbc=mthbc,
+                  regrid_interval=regrid, refine=FRONT, phys_slot=SLOT, subcycle=subcycle)
+    if hydro is not None:
+        F.set_hydrograph(*hydro)
+    F.init()
+    return F
+
+
+def test_subcycled_forests_in_a_batch_equal_their_own_runs(ctx):
+    """Subcycled forests run side by side in gf_forest_batch_run (each
+    coarse step its own graph on one of the runner's streams), beside
+    forests that share rounds: every forest ends as its own gf_forest_run."""
+    from geoflood_gb300.forest import batch_run
+
+    ctx.set_phys(SLOT, gf.Phys(manning_coefficient=(0.035,), manning_break=(1e10,)))
+    specs = [dict(m=8, seed=3, regrid=2), dict(m=16, seed=5, regrid=3, mthbc=(0, 3, 3, 3), hydro=HYDRO),
+             dict(m=8, seed=7, regrid=2, subcycle=False), dict(m=32, seed=6, regrid=4)]
+    alone = []
+    for sp in specs:
+        F = forest(ctx, **sp)
+        st = F.run(30.0, 2, 5.0, 0.9, 1.0)
+        alone.append((F.patches(), F.download(), st))
+        F.close()
+    fs = [forest(ctx, **sp) for sp in specs]
+    bst = batch_run(fs, 30.0, 2, 5.0, 0.9, 1.0)
+    for F, (P, q, st) in zip(fs, alone):
+        got = F.stats()
+        assert np.array_equal(F.patches(), P)
+        assert np.array_equal(F.download()[S], q[S])
+        for k in ("steps", "rejects", "regrids", "cell_updates", "t"):
+            assert got[k] == st[k], k
+    assert bst["regrids"] == sum(F.stats()["regrids"] for F in fs)
+    for F in fs:
+        F.close()
