@@ -148,10 +148,11 @@ class gf_forest_request_info(C.Structure):
 
 class gf_fserver_stats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("done", C.c_longlong),
-                ("failed", C.c_longlong), ("lane_admitted", C.c_longlong * 2),
+                ("failed", C.c_longlong), ("lane_admitted", C.c_longlong * 3),
                 ("iterations", C.c_longlong), ("epochs", C.c_longlong),
                 ("rounds", C.c_longlong), ("launches", C.c_longlong), ("regrids", C.c_longlong),
-                ("cell_updates", C.c_longlong), ("s_admit", C.c_double), ("s_epoch", C.c_double),
+                ("cell_updates", C.c_longlong), ("sub_steps", C.c_longlong),
+                ("s_admit", C.c_double), ("s_epoch", C.c_double),
                 ("s_rounds", C.c_double), ("s_regrid", C.c_double), ("bytes_in_use", C.c_size_t),
                 ("bytes_peak", C.c_size_t), ("active", C.c_int), ("queued", C.c_int),
                 ("held", C.c_int)]

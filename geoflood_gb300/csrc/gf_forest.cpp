@@ -2624,6 +2624,52 @@ struct gf::ForestBatch {
     BatchRun R;
 };
 
+struct gf::SubForests {
+    SubRunner U;
+};
+
+int gf::subforests_create(gf_ctx* c, SubForests** out)
+{
+    if (!c || !out) return GF_ERR_ARG;
+    SubForests* s = new SubForests;
+    s->U.ctx = c;
+    *out = s;
+    return GF_OK;
+}
+
+void gf::subforests_destroy(SubForests* s) { delete s; }
+
+int gf::subforests_add(SubForests* s, gf_forest* f, double t_final, int nout, double initial_dt,
+                       double desired_cfl, double max_cfl)
+{
+    if (!s || !(t_final > 0) || nout < 1 || !(initial_dt > 0) || !(desired_cfl > 0) || !(max_cfl > 0))
+        return GF_ERR_ARG;
+    return sub_run_add(s->U, f, t_final, nout, initial_dt, desired_cfl, max_cfl);
+}
+
+int gf::subforests_pass(SubForests* s, int* live, int* progress) { return sub_run_pass(s->U, 0, live, progress); }
+
+bool gf::subforests_pending(const gf_forest* f) { return f->sr.pending; }
+
+bool gf::subforests_running(const gf_forest* f) { return f->sr.pending || (f->sr.active && !f->sr.cancel); }
+
+void gf::subforests_stop(gf_forest* f) { f->sr.cancel = true; }
+
+void gf::subforests_remove(SubForests* s, gf_forest* f)
+{
+    std::vector<gf_forest*>& fs = s->U.fs;
+    auto it = std::find(fs.begin(), fs.end(), f);
+    if (it != fs.end()) fs.erase(it);
+}
+
+void gf::subforests_get_stats(const SubForests* s, long long* steps_launched, long long* regrids,
+                              long long* cell_updates)
+{
+    *steps_launched = s->U.launched;
+    *regrids = s->U.regrids;
+    *cell_updates = s->U.cell_updates;
+}
+
 int gf::forest_batch_create(gf_ctx* c, ForestBatch** out, int stream_priority, int max_ctas)
 {
     if (!c || !out) return GF_ERR_ARG;

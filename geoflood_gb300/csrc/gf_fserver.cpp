@@ -65,6 +65,7 @@ struct gf_fserver {
     gf_ctx* ctx = nullptr;
     int nlanes = 1;
     int cap_large = 0; /* the large lane's update grid while the small lane has members */
+    gf::SubForests* sub = nullptr; /* lane 2: subcycled forests side by side */
     gf::ForestBatch* lanes[2] = {nullptr, nullptr};
     std::vector<Req*> joining[2]; /* built forests waiting for their lane to be idle */
     Clock::time_point t0;
@@ -100,7 +101,6 @@ const char* validate(const gf_forest_request& r)
     if (o.nbx < 1 || o.nby < 1) return "nbx, nby must be positive";
     if (o.minlevel < 0 || o.maxlevel < o.minlevel || o.maxlevel > 10) return "need 0 <= minlevel <= maxlevel <= 10";
     if (!(o.dx0 > 0) || !(o.dy0 > 0)) return "dx0, dy0 must be positive";
-    if (o.subcycle) return "batched rounds step every level together (subcycle = 0)";
     if (!(r.t_final > 0) || r.nout < 1 || !(r.initial_dt > 0) || !(r.desired_cfl > 0) || !(r.max_cfl > 0))
         return "bad time-stepping parameters";
     if (r.nhydro < 0 || (r.nhydro > 0 && (!r.hydro_time || !r.hydro_hu))) return "bad hydrograph";
@@ -179,6 +179,23 @@ int admit(gf_fserver* s, Req* x)
         drop(s, x);
         return rc;
     }
+    if (x->r.opts.subcycle) {
+        /* subcycled: its own graph per coarse step, side by side with the
+         * other subcycled forests; it joins at once */
+        x->lane = 2;
+        x->info.lane = 2;
+        s->stats.lane_admitted[2]++;
+        rc = gf::subforests_add(s->sub, x->f, x->r.t_final, x->r.nout, x->r.initial_dt, x->r.desired_cfl,
+                                x->r.max_cfl);
+        if (rc) {
+            s->last_error = gf_ctx_last_error(s->ctx);
+            finish(s, x, GF_SCEN_FAILED);
+            drop(s, x);
+            return rc;
+        }
+        s->active.push_back(x);
+        return GF_OK;
+    }
     const long long cells = (long long)gf_forest_npatch(x->f) * x->r.opts.mx * x->r.opts.mx;
     x->lane = (s->nlanes > 1 && cells >= s->o.lane_cells) ? 1 : 0;
     x->info.lane = x->lane;
@@ -246,10 +263,35 @@ int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
             moved = 1;
         }
     }
+    /* subcycled forests: take in finished steps, launch the next ones */
+    {
+        int live = 0, prog = 0;
+        int rc = gf::subforests_pass(s->sub, &live, &prog);
+        if (rc) return fail_all(s, rc);
+        moved |= prog;
+    }
     /* idle lanes: cancelled and finished members leave (a finished forest
      * stays resident for the caller; its physics slot is free again) */
     std::vector<Req*> still;
     for (Req* x : s->active) {
+        if (x->lane == 2) {
+            if (x->cancel_req) gf::subforests_stop(x->f);
+            if (gf::subforests_running(x->f)) {
+                still.push_back(x);
+                continue;
+            }
+            gf::subforests_remove(s->sub, x->f);
+            if (x->cancel_req) {
+                finish(s, x, GF_SCEN_CANCELLED);
+                drop(s, x);
+            } else {
+                finish(s, x, GF_SCEN_DONE);
+                s->free_slots.push_back(x->slot);
+                x->slot = -1;
+            }
+            moved = 1;
+            continue;
+        }
         gf::ForestBatch* b = s->lanes[x->lane];
         if (gf::forest_batch_inflight(b)) {
             still.push_back(x);
@@ -314,11 +356,14 @@ int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
         sum.s_rounds += b.s_rounds;
         sum.s_regrid += b.s_regrid;
     }
+    long long sub_steps = 0, sub_regrids = 0, sub_cu = 0;
+    gf::subforests_get_stats(s->sub, &sub_steps, &sub_regrids, &sub_cu);
     s->stats.epochs = sum.epochs;
     s->stats.rounds = sum.rounds;
     s->stats.launches = sum.launches;
-    s->stats.regrids = sum.regrids;
-    s->stats.cell_updates = sum.cell_updates;
+    s->stats.regrids = sum.regrids + sub_regrids;
+    s->stats.cell_updates = sum.cell_updates + sub_cu;
+    s->stats.sub_steps = sub_steps;
     s->stats.s_epoch = sum.s_epoch;
     s->stats.s_rounds = sum.s_rounds;
     s->stats.s_regrid = sum.s_regrid;
@@ -334,6 +379,8 @@ void drain(gf_fserver* s)
         int done = 0;
         if (s->lanes[k] && gf::forest_batch_inflight(s->lanes[k])) gf::forest_batch_test(s->lanes[k], 1, &done);
     }
+    cudaSetDevice(s->device);
+    cudaDeviceSynchronize(); /* subcycled steps on the runner's streams */
 }
 
 void loop_main(gf_fserver* s)
@@ -399,6 +446,7 @@ int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out)
     } else if (!rc) {
         rc = gf::forest_batch_create(s->ctx, &s->lanes[0]);
     }
+    if (!rc) rc = gf::subforests_create(s->ctx, &s->sub);
     if (rc) {
         gf_fserver_destroy(s);
         return rc;
@@ -419,6 +467,7 @@ void gf_fserver_destroy(gf_fserver* s)
     }
     for (int k = 0; k < 2; ++k)
         if (s->lanes[k]) gf::forest_batch_destroy(s->lanes[k]);
+    if (s->sub) gf::subforests_destroy(s->sub);
     if (s->ctx) gf_ctx_destroy(s->ctx);
     delete s;
 }

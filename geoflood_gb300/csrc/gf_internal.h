@@ -144,6 +144,22 @@ bool forest_batch_running(const gf_forest* f);
 void forest_batch_get_stats(const ForestBatch* b, gf_forest_batch_stats* st);
 size_t forest_device_bytes(const gf_forest* f);
 
+/* Subcycled forests side by side (gf_forest.cpp): each coarse step is the
+ * forest's captured graph on a stream of a pool; a pass takes in finished
+ * steps and launches the next ones without waiting on the device. */
+struct SubForests;
+int subforests_create(gf_ctx* c, SubForests** out);
+void subforests_destroy(SubForests* s);
+int subforests_add(SubForests* s, gf_forest* f, double t_final, int nout, double initial_dt,
+                   double desired_cfl, double max_cfl);
+int subforests_pass(SubForests* s, int* live, int* progress);
+bool subforests_pending(const gf_forest* f);   /* a step in flight */
+bool subforests_running(const gf_forest* f);   /* in flight or more to run */
+void subforests_stop(gf_forest* f);            /* no further step */
+void subforests_remove(SubForests* s, gf_forest* f); /* when nothing is in flight */
+void subforests_get_stats(const SubForests* s, long long* steps_launched, long long* regrids,
+                          long long* cell_updates);
+
 } // namespace gf
 
 #endif

@@ -246,12 +246,14 @@ class ForestRequest:
     initial_dt: float = 1.0
     desired_cfl: float = 0.9
     max_cfl: float = 1.0
+    subcycle: bool = False
 
     def opts(self, maux: int | None = None):
         from .forest import forest_opts
         return forest_opts(self.mx, self.nbx, self.nby, self.minlevel, self.maxlevel, self.dx0,
                            self.dy0, self.maux if maux is None else maux, self.x0, self.y0, 0,
-                           self.mthbc, self.regrid_interval, self.max_patches, self.refine)
+                           self.mthbc, self.regrid_interval, self.max_patches, self.refine,
+                           self.subcycle)
 
     def prepare(self) -> "ForestRequest":
         """Build the C request (and its raster block) now, so that a later

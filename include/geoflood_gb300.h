@@ -646,8 +646,9 @@ double gf_server_clock(const gf_server* s);
  * the budget, until gf_fserver_release; read it meanwhile through
  * gf_fserver_forest (or gf_fserver_download while the loop thread runs).
  * The caller keeps fields and topo alive until the request leaves QUEUED.
- * Subcycled forests (opts.subcycle = 1) are refused: batched rounds step
- * every level together. */
+ * Subcycled forests (opts.subcycle = 1) run in a third lane, side by side
+ * as in gf_forest_batch_run (each coarse step the forest's own graph on a
+ * stream of a pool). */
 typedef struct gf_fserver gf_fserver;
 
 typedef struct gf_forest_request {
@@ -684,13 +685,14 @@ typedef struct gf_forest_request_info {
     int npatch, npatch_max;
     size_t footprint;      /* bytes reserved at admission                       */
     size_t device_bytes;   /* bytes the forest holds (0 before admission)       */
-    int lane;              /* 0 small, 1 large (-1 before admission)            */
+    int lane;              /* 0 small, 1 large, 2 subcycled (-1 before admission) */
 } gf_forest_request_info;
 
 typedef struct gf_fserver_stats {
     long long submitted, admitted, done, failed;
-    long long lane_admitted[2];  /* per lane (small, large)                     */
+    long long lane_admitted[3];  /* per lane (small, large, subcycled)          */
     long long iterations, epochs, rounds, launches, regrids, cell_updates;
+    long long sub_steps;     /* subcycled coarse steps launched               */
     double s_admit, s_epoch, s_rounds, s_regrid; /* host seconds per phase      */
     size_t bytes_in_use, bytes_peak;
     int active, queued, held;

@@ -39,7 +39,7 @@ def own_run(ctx, req: ForestRequest):
     ctx.set_phys(5, req.phys)
     F = gf.Forest(ctx, req.mx, req.nbx, req.nby, req.minlevel, req.maxlevel, req.dx0, req.dy0,
                   req.aux, req.q, mthbc=req.mthbc, regrid_interval=req.regrid_interval,
-                  refine=req.refine, phys_slot=5)
+                  refine=req.refine, phys_slot=5, subcycle=req.subcycle)
     if req.hydro is not None:
         h = req.hydro
         F.set_hydrograph(h.time, h.hu, h.side, h.width, h.x0, h.y0)
@@ -100,9 +100,9 @@ def test_lanes_give_the_same_results(ctx, lane_cells):
         lanes = [srv.poll(s)["lane"] for s in ids]
         st = srv.stats()
         if lane_cells:
-            assert set(lanes) == {0, 1} and st["lane_admitted"] == [lanes.count(0), lanes.count(1)]
+            assert set(lanes) == {0, 1} and st["lane_admitted"] == [lanes.count(0), lanes.count(1), 0]
         else:
-            assert set(lanes) == {0} and st["lane_admitted"] == [len(ids), 0]
+            assert set(lanes) == {0} and st["lane_admitted"] == [len(ids), 0, 0]
 
 
 def test_arrivals_join_a_running_batch(ctx):
@@ -202,3 +202,29 @@ def test_topo_request_and_loop_thread(ctx):
         srv.stop()
         assert info["state"] == "done"
         check_same(srv, sid, want)
+
+
+def test_subcycled_requests_run_beside_the_batched_lanes(ctx):
+    """Subcycled requests (a third lane: each coarse step the forest's own
+    graph, side by side) and round-sharing requests in one server: every
+    result equals its own gf_forest_run; cancelling a running subcycled
+    request leaves the others unchanged."""
+    reqs = [request(m=8, seed=3, regrid=2), request(m=16, seed=5, regrid=3, mthbc=(0, 3, 3, 3), hydro=HYDRO),
+            request(m=8, seed=9, regrid=2), request(m=32, seed=6, regrid=4)]
+    reqs[0].subcycle = reqs[1].subcycle = reqs[3].subcycle = True
+    want = [own_run(ctx, r) for r in reqs]
+    with ForestServer(lane_cells=4096) as srv:
+        ids = [srv.submit(r) for r in reqs]
+        sub_extra = request(m=8, seed=11, t_final=200.0)
+        sub_extra.subcycle = True
+        extra = srv.submit(sub_extra)
+        pump_until(srv, lambda: srv.poll(extra)["steps"] > 0)
+        srv.cancel(extra)
+        srv.run_until_idle()
+        for sid, w in zip(ids, want):
+            check_same(srv, sid, w)
+        lanes = [srv.poll(s)["lane"] for s in ids]
+        assert lanes[0] == lanes[1] == lanes[3] == 2 and lanes[2] in (0, 1)
+        assert srv.poll(extra)["state"] == "cancelled"
+        st = srv.stats()
+        assert st["lane_admitted"][2] == 4 and st["sub_steps"] > 0
