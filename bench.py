@@ -680,6 +680,45 @@ def forest_leg(args, dev=0):
         horizon["subcycled" if sub else "advance_one_step"] = {
             "seconds": sec, "coarse_or_global_steps": hs["steps"], "rejects": hs["rejects"],
             "cell_updates": hs["cell_updates"], "value": hs["cell_updates"] / sec, "unit": METRIC}
+    # 16 subcycled dam-break forests (bed seeds differ) to the 60 s horizon:
+    # side by side in one batched call vs one after another
+    from geoflood_gb300.forest import batch_run
+    nsub = 16
+    cs = [forest_dambreak_config(seed=SEED + 40 + k) for k in range(nsub)]
+
+    def sub_forests():
+        fs = []
+        for cc in cs:
+            G = gf.Forest(ctx, cc["mx"], cc["nbx"], cc["nby"], cc["lmin"], cc["lmax"], cc["dx0"], cc["dx0"],
+                          cc["b"], cc["q"], mthbc=cc["mthbc"], regrid_interval=cc["regrid"], refine=cc["rf"],
+                          subcycle=True)
+            G.init()
+            fs.append(G)
+        return fs
+
+    fs = sub_forests()
+    t0 = time.perf_counter()
+    for G in fs:
+        G.run(60.0, 1, 5.0, 0.9, 1.0)
+    seq_s = time.perf_counter() - t0
+    seq = [(G.patches(), G.download(), G.stats()["cell_updates"]) for G in fs]
+    for G in fs:
+        G.close()
+    fs = sub_forests()
+    t0 = time.perf_counter()
+    batch_run(fs, 60.0, 1, 5.0, 0.9, 1.0)
+    bat_s = time.perf_counter() - t0
+    work = sum(G.stats()["cell_updates"] for G in fs)
+    same = all(np.array_equal(P, G.patches()) and np.array_equal(q[:, 2:-2, 2:-2], G.download()[:, 2:-2, 2:-2])
+               for (P, q, _), G in zip(seq, fs))
+    for G in fs:
+        G.close()
+    horizon["subcycled_batch"] = {
+        "forests": nsub, "value": work / bat_s, "unit": METRIC, "seconds": bat_s,
+        "one_by_one": {"value": work / seq_s, "seconds": seq_s},
+        "speedup_vs_one_by_one": seq_s / bat_s, "batch_equals_one_by_one": bool(same),
+        "note": "gf_forest_batch_run of subcycled forests: each coarse step the forest's own graph "
+                "on a stream of a pool, the host loop waiting on no forest"}
     ctx.close()
     oracle.load()
     O = of.Forest(c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"], c["b"],
