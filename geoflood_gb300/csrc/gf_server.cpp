@@ -100,7 +100,7 @@ struct Lane {
     char* d_ep = nullptr;
     size_t ep_cap = 0;
     size_t off_blk = 0, off_gs = 0, off_dt = 0, off_par = 0, off_rb = 0, off_hyt = 0, off_hyu = 0;
-    size_t off_ref[3] = {0, 0, 0}, off_work[3] = {0, 0, 0};
+    size_t off_ref[3] = {0, 0, 0}, off_work[3] = {0, 0, 0}, off_sched = 0;
     int npm[3] = {0, 0, 0};
     /* two readback slots: [err (8 B)][states] */
     char* h_rb[2] = {nullptr, nullptr};
@@ -130,6 +130,7 @@ struct gf_server {
     std::vector<int> free_slots;
     gf_server_stats stats{};
     int cta_cap[GF_SERVER_MAX_LANES][3] = {}; /* update-kernel grid caps per lane and mx */
+    int mix_cap[GF_SERVER_MAX_LANES] = {};    /* the one-launch update's grid cap per lane */
     std::thread loop;
     std::atomic<bool> running{false};
 
@@ -420,10 +421,15 @@ int rebuild_epoch(gf_server* srv, Lane& L)
     for (int c = 0; c < 3; ++c) {
         L.off_ref[c] = off;
         off = align256(off + npm[c] * sizeof(gf_ghost_ref));
-        L.off_work[c] = off;
-        off = align256(off + npm[c] * sizeof(gf_patch_work));
         L.npm[c] = npm[c];
     }
+    /* work items of all sizes contiguous, mx 32 first (the one-launch update's list) */
+    L.off_work[2] = off;
+    L.off_work[1] = L.off_work[2] + (size_t)npm[2] * sizeof(gf_patch_work);
+    L.off_work[0] = L.off_work[1] + (size_t)npm[1] * sizeof(gf_patch_work);
+    off = align256(off + (size_t)(npm[0] + npm[1] + npm[2]) * sizeof(gf_patch_work));
+    L.off_sched = off;
+    off = align256(off + 2 * sizeof(unsigned int));
     const size_t need = off;
     if (need > L.ep_cap) {
         if (L.d_ep) cudaFreeAsync(L.d_ep, L.st);
@@ -444,6 +450,7 @@ int rebuild_epoch(gf_server* srv, Lane& L)
     }
     char* h = L.h_ep;
     std::memset(h + L.off_rb, 0, (nm + 1) * sizeof(unsigned long long));
+    std::memset(h + L.off_sched, 0, 2 * sizeof(unsigned int));
     gf_ghost_block* hb = reinterpret_cast<gf_ghost_block*>(h + L.off_blk);
     gf_group_state* hg = reinterpret_cast<gf_group_state*>(h + L.off_gs);
     double* hyt = reinterpret_cast<double*>(h + L.off_hyt);
@@ -525,15 +532,28 @@ int enqueue_round(gf_server* srv, Lane& L)
                                              L.npm[c], srv->d_phys, L.st));
             ++n;
         }
-    for (int c = 0; c < 3; ++c)
-        if (L.npm[c]) {
-            /* the smallest lane's step time is one patch's critical path: latency tiles */
-            const int goal = (L.idx == 0 && srv->o.nlanes > 1) ? 1 : 0;
-            SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
-                                               L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux, nullptr,
-                                               rb + 1, err, L.st, srv->cta_cap[L.idx][c], goal));
+    if (srv->o.mixed_update && L.idx > 0) {
+        /* later lanes: every size in one persistent launch (a device cursor
+         * over the contiguous work list), on the lane's capped grid */
+        const int nw[3] = {L.npm[2], L.npm[1], L.npm[0]};
+        if (nw[0] + nw[1] + nw[2]) {
+            SV_CK(srv, gf::launch_patch_update_mixed(reinterpret_cast<const gf_patch_work*>(d + L.off_work[2]), nw,
+                                                     srv->d_phys, 0.0, gdt, gpar, kLaneMaux, nullptr, rb + 1, err,
+                                                     reinterpret_cast<unsigned int*>(d + L.off_sched), L.st,
+                                                     srv->mix_cap[L.idx]));
             ++n;
         }
+    } else {
+        for (int c = 0; c < 3; ++c)
+            if (L.npm[c]) {
+                /* the smallest lane's step time is one patch's critical path: latency tiles */
+                const int goal = (L.idx == 0 && srv->o.nlanes > 1) ? 1 : 0;
+                SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
+                                                   L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux, nullptr,
+                                                   rb + 1, err, L.st, srv->cta_cap[L.idx][c], goal));
+                ++n;
+            }
+    }
     SV_CK(srv, gf::launch_served_finish(gs, gdt, rb + 1, err, nm, L.st));
     ++n;
     L.launches_per_round = n;
@@ -703,6 +723,7 @@ void gf_server_opts_default(gf_server_opts* o)
     o->priority = 1;
     o->backfill = 1;
     o->reserve_sms = 16;
+    o->mixed_update = 0; /* per-size launches: measured faster for served scenarios */
 }
 
 int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
@@ -759,12 +780,17 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
     for (int c = 0; c < 3; ++c) /* sets the kernels' shared-memory attribute outside capture */
         gf::launch_patch_update(ms[c], nullptr, 0, nullptr, 0.0, nullptr, nullptr, 0, nullptr,
                                 nullptr, nullptr, nullptr);
-    for (int k = 1; k < o.nlanes; ++k)
+    const int none[3] = {0, 0, 0};
+    gf::launch_patch_update_mixed(nullptr, none, nullptr, 0.0, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
+                                  nullptr, nullptr);
+    for (int k = 1; k < o.nlanes; ++k) {
+        const int sms = nsm - o.reserve_sms;
         for (int c = 0; c < 3; ++c) {
             const int occ = gf::patch_update_occupancy(ms[c]);
-            const int sms = nsm - o.reserve_sms;
             s->cta_cap[k][c] = (o.reserve_sms > 0 && sms > 0 && occ > 0) ? sms * occ : 0;
         }
+        s->mix_cap[k] = (o.reserve_sms > 0 && sms > 0) ? sms : 0; /* one CTA per SM */
+    }
     s->h_phys.resize(kMaxSlots);
     for (int k = kMaxSlots - 1; k >= 0; --k) s->free_slots.push_back(k);
     *out = s;

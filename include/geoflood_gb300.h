@@ -584,6 +584,9 @@ typedef struct gf_server_opts {
     int priority;           /* 1: smaller lanes on higher-priority streams       */
     int backfill;           /* 1: admit later arrivals that fit while the head waits */
     int reserve_sms;        /* lanes after the first leave this many SMs free for it */
+    int mixed_update;       /* 1: lanes after the first update every patch size in one
+                               persistent launch (same results); 0 (default): one launch
+                               per size, which keeps the small sizes' occupancy */
 } gf_server_opts;
 
 typedef struct gf_scenario_info {

@@ -80,6 +80,28 @@ def test_result_is_the_same_alone_and_in_the_mix(lanes):
     assert np.array_equal(outs["b"], b_alone)
 
 
+def test_one_launch_update_of_later_lanes_gives_the_same_bits():
+    """Lanes after the first update every patch size in one persistent launch
+    (capped grid); per-size launches and each scenario alone give the same
+    bits."""
+    scs = [scen(31, 1200, 8), scen(32, 4096, 16), scen(33, 9000, 32), scen(34, 3000, 8)]
+    runs = []
+    for mixed in (True, False):
+        with gf.Server(lanes=(1000,), mixed_update=mixed) as srv:
+            outs = [np.zeros_like(s.q) for s in scs]
+            ids = [srv.submit(s, o) for s, o in zip(scs, outs)]
+            srv.run_until_idle()
+            infos = [srv.poll(i) for i in ids]
+        assert all(i["state"] == "done" for i in infos)
+        assert {i["lane"] for i in infos} == {1}
+        runs.append((outs, [i["steps"] for i in infos]))
+    for a, b in zip(runs[0][0], runs[1][0]):
+        assert np.array_equal(a, b)
+    assert runs[0][1] == runs[1][1]
+    alone, _ = serve_alone(scs[2], lanes=(1000,))
+    assert np.array_equal(runs[0][0][2], alone)
+
+
 def test_admission_waits_for_hbm_budget():
     a = scen(31, 2048, 16)
     b = scen(32, 2048, 16)
