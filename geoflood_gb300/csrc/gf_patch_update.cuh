@@ -23,8 +23,9 @@
  * uniform warps:
  *   - per-cell quotients computed once (hu/h, hv/h, sqrt(g h), and in the
  *     contracted build 1/h and 1/sqrt(g h));
- *   - the faces of each band are listed by class (both cells wet, one wet,
- *     both dry) so a warp runs one code path; dry faces only store zeros;
+ *   - the faces of each band are listed by class (both cells wet, grouped
+ *     by the wave structure riemanntype will find; one wet; both dry) so a
+ *     warp runs one code path; dry faces only store zeros;
  *   - the per-face outputs of a band go to shared memory and each interior
  *     cell gathers its six contributing faces in slice order, so every cell
  *     is written by one thread per band, in a fixed order: deterministic and
