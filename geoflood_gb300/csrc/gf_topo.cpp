@@ -24,6 +24,7 @@
 #include <cctype>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -120,8 +121,254 @@ std::string lower(std::string s)
 }
 
 /* returns an error text or nullptr */
+/* ---- NetCDF classic files (topo type 4) ----
+ * The classic format's header, big-endian throughout: "CDF" and a version
+ * byte (1: 32-bit offsets, 2: 64-bit offsets, 5: 64-bit sizes), the record
+ * count, then the dimension, global attribute and variable lists, each a tag
+ * (0x0A / 0x0C / 0x0B, or 0 when absent) and a count. Names and attribute
+ * values are padded to 4 bytes. A non-record variable's values lie
+ * contiguous at its `begin` offset, last dimension fastest. NetCDF-4 files
+ * (HDF5 containers) are not read. */
+struct NcVar {
+    std::string name;
+    std::vector<int> dims;
+    int type = 0;
+    uint64_t begin = 0;
+    std::string positive; /* the text attribute "positive", if any */
+};
+
+struct NcFile {
+    std::vector<std::pair<std::string, uint64_t>> dims;
+    std::vector<NcVar> vars;
+    std::vector<unsigned char> buf;
+};
+
+int nc_type_size(int t)
+{
+    switch (t) {
+    case 1: case 2: case 7: return 1;  /* byte, char, ubyte */
+    case 3: case 8: return 2;          /* short, ushort     */
+    case 4: case 5: case 9: return 4;  /* int, float, uint  */
+    case 6: case 10: case 11: return 8; /* double, int64, uint64 */
+    default: return 0;
+    }
+}
+
+struct NcReader {
+    const std::vector<unsigned char>& b;
+    size_t i = 0;
+    bool ok = true;
+    bool wide = false; /* CDF-5: 64-bit counts */
+    explicit NcReader(const std::vector<unsigned char>& buf) : b(buf) {}
+    uint64_t be(int n)
+    {
+        if (i + n > b.size()) {
+            ok = false;
+            return 0;
+        }
+        uint64_t v = 0;
+        for (int k = 0; k < n; ++k) v = (v << 8) | b[i + k];
+        i += n;
+        return v;
+    }
+    uint64_t count() { return be(wide ? 8 : 4); }
+    void pad() { i = (i + 3) & ~(size_t)3; }
+    std::string name()
+    {
+        const uint64_t n = count();
+        if (!ok || i + n > b.size()) {
+            ok = false;
+            return {};
+        }
+        std::string s(reinterpret_cast<const char*>(&b[i]), (size_t)n);
+        i += n;
+        pad();
+        return s;
+    }
+    /* an attribute list; returns the text attribute `want` (or "") */
+    std::string atts(const char* want)
+    {
+        std::string found;
+        const uint64_t tag = be(4), n = count();
+        if (tag == 0) return found;
+        if (tag != 0x0C) {
+            ok = false;
+            return found;
+        }
+        for (uint64_t k = 0; k < n && ok; ++k) {
+            const std::string nm = name();
+            const int type = (int)be(4);
+            const uint64_t nel = count();
+            const int sz = nc_type_size(type);
+            if (!sz || i + nel * sz > b.size()) {
+                ok = false;
+                break;
+            }
+            if (type == 2 && nm == want) found.assign(reinterpret_cast<const char*>(&b[i]), (size_t)nel);
+            i += nel * sz;
+            pad();
+        }
+        return found;
+    }
+};
+
+const char* nc_parse(NcFile* f)
+{
+    const std::vector<unsigned char>& b = f->buf;
+    if (b.size() >= 4 && b[0] == 0x89 && b[1] == 'H' && b[2] == 'D' && b[3] == 'F')
+        return "NetCDF-4 (HDF5) topo files are not read: convert to the classic format";
+    if (b.size() < 8 || b[0] != 'C' || b[1] != 'D' || b[2] != 'F' || !(b[3] == 1 || b[3] == 2 || b[3] == 5))
+        return "not a NetCDF classic file";
+    const int version = b[3];
+    NcReader r(b);
+    r.i = 4;
+    r.wide = version == 5;
+    r.count(); /* record count */
+    uint64_t tag = r.be(4), n = r.count();
+    if (tag != 0 && tag != 0x0A) return "NetCDF header: bad dimension list";
+    for (uint64_t k = 0; k < n && r.ok; ++k) {
+        std::string nm = r.name();
+        const uint64_t len = r.count();
+        f->dims.emplace_back(nm, len);
+    }
+    r.atts("");
+    tag = r.be(4);
+    n = r.count();
+    if (tag != 0 && tag != 0x0B) return "NetCDF header: bad variable list";
+    for (uint64_t k = 0; k < n && r.ok; ++k) {
+        NcVar v;
+        v.name = r.name();
+        const uint64_t nd = r.count();
+        for (uint64_t d = 0; d < nd && r.ok; ++d) {
+            const uint64_t id = r.count();
+            if (id >= f->dims.size()) return "NetCDF header: bad dimension id";
+            v.dims.push_back((int)id);
+        }
+        v.positive = r.atts("positive");
+        v.type = (int)r.be(4);
+        r.count(); /* vsize */
+        v.begin = r.be(version == 1 ? 4 : 8);
+        f->vars.push_back(std::move(v));
+    }
+    return r.ok ? nullptr : "NetCDF header ends early";
+}
+
+/* a non-record variable's values as doubles, last dimension fastest */
+const char* nc_values(const NcFile& f, const NcVar& v, std::vector<double>* out)
+{
+    uint64_t n = 1;
+    for (int d : v.dims) {
+        if (f.dims[d].second == 0) return "NetCDF record variables are not read";
+        n *= f.dims[d].second;
+    }
+    const int sz = nc_type_size(v.type);
+    if (!sz || v.type == 2) return "NetCDF variable of a non-numeric type";
+    if (v.begin + n * sz > f.buf.size()) return "NetCDF variable beyond the end of the file";
+    out->resize((size_t)n);
+    const unsigned char* p = &f.buf[(size_t)v.begin];
+    for (uint64_t k = 0; k < n; ++k, p += sz) {
+        uint64_t u = 0;
+        for (int j = 0; j < sz; ++j) u = (u << 8) | p[j];
+        double x;
+        switch (v.type) {
+        case 1: x = (double)(int8_t)u; break;
+        case 3: x = (double)(int16_t)u; break;
+        case 4: x = (double)(int32_t)u; break;
+        case 5: {
+            uint32_t w = (uint32_t)u;
+            float fl;
+            std::memcpy(&fl, &w, 4);
+            x = fl;
+            break;
+        }
+        case 6: std::memcpy(&x, &u, 8); break;
+        case 7: x = (double)(uint8_t)u; break;
+        case 8: x = (double)(uint16_t)u; break;
+        case 9: x = (double)(uint32_t)u; break;
+        case 10: x = (double)(int64_t)u; break;
+        default: x = (double)u; break;
+        }
+        (*out)[(size_t)k] = x;
+    }
+    return nullptr;
+}
+
+/* topo type 4 as read_topo_file / read_topo_header read it
+ * (geolib_source/topo_module.f90:624-732, :926-1035, get_dim_info :1599-1623):
+ * x and y dimensions named lon / longitude / x and lat / latitude / y (any
+ * case), their coordinate variables of the same names, and the last 2-D
+ * variable as z in either dimension order; rows stored north first; z
+ * negated when its attribute positive is "down" and the type is negative.
+ * The whole grid is kept (the reference crops it to the domain plus one
+ * spacing, which leaves every cell integral inside the domain unchanged). */
+const char* read_netcdf(const char* path, int topo_type, TopoGrid* g)
+{
+    NcFile f;
+    {
+        std::FILE* fp = std::fopen(path, "rb");
+        if (!fp) return "cannot open the topo file";
+        unsigned char chunk[65536];
+        size_t got;
+        while ((got = std::fread(chunk, 1, sizeof chunk, fp)) > 0) f.buf.insert(f.buf.end(), chunk, chunk + got);
+        std::fclose(fp);
+    }
+    if (const char* e = nc_parse(&f)) return e;
+    auto upper = [](std::string s) {
+        for (char& c : s) c = (char)std::toupper((unsigned char)c);
+        return s;
+    };
+    int xd = -1, yd = -1;
+    for (size_t d = 0; d < f.dims.size(); ++d) {
+        const std::string u = upper(f.dims[d].first);
+        if (u == "LON" || u == "LONGITUDE" || u == "X") xd = (int)d;
+        else if (u == "LAT" || u == "LATITUDE" || u == "Y") yd = (int)d;
+    }
+    if (xd < 0 || yd < 0) return "NetCDF topo: no x / y (lon / lat) dimensions";
+    const NcVar *xv = nullptr, *yv = nullptr, *zv = nullptr;
+    for (const NcVar& v : f.vars) {
+        if (v.name == f.dims[xd].first) xv = &v;
+        else if (v.name == f.dims[yd].first) yv = &v;
+        else if (v.dims.size() == 2) zv = &v;
+    }
+    if (!xv || !yv) return "NetCDF topo: no coordinate variables for x and y";
+    if (!zv) return "NetCDF topo: no topography variable";
+    std::vector<double> xs, ys, zs;
+    if (const char* e = nc_values(f, *xv, &xs)) return e;
+    if (const char* e = nc_values(f, *yv, &ys)) return e;
+    if (const char* e = nc_values(f, *zv, &zs)) return e;
+    const int mx = (int)xs.size(), my = (int)ys.size();
+    if (mx < 2 || my < 2) return "NetCDF topo: need at least 2 x 2 nodes";
+    const bool yx = zv->dims[0] == yd && zv->dims[1] == xd; /* x fastest */
+    const bool xy = zv->dims[0] == xd && zv->dims[1] == yd;
+    if (!yx && !xy) return "NetCDF z variable has dimensions that don't align with x and y";
+    g->mx = mx;
+    g->my = my;
+    g->xlow = xs[0];
+    g->ylow = ys[0];
+    g->dx = xs[1] - xs[0];
+    g->dy = ys[1] - ys[0];
+    g->xhi = xs[mx - 1];
+    g->yhi = ys[my - 1];
+    g->z.resize((size_t)mx * my);
+    for (int j = 0; j < my; ++j)
+        for (int i = 0; i < mx; ++i) {
+            const int jy = my - 1 - j; /* row 0 is the northernmost */
+            g->z[(size_t)j * mx + i] = yx ? zs[(size_t)jy * mx + i] : zs[(size_t)i * my + jy];
+        }
+    if (topo_type < 0 && lower(zv->positive) == "down")
+        for (double& z : g->z) z = -z;
+    return nullptr;
+}
+
 const char* read_topo(const char* path, int topo_type, double topo_missing, TopoGrid* g)
 {
+    if (std::abs(topo_type) == 4) {
+        if (const char* e = read_netcdf(path, topo_type, g)) return e;
+        if (!(g->dx > 0) || !(g->dy > 0)) return "topo grid spacing must be positive";
+        if (topo_type < 0)
+            for (double& z : g->z) z = -z;
+        return nullptr;
+    }
     std::vector<std::string> lines;
     if (!read_lines(path, &lines)) return "cannot open the topo file";
     const int t = std::abs(topo_type);
@@ -208,7 +455,7 @@ const char* read_topo(const char* path, int topo_type, double topo_missing, Topo
         if (missing > 0 && topo_missing == 99999.0)
             return "the topo file has missing data and topo_missing is the default 99999";
     } else {
-        return "topo type must be +-1, +-2 or +-3";
+        return "topo type must be +-1, +-2, +-3 or +-4";
     }
     if (!(g->dx > 0) || !(g->dy > 0)) return "topo grid spacing must be positive";
     if (topo_type < 0)

@@ -438,7 +438,11 @@ void gf_topo_destroy(gf_topo* t);
 /* Value stored for no-data nodes of later files (default 99999, which the
  * reference refuses when a file has missing data: so do these readers). */
 int gf_topo_set_missing(gf_topo* t, double topo_missing);
-/* Append a topo file of type +-1, +-2 or +-3 (negative: z is negated). */
+/* Append a topo file of type +-1, +-2, +-3 or +-4 (negative: z is negated).
+ * Type 4 is a classic NetCDF file (CDF-1, -2 or -5) read as the reference
+ * reads it: x / y dimensions named lon / longitude / x and lat / latitude /
+ * y, coordinate variables of the same names, the last 2-D variable as z;
+ * NetCDF-4 (HDF5) files are refused. The whole grid is kept. */
 int gf_topo_read_file(gf_topo* t, const char* path, int topo_type);
 /* Append every file that a topo.data (test_topography = 0) lists; relative
  * names are taken relative to the directory of topo.data. */

@@ -88,8 +88,56 @@ def read_topo_header(path: str, topo_type: int) -> dict:
     return dict(mx=mx, my=my, xlow=xll, ylow=yll, xhi=xhi, yhi=yhi, dx=dx, dy=dy)
 
 
+def read_netcdf_topo(path: str, topo_type: int) -> dict:
+    """Topo type 4 (geolib_source/topo_module.f90:624-732 and :926-1035,
+    get_dim_info :1599-1623), parsed with scipy's classic-NetCDF reader: x / y
+    dimensions named lon / longitude / x and lat / latitude / y in any case,
+    coordinate variables of the same names, the last 2-D variable as z in
+    either dimension order, rows north first, z negated when its attribute
+    positive is "down" and the type is negative. The whole grid (the
+    reference crops to the domain plus one spacing)."""
+    from scipy.io import netcdf_file
+
+    with netcdf_file(path, "r", mmap=False) as f:
+        xd = yd = None
+        for name in f.dimensions:
+            u = name.upper()
+            if u in ("LON", "LONGITUDE", "X"):
+                xd = name
+            elif u in ("LAT", "LATITUDE", "Y"):
+                yd = name
+        zname = None
+        for name, v in f.variables.items():
+            if name in (xd, yd):
+                continue
+            if len(v.dimensions) == 2:
+                zname = name
+        xs = np.array(f.variables[xd].data, dtype=np.float64)
+        ys = np.array(f.variables[yd].data, dtype=np.float64)
+        zv = f.variables[zname]
+        data = np.array(zv.data, dtype=np.float64)
+        if tuple(zv.dimensions) == (yd, xd):
+            grid = data
+        elif tuple(zv.dimensions) == (xd, yd):
+            grid = data.T
+        else:
+            raise ValueError("NetCDF z variable has dimensions that don't align with x and y")
+        pos = getattr(zv, "positive", b"")
+        pos = pos.decode() if isinstance(pos, bytes) else str(pos)
+    z = np.ascontiguousarray(grid[::-1, :]).reshape(-1)
+    if topo_type < 0 and pos.lower() == "down":
+        z = -z
+    return dict(mx=len(xs), my=len(ys), xlow=xs[0], ylow=ys[0], xhi=xs[-1], yhi=ys[-1],
+                dx=xs[1] - xs[0], dy=ys[1] - ys[0], z=z)
+
+
 def read_topo_file(path: str, topo_type: int, topo_missing: float = 99999.0) -> dict:
     """Header plus z (mx*my,) in file order: rows north to south, x fastest."""
+    if abs(topo_type) == 4:
+        h = read_netcdf_topo(path, topo_type)
+        if topo_type < 0:
+            h["z"] = -h["z"]
+        return h
     h = read_topo_header(path, topo_type)
     mx, my = h["mx"], h["my"]
     t = abs(topo_type)

@@ -79,7 +79,11 @@ def test_reader_errors(gpu_lib, tmp_path):
     with pytest.raises(GeoFloodError):
         t.read_file(str(tmp_path / "absent.tt3"), 3)
     with pytest.raises(GeoFloodError):
-        t.read_file(str(GOLD / "A.tt3"), 4)        # NetCDF is not read here
+        t.read_file(str(GOLD / "A.tt3"), 4)        # not a NetCDF file
+    hdf = tmp_path / "nc4.nc"
+    hdf.write_bytes(b"\x89HDF\r\n\x1a\n" + bytes(64))
+    with pytest.raises(GeoFloodError):
+        t.read_file(str(hdf), 4)                   # NetCDF-4 (HDF5) is not read
     bad = tmp_path / "short.tt3"
     bad.write_text("4 ncols\n3 nrows\n0 xll\n0 yll\n1 cellsize\n-9999 nodata\n1 2 3 4\n")
     with pytest.raises(GeoFloodError):
@@ -185,3 +189,62 @@ def test_native_covered_area_matches_oracle(gpu_lib, parsed):
     ts = ot.TopoSet([ot.read_topo_file(str(GOLD / n), ty, missing) for n, ty in files])
     for rect in ((0, 800, 0, 600), (-200, 1000, -100, 800), (320, 420, 250, 480)):
         assert t.covered_area(*rect) == ts.area(*rect)
+
+
+def write_nc(path, version, dims, z, zdims, ztype, positive=None, extra_2d=False):
+    """A classic NetCDF topo file written by scipy (an independent writer)."""
+    from scipy.io import netcdf_file
+
+    with netcdf_file(str(path), "w", version=version) as f:
+        for name, vals in dims:
+            f.createDimension(name, len(vals))
+        for name, vals in dims:
+            v = f.createVariable(name, "d", (name,))
+            v[:] = vals
+        if extra_2d:                               # an earlier 2-D variable: the last one is z
+            e = f.createVariable("mask", "i", zdims)
+            e[:] = np.zeros(z.shape, dtype=np.int32)
+        v = f.createVariable("elevation", ztype, zdims)
+        v[:] = z.astype(ztype)
+        if positive is not None:
+            v.positive = positive
+
+
+@pytest.mark.parametrize("case", range(5))
+def test_netcdf_topo_native_equals_oracle(gpu_lib, tmp_path, case):
+    """Topo type +-4: the native classic-NetCDF reader and the oracle (scipy's
+    parser, the reference's rules) give the same grid; the grid holds the
+    written nodes, rows north first."""
+    from geoflood_gb300.topo import Topo
+
+    rng = np.random.default_rng(case)
+    mx, my = 7 + case, 5 + 2 * case
+    xs = -120.0 + 0.25 * np.arange(mx)
+    ys = 40.0 + 0.5 * np.arange(my)
+    zyx = rng.uniform(-50.0, 30.0, (my, mx)).round(2)       # z[y][x]
+    spec = [
+        dict(version=1, names=("lon", "lat"), order="yx", ztype="d", positive=None, ttype=4),
+        dict(version=2, names=("x", "y"), order="xy", ztype="f", positive="down", ttype=-4),
+        dict(version=1, names=("LONGITUDE", "Latitude"), order="yx", ztype="h", positive="down", ttype=4),
+        dict(version=2, names=("lon", "lat"), order="yx", ztype="d", positive=None, ttype=-4),
+        dict(version=1, names=("x", "y"), order="xy", ztype="i", positive="Down", ttype=-4),
+    ][case]
+    xn, yn = spec["names"]
+    z_store = zyx if spec["order"] == "yx" else zyx.T
+    zdims = (yn, xn) if spec["order"] == "yx" else (xn, yn)
+    dims = [(yn, ys), (xn, xs)] if case % 2 else [(xn, xs), (yn, ys)]
+    path = tmp_path / f"t{case}.nc"
+    write_nc(path, spec["version"], dims, z_store, zdims, spec["ztype"], spec["positive"], extra_2d=case == 3)
+    t = Topo()
+    t.read_file(str(path), spec["ttype"])
+    g = t.grid(0)
+    o = ot.read_topo_file(str(path), spec["ttype"])
+    for f in ("mx", "my", "xlow", "ylow", "xhi", "yhi", "dx", "dy"):
+        assert g[f] == o[f], f
+    assert np.array_equal(g["z"], o["z"])
+    want = zyx.astype(spec["ztype"]).astype(np.float64)[::-1, :].reshape(-1)
+    neg = spec["ttype"] < 0
+    if neg and spec["positive"] is not None and spec["positive"].lower() == "down":
+        neg = False                                  # negated twice, as the reference does
+    assert np.array_equal(g["z"], -want if neg else want)
+    assert (g["mx"], g["my"], g["xlow"], g["ylow"]) == (mx, my, xs[0], ys[0])
