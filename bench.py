@@ -40,6 +40,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
+# DRAM traffic of one patch-update launch of this workload (one ncu capture:
+# dram__bytes_read.sum + dram__bytes_write.sum), against 234.9 MB algorithmic
+DRAM_BYTES_PER_LAUNCH = 170.374656e6 + 63.300096e6
 # FP64 pipe issue slots per cell-update of this workload: 39.74 M FP64 warp
 # instructions (ncu sm__inst_executed_pipe_fp64.sum) x 32 lanes / 4 194 304
 # cell-updates
@@ -584,7 +587,11 @@ def run_gpu(args):
                 "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes + 16},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": DRAM_BYTES_PER_LAUNCH,
+                     "traffic_unit": "bytes per launch",
+                     "traffic_source": "profiles/patch_update_m32_dambreak4096.md (ncu "
+                                       "dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "algorithmic_bytes_per_launch": algo,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": kernel_ms,
                      "note": "FP64-issue bound, not HBM bound: see fp64"},
