@@ -68,7 +68,8 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
     if (d_gtz<FAST>(F_min)) { /* 2-rarefactions */
         const double t = d_max<FAST>(0.0, -delu + 2.0 * (cL + cR));
         hm = c16g * (t * t);
-        const double cm = sqrt(g * hm);
+        /* sqrt(g hm) = t / 4 up to rounding: the contracted build takes it */
+        const double cm = FAST ? 0.25 * t : sqrt(g * hm);
         s1m = uL + 2.0 * cL - 3.0 * cm;
         s2m = uR - 2.0 * cR + 3.0 * cm;
     } else if (d_lez<FAST>(F_max)) { /* 2 shocks, one Newton step on sqrt(h) */
@@ -102,7 +103,8 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
         const double rm = d_div<FAST>(1.0, hm);
         const double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (rm + rL));
         const double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (rm + rR));
-        const double cm = sqrt(g * hm);
+        /* hm = t^2: sqrt(g hm) = sqrt(g) |t| up to rounding in the contracted build */
+        const double cm = FAST ? (g * rsg) * fabs(t) : sqrt(g * hm);
         s1m = u1m - cm;
         s2m = u2m + cm;
     } else { /* one shock, one rarefaction, one secant step.
