@@ -62,9 +62,16 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
     const double F_min = delu + 2.0 * (c_min - c_max);
     /* (h_max + h_min)/(h_max h_min) = 1/h_min + 1/h_max: the contracted
      * build uses the per-cell reciprocals instead of a division. */
-    const double F_max =
-        FAST ? delu + (h_max - h_min) * sqrt(0.5 * g * (d_max<FAST>(rhL, rhR) + d_min<FAST>(rhL, rhR)))
-             : delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
+    double F_max, q_fm = 0.0, s_fm = 0.0;
+    if (FAST) {
+        /* the root through rsqrt, whose value the two-shock step reuses */
+        const double a_fm = 0.5 * g * (d_max<FAST>(rhL, rhR) + d_min<FAST>(rhL, rhR));
+        q_fm = rsqrt(a_fm);
+        s_fm = a_fm * q_fm;
+        F_max = delu + (h_max - h_min) * s_fm;
+    } else {
+        F_max = delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
+    }
     if (d_gtz<FAST>(F_min)) { /* 2-rarefactions */
         const double t = d_max<FAST>(0.0, -delu + 2.0 * (cL + cR));
         hm = c16g * (t * t);
@@ -78,13 +85,16 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
         if (FAST) {
             rL = rhL;
             rR = rhR;
+            /* h0 = h_max: the deeper side's root is sqrt(g / h_max) = c_max / h_max
+             * and its (h0 - h) terms vanish; the shallower side's root is
+             * F_max's, sqrt(g (1/h_min + 1/h_max) / 2) */
             const double r0 = d_min<FAST>(rhL, rhR); /* 1/h_max */
-            const double aL = 0.5 * g * (r0 + rL), aR = 0.5 * g * (r0 + rR);
-            const double qL = rsqrt(aL), qR = rsqrt(aR);
-            gL = aL * qL;
-            gR = aR * qR;
+            const double gmx = d_max<FAST>(cL, cR) * r0;
+            const bool lmax = d_ge<FAST>(hL, hR);
+            gL = lmax ? gmx : s_fm;
+            gR = lmax ? s_fm : gmx;
             const double w = 0.25 * (r0 * r0) * g;
-            dfdh = gL - (h0 - hL) * w * qL + gR - (h0 - hR) * w * qR;
+            dfdh = gmx + s_fm - (h0 - h_min) * w * q_fm;
             sh0 = d_max<FAST>(cL, cR) * rsg; /* sqrt(h_max) = sqrt(g h_max)/sqrt(g) */
         } else {
             rL = 1.0 / hL;
