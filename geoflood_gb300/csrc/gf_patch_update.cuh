@@ -588,7 +588,7 @@ __device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double ba
         if (FAST) {
             const double rh = 1.0 / h;
             const double gamma =
-                sqrt(hu * hu + hv * hv) * P.grav * (coeff * coeff) * ((rh * rh) * rcbrt(h));
+                d_sqrt<FAST>(hu * hu + hv * hv) * P.grav * (coeff * coeff) * ((rh * rh) * rcbrt(h));
             const double rdg = 1.0 / (1.0 + dt * gamma);
             hu = hu * rdg;
             hv = hv * rdg;

@@ -36,6 +36,20 @@ struct gf_cell {
     bool wet;    /* h > dry_tolerance                           */
 };
 
+/* sqrt(a): the IEEE root, or, in the contracted build and for positive
+ * finite a, a * rsqrt(a) (within an ulp or two, fewer FP64 instructions;
+ * zero, infinity and negative values keep the IEEE root, one integer test
+ * on the bit pattern decides) */
+template <bool FAST>
+__device__ __forceinline__ double d_sqrt(double a)
+{
+    if (FAST) {
+        const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(a));
+        if (u - 1ull < 0x7fefffffffffffffull) return a * rsqrt(a);
+    }
+    return sqrt(a);
+}
+
 /* riemanntype (geoclaw_riemann_utils.f:566-677), maxiter = 1.
  * cL = sqrt(g hL), cR = sqrt(g hR) are supplied by the caller (they equal
  * the Fortran's sqrt(g*hL), sqrt(g*hR) bit for bit). Returns hm, s1m, s2m. */
@@ -111,8 +125,8 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
         const double t = sh0 - d_div<FAST>(F0, slope);
         hm = t * t;
         const double rm = d_div<FAST>(1.0, hm);
-        const double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (rm + rL));
-        const double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (rm + rR));
+        const double u1m = uL - (hm - hL) * d_sqrt<FAST>((0.5 * g) * (rm + rL));
+        const double u2m = uR + (hm - hR) * d_sqrt<FAST>((0.5 * g) * (rm + rR));
         /* hm = t^2: sqrt(g hm) = sqrt(g) |t| up to rounding in the contracted build */
         const double cm = FAST ? (g * rsg) * fabs(t) : sqrt(g * hm);
         s1m = u1m - cm;
@@ -126,7 +140,7 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
             const double slope = (F_max - F0) / (h_max - h_min);
             hm = h_min - F0 / slope;
         }
-        const double cm = sqrt(g * hm);
+        const double cm = d_sqrt<FAST>(g * hm);
         if (d_gt<FAST>(hL, hR)) {
             s1m = uL + 2.0 * cL - 3.0 * cm;
             s2m = uL + 2.0 * cL - cm;
@@ -193,7 +207,7 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double sL = uL - cL;
     const double sR = uR + cR;
     const double uhat = d_div<FAST>(cL * uL + cR * uR, cR + cL);
-    const double chat = sqrt(g * 0.5 * (hR + hL));
+    const double chat = d_sqrt<FAST>(g * 0.5 * (hR + hL));
     double sE1 = d_min<FAST>(sL, uhat - chat);
     double sE2 = d_max<FAST>(sR, uhat + chat);
 
