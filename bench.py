@@ -43,10 +43,10 @@ BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
 # DRAM traffic of one patch-update launch of this workload (one ncu capture:
 # dram__bytes_read.sum + dram__bytes_write.sum), against 234.9 MB algorithmic
 DRAM_BYTES_PER_LAUNCH = 170.374656e6 + 63.300096e6
-# FP64 pipe issue slots per cell-update of this workload: 38.02 M FP64 warp
+# FP64 pipe issue slots per cell-update of this workload: 37.46 M FP64 warp
 # instructions (ncu sm__inst_executed_pipe_fp64.sum) x 32 lanes / 4 194 304
 # cell-updates
-FP64_LANE_OPS_PER_CELL_UPDATE = 38.018724e6 * 32 / 4194304.0
+FP64_LANE_OPS_PER_CELL_UPDATE = 37.456333e6 * 32 / 4194304.0
 M = 32
 NPX = NPY = 64
 DX = 1.0

@@ -493,10 +493,12 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                                      r2 = (DIR == 0) ? qr[2] : qr[1];
                         const double wnorm2 = a0 * a0 + a1 * a1 + a2 * a2;
                         if (!d_eqz<FAST>(wnorm2)) {
-                            const double dotl = l0 * a0 + l1 * a1 + l2 * a2;
-                            const double dotr = a0 * r0 + a1 * r1 + a2 * r2;
-                            lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[mw]) ? dotl : dotr,
-                                                  P.mthlim[mw]);
+                            /* the upwind neighbour's projection only (the
+                             * same products in the same order) */
+                            const bool up = d_gtz<FAST>(s[mw]);
+                            const double p0 = up ? l0 : r0, p1 = up ? l1 : r1, p2 = up ? l2 : r2;
+                            const double dot = p0 * a0 + p1 * a1 + p2 * a2;
+                            lim = gf_philim<FAST>(wnorm2, dot, P.mthlim[mw]);
                         }
                     }
                     const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
