@@ -971,7 +971,7 @@ def fserved_leg(args, dev=0):
     sat_work = sum(i["cell_updates"] for i in cal_info)
     sat_s = max(i["t_done"] for i in cal_info) - t0
     order = np.argsort(targets)
-    sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 6)})
+    sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, 12)})
     reqs = [req(sp).prepare() for sp in specs]   # raster blocks built before the stream
 
     def stream(rate, seed):
