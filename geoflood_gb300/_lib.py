@@ -134,7 +134,7 @@ class gf_forest_request(C.Structure):
 
 class gf_fserver_opts(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("backfill", C.c_int),
-                ("lane_cells", C.c_longlong), ("reserve_sms", C.c_int)]
+                ("lane_cells", C.c_longlong * 2), ("reserve_sms", C.c_int)]
 
 
 class gf_forest_request_info(C.Structure):
@@ -148,7 +148,7 @@ class gf_forest_request_info(C.Structure):
 
 class gf_fserver_stats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("done", C.c_longlong),
-                ("failed", C.c_longlong), ("lane_admitted", C.c_longlong * 3),
+                ("failed", C.c_longlong), ("lane_admitted", C.c_longlong * 4),
                 ("iterations", C.c_longlong), ("epochs", C.c_longlong),
                 ("rounds", C.c_longlong), ("launches", C.c_longlong), ("regrids", C.c_longlong),
                 ("cell_updates", C.c_longlong), ("sub_steps", C.c_longlong),

@@ -2222,9 +2222,9 @@ struct BatchRun {
     std::chrono::steady_clock::time_point t_launch;
 };
 
-/* stream_priority: 0 runs the rounds on the context's stream; otherwise on
- * a stream of their own with that priority (1 = the greatest the device
- * offers, 2 = the least), so that batches can overlap on the device. */
+/* stream_priority: 0 runs the rounds on the context's stream; k >= 1 on a
+ * stream of their own, k = 1 at the greatest priority the device offers and
+ * each further k a step lower, so that batches can overlap on the device. */
 int batch_begin(BatchRun& R, gf_ctx* ctx, int stream_priority = 0, int max_ctas = 0)
 {
     Batch& B = R.B;
@@ -2235,7 +2235,9 @@ int batch_begin(BatchRun& R, gf_ctx* ctx, int stream_priority = 0, int max_ctas 
     if (stream_priority) {
         int lo = 0, hi = 0;
         cudaDeviceGetStreamPriorityRange(&lo, &hi); /* hi: the numerically lowest, greatest priority */
-        BK(B, cudaStreamCreateWithPriority(&B.st, cudaStreamNonBlocking, stream_priority == 1 ? hi : lo));
+        const int step = std::max(1, (lo - hi) / 2);
+        BK(B, cudaStreamCreateWithPriority(&B.st, cudaStreamNonBlocking,
+                                           std::min(lo, hi + (stream_priority - 1) * step)));
         B.own_stream = true;
     }
     BK(B, cudaEventCreateWithFlags(&B.ev_ctx, cudaEventDisableTiming));

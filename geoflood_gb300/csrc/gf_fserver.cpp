@@ -44,6 +44,7 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+constexpr int kSubLane = GF_FSERVER_LANES; /* subcycled forests, side by side */
 
 struct Req {
     long long id = 0;
@@ -63,11 +64,11 @@ struct gf_fserver {
     int device = 0;
     gf_fserver_opts o{};
     gf_ctx* ctx = nullptr;
-    int nlanes = 1;
-    int cap_large = 0; /* the large lane's update grid while the small lane has members */
+    int nlanes = 1;   /* lanes of shared rounds (subcycled forests are lane kSubLane) */
+    int nsm = 0;
     gf::SubForests* sub = nullptr; /* lane 2: subcycled forests side by side */
-    gf::ForestBatch* lanes[2] = {nullptr, nullptr};
-    std::vector<Req*> joining[2]; /* built forests waiting for their lane to be idle */
+    gf::ForestBatch* lanes[GF_FSERVER_LANES] = {};
+    std::vector<Req*> joining[GF_FSERVER_LANES]; /* built forests waiting for their lane to be idle */
     Clock::time_point t0;
     std::mutex mu;
     std::condition_variable cv;
@@ -182,9 +183,9 @@ int admit(gf_fserver* s, Req* x)
     if (x->r.opts.subcycle) {
         /* subcycled: its own graph per coarse step, side by side with the
          * other subcycled forests; it joins at once */
-        x->lane = 2;
-        x->info.lane = 2;
-        s->stats.lane_admitted[2]++;
+        x->lane = kSubLane;
+        x->info.lane = kSubLane;
+        s->stats.lane_admitted[kSubLane]++;
         rc = gf::subforests_add(s->sub, x->f, x->r.t_final, x->r.nout, x->r.initial_dt, x->r.desired_cfl,
                                 x->r.max_cfl);
         if (rc) {
@@ -197,7 +198,8 @@ int admit(gf_fserver* s, Req* x)
         return GF_OK;
     }
     const long long cells = (long long)gf_forest_npatch(x->f) * x->r.opts.mx * x->r.opts.mx;
-    x->lane = (s->nlanes > 1 && cells >= s->o.lane_cells) ? 1 : 0;
+    x->lane = 0;
+    while (x->lane + 1 < s->nlanes && cells >= s->o.lane_cells[x->lane]) ++x->lane;
     x->info.lane = x->lane;
     s->stats.lane_admitted[x->lane]++;
     s->joining[x->lane].push_back(x);
@@ -232,7 +234,7 @@ int fail_all(gf_fserver* s, int rc)
     s->last_error = gf_ctx_last_error(s->ctx);
     for (Req* x : s->active) finish(s, x, GF_SCEN_FAILED);
     s->active.clear();
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < GF_FSERVER_LANES; ++k) {
         for (Req* x : s->joining[k]) finish(s, x, GF_SCEN_FAILED);
         s->joining[k].clear();
     }
@@ -241,7 +243,8 @@ int fail_all(gf_fserver* s, int rc)
 
 bool fits(const gf_fserver* s, const Req* x)
 {
-    const size_t running = s->active.size() + s->joining[0].size() + s->joining[1].size();
+    size_t running = s->active.size();
+    for (int k = 0; k < GF_FSERVER_LANES; ++k) running += s->joining[k].size();
     return (int)running < s->o.max_active && !s->free_slots.empty() &&
            s->bytes_in_use + x->info.footprint <= s->o.hbm_budget;
 }
@@ -274,7 +277,7 @@ int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
      * stays resident for the caller; its physics slot is free again) */
     std::vector<Req*> still;
     for (Req* x : s->active) {
-        if (x->lane == 2) {
+        if (x->lane == kSubLane) {
             if (x->cancel_req) gf::subforests_stop(x->f);
             if (gf::subforests_running(x->f)) {
                 still.push_back(x);
@@ -333,10 +336,15 @@ int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
         if (gf::forest_batch_inflight(s->lanes[k])) continue;
         if (!s->joining[k].empty()) join(s, k);
         if (!gf::forest_batch_members(s->lanes[k])) continue;
-        if (k == 1) {
-            /* the large lane leaves SMs free only while small forests run */
-            const bool small = gf::forest_batch_members(s->lanes[0]) > 0 || !s->joining[0].empty();
-            gf::forest_batch_set_max_ctas(s->lanes[1], small ? s->cap_large : 0);
+        if (k > 0) {
+            /* a lane leaves reserve_sms SMs free per smaller lane with forests running */
+            int smaller = 0;
+            for (int j = 0; j < k; ++j)
+                smaller += gf::forest_batch_members(s->lanes[j]) > 0 || !s->joining[j].empty();
+            int cap = 0;
+            if (smaller && s->o.reserve_sms > 0)
+                cap = std::max(s->nsm / 4, s->nsm - s->o.reserve_sms * smaller);
+            gf::forest_batch_set_max_ctas(s->lanes[k], cap);
         }
         int live = 0;
         int rc = gf::forest_batch_launch(s->lanes[k], &live);
@@ -367,7 +375,9 @@ int pump_locked(gf_fserver* s, int* busy, int* progress = nullptr)
     s->stats.s_epoch = sum.s_epoch;
     s->stats.s_rounds = sum.s_rounds;
     s->stats.s_regrid = sum.s_regrid;
-    if (busy) *busy = !s->queue.empty() || !s->active.empty() || !s->joining[0].empty() || !s->joining[1].empty();
+    bool joining = false;
+    for (int k = 0; k < GF_FSERVER_LANES; ++k) joining |= !s->joining[k].empty();
+    if (busy) *busy = !s->queue.empty() || !s->active.empty() || joining;
     if (progress) *progress = moved;
     return GF_OK;
 }
@@ -414,8 +424,9 @@ void gf_fserver_opts_default(gf_fserver_opts* o)
     o->hbm_budget = (size_t)64 << 30;
     o->max_active = 256;
     o->backfill = 1;
-    o->lane_cells = 1 << 18;
-    o->reserve_sms = 48;
+    o->lane_cells[0] = 1 << 18;
+    o->lane_cells[1] = 1 << 20;
+    o->reserve_sms = 40;
 }
 
 int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out)
@@ -425,26 +436,25 @@ int gf_fserver_create(int device, const gf_fserver_opts* opts, gf_fserver** out)
     gf_fserver_opts o;
     if (opts) o = *opts;
     else gf_fserver_opts_default(&o);
-    if (o.max_active < 1 || o.max_active > GF_MAX_PHYS || o.hbm_budget == 0 || o.lane_cells < 0 ||
-        o.reserve_sms < 0)
+    if (o.max_active < 1 || o.max_active > GF_MAX_PHYS || o.hbm_budget == 0 || o.reserve_sms < 0)
         return GF_ERR_ARG;
+    int nl = 1;
+    for (int k = 0; k < GF_FSERVER_LANES - 1 && o.lane_cells[k] > 0; ++k) {
+        if (k > 0 && o.lane_cells[k] <= o.lane_cells[k - 1]) return GF_ERR_ARG;
+        ++nl;
+    }
     gf_fserver* s = new gf_fserver;
     s->device = device;
     s->o = o;
     s->t0 = Clock::now();
     int rc = gf_ctx_create(device, &s->ctx);
-    if (!rc && o.lane_cells > 0) {
-        /* the small lane on the greatest stream priority; the large lane's
-         * update grid leaves reserve_sms SMs to it */
-        s->nlanes = 2;
-        int nsm = 0;
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-        const int cap = (o.reserve_sms > 0 && nsm - o.reserve_sms > 0) ? nsm - o.reserve_sms : 0;
-        s->cap_large = cap;
-        rc = gf::forest_batch_create(s->ctx, &s->lanes[0], 1, 0);
-        if (!rc) rc = gf::forest_batch_create(s->ctx, &s->lanes[1], 2, 0);
-    } else if (!rc) {
-        rc = gf::forest_batch_create(s->ctx, &s->lanes[0]);
+    if (!rc) {
+        cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, device);
+        s->nlanes = nl;
+        /* one lane: the context's stream; several: a stream each, smaller
+         * lanes at higher priority */
+        for (int k = 0; k < nl && !rc; ++k)
+            rc = gf::forest_batch_create(s->ctx, &s->lanes[k], nl > 1 ? k + 1 : 0, 0);
     }
     if (!rc) rc = gf::subforests_create(s->ctx, &s->sub);
     if (rc) {
@@ -465,7 +475,7 @@ void gf_fserver_destroy(gf_fserver* s)
         if (kv.second->f) gf_forest_destroy(kv.second->f);
         delete kv.second;
     }
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < GF_FSERVER_LANES; ++k)
         if (s->lanes[k]) gf::forest_batch_destroy(s->lanes[k]);
     if (s->sub) gf::subforests_destroy(s->sub);
     if (s->ctx) gf_ctx_destroy(s->ctx);

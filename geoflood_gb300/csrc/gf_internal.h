@@ -122,8 +122,9 @@ cudaError_t launch_gauge_sample(const gf_gauge_task* tasks, int n, const double*
  * dropped); each iteration runs about half a millisecond of rounds, then
  * regrids the members that wait for it. */
 struct ForestBatch;
-/* stream_priority 0: the context's stream; 1 / 2: a stream of its own at the
- * greatest / least priority. max_ctas > 0 caps the update grid. */
+/* stream_priority 0: the context's stream; k >= 1: a stream of its own, k = 1
+ * at the greatest priority and each further k lower. max_ctas > 0 caps the
+ * update grid. */
 int forest_batch_create(gf_ctx* c, ForestBatch** out, int stream_priority = 0, int max_ctas = 0);
 void forest_batch_destroy(ForestBatch* b);
 /* checks the forest and starts its outstyle-1 run at its current time */

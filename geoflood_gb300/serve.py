@@ -299,9 +299,9 @@ class ForestServer:
     def __init__(self, device: int = 0, hbm_budget: int | None = None, max_active: int = 256,
                  backfill: bool = True, exact: bool | None = None, lane_cells: int | None = None,
                  reserve_sms: int | None = None):
-        """lane_cells: forests with fewer cells after initial refinement batch
-        in the small lane (0: one lane); reserve_sms: SMs the large lane's
-        update leaves to the small lane."""
+        """lane_cells: ascending cell counts after initial refinement that
+        split the forests into up to three lanes (0 or (): one lane);
+        reserve_sms: SMs a lane's update leaves per smaller running lane."""
         self._lib = _lib.load()
         o = _lib.gf_fserver_opts()
         self._lib.gf_fserver_opts_default(C.byref(o))
@@ -310,7 +310,9 @@ class ForestServer:
         o.max_active = int(max_active)
         o.backfill = int(bool(backfill))
         if lane_cells is not None:
-            o.lane_cells = int(lane_cells)
+            cells = (lane_cells,) if np.ndim(lane_cells) == 0 else tuple(lane_cells)
+            for k in range(2):
+                o.lane_cells[k] = int(cells[k]) if k < len(cells) else 0
         if reserve_sms is not None:
             o.reserve_sms = int(reserve_sms)
         h = C.c_void_p()

@@ -646,16 +646,16 @@ double gf_server_clock(const gf_server* s);
  *
  * Admission is by device footprint (gf_forest_footprint) against the
  * budget, first come first served (backfill: later requests that fit pass
- * a head that does not). With two lanes, small and large forests batch
- * separately on two streams: the small lane's short rounds run on the
- * higher-priority stream and on SMs the large lane's update leaves free, so
- * they are not held behind the large forests' updates. A finished forest stays resident, counted against
+ * a head that does not). Forests batch in up to three lanes by size, each
+ * on its own stream: a lane's rounds last as long as its largest member's
+ * update, so smaller forests run in their own lanes, at higher priority and
+ * on SMs the larger lanes' updates leave free. A finished forest stays resident, counted against
  * the budget, until gf_fserver_release; read it meanwhile through
  * gf_fserver_forest (or gf_fserver_download while the loop thread runs).
  * The caller keeps fields and topo alive until the request leaves QUEUED.
- * Subcycled forests (opts.subcycle = 1) run in a third lane, side by side
- * as in gf_forest_batch_run (each coarse step the forest's own graph on a
- * stream of a pool). */
+ * Subcycled forests (opts.subcycle = 1) run in lane 3, side by side as in
+ * gf_forest_batch_run (each coarse step the forest's own graph on a stream
+ * of a pool). */
 typedef struct gf_fserver gf_fserver;
 
 typedef struct gf_forest_request {
@@ -674,14 +674,17 @@ typedef struct gf_forest_request {
     double initial_dt, desired_cfl, max_cfl;
 } gf_forest_request;
 
+#define GF_FSERVER_LANES 3 /* lanes of shared rounds at most                    */
 typedef struct gf_fserver_opts {
     size_t hbm_budget;     /* device bytes admitted and unreleased forests may hold */
     int max_active;        /* forests running at once (1..GF_MAX_PHYS)          */
     int backfill;
-    long long lane_cells;  /* > 0: forests with fewer cells after initial refinement
-                              run in a small lane (its own high-priority stream),
-                              the others in a large lane; 0: one lane            */
-    int reserve_sms;       /* the large lane's update leaves this many SMs free  */
+    long long lane_cells[GF_FSERVER_LANES - 1]; /* ascending, 0 ends the list: lane k
+                              takes forests with fewer cells after initial refinement
+                              than lane_cells[k], the last lane the rest; each lane
+                              its own stream, smaller lanes at higher priority     */
+    int reserve_sms;       /* a lane's update leaves this many SMs free per smaller
+                              lane that has forests running                      */
 } gf_fserver_opts;
 
 typedef struct gf_forest_request_info {
@@ -692,12 +695,12 @@ typedef struct gf_forest_request_info {
     int npatch, npatch_max;
     size_t footprint;      /* bytes reserved at admission                       */
     size_t device_bytes;   /* bytes the forest holds (0 before admission)       */
-    int lane;              /* 0 small, 1 large, 2 subcycled (-1 before admission) */
+    int lane;              /* 0..2 shared-round lanes by size, 3 subcycled (-1 before admission) */
 } gf_forest_request_info;
 
 typedef struct gf_fserver_stats {
     long long submitted, admitted, done, failed;
-    long long lane_admitted[3];  /* per lane (small, large, subcycled)          */
+    long long lane_admitted[4];  /* per lane (shared-round lanes 0..2, subcycled 3) */
     long long iterations, epochs, rounds, launches, regrids, cell_updates;
     long long sub_steps;     /* subcycled coarse steps launched               */
     double s_admit, s_epoch, s_rounds, s_regrid; /* host seconds per phase      */
