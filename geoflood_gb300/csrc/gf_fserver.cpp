@@ -18,12 +18,14 @@
  * HBM budget, by the footprint bound of their options; each active forest
  * has its own physics slot of the server's context.
  *
- * With two lanes the loop keeps one batch per lane in flight at once: small
- * forests (by cells after their initial refinement) on a high-priority
- * stream, large ones on a low-priority stream whose update grid leaves
- * reserve_sms SMs free. A pass takes in the iterations that have finished,
- * lets members leave and join the idle lanes, admits, and launches the idle
- * lanes again; it never waits on the device.
+ * The loop keeps one batch per lane in flight at once. Forests go to up to
+ * three lanes by their cells after the initial refinement (lane_cells),
+ * each on its own stream, smaller lanes at higher priority; a lane's update
+ * grid leaves reserve_sms SMs per smaller lane that has forests running.
+ * Subcycled forests form a fourth lane that steps each forest's own graphs
+ * side by side. A pass takes in the iterations that have finished, lets
+ * members leave and join the idle lanes, admits, and launches the idle lanes
+ * again; it never waits on the device.
  */
 #include <cuda_runtime.h>
 
