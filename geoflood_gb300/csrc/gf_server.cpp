@@ -722,7 +722,7 @@ void gf_server_opts_default(gf_server_opts* o)
     o->lane_cells[2] = 0;
     o->priority = 1;
     o->backfill = 1;
-    o->reserve_sms = 16;
+    o->reserve_sms = 0; /* one CTA per patch: priority hands freed SMs to smaller lanes */
     o->mixed_update = 0; /* per-size launches: measured faster for served scenarios */
 }
 
@@ -771,9 +771,11 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
         gf_server_destroy(s);
         return GF_ERR_CUDA;
     }
-    /* later lanes run persistent update grids that leave reserve_sms SMs to
-     * the first lane, whose short rounds then start without waiting for
-     * resident CTAs of the large scenarios to retire */
+    /* with reserve_sms > 0 later lanes run persistent update grids that
+     * leave that many SMs to the first lane; with 0 (the default) every lane
+     * launches one CTA per patch, each resident for about a tenth of a
+     * millisecond, and the higher priority of the smaller lanes' streams
+     * gives them the SMs those CTAs free */
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     static const int ms[3] = {8, 16, 32};

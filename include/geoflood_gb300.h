@@ -587,7 +587,9 @@ typedef struct gf_server_opts {
     long long lane_cells[GF_SERVER_MAX_LANES]; /* lane k: cells < lane_cells[k]; last lane takes the rest */
     int priority;           /* 1: smaller lanes on higher-priority streams       */
     int backfill;           /* 1: admit later arrivals that fit while the head waits */
-    int reserve_sms;        /* lanes after the first leave this many SMs free for it */
+    int reserve_sms;        /* > 0: lanes after the first run persistent grids that
+                               leave this many SMs free for it; 0 (default): one CTA
+                               per patch, stream priority shares the SMs */
     int mixed_update;       /* 1: lanes after the first update every patch size in one
                                persistent launch (same results); 0 (default): one launch
                                per size, which keeps the small sizes' occupancy */

@@ -80,14 +80,15 @@ def test_result_is_the_same_alone_and_in_the_mix(lanes):
     assert np.array_equal(outs["b"], b_alone)
 
 
-def test_one_launch_update_of_later_lanes_gives_the_same_bits():
-    """Lanes after the first update every patch size in one persistent launch
-    (capped grid); per-size launches and each scenario alone give the same
-    bits."""
+@pytest.mark.parametrize("reserve_sms", [0, 24])
+def test_one_launch_update_of_later_lanes_gives_the_same_bits(reserve_sms):
+    """Lanes after the first update every patch size in one persistent launch,
+    or per size (one CTA per patch, or a grid capped to leave reserve_sms
+    SMs): every form and each scenario alone give the same bits."""
     scs = [scen(31, 1200, 8), scen(32, 4096, 16), scen(33, 9000, 32), scen(34, 3000, 8)]
     runs = []
     for mixed in (True, False):
-        with gf.Server(lanes=(1000,), mixed_update=mixed) as srv:
+        with gf.Server(lanes=(1000,), mixed_update=mixed, reserve_sms=reserve_sms) as srv:
             outs = [np.zeros_like(s.q) for s in scs]
             ids = [srv.submit(s, o) for s, o in zip(scs, outs)]
             srv.run_until_idle()
