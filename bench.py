@@ -42,11 +42,11 @@ METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
 # DRAM traffic of one patch-update launch of this workload (one ncu capture:
 # dram__bytes_read.sum + dram__bytes_write.sum), against 234.9 MB algorithmic
-DRAM_BYTES_PER_LAUNCH = 170.41664e6 + 62.9056e6
+DRAM_BYTES_PER_LAUNCH = 170.340864e6 + 62.683392e6
 # FP64 pipe issue slots per cell-update of this workload: 37.46 M FP64 warp
 # instructions (ncu sm__inst_executed_pipe_fp64.sum) x 32 lanes / 4 194 304
 # cell-updates
-FP64_LANE_OPS_PER_CELL_UPDATE = 37.456333e6 * 32 / 4194304.0
+FP64_LANE_OPS_PER_CELL_UPDATE = 37.356532e6 * 32 / 4194304.0
 M = 32
 NPX = NPY = 64
 DX = 1.0

@@ -673,12 +673,14 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
         double u = 0.0, v = 0.0, c = 0.0, rh = 0.0, rc = 0.0;
         if (w) {
             if (FAST) {
-                rh = gf_rcp(h);
-                u = sm[L::OFF_HU + k] * rh;
-                v = sm[L::OFF_HV + k] * rh;
+                /* rc^2 = 1 / (g h), so 1 / h = g rc^2 within a few ulps:
+                 * two products instead of a reciprocal */
                 const double gh = g * h;
                 rc = rsqrt(gh);
                 c = gh * rc;
+                rh = g * (rc * rc);
+                u = sm[L::OFF_HU + k] * rh;
+                v = sm[L::OFF_HV + k] * rh;
             } else {
                 u = sm[L::OFF_HU + k] / h;
                 v = sm[L::OFF_HV + k] / h;
