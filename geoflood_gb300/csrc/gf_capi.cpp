@@ -158,10 +158,13 @@ int cuda_fail(gf_ctx* c, cudaError_t e, const char* what)
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
     } while (0)
 
-int check_phys_slot(gf_ctx* c, int slot)
+/* maux > 0: the slot must also suit a patch with maux aux fields (a variable
+ * friction field inside them). */
+int check_phys_slot(gf_ctx* c, int slot, int maux = 0)
 {
     if (slot < 0 || slot >= GF_MAX_PHYS) return fail(c, GF_ERR_ARG, "physics slot out of range");
     if (!c->phys_set[slot]) return fail(c, GF_ERR_STATE, "physics slot not set");
+    if (const char* why = gf::phys_problem(&c->h_phys[slot], maux)) return fail(c, GF_ERR_ARG, why);
     return GF_OK;
 }
 
@@ -294,11 +297,7 @@ int gf_ctx_set_phys(gf_ctx* c, int slot, const gf_phys* p)
 {
     if (!c || !p) return GF_ERR_ARG;
     if (slot < 0 || slot >= GF_MAX_PHYS) return fail(c, GF_ERR_ARG, "physics slot out of range");
-    if (p->num_manning < 0 || p->num_manning > GF_MAX_MANNING)
-        return fail(c, GF_ERR_ARG, "num_manning out of range");
-    if (p->order != 1 && p->order != 2) return fail(c, GF_ERR_ARG, "order must be 1 or 2");
-    if (p->transverse < 0 || p->transverse > 2) return fail(c, GF_ERR_ARG, "transverse must be 0..2");
-    if (!(p->grav > 0.0) || !(p->dry_tolerance >= 0.0)) return fail(c, GF_ERR_ARG, "bad grav / dry_tolerance");
+    if (const char* why = gf::phys_problem(p, 0)) return fail(c, GF_ERR_ARG, why);
     GF_CK(c, cudaSetDevice(c->device));
     c->h_phys[slot] = *p;
     c->phys_set[slot] = 1;
@@ -331,7 +330,7 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
     if (rc) return rc;
     if (npatch < 0 || (npatch > 0 && (!dx || !dy || !q || !aux)))
         return fail(c, GF_ERR_ARG, "null argument");
-    if ((rc = check_phys_slot(c, 0))) return rc;
+    if ((rc = check_phys_slot(c, 0, maux))) return rc;
     if (npatch == 0) {
         if (maxcfl) *maxcfl = 0.0;
         return GF_OK;
@@ -650,7 +649,7 @@ static int level_prepare(gf_level* L)
     gf_ctx* c = L->ctx;
     if (!L->aux_loaded) return fail(c, GF_ERR_STATE, "level aux (bathymetry) not uploaded");
     for (int k = 0; k < L->npatch; ++k) {
-        int rc = check_phys_slot(c, L->phys[k]);
+        int rc = check_phys_slot(c, L->phys[k], L->maux);
         if (rc) return rc;
     }
     if (!L->work_dirty) return GF_OK;
@@ -1038,13 +1037,27 @@ int gf_level_tag4coarsening(gf_level* L, const gf_refine* rf, int nfam, const in
 
 /* Context access for the other host translation units (gf_forest.cpp). */
 namespace gf {
+const char* phys_problem(const gf_phys* p, int maux)
+{
+    if (!p) return "null physics";
+    if (p->num_manning < 0 || p->num_manning > GF_MAX_MANNING) return "num_manning out of range";
+    if (p->order != 1 && p->order != 2) return "order must be 1 or 2";
+    if (p->transverse < 0 || p->transverse > 2) return "transverse must be 0..2";
+    if (!(p->grav > 0.0) || !(p->dry_tolerance >= 0.0)) return "bad grav / dry_tolerance";
+    if (p->variable_friction && p->friction_index < 1)
+        return "variable friction needs friction_index >= 1";
+    if (p->variable_friction && maux > 0 && p->friction_index > maux)
+        return "variable friction needs friction_index <= maux";
+    return nullptr;
+}
+
 cudaStream_t ctx_stream(gf_ctx* c) { return c->stream; }
 int ctx_device(gf_ctx* c) { return c->device; }
 bool ctx_exact(gf_ctx* c) { return c->exact; }
 bool ctx_mixed(gf_ctx* c) { return c->mixed; }
 const gf_phys* ctx_device_phys(gf_ctx* c) { return c->d_phys; }
 const gf_phys* ctx_host_phys(gf_ctx* c, int slot) { return &c->h_phys[slot]; }
-int ctx_check_phys(gf_ctx* c, int slot) { return check_phys_slot(c, slot); }
+int ctx_check_phys(gf_ctx* c, int slot, int maux) { return check_phys_slot(c, slot, maux); }
 int ctx_fail(gf_ctx* c, int code, const char* msg) { return fail(c, code, msg); }
 int ctx_cuda_fail(gf_ctx* c, cudaError_t e, const char* what) { return cuda_fail(c, e, what); }
 } // namespace gf

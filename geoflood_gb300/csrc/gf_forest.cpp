@@ -1529,7 +1529,7 @@ int gf_forest_create(gf_ctx* c, const gf_forest_opts* o, const double* fields, g
         o->refine.num_flowgrades < 0 || o->refine.num_flowgrades > GF_MAX_FLOWGRADES ||
         o->refine.num_regions < 0 || o->refine.num_regions > GF_MAX_REGIONS)
         return gf::ctx_fail(c, GF_ERR_ARG, "refinement parameter counts out of range");
-    int rc = gf::ctx_check_phys(c, o->phys_slot);
+    int rc = gf::ctx_check_phys(c, o->phys_slot, o->maux);
     if (rc) return rc;
     /* a regrid holds the new patches and the ones they replace at once: at
      * most full refinement plus the parents being split (a quarter of it) */

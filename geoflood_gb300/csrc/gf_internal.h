@@ -5,9 +5,37 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <atomic>
+
 #include "gf_types.h"
 
 namespace gf {
+
+/* Raise a kernel's dynamic shared-memory limit to `bytes` on the current
+ * device. The attribute belongs to the kernel in one device's context, so
+ * it is set once per device: `done` keeps one bit per device ordinal
+ * (ordinals of 64 and above are set on every call). */
+template <class Kernel>
+inline cudaError_t smem_attr_per_device(Kernel kern, int bytes,
+                                        std::atomic<unsigned long long>& done)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    if (bit) done.fetch_or(bit, std::memory_order_release);
+    return cudaSuccess;
+}
+
+/* What is wrong with a set of physics parameters, or nullptr when they are
+ * usable: num_manning within the table, order 1 or 2, transverse 0..2,
+ * g > 0, dry tolerance >= 0, and with variable friction a friction_index of
+ * at least 1 and, when maux > 0, at most maux (the kernel reads that aux
+ * field of every cell). maux = 0 skips the upper bound (not yet known). */
+const char* phys_problem(const gf_phys* p, int maux);
 
 /* gdt / gpar (nullable): per-group dt (<= 0 skips the group) and state
  * parity (1: the group's state is in the work items' qout buffers). */
@@ -88,7 +116,7 @@ bool ctx_exact(gf_ctx* c); /* contraction-free update build selected */
 bool ctx_mixed(gf_ctx* c); /* batched forms: one launch for all patch sizes */
 const gf_phys* ctx_device_phys(gf_ctx* c);
 const gf_phys* ctx_host_phys(gf_ctx* c, int slot);
-int ctx_check_phys(gf_ctx* c, int slot);
+int ctx_check_phys(gf_ctx* c, int slot, int maux = 0);
 int ctx_fail(gf_ctx* c, int code, const char* msg);
 int ctx_cuda_fail(gf_ctx* c, cudaError_t e, const char* what);
 

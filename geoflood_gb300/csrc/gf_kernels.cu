@@ -22,13 +22,9 @@ static cudaError_t launch_update(const gf_patch_work* work, int nwork, const gf_
 {
     using L = Smem<M, RB, false>;
     auto kern = patch_update_kernel<M, NT, RB, MINB, false>;
-    static bool attr_set = false; /* per process; the attribute is per function */
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)L::BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_done{0};
+    cudaError_t ae = smem_attr_per_device(kern, (int)L::BYTES, attr_done);
+    if (ae != cudaSuccess) return ae;
     if (nwork <= 0) return cudaSuccess;
     const int grid = (max_ctas > 0 && max_ctas < nwork) ? max_ctas : nwork;
     kern<<<grid, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err);
@@ -156,12 +152,9 @@ cudaError_t launch_patch_update_mixed(const gf_patch_work* work, const int n[3],
 {
     using X = MixedSmem<kMixRB8, kMixRB16, kMixRB32, false>;
     auto kern = patch_update_mixed_kernel<kMixNT, kMixRB8, kMixRB16, kMixRB32, false>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X::BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_done{0};
+    cudaError_t ae = smem_attr_per_device(kern, (int)X::BYTES, attr_done);
+    if (ae != cudaSuccess) return ae;
     const int nwork = n[0] + n[1] + n[2];
     if (nwork <= 0) return cudaSuccess;
     int grid = sm_count();

@@ -22,13 +22,9 @@ static cudaError_t launch_exact(const gf_patch_work* work, int nwork, const gf_p
 {
     using L = gf_exact::Smem<M, RB, true>;
     auto kern = gf_exact::patch_update_kernel<M, NT, RB, 1, true>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)L::BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_done{0};
+    cudaError_t ae = smem_attr_per_device(kern, (int)L::BYTES, attr_done);
+    if (ae != cudaSuccess) return ae;
     if (nwork <= 0) return cudaSuccess;
     kern<<<nwork, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err);
     return cudaGetLastError();
@@ -56,12 +52,9 @@ cudaError_t launch_patch_update_mixed_exact(const gf_patch_work* work, const int
     /* the per-size exact tiles at 256 threads: mx = 32 keeps 4 slices per band */
     using X = gf_exact::MixedSmem<10, 13, 4, true>;
     auto kern = gf_exact::patch_update_mixed_kernel<256, 10, 13, 4, true>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)X::BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_done{0};
+    cudaError_t ae = smem_attr_per_device(kern, (int)X::BYTES, attr_done);
+    if (ae != cudaSuccess) return ae;
     const int nwork = n[0] + n[1] + n[2];
     if (nwork <= 0) return cudaSuccess;
     int grid = sm_count();

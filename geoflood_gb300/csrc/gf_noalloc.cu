@@ -72,6 +72,10 @@ int scratch_on(int device, unsigned char** out)
     return GF_OK;
 }
 
+int update_on_device(int device, const gf_phys* phys, int npatch, int mx, int my, int maux,
+                     const double* dx, const double* dy, double dt, double* q, const double* aux,
+                     double* cfl, double* maxcfl, cudaStream_t st);
+
 } // namespace
 
 extern "C" int gf_patch_update_noalloc(int device, const gf_phys* phys, int npatch, int mx, int my,
@@ -84,14 +88,31 @@ extern "C" int gf_patch_update_noalloc(int device, const gf_phys* phys, int npat
     if (mbc != GF_MBC || meqn != GF_MEQN) return GF_ERR_UNSUPPORTED;
     if (maux < 1 || maux > kMaxMaux) return GF_ERR_ARG;         /* beyond the scratch size */
     if (npatch < 1 || npatch > kMaxPatches) return GF_ERR_ARG;  /* beyond the scratch size */
+    /* the same rules as gf_ctx_set_phys, and a variable-friction field that
+     * lies inside the maux fields the kernel stages */
+    if (gf::phys_problem(phys, maux)) return GF_ERR_ARG;
     for (int k = 0; k < npatch; ++k)
         if (!(dx[k] > 0.0) || !(dy[k] > 0.0)) return GF_ERR_ARG;
+    /* the caller's current device is put back on every return below */
+    int caller_device = -1;
+    if (cudaGetDevice(&caller_device) != cudaSuccess) return GF_ERR_CUDA;
     if (cudaSetDevice(device) != cudaSuccess) return GF_ERR_CUDA;
+    const int rc = update_on_device(device, phys, npatch, mx, my, maux, dx, dy, dt, q, aux, cfl,
+                                    maxcfl, static_cast<cudaStream_t>(stream));
+    if (cudaSetDevice(caller_device) != cudaSuccess && rc == GF_OK) return GF_ERR_CUDA;
+    return rc;
+}
+
+namespace {
+
+int update_on_device(int device, const gf_phys* phys, int npatch, int mx, int my, int maux,
+                     const double* dx, const double* dy, double dt, double* q, const double* aux,
+                     double* cfl, double* maxcfl, cudaStream_t st)
+{
     unsigned char* base = nullptr;
     int rc = scratch_on(device, &base);
     if (rc) return rc;
 
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     const long S = (long)(mx + 2 * GF_MBC) * (my + 2 * GF_MBC);
     NoallocStatus* d_status = reinterpret_cast<NoallocStatus*>(base + kOffStatus);
     gf_phys* d_phys = reinterpret_cast<gf_phys*>(base + kOffPhys);
@@ -132,3 +153,5 @@ extern "C" int gf_patch_update_noalloc(int device, const gf_phys* phys, int npat
     *maxcfl = v;
     return GF_OK;
 }
+
+} // namespace

@@ -297,10 +297,16 @@ int gf_level_tag4coarsening(gf_level* lev, const gf_refine* rf, int nfam,
  * GF_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * exit. Limits: npatch <= GF_NOALLOC_MAX_PATCHES (16), maux <=
  * GF_NOALLOC_MAX_MAUX (4), mx = my in {8, 16, 32}; larger sizes return
- * GF_ERR_ARG, other shapes GF_ERR_UNSUPPORTED. The first call on a device
- * looks up the array's device address, so make that first call before any
- * stream capture. All calls share the array: calls whose GPU work overlaps
- * race, so issue them one after another. */
+ * GF_ERR_ARG, other shapes GF_ERR_UNSUPPORTED, and `phys` is held to the
+ * rules of gf_ctx_set_phys (with variable friction, friction_index must
+ * lie in 1..maux), GF_ERR_ARG otherwise; all of these are checked before
+ * any device memory is touched. The first call on a device looks up the
+ * array's device address, so make that first call before any stream
+ * capture. The call is synchronous: it waits for `stream` to finish its
+ * work before it returns. It makes `device` current while it runs and
+ * puts the caller's current device back before returning. All calls share
+ * the array: calls whose GPU work overlaps race, so issue them one after
+ * another. */
 #define GF_NOALLOC_MAX_PATCHES 16
 #define GF_NOALLOC_MAX_MAUX 4
 #define GF_NOALLOC_SCRATCH_BYTES 1162752
