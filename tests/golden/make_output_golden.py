@@ -130,4 +130,9 @@ def main(reference: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GF_REFERENCE_ROOT")
+    if not ref:
+        raise SystemExit("usage: name the GeoFlood reference tree (argument or GF_REFERENCE_ROOT)")
+    main(ref)

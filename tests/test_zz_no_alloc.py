@@ -62,6 +62,7 @@ def _case(m, n, maux):
     dx = 32.0 / m
     q, b, _, _ = synth.uniform_dam_break_level(npx, npy, m, dx, seed=91 + m + n,
                                                x_dam=0.45 * npx * m * dx)
+    q = np.array(q)
     q[..., 1] = 0.4 * q[..., 0]
     q[..., 2] = -0.1 * q[..., 0]
     rng = np.random.default_rng(5 * m + n)
