@@ -62,14 +62,12 @@ def workload():
     return q, aux, py, px
 
 
-def config(extra=None):
-    c = {"workload": "uniform dam-break level, 4096 patches of 32x32 (2048x2048 cells), "
-                     "fractal DEM Hurst 0.8 relief 30 m + 5x40 m channel, FP64",
-         "patches": NPX * NPY, "mx": M, "mbc": 2, "cells": NPX * NPY * M * M,
-         "dx_m": DX, "dt_s": DT, "l2": "inputs (170 MB) larger than L2; no flush"}
-    if extra:
-        c.update(extra)
-    return c
+def config():
+    """The workload both arms run (the same dict in both JSON lines)."""
+    return {"workload": "dam-break level step: 4096 patches of 32x32 (2048x2048 cells, dx 1 m), "
+                        "fractal DEM Hurst 0.8 relief 30 m + 5x40 m channel, FP64",
+            "patches": NPX * NPY, "mx": M, "cells": NPX * NPY * M * M, "dt_s": DT,
+            "l2": "inputs 170 MB > L2, no flush"}
 
 
 def load_peaks():
@@ -156,21 +154,50 @@ def cpu_oracle_rate(q, aux, seconds=12.0, rows=8, threads=0):
     return cells / el, cores, f"{reps} step(s) of {rows} patch rows ({n} patches, {n * M * M} cells)"
 
 
-def plain_per_patch_rate(ctx, q, aux, npatch=256):
-    """The plain per-patch drop-in: gf_patch_update once per patch with host
-    buffers (one launch, host<->device copies per call), as ForestClaw's
-    single_step_update would drive it. Sample: npatch patches across the
-    dam-break front (same wet fraction as the level)."""
-    start = (NPY // 2) * NPX
-    qs = [np.ascontiguousarray(q[start + k]) for k in range(npatch)]
-    aus = [np.ascontiguousarray(aux[start + k]) for k in range(npatch)]
-    for k in range(8):
-        ctx.patch_update(qs[k].copy(), aus[k], DX, DX, 0.0, DT)
+def buffered_hook_rate(ctx, q, aux, dx, dt, steps=3, buffer_len=1024):
+    """The plain per-patch GPU drop-in as ForestClaw drives the reference's
+    GPU build: every patch of the level handed to the buffered
+    single_step_update hook (gf_step_buffer_update, as cudaclaw_update,
+    src/fc2d_cpu_cuda/fc2d_cpucuda.cpp:410-495) one at a time from its own
+    host array, flushed every buffer_len patches (1024, the reference
+    examples' buffer_length). Returns cell-updates/s over `steps` level
+    steps after one untimed step."""
+    import geoflood_gb300 as gf
+
+    n, m = q.shape[0], q.shape[1] - 4
+    qs = [np.array(q[k]) for k in range(n)]
+    auxs = [np.ascontiguousarray(aux[k]) for k in range(n)]
+    buf = gf.StepBuffer(ctx, buffer_len)
+
+    def level_step():
+        mc = 0.0
+        for k in range(n):
+            mc = max(mc, buf.update(k, n, qs[k], auxs[k], dx, dx, 0.0, dt))
+        return mc
+
+    level_step()
     t0 = time.perf_counter()
-    for k in range(npatch):
-        ctx.patch_update(qs[k], aus[k], DX, DX, 0.0, DT)
+    for _ in range(steps):
+        level_step()
     el = time.perf_counter() - t0
-    return npatch * M * M / el, f"{npatch} patches of 32x32, one gf_patch_update call each"
+    buf.close()
+    return steps * n * m * m / el
+
+
+def lone_patch_latency_us(ctx, q, aux, reps=50):
+    """One wet 32 x 32 patch through gf_patch_update (host buffers, one call):
+    the median latency of a lone patch, the drop-in's single-patch path."""
+    k = int(np.argmax((q[:, 2:-2, 2:-2, 0] > 1e-3).sum(axis=(1, 2))))
+    qk, ak = np.array(q[k]), np.ascontiguousarray(aux[k])
+    for _ in range(5):
+        ctx.patch_update(qk.copy(), ak, DX, DX, 0.0, DT)
+    ts = []
+    for _ in range(reps):
+        w = qk.copy()
+        t0 = time.perf_counter()
+        ctx.patch_update(w, ak, DX, DX, 0.0, DT)
+        ts.append(time.perf_counter() - t0)
+    return 1e6 * float(np.median(ts))
 
 
 def reduce_over_ranks(dist, values: dict, ops: dict) -> dict:
@@ -211,9 +238,10 @@ def served_stream(args):
     """Served scenario stream: Poisson arrivals of flood scenarios
     (finest-level cells log-uniform in [1e4, 4e6], mx drawn from {8,16,32},
     fractal valley DEM with a channel, hydrograph peak 10-500 m^3/s rising
-    over 0.5-2 h, n ~ U[0.02, 0.08], horizon 1-6 h; times scaled by
-    --served-time-scale) through the continuous-batching server at 80 % of
-    the capacity measured in a saturated calibration pass."""
+    over 0.5-2 h, n ~ U[0.02, 0.08], horizon 1-6 h; times multiplied by
+    --served-time-scale, 1 = the horizons as drawn) through the
+    continuous-batching server at 80 % of the capacity measured in a
+    saturated calibration window."""
     import threading
 
     import geoflood_gb300 as gf
@@ -232,6 +260,9 @@ def served_stream(args):
         sc = synth.flood_scenario(seeds[k], float(cells[k]), time_scale=ts, alloc=_pinned)
         return sc, _pinned(sc.q.shape)
 
+    def wet_fraction(q, drytol):
+        return float((q[:, 2:-2, 2:-2, 0] > drytol).mean())
+
     # warm the shared DEM lattices so generation keeps ahead of arrivals
     synth.flood_scenario(1, 3e6, mx=32, time_scale=ts)
     synth.flood_scenario(2, 3e6, mx=32, time_scale=ts)
@@ -240,34 +271,40 @@ def served_stream(args):
     srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms, lanes=lanes)
     srv.start()
 
-    # -- calibration: a saturated batch, throughput while most are in flight
-    ncal = min(32, n)
+    # -- calibration: a saturated batch; throughput over a bounded window
+    #    (until half of it has finished, or --served-cal-seconds), the rest
+    #    cancelled
+    ncal = min(16, n)
     cal_items = [make(k) for k in range(ncal)]
     st_a = srv.stats()
     t0 = srv.clock()
     cal_ids = [srv.submit(sc, qo) for sc, qo in cal_items]
-    samples = []
     while True:
         st = srv.stats()
-        samples.append((srv.clock(), st["cell_updates"] - st_a["cell_updates"],
-                        st["active"] + st["queued"]))
-        if st["active"] + st["queued"] == 0:
+        t_now = srv.clock()
+        left = st["active"] + st["queued"]
+        if left <= ncal // 2 or t_now - t0 >= args.served_cal_seconds:
             break
         time.sleep(0.002)
-    half = next((t, w) for t, w, left in samples if left <= ncal // 2)
-    cap = half[1] / (half[0] - t0)
-    cal_info = [srv.wait(i, timeout=600) for i in cal_ids]
+    cap = (st["cell_updates"] - st_a["cell_updates"]) / (t_now - t0)
+    cal_info = [srv.poll(i) for i in cal_ids]
     for i in cal_ids:
+        if srv.poll(i)["state"] not in ("done", "failed", "cancelled"):
+            srv.cancel(i)
+    for i in cal_ids:
+        srv.wait(i, timeout=600)
         srv.release(i)
     del cal_items
-    steps_per_sim_s = sum(i["steps"] for i in cal_info) / sum(p["horizon"] for p in params[:ncal])
+    steps_per_sim_s = (sum(i["steps"] for i in cal_info) /
+                       max(sum(i["t"] for i in cal_info), 1e-9))
     est_work = float(np.mean([cells[k] * params[k]["horizon"] * steps_per_sim_s for k in range(n)]))
     rate = 0.8 * cap / est_work
     gaps = np.random.default_rng(SERVED_SEED + 7).exponential(1.0 / rate, n)
     arrivals = np.cumsum(gaps) - gaps[0]
-    # size-stratified sample from the first half (which both loads run)
-    order = np.argsort(cells[: n // 2])
-    sample = sorted({int(order[int(round(f * (n // 2 - 1)))]) for f in np.linspace(0.0, 1.0, 12)})
+    # size-stratified sample for the isolated re-runs
+    ns = min(args.served_sample, n)
+    order = np.argsort(cells)
+    sample = sorted({int(order[int(round(f * (n - 1)))]) for f in np.linspace(0.0, 1.0, ns)})
 
     def run_stream(arrivals, count):
         """The first `count` scenarios at the given arrival times: producer
@@ -308,6 +345,7 @@ def served_stream(args):
         st0 = srv.stats()
         t_start = srv.clock()
         ids, pending, infos, outs, late, mx_of = {}, [], {}, {}, 0, {}
+        qout_of, drytol_of, wet0, wet1 = {}, {}, {}, {}
 
         def sweep(block=False):
             for k in list(pending):
@@ -315,6 +353,7 @@ def served_stream(args):
                 if info["state"] in ("done", "failed", "cancelled"):
                     infos[k] = info
                     pending.remove(k)
+                    wet1[k] = wet_fraction(qout_of.pop(k), drytol_of[k])
                     if k not in sample:
                         srv.release(ids[k])
 
@@ -327,6 +366,9 @@ def served_stream(args):
                 late += 1
             ids[k] = srv.submit(sc, qo)
             mx_of[k] = sc.mx
+            drytol_of[k] = sc.phys.dry_tolerance
+            wet0[k] = wet_fraction(sc.q, sc.phys.dry_tolerance)
+            qout_of[k] = qo
             pending.append(k)
             if k in sample:
                 outs[k] = qo
@@ -338,58 +380,53 @@ def served_stream(args):
         for k in sample:
             if k in ids:
                 srv.release(ids[k])
-        return infos, outs, late, mx_of, st0, srv.stats(), t_start, max(i["t_done"] for i in infos.values())
+        return (infos, outs, late, mx_of, st0, srv.stats(), t_start,
+                max(i["t_done"] for i in infos.values()), wet0, wet1)
 
-    infos, outs, late, mx_of, st0, st1, t_start, t_end = run_stream(arrivals, n)
-    # the first half of the stream again at 50 % load (arrival gaps x 1.6)
-    n_low = n // 2
-    low = run_stream(arrivals[:n_low] * 1.6, n_low)
+    infos, outs, late, mx_of, st0, st1, t_start, t_end, wet0, wet1 = run_stream(arrivals, n)
+    low = None
+    if args.served_low_load:
+        # the first half of the stream again at 50 % load (arrival gaps x 1.6)
+        low = run_stream(arrivals[: n // 2] * 1.6, n // 2)
     failed = sum(1 for i in infos.values() if i["state"] != "done")
     lat = np.array([i["t_done"] - i["t_submit"] for i in infos.values()])
     work = sum(i["cell_updates"] for i in infos.values())
     served_rate = work / (t_end - t_start)
+    # wet cell-updates: each scenario's cell-updates times the mean of its
+    # start and end wet fractions
+    wet_work = sum(i["cell_updates"] * 0.5 * (wet0[k] + wet1[k]) for k, i in infos.items())
 
     # -- isolated re-runs of a size-stratified sample: latency alone, same bits
     slow, slow_low, same, detail = [], [], True, []
-    infos_low, outs_low = low[0], low[1]
     for k in sample:
         sc, qo = make(k)
         sid = srv.submit(sc, qo)
-        ik = srv.wait(sid, timeout=600)
+        ik = srv.wait(sid, timeout=3600)
         t_iso = ik["t_done"] - ik["t_submit"]
         t_mix = infos[k]["t_done"] - infos[k]["t_submit"]
         slow.append(t_mix / t_iso)
         same &= bool(np.array_equal(qo, outs[k])) and ik["steps"] == infos[k]["steps"]
-        if k in infos_low:
-            slow_low.append((infos_low[k]["t_done"] - infos_low[k]["t_submit"]) / t_iso)
-            same &= bool(np.array_equal(qo, outs_low[k]))
+        if low is not None and k in low[0]:
+            slow_low.append((low[0][k]["t_done"] - low[0][k]["t_submit"]) / t_iso)
+            same &= bool(np.array_equal(qo, low[1][k]))
         detail.append({"cells": int(sc.cells), "mx": sc.mx, "lane": ik["lane"], "steps": ik["steps"],
-                       "isolated_s": t_iso, "mixed_s": t_mix,
+                       "isolated_s": t_iso, "mixed_s": t_mix, "wet_end": wet1[k],
                        "queued_s": infos[k]["t_admit"] - infos[k]["t_submit"]})
         srv.release(sid)
     srv.stop()
     srv.close()
-    lat_low = np.array([i["t_done"] - i["t_submit"] for i in infos_low.values()])
 
-    # -- the plain per-patch drop-in on the same work mix
+    # -- the plain per-patch drop-in (the buffered hook) on the same work mix
     ctx = gf.Context(dev)
     rate_mx = {}
     for mx in (8, 16, 32):
-        sc = synth.flood_scenario(SERVED_SEED, 200000, mx=mx, time_scale=ts)
+        sc = synth.flood_scenario(SERVED_SEED, 2.0e6, mx=mx, time_scale=ts)
         ctx.set_phys(0, sc.phys)
-        npt = min(256, sc.q.shape[0])
-        qs = [np.ascontiguousarray(sc.q[k]) for k in range(npt)]
-        aus = [np.ascontiguousarray(sc.aux[k]) for k in range(npt)]
-        for k in range(min(8, npt)):
-            ctx.patch_update(qs[k].copy(), aus[k], sc.dx, sc.dy, 0.0, 0.2)
-        tp = time.perf_counter()
-        for k in range(npt):
-            ctx.patch_update(qs[k], aus[k], sc.dx, sc.dy, 0.0, 0.2)
-        rate_mx[mx] = npt * mx * mx / (time.perf_counter() - tp)
+        rate_mx[mx] = buffered_hook_rate(ctx, sc.q, sc.aux, sc.dx, 0.2, steps=2)
     ctx.close()
     plain_time = sum(i["cell_updates"] / rate_mx[mx_of[k]] for k, i in infos.items())
     plain_rate = work / plain_time
-    return {
+    out = {
         "value": served_rate, "unit": METRIC, "scenarios": n, "failed": failed,
         "p50_latency_s": float(np.percentile(lat, 50)),
         "p99_latency_s": float(np.percentile(lat, 99)),
@@ -397,28 +434,35 @@ def served_stream(args):
                                  "p99": float(np.percentile(slow, 99)), "max": float(max(slow)),
                                  "sample": len(sample), "detail": detail},
         "alone_equals_mix": same,
-        "at_50pct_load": {"scenarios": n_low, "arrival_rate_per_s": rate / 1.6,
-                          "p50_latency_s": float(np.percentile(lat_low, 50)),
-                          "p99_latency_s": float(np.percentile(lat_low, 99)),
-                          "slowdown_vs_isolated": {"p50": float(np.percentile(slow_low, 50)),
-                                                   "p99": float(np.percentile(slow_low, 99)),
-                                                   "max": float(max(slow_low)), "sample": len(slow_low)},
-                          "note": "the first half of the stream, arrival gaps x 1.6"},
+        "wet_fraction": wet_work / max(work, 1),
+        "wet_cell_updates_per_s": wet_work / (t_end - t_start),
         "plain_per_patch": {"value": plain_rate, "unit": METRIC,
                             "per_mx": {str(k): v for k, v in rate_mx.items()},
-                            "note": "gf_patch_update per patch with host buffers, weighted by "
-                                    "the stream's work per mx"},
+                            "note": "buffered single_step_update hook (gf_step_buffer_update, "
+                                    "buffer 1024) with host buffers, weighted by the stream's "
+                                    "work per mx"},
         "vs_plain_per_patch": served_rate / plain_rate,
-        "capacity": {"value": cap, "unit": METRIC, "scenarios": ncal,
-                     "window_s": half[0] - t0,
-                     "note": "saturated batch, until half of it has finished"},
+        "capacity": {"value": cap, "unit": METRIC, "scenarios": ncal, "window_s": t_now - t0,
+                     "note": "saturated batch, until half of it had finished or the window "
+                             "closed"},
         "arrival_rate_per_s": rate, "offered_load": 0.8, "late_submissions": late,
         "stream_seconds": t_end - t_start, "cell_updates": work,
         "launches": st1["launches"] - st0["launches"], "rounds": st1["rounds"] - st0["rounds"],
         "peak_device_bytes": st1["bytes_peak"],
         "workload": f"{n} flood scenarios, cells log-uniform [1e4, 4e6], mx in {{8,16,32}}, "
-                    f"dx 5 m, times x{ts:.5g} (horizon 1-6 h -> {3600 * ts:.0f}-{21600 * ts:.0f} s)",
+                    f"dx 5 m, horizons 1-6 h x{ts:.4g}",
     }
+    if low is not None:
+        lat_low = np.array([i["t_done"] - i["t_submit"] for i in low[0].values()])
+        out["at_50pct_load"] = {
+            "scenarios": n // 2, "arrival_rate_per_s": rate / 1.6,
+            "p50_latency_s": float(np.percentile(lat_low, 50)),
+            "p99_latency_s": float(np.percentile(lat_low, 99)),
+            "slowdown_vs_isolated": {"p50": float(np.percentile(slow_low, 50)),
+                                     "p99": float(np.percentile(slow_low, 99)),
+                                     "max": float(max(slow_low)), "sample": len(slow_low)},
+            "note": "the first half of the stream, arrival gaps x 1.6"}
+    return out
 
 
 def run_reference(args):
@@ -453,13 +497,78 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": config({"sample": f"{rows} patch rows ({n} patches, {cells} cells) per step"}),
+            "config": config(),
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
                              "sample": f"{rows} patch rows ({n} patches) per step; reference "
                                        "Fortran not buildable (no Fortran compiler/ForestClaw)"},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def _sig(x, n=4):
+    """x rounded to n significant digits (floats only)."""
+    if isinstance(x, float) and x != 0.0 and np.isfinite(x):
+        return float(f"{x:.{n}g}")
+    return x
+
+
+def compact(r: dict) -> dict:
+    """The one-line record: the contract's keys and a short summary of every
+    leg (the full figures go to --detail)."""
+    keep = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+            "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "gpu_launches",
+            "config", "e2e", "cpu_baseline")
+    out = {k: r[k] for k in keep if k in r}
+    out["value"], out["ms_per_step"] = _sig(r["value"]), _sig(r["ms_per_step"])
+    if "e2e" in out:
+        out["e2e"] = dict(out["e2e"], value=_sig(out["e2e"]["value"]))
+    if "cpu_baseline" in out:
+        out["cpu_baseline"] = dict(out["cpu_baseline"], value=_sig(out["cpu_baseline"]["value"]))
+    rl = r["roofline"]
+    out["roofline"] = {"bound": rl["bound"], "achieved": _sig(rl["achieved"]), "peak": rl["peak"],
+                       "unit": rl["unit"], "frac": _sig(rl["frac"], 3), "traffic": rl["traffic"]}
+    ck = r.get("clocks") or {}
+    out["clocks"] = {"sm_mhz": ck.get("sm_mhz"), "sm_max_mhz": ck.get("sm_max_mhz"),
+                     "reasons": ck.get("reasons")}
+    fp = r.get("fp64")
+    if fp:
+        out["fp64"] = {"frac_of_measured_dfma": _sig(fp["frac_of_measured_dfma"], 3),
+                       "achieved_gops": _sig(fp["achieved_gops"]),
+                       "peak_gops": _sig(fp["peak_dfma_gops"])}
+    pp = r.get("plain_per_patch")
+    if pp:
+        out["plain_per_patch"] = {"value": _sig(pp["value"]), "lone_patch_us": _sig(pp["lone_patch_us"])}
+    sv = r.get("served")
+    if sv:
+        out["served"] = {"value": _sig(sv["value"]), "scenarios": sv["scenarios"],
+                         "horizons": sv["workload"].split("horizons ")[-1],
+                         "p50_s": _sig(sv["p50_latency_s"], 3), "p99_s": _sig(sv["p99_latency_s"], 3),
+                         "slowdown_p50": _sig(sv["slowdown_vs_isolated"]["p50"], 3),
+                         "slowdown_p99": _sig(sv["slowdown_vs_isolated"]["p99"], 3),
+                         "wet_frac": _sig(sv["wet_fraction"], 3),
+                         "vs_plain_per_patch": _sig(sv["vs_plain_per_patch"], 3),
+                         "alone_equals_mix": sv["alone_equals_mix"]}
+    bt = r.get("batched")
+    if bt:
+        out["batched"] = {"value": _sig(bt["value"]),
+                          "vs_one_by_one": _sig(bt.get("speedup_vs_one_by_one"), 3),
+                          "equal": bt.get("batch_equals_one_by_one")}
+    fs = r.get("forest")
+    if fs:
+        out["forest"] = {"value": _sig(fs["value"]),
+                         "regrid_mismatches": fs.get("regrid_parity", {}).get("mismatching_regrids"),
+                         "subcycled_batch_x": _sig(fs["to_60s"]["subcycled_batch"]["speedup_vs_one_by_one"], 3)}
+    sa = r.get("served_amr")
+    if sa:
+        sl = sa.get("slowdown_vs_isolated", {})
+        out["served_amr"] = {"value": _sig(sa["value"]), "p99_s": _sig(sa.get("p99_latency_s"), 3),
+                             "slowdown_p99": _sig(sl.get("p99"), 3)}
+    if r.get("large"):
+        out["large"] = _sig(r["large"]["value"])
+    if r.get("dem"):
+        out["dem"] = _sig(r["dem"]["value"])
+    return out
 
 
 def run_gpu(args):
@@ -554,7 +663,8 @@ def run_gpu(args):
     e2e_ms = reduce_over_ranks(dist, {"ms": e2e_ms}, {"ms": "max"})["ms"]
     qbytes = q.size * 8
 
-    plain_v, plain_sample = plain_per_patch_rate(ctx, q, aux)
+    plain_v = buffered_hook_rate(ctx, q, aux, DX, DT)
+    lone_us = lone_patch_latency_us(ctx, q, aux)
 
     hbm_peak, peak_kind = load_peaks()
     algo = BYTES_PER_CELL_UPDATE * ncell
@@ -574,23 +684,24 @@ def run_gpu(args):
         ach = ops * ncell / (kernel_ms * 1e-3) / 1e9
         fp64.update({"lane_ops_per_cell_update": ops, "achieved_gops": ach,
                      "frac_of_measured_dfma": ach / (rates["dfma"] / 1e9),
-                     "ops_source": "profiles/patch_update_m32_dambreak4096.md (ncu)"})
+                     "ops_source": "ncu sm__inst_executed_pipe_fp64.sum of this kernel on "
+                                   "this workload x 32 lanes / cell-updates (one capture)"})
     result = {
         "metric": METRIC, "value": world * ncell / (ms * 1e-3), "unit": METRIC,
         "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": config({"parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                          "step": "patch update + ghost fill (same-level copy, extrapolation BC)",
-                          "max_cfl_last_step": maxcfl}),
+        "config": config(),
+        "max_cfl_last_step": maxcfl,
+        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         "e2e": {"value": world * ncell / (e2e_ms * 1e-3), "unit": METRIC,
                 "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes + 16},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": DRAM_BYTES_PER_LAUNCH,
                      "traffic_unit": "bytes per launch",
-                     "traffic_source": "profiles/patch_update_m32_dambreak4096.md (ncu "
-                                       "dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum "
+                                       "of one launch (one capture)",
                      "algorithmic_bytes_per_launch": algo,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": kernel_ms,
@@ -598,8 +709,10 @@ def run_gpu(args):
         "fp64": fp64,
         "clocks": clk,
         "tiles": tiles,
-        "plain_per_patch": {"value": plain_v, "unit": METRIC, "sample": plain_sample,
-                            "note": "single_step_update-style drop-in, host buffers per patch"},
+        "plain_per_patch": {"value": plain_v, "unit": METRIC, "lone_patch_us": lone_us,
+                            "note": "buffered single_step_update hook over the whole level "
+                                    "(gf_step_buffer_update, buffer 1024, one host array per "
+                                    "patch); lone_patch_us: one gf_patch_update call"},
     }
     if rank == 0 and not args.no_served:
         result["served"] = served_stream(args)
@@ -616,7 +729,9 @@ def run_gpu(args):
             v, cores, sample = cpu_oracle_rate(q, aux, seconds=args.cpu_seconds)
             result["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
                                       "sample": sample}
-        print(json.dumps(result))
+        if args.detail:
+            Path(args.detail).write_text(json.dumps(result, indent=1))
+        print(json.dumps(compact(result)))
     lev.close()
     ctx.close()
     if dist:
@@ -645,6 +760,73 @@ def forest_dambreak_config(mx=16, lmin=1, lmax=3, seed=SEED):
     phys = gf.Phys(manning_coefficient=(0.035,), manning_break=(1e10,))
     return dict(mx=mx, nbx=nbx, nby=nby, lmin=lmin, lmax=lmax, dx0=dx0, b=b, q=q, rf=rf,
                 phys=phys, mthbc=(3, 3, 3, 3), regrid=2)
+
+
+def regrid_parity(ctx, c, attempts, resync, exact=False):
+    """Config-1 dam break driven step by step on the GPU forest and the
+    oracle's forest driver with the outstyle-1 control of
+    fc2d_geoclaw_run.c:229-395 (advance-one-step, reject / retake, a regrid
+    every `regrid` accepted steps). resync = True: before every regrid the
+    oracle restarts from the GPU's leaves and state, so each regrid is
+    compared from identical states (tags and the regridded patch list);
+    resync = False: both sides run free, each with its own dt control. Returns
+    (regrids, regrids whose patch lists differ)."""
+    import geoflood_gb300 as gf
+    from oracle import forest as of
+
+    if exact:
+        ctx.set_fp_contract(False)
+    G = gf.Forest(ctx, c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"],
+                  c["b"], c["q"], mthbc=c["mthbc"], regrid_interval=0, refine=c["rf"])
+    G.init()
+    O = of.Forest(c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"], c["b"],
+                  c["q"], phys=c["phys"], mthbc=c["mthbc"], regrid_interval=0, rf=c["rf"])
+    O.init()
+    level_factor = float(1 << (c["lmax"] - c["lmin"]))
+    desired, max_cfl = 0.9, 1.0
+    state = {"G": [0.0, 5.0, 0], "O": [0.0, 5.0, 0]}   # t, dt_minlevel, accepted
+
+    def attempt(name):
+        t, dtm, acc = state[name]
+        dt = dtm / level_factor
+        if name == "G":
+            cfl = G.step(t, dt)
+            G.accept(cfl <= max_cfl)
+        else:
+            snap = O.snapshot()
+            cfl = O.step(t, dt)
+            if cfl > max_cfl:
+                O.restore(snap)
+        if cfl > max_cfl:
+            state[name] = [t, dtm * desired / cfl, acc]
+            return False
+        state[name] = [t + dt, dtm * desired / cfl if cfl > 0.0 else dtm, acc + 1]
+        return state[name][2] % c["regrid"] == 0
+
+    regrids = mism = 0
+    for _ in range(attempts):
+        due = attempt("G")
+        if resync:
+            if due:
+                O.adopt(G.patches(), G.download())
+                t = state["G"][0]
+                G.regrid(t)
+                O.regrid(t)
+                regrids += 1
+                mism += int(not np.array_equal(G.patches(), O.patches()))
+        else:
+            due_o = attempt("O")
+            if due or due_o:
+                if due:
+                    G.regrid(state["G"][0])
+                if due_o:
+                    O.regrid(state["O"][0])
+                regrids += 1
+                mism += int(not (due and due_o and np.array_equal(G.patches(), O.patches())))
+    G.close()
+    if exact:
+        ctx.set_fp_contract(True)
+    return regrids, mism
 
 
 def forest_leg(args, dev=0):
@@ -726,6 +908,8 @@ def forest_leg(args, dev=0):
         "speedup_vs_one_by_one": seq_s / bat_s, "batch_equals_one_by_one": bool(same),
         "note": "gf_forest_batch_run of subcycled forests: each coarse step the forest's own graph "
                 "on a stream of a pool, the host loop waiting on no forest"}
+    rp = regrid_parity(ctx, c, steps, resync=True)
+    fr = regrid_parity(ctx, c, steps, resync=False, exact=True)
     ctx.close()
     oracle.load()
     O = of.Forest(c["mx"], c["nbx"], c["nby"], c["lmin"], c["lmax"], c["dx0"], c["dx0"], c["b"],
@@ -744,7 +928,11 @@ def forest_leg(args, dev=0):
         "cpu_oracle": {"value": O.cell_updates / cpu_s, "unit": METRIC, "seconds": cpu_s,
                        "cores": 1, "kind": "port",
                        "note": "oracle forest driver (Python tree + C kernels, one thread)"},
-        "patch_lists_equal_to_oracle": bool(np.array_equal(gpu_patches, O.patches())),
+        "regrid_parity": {"regrids": rp[0], "mismatching_regrids": rp[1],
+                          "exact_free_run": {"regrids": fr[0], "mismatching_regrids": fr[1]},
+                          "note": "production build, oracle restarted from the GPU state before "
+                                  "each regrid; exact_free_run: contraction-free build and oracle "
+                                  "each on their own"},
         "to_60s": horizon,
         "ascii_frame": {"cells": frame_cells, "bytes": frame_bytes, "seconds": frame_s,
                         "cells_per_s": frame_cells / frame_s, "MB_per_s": frame_bytes / frame_s / 1e6,
@@ -1180,8 +1368,16 @@ def main():
     ap.add_argument("--large-steps", type=int, default=24)
     ap.add_argument("--no-dem", action="store_true")
     ap.add_argument("--dem-only", action="store_true")
-    ap.add_argument("--served-scenarios", type=int, default=512)
-    ap.add_argument("--served-time-scale", type=float, default=1.0 / 150.0)
+    ap.add_argument("--served-scenarios", type=int, default=32)
+    ap.add_argument("--served-time-scale", type=float, default=1.0,
+                    help="multiplies every scenario time (horizon, hydrograph rise)")
+    ap.add_argument("--served-cal-seconds", type=float, default=8.0)
+    ap.add_argument("--served-sample", type=int, default=8,
+                    help="scenarios re-run alone for the slowdown (size-stratified)")
+    ap.add_argument("--served-low-load", action="store_true",
+                    help="also run the first half of the stream at 50 %% load")
+    ap.add_argument("--detail", default=None,
+                    help="write every figure of the run (per-leg detail) to this JSON file")
     ap.add_argument("--served-reserve-sms", type=int, default=None)
     ap.add_argument("--served-lanes", default="1e5,1e6",
                     help="cell-count boundaries between the server's size lanes")

@@ -232,6 +232,44 @@ class Context:
         return cfl, mc.value
 
 
+class StepBuffer:
+    """The buffered per-patch hook of the reference's GPU build
+    (cudaclaw_update, src/fc2d_cpu_cuda/fc2d_cpucuda.cpp:410-495) over
+    gf_step_buffer: ``update(iter, total, q, aux, ...)`` records a patch and
+    every ``buffer_len``-th call (and the last of a level step) updates the
+    recorded patches in one batch, returning its largest CFL (0 otherwise).
+    The arrays must stay alive and unmoved until the flush."""
+
+    def __init__(self, ctx: Context, buffer_len: int = 1024):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        h = C.c_void_p()
+        _check(ctx.h, self._lib.gf_step_buffer_create(ctx.h, int(buffer_len), C.byref(h)))
+        self.h = h
+        self.buffer_len = int(buffer_len)
+        self._held = []
+
+    def update(self, it: int, total: int, q: np.ndarray, aux: np.ndarray, dx: float, dy: float,
+               t: float, dt: float) -> float:
+        my4, mx4, meqn = q.shape
+        if it == 0:
+            self._held = []
+        self._held.append((q, aux))
+        mc = C.c_double()
+        _check(self.ctx.h, self._lib.gf_step_buffer_update(
+            self.h, int(it), int(total), mx4 - 2 * MBC, my4 - 2 * MBC, MBC, meqn,
+            aux.shape[-1], float(dx), float(dy), float(t), float(dt), dptr(q), dptr(aux),
+            C.byref(mc)))
+        if (it + 1) % self.buffer_len == 0 or it + 1 == total:
+            self._held = []   # flushed: the library holds no pointer to them now
+        return mc.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.gf_step_buffer_destroy(self.h)
+            self.h = None
+
+
 class Level:
     """Device-resident batch of patches (gf_level)."""
 

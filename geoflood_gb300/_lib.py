@@ -186,6 +186,11 @@ SIGNATURES = [
     ("gf_patch_update_batch", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         _dp, _dp, C.c_double, C.c_double, C.POINTER(_dp),
                                         C.POINTER(_dp), _dp, _dp]),
+    ("gf_step_buffer_create", C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    ("gf_step_buffer_destroy", None, [_vp]),
+    ("gf_step_buffer_update", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        _dp, _dp, _dp]),
     ("gf_level_create", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
     ("gf_level_destroy", None, [_vp]),
     ("gf_level_set_geometry", C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_int)]),

@@ -348,13 +348,19 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
     GF_CK(c, c->h_work.reserve(npatch));
     GF_CK(c, c->h_cfl.reserve(npatch));
 
-    /* Gather the patches into one pinned block, one copy in each direction. */
+    /* Gather the patches into one pinned block, one copy in each direction;
+     * large batches gather on several host threads. */
     double* hq = c->h_stage.p;
     double* ha = c->h_stage.p + qn;
-    for (int k = 0; k < npatch; ++k) {
+    for (int k = 0; k < npatch; ++k)
         if (!q[k] || !aux[k]) return fail(c, GF_ERR_ARG, "null patch pointer");
-        std::memcpy(hq + (size_t)k * 3 * S, q[k], sizeof(double) * 3 * S);
-        std::memcpy(ha + (size_t)k * maux * S, aux[k], sizeof(double) * maux * S);
+    gf::host_parallel_for(npatch, (long)((qn + an) * sizeof(double)), [&](long lo, long hi) {
+        for (long k = lo; k < hi; ++k) {
+            std::memcpy(hq + (size_t)k * 3 * S, q[k], sizeof(double) * 3 * S);
+            std::memcpy(ha + (size_t)k * maux * S, aux[k], sizeof(double) * maux * S);
+        }
+    });
+    for (int k = 0; k < npatch; ++k) {
         gf_patch_work w{};
         w.q = c->q_soa.p + (size_t)k * 3 * S;
         w.aux = c->aux_soa.p + (size_t)k * maux * S;
@@ -380,9 +386,88 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
         GF_CK(c, cudaMemcpyAsync(c->h_cfl.p, c->cfl.p, sizeof(double) * npatch,
                                  cudaMemcpyDeviceToHost, c->stream));
     GF_CK(c, cudaStreamSynchronize(c->stream));
-    for (int k = 0; k < npatch; ++k) std::memcpy(q[k], hq + (size_t)k * 3 * S, sizeof(double) * 3 * S);
+    gf::host_parallel_for(npatch, (long)(qn * sizeof(double)), [&](long lo, long hi) {
+        for (long k = lo; k < hi; ++k)
+            std::memcpy(q[k], hq + (size_t)k * 3 * S, sizeof(double) * 3 * S);
+    });
     if (cfl) std::memcpy(cfl, c->h_cfl.p, sizeof(double) * npatch);
     if (maxcfl) *maxcfl = mc;
+    return GF_OK;
+}
+
+/* ------------------------------------------------- buffered per-patch hook */
+
+} /* extern "C" */
+
+struct gf_step_buffer {
+    gf_ctx* ctx = nullptr;
+    int len = 0;
+    int next_iter = 0;               /* the iter the next call must carry */
+    int mx = 0, my = 0, maux = 0;
+    std::vector<double*> q;
+    std::vector<const double*> aux;
+    std::vector<double> dx, dy;
+};
+
+extern "C" {
+
+int gf_step_buffer_create(gf_ctx* c, int buffer_len, gf_step_buffer** out)
+{
+    if (!c || !out) return GF_ERR_ARG;
+    *out = nullptr;
+    if (buffer_len < 1) return fail(c, GF_ERR_ARG, "buffer_len must be >= 1");
+    gf_step_buffer* b = new gf_step_buffer();
+    b->ctx = c;
+    b->len = buffer_len;
+    b->q.reserve(buffer_len);
+    b->aux.reserve(buffer_len);
+    b->dx.reserve(buffer_len);
+    b->dy.reserve(buffer_len);
+    *out = b;
+    return GF_OK;
+}
+
+void gf_step_buffer_destroy(gf_step_buffer* b) { delete b; }
+
+int gf_step_buffer_update(gf_step_buffer* b, int iter, int total, int mx, int my, int mbc,
+                          int meqn, int maux, double dx, double dy, double t, double dt, double* q,
+                          const double* aux, double* maxcfl)
+{
+    if (!b || !q || !aux || !maxcfl) return GF_ERR_ARG;
+    gf_ctx* c = b->ctx;
+    *maxcfl = 0.0;
+    int rc = check_shape(c, mx, my, mbc, meqn, maux);
+    if (rc) return rc;
+    if (total < 1 || iter < 0 || iter >= total) return fail(c, GF_ERR_ARG, "need 0 <= iter < total");
+    if (iter == 0) { /* a new level step: forget a partial buffer of an abandoned one */
+        b->q.clear();
+        b->aux.clear();
+        b->dx.clear();
+        b->dy.clear();
+        b->next_iter = 0;
+    }
+    if (iter != b->next_iter) return fail(c, GF_ERR_STATE, "iter out of sequence");
+    if (!b->q.empty() && (mx != b->mx || my != b->my || maux != b->maux))
+        return fail(c, GF_ERR_ARG, "patches of one buffer must share mx, my and maux");
+    b->mx = mx;
+    b->my = my;
+    b->maux = maux;
+    b->q.push_back(q);
+    b->aux.push_back(aux);
+    b->dx.push_back(dx);
+    b->dy.push_back(dy);
+    b->next_iter = iter + 1;
+    if ((iter + 1) % b->len != 0 && iter + 1 != total) return GF_OK;
+    const int n = (int)b->q.size();
+    double mc = 0.0;
+    rc = gf_patch_update_batch(c, n, mx, my, mbc, meqn, maux, b->dx.data(), b->dy.data(), t, dt,
+                               b->q.data(), b->aux.data(), nullptr, &mc);
+    b->q.clear();
+    b->aux.clear();
+    b->dx.clear();
+    b->dy.clear();
+    if (rc) return rc;
+    *maxcfl = mc;
     return GF_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <stddef.h>
 
 #include <atomic>
+#include <functional>
 
 #include "gf_types.h"
 
@@ -36,6 +37,11 @@ inline cudaError_t smem_attr_per_device(Kernel kern, int bytes,
  * at least 1 and, when maux > 0, at most maux (the kernel reads that aux
  * field of every cell). maux = 0 skips the upper bound (not yet known). */
 const char* phys_problem(const gf_phys* p, int maux);
+
+/* fn(lo, hi) over shares of [0, n) on a persistent pool of host threads
+ * (the caller takes a share); `bytes` is the memory the whole range moves,
+ * and small ranges run on the calling thread alone (gf_hostpool.cpp). */
+void host_parallel_for(long n, long bytes, const std::function<void(long, long)>& fn);
 
 /* gdt / gpar (nullable): per-group dt (<= 0 skips the group) and state
  * parity (1: the group's state is in the work items' qout buffers). */

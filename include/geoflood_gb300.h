@@ -116,6 +116,27 @@ int gf_patch_update_batch(gf_ctx* ctx, int npatch, int mx, int my, int mbc,
                           double* const* q, const double* const* aux,
                           double* cfl, double* maxcfl);
 
+/* The buffered per-patch hook of the reference's GPU build, cudaclaw_update
+ * (src/fc2d_cpu_cuda/fc2d_cpucuda.cpp:410-495, buffer_len from the
+ * [cudaclaw] buffer-len option, 1024 in the reference's examples):
+ * ForestClaw's level step hands the patches one at a time with iter =
+ * 0..total-1. Each call records the patch (q and aux stay in the caller's
+ * storage); when (iter+1) % buffer_len == 0 or iter+1 == total, every
+ * recorded patch is updated as gf_patch_update_batch updates it and
+ * *maxcfl receives the largest patch CFL of that flush. Other calls set
+ * *maxcfl = 0 and leave q as it is until the flush (ForestClaw takes the
+ * maximum over all returns). A patch's CFL is capped as gf_patch_update
+ * caps it (above maxcfl_cap: 0); the reference's GPU build caps the
+ * flush's maximum instead (:488). Patches of one buffer share mx, my,
+ * maux; iter must count up from 0 without gaps (GF_ERR_STATE otherwise). */
+typedef struct gf_step_buffer gf_step_buffer;
+int gf_step_buffer_create(gf_ctx* ctx, int buffer_len, gf_step_buffer** out);
+void gf_step_buffer_destroy(gf_step_buffer* buf);
+int gf_step_buffer_update(gf_step_buffer* buf, int iter, int total, int mx,
+                          int my, int mbc, int meqn, int maux, double dx,
+                          double dy, double t, double dt, double* q,
+                          const double* aux, double* maxcfl);
+
 /* ------------------------------------------- device-resident level batch */
 typedef struct gf_level gf_level;
 

@@ -604,3 +604,13 @@ class Forest:
     def upload(self, q):
         for n, k in enumerate(self.canonical()):
             self.leaves[k][0][...] = q[n]
+
+    def adopt(self, patches, q):
+        """Take another forest's leaves and states: patches (n, 3) of (level,
+        I, J) in canonical order with q (n, my+4, mx+4, 3); each leaf's aux
+        comes from this forest's own raster pyramid. Lets a checker restart
+        this forest from the state of the forest it checks."""
+        self.leaves = {}
+        for n, p in enumerate(np.asarray(patches).reshape(-1, 3)):
+            key = (int(p[0]), int(p[1]), int(p[2]))
+            self.leaves[key] = [np.array(q[n], np.float64), self.new_patch(key, False)[1]]

@@ -113,3 +113,20 @@ def test_regrid_to_full_refinement_fits_default_pool(ctx):
     P = G.patches()
     assert len(P) == NBX * NBY * 4 ** LMAX and set(P[:, 0]) == {LMAX}
     G.close()
+
+
+def test_config1_regrids_match_oracle_from_identical_states(ctx):
+    """The 200-attempt config-1 dam break (2 x 1 blocks, mx 16, levels 1-3,
+    regrid every 2 accepted steps) in the production build: before every
+    regrid the oracle restarts from the device forest's leaves and state,
+    and every regrid must give the same patch list on both sides."""
+    import bench
+
+    c = bench.forest_dambreak_config()
+    ctx.set_phys(0, c["phys"])
+    try:
+        regrids, mismatches = bench.regrid_parity(ctx, c, 200, resync=True)
+    finally:
+        ctx.set_phys(0, gf.Phys())
+    assert regrids >= 50
+    assert mismatches == 0, f"{mismatches} of {regrids} regrids differ"
