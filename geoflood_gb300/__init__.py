@@ -384,6 +384,19 @@ class Level:
             arr[k] = _lib.gf_transfer(*[int(v) for v in t])
         _check(self.ctx.h, self._lib.gf_level_transfer(self.h, fine.h, len(tasks), arr))
 
+    def qad(self, fine: "Level", tasks, dt: float, svdflx: np.ndarray):
+        """qad (qad.f:4-371) on sides of fine patches over this coarse level:
+        tasks iterable of (fine_patch, coarse_patch, side, ox, oy); svdflx
+        (ntask, mx/2, 3) float64, accumulated in place."""
+        tasks = list(tasks)
+        arr = (_lib.gf_qad_task * max(1, len(tasks)))()
+        for k, t in enumerate(tasks):
+            arr[k] = _lib.gf_qad_task(*[int(v) for v in t])
+        if svdflx.shape != (len(tasks), self.m // 2, 3) or not svdflx.flags["C_CONTIGUOUS"]:
+            raise ValueError("svdflx must be contiguous (ntask, mx/2, 3)")
+        _check(self.ctx.h, self._lib.gf_level_qad(self.h, fine.h, len(tasks), arr, float(dt),
+                                                  dptr(svdflx)))
+
     def timeinterp(self, curr: "Level", last: "Level", alpha: float):
         _check(self.ctx.h, self._lib.gf_level_timeinterp(self.h, curr.h, last.h, alpha))
 

@@ -23,6 +23,11 @@ STATUS_NAMES = {
 }
 
 
+class gf_qad_task(C.Structure):
+    _fields_ = [("fine", C.c_int), ("coarse", C.c_int), ("side", C.c_int), ("ox", C.c_int),
+                ("oy", C.c_int)]
+
+
 class gf_phys(C.Structure):
     _fields_ = [
         ("grav", C.c_double),
@@ -215,6 +220,7 @@ SIGNATURES = [
     ("gf_measure_fp64_rates", C.c_int, [C.c_int, _dp]),
     ("gf_level_transfer", C.c_int, [_vp, _vp, C.c_int, C.POINTER(gf_transfer)]),
     ("gf_level_timeinterp", C.c_int, [_vp, _vp, _vp, C.c_double]),
+    ("gf_level_qad", C.c_int, [_vp, _vp, C.c_int, C.POINTER(gf_qad_task), C.c_double, _dp]),
     ("gf_level_tag4refinement", C.c_int, [_vp, C.POINTER(gf_refine), C.c_int, C.c_int, C.c_int,
                                           C.c_double, C.POINTER(C.c_int)]),
     ("gf_level_tag4coarsening", C.c_int, [_vp, C.POINTER(gf_refine), C.c_int,

@@ -43,6 +43,7 @@ PER_FILE = {"gf_kernels_exact.cu": ["-fmad=false"],
             # refinement tags, transfers and the served time-step controller
             # must match the oracle bit for bit: no contraction
             "gf_amr.cu": ["-fmad=false"],
+            "gf_qad.cu": ["-fmad=false"],
             "gf_served.cu": ["-fmad=false"],
             "gf_forest_kernels.cu": ["-fmad=false"],
             "gf_topo_kernels.cu": ["-fmad=false"]}

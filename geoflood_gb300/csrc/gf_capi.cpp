@@ -99,6 +99,9 @@ struct gf_ctx {
     DevBuf<gf_tag_task> tagt;
     DevBuf<int> tags;
     DevBuf<gf_refine> refine;
+    /* qad */
+    DevBuf<gf_qad_dev_task> qad;
+    DevBuf<double> qad_flux;
 };
 
 struct gf_level {
@@ -282,6 +285,8 @@ void gf_ctx_destroy(gf_ctx* c)
     c->tagt.release();
     c->tags.release();
     c->refine.release();
+    c->qad.release();
+    c->qad_flux.release();
     if (c->d_phys) cudaFree(c->d_phys);
     if (c->d_status) cudaFree(c->d_status);
     if (c->h_status) cudaFreeHost(c->h_status);
@@ -1019,6 +1024,67 @@ int gf_level_transfer(gf_level* Cl, gf_level* Fl, int ntask, const gf_transfer* 
     GF_CK(c, cudaMemcpyAsync(c->xfer.p, t.data(), ntask * sizeof(gf_xfer_task),
                              cudaMemcpyHostToDevice, c->stream));
     GF_CK(c, gf::launch_transfer(Cl->mx, c->xfer.p, ntask, c->d_phys, c->stream));
+    GF_CK(c, cudaStreamSynchronize(c->stream));
+    return GF_OK;
+}
+
+int gf_level_qad(gf_level* Cl, gf_level* Fl, int ntask, const gf_qad_task* tasks, double dt,
+                 double* svdflx)
+{
+    if (!Cl || !Fl || ntask < 0 || (ntask > 0 && (!tasks || !svdflx))) return GF_ERR_ARG;
+    gf_ctx* c = Cl->ctx;
+    if (Fl->ctx != c) return fail(c, GF_ERR_ARG, "levels belong to different contexts");
+    if (Cl->mx != Fl->mx || Cl->maux != Fl->maux)
+        return fail(c, GF_ERR_ARG, "coarse and fine levels need the same patch size and maux");
+    if (!(dt >= 0.0)) return fail(c, GF_ERR_ARG, "dt must be >= 0");
+    if (ntask == 0) return GF_OK;
+    const int m = Fl->mx, per = 3 * (m / 2);
+    auto coarse_of = [](int fi, int o) { /* coarse 1-based index of fine 1-based fi */
+        const int v = fi - o + 1;
+        return v >= 0 ? v / 2 : -((1 - v) / 2); /* floor(v / 2) */
+    };
+    std::vector<gf_qad_dev_task> t(ntask);
+    for (int k = 0; k < ntask; ++k) {
+        const gf_qad_task& u = tasks[k];
+        if (u.coarse < 0 || u.coarse >= Cl->npatch || u.fine < 0 || u.fine >= Fl->npatch)
+            return fail(c, GF_ERR_ARG, "qad patch index out of range");
+        if (u.side < 1 || u.side > 4) return fail(c, GF_ERR_ARG, "qad side must be 1..4");
+        /* every coarse cell the side's ghost cells fall in must be interior */
+        for (int f : {0, m - 1}) {
+            int fi, fj;
+            if (u.side == 1) { fi = 0; fj = 1 + f; }
+            else if (u.side == 2) { fi = 1 + f; fj = m + 1; }
+            else if (u.side == 3) { fi = m + 1; fj = 1 + f; }
+            else { fi = 1 + f; fj = 0; }
+            const int ci = coarse_of(fi, u.ox), cj = coarse_of(fj, u.oy);
+            if (ci < 1 || ci > m || cj < 1 || cj > m)
+                return fail(c, GF_ERR_ARG, "qad side's ghost cells are not over the coarse patch");
+        }
+        gf_qad_dev_task& x = t[k];
+        x.qf = Fl->d_q + (size_t)u.fine * 3 * Fl->S;
+        x.af = Fl->d_aux + (size_t)u.fine * Fl->maux * Fl->S;
+        x.qc = Cl->d_q + (size_t)u.coarse * 3 * Cl->S;
+        x.ac = Cl->d_aux + (size_t)u.coarse * Cl->maux * Cl->S;
+        x.hx = Fl->dx[u.fine];
+        x.hy = Fl->dy[u.fine];
+        x.side = u.side;
+        x.ox = u.ox;
+        x.oy = u.oy;
+        x.phys = Fl->phys[u.fine];
+        int rc = check_phys_slot(c, x.phys);
+        if (rc) return rc;
+    }
+    GF_CK(c, cudaSetDevice(c->device));
+    GF_CK(c, c->qad.reserve(ntask));
+    GF_CK(c, c->qad_flux.reserve((size_t)ntask * per));
+    for (int k = 0; k < ntask; ++k) t[k].svdflx = c->qad_flux.p + (size_t)k * per;
+    GF_CK(c, cudaMemcpyAsync(c->qad_flux.p, svdflx, sizeof(double) * ntask * per,
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, cudaMemcpyAsync(c->qad.p, t.data(), ntask * sizeof(gf_qad_dev_task),
+                             cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_qad(m, c->qad.p, ntask, c->d_phys, dt, c->stream));
+    GF_CK(c, cudaMemcpyAsync(svdflx, c->qad_flux.p, sizeof(double) * ntask * per,
+                             cudaMemcpyDeviceToHost, c->stream));
     GF_CK(c, cudaStreamSynchronize(c->stream));
     return GF_OK;
 }

@@ -109,6 +109,10 @@ cudaError_t launch_ghost_fill(int m, const gf_ghost_block* blocks, const gf_ghos
  * pointers, selecting each group's current state buffer. */
 cudaError_t launch_transfer(int m, const gf_xfer_task* tasks, int ntask, const gf_phys* phys,
                             cudaStream_t st, const long long* qdelta = nullptr);
+/* qad (geolib_source/qad.f:4-371) over ntask fine-patch sides, svdflx
+ * accumulated; built without contraction like the other transfers. */
+cudaError_t launch_qad(int m, const gf_qad_dev_task* tasks, int ntask, const gf_phys* phys,
+                       double dt, cudaStream_t st);
 cudaError_t launch_timeinterp(int m, const gf_tinterp_task* tasks, int ntask, double alpha,
                               cudaStream_t st);
 cudaError_t launch_tags(int m, const gf_tag_task* tasks, int ntask, const gf_refine* rf,

@@ -109,6 +109,21 @@ typedef struct gf_xfer_task {
     int group; /* with a per-group offset table: q pointers are shifted by it */
 } gf_xfer_task;
 
+/* One side of one fine patch for qad (gf_amr.cu): the fine patch's q and
+ * aux, the coarse patch holding the coarse cells along that side, qad.f's
+ * side number (1 left, 2 top, 3 right, 4 bottom), (ox, oy) as in
+ * gf_xfer_task, the fine spacings, and the side's svdflx entries
+ * (3 x mx/2 doubles, accumulated). */
+typedef struct gf_qad_dev_task {
+    const double* qf;
+    const double* af;
+    const double* qc;
+    const double* ac;
+    double* svdflx;
+    double hx, hy;
+    int side, ox, oy, phys;
+} gf_qad_dev_task;
+
 typedef struct gf_tinterp_task {
     const double* qcurr;
     const double* qlast;

@@ -302,6 +302,24 @@ int gf_level_tag4coarsening(gf_level* lev, const gf_refine* rf, int nfam,
                             const int* fam, int level, int maxlevel,
                             int init_flag, double t, int* tags);
 
+/* Coarse/fine conservation fix-up qad (src/fc2d_geoclaw/geolib_source/
+ * qad.f:4-371, AMRClaw's routine as GeoClaw carries it; the reference tree
+ * does not compile it and no GeoFlood path calls it). For each task, one
+ * side of fine patch `fine` (side 1 left, 2 top, 3 right, 4 bottom, qad.f's
+ * numbering) whose first ghost layer lies in coarse patch `coarse` ((ox,
+ * oy) as in gf_transfer): the Riemann problem between each fine ghost cell
+ * and the coarse cell holding it is solved, and the fluctuations times the
+ * fine face length and dt are added into svdflx[task][c][m] (host array of
+ * ntask x mx/2 x 3 doubles, accumulated in place), one entry per coarse cell
+ * c along the side (bottom to top on sides 1 and 3, left to right on 2 and
+ * 4), signed as qad.f signs each side. The fine patch's ghost cells must be
+ * filled. Physics from the fine patch's slot. */
+typedef struct gf_qad_task {
+    int fine, coarse, side, ox, oy;
+} gf_qad_task;
+int gf_level_qad(gf_level* coarse, gf_level* fine, int ntask,
+                 const gf_qad_task* tasks, double dt, double* svdflx);
+
 /* ------------------------------------------- allocation-free drop-in */
 /* For callers that cannot allocate device memory at step time: memory owned
  * by another allocator (a framework's caching pool or a fixed budget a raw

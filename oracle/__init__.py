@@ -38,7 +38,7 @@ class orc_params(C.Structure):
 
 def build(force: bool = False) -> Path:
     srcs = [HERE / "geoclaw_oracle.c", HERE / "geoclaw_oracle_ghost.c", HERE / "geoclaw_oracle_amr.c",
-            HERE / "geoclaw_oracle_topo.c"]
+            HERE / "geoclaw_oracle_topo.c", HERE / "geoclaw_oracle_qad.c"]
     deps = srcs + [HERE / "geoclaw_oracle.h"]
     if not force and LIB.exists() and all(d.stat().st_mtime <= LIB.stat().st_mtime for d in deps):
         return LIB
@@ -129,6 +129,9 @@ def load():
                                  _dp]
         lib.orc_rpt2.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp,
                                  C.c_int, _dp, _dp, _dp]
+        lib.orc_qad_side.restype = None
+        lib.orc_qad_side.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                     _dp, _dp, C.c_double, C.c_double, C.c_double, _dp]
         lib.orc_rpn2_face.argtypes = [P, C.c_int, _dp, _dp, C.c_double, C.c_double, _dp, _dp,
                                       _dp, _dp]
         lib.orc_rpt2_face.argtypes = [P, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
@@ -252,6 +255,17 @@ def level_ghost_fill(q: np.ndarray, aux: np.ndarray, nbr: np.ndarray, xlower, yl
     load().orc_level_ghost_fill(C.byref(p), C.byref(h), n, MBC, mx4 - 2 * MBC, my4 - 2 * MBC,
                                 _ptr(q), _ptr(aux), aux.shape[-1], nb.ctypes.data_as(ip),
                                 _ptr(xl), _ptr(yl), dx, dy, t, mb.ctypes.data_as(ip))
+
+
+def qad_side(side: int, qf: np.ndarray, af: np.ndarray, qc1d: np.ndarray, auxc1d: np.ndarray,
+             hx: float, hy: float, delt: float, svdflx: np.ndarray, phys=None):
+    """qad (qad.f:4-371) on one side of a fine patch qf (my+4, mx+4, 3) with
+    aux af (my+4, mx+4, maux): qc1d (n, 3) / auxc1d (n, maux) are the coarse
+    cells along the side; svdflx (n, 3) accumulates in place."""
+    p = params(phys)
+    my4, mx4, _ = qf.shape
+    load().orc_qad_side(C.byref(p), int(side), MBC, mx4 - 2 * MBC, my4 - 2 * MBC, af.shape[-1],
+                        _ptr(qf), _ptr(af), _ptr(qc1d), _ptr(auxc1d), hx, hy, delt, _ptr(svdflx))
 
 
 def rpn2_face(ixy: int, ql, qr, bl: float, br: float, phys=None):

@@ -99,6 +99,11 @@ void orc_rpt2(const orc_params* p, int ixy, int imp, int mbc, int mx,
 /* Single-face views of rpn2 / rpt2 (see geoclaw_oracle.c). */
 void orc_rpn2_face(const orc_params* p, int ixy, const double* ql, const double* qr, double bl,
                    double br, double* fwave, double* s, double* amdq, double* apdq);
+/* qad (geolib_source/qad.f:4-371), one side of a fine patch (see
+ * geoclaw_oracle_qad.c). */
+void orc_qad_side(const orc_params* p, int side, int mbc, int mx, int my, int maux,
+                  const double* qf, const double* af, const double* qc1d, const double* auxc1d,
+                  double hx, double hy, double delt, double* svdflx);
 void orc_rpt2_face(const orc_params* p, int ixy, int imp, const double* ql, const double* qr,
                    const double* aux1, const double* aux2, const double* aux3, const double* asdq,
                    double* bmasdq, double* bpasdq);
