@@ -61,7 +61,8 @@ struct Tile {
 #define GF_TILE(M, NT, RB) {NT, RB, &launch_update<M, NT, RB, 1>, &occupancy_of<M, NT, RB>}
 static const Tile kTiles8[] = {GF_TILE(8, 64, 5), GF_TILE(8, 128, 10), GF_TILE(8, 128, 5)};
 static const Tile kTiles16[] = {GF_TILE(16, 128, 6), GF_TILE(16, 256, 13), GF_TILE(16, 256, 9)};
-static const Tile kTiles32[] = {GF_TILE(32, 256, 7), GF_TILE(32, 256, 5)};
+static const Tile kTiles32[] = {GF_TILE(32, 256, 7), GF_TILE(32, 256, 5), GF_TILE(32, 384, 7),
+                                GF_TILE(32, 384, 9), GF_TILE(32, 512, 8), GF_TILE(32, 512, 9)};
 #undef GF_TILE
 
 static const Tile* tiles_of(int m, int* n)
