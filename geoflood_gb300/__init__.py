@@ -169,11 +169,16 @@ class Context:
         for r in res:
             n = r.nvariant
             out.append({"mx": r.mx,
-                        "tiles": [(r.threads[v], r.band[v]) for v in range(n)],
+                        "tiles": [(r.threads[v], r.band[v], r.cluster[v]) for v in range(n)],
                         "throughput": [r.throughput[v] for v in range(n)],
                         "latency_us": [r.latency_us[v] for v in range(n)],
                         "best_throughput": r.best_throughput, "best_latency": r.best_latency})
         return out
+
+    @staticmethod
+    def tile_count(mx: int) -> int:
+        """Number of tile variants of the patch kernel for patch size mx."""
+        return int(_lib.load().gf_tile_count(int(mx)))
 
     @staticmethod
     def tile(mx: int, goal: int = 0) -> int:

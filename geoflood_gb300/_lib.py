@@ -89,7 +89,8 @@ class gf_scenario(C.Structure):
 class gf_server_opts(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("nlanes", C.c_int),
                 ("lane_cells", C.c_longlong * GF_SERVER_MAX_LANES), ("priority", C.c_int),
-                ("backfill", C.c_int), ("reserve_sms", C.c_int), ("mixed_update", C.c_int)]
+                ("backfill", C.c_int), ("reserve_sms", C.c_int), ("mixed_update", C.c_int),
+                ("cull_dry", C.c_int)]
 
 
 class gf_scenario_info(C.Structure):
@@ -163,12 +164,13 @@ class gf_fserver_stats(C.Structure):
                 ("held", C.c_int)]
 
 
-GF_MAX_TILES = 4
+GF_MAX_TILES = 12
 
 
 class gf_tile_result(C.Structure):
     _fields_ = [("mx", C.c_int), ("nvariant", C.c_int), ("threads", C.c_int * GF_MAX_TILES),
-                ("band", C.c_int * GF_MAX_TILES), ("throughput", C.c_double * GF_MAX_TILES),
+                ("band", C.c_int * GF_MAX_TILES), ("cluster", C.c_int * GF_MAX_TILES),
+                ("throughput", C.c_double * GF_MAX_TILES),
                 ("latency_us", C.c_double * GF_MAX_TILES), ("best_throughput", C.c_int),
                 ("best_latency", C.c_int)]
 
@@ -280,6 +282,7 @@ SIGNATURES = [
     ("gf_forest_sample_gauges", C.c_int, [_vp, C.c_double]),
     ("gf_forest_flush_gauges", C.c_int, [_vp]),
     ("gf_autotune", C.c_int, [_vp, C.c_int, C.POINTER(gf_tile_result)]),
+    ("gf_tile_count", C.c_int, [C.c_int]),
     ("gf_tile_get", C.c_int, [C.c_int, C.c_int]),
     ("gf_tile_set", C.c_int, [C.c_int, C.c_int, C.c_int]),
     ("gf_server_opts_default", None, [C.POINTER(gf_server_opts)]),

@@ -171,9 +171,19 @@ int check_phys_slot(gf_ctx* c, int slot, int maux = 0)
     return GF_OK;
 }
 
+/* Tile goal of a batch of nwork patches: the latency tile (goal 1) when
+ * even split over its cluster the batch leaves SMs idle, so that a lone patch
+ * or a handful of them spread over more SMs; the throughput tile otherwise. */
+int small_batch_goal(int m, int nwork)
+{
+    int nt = 0, rb = 0, k = 1;
+    if (gf::tile_shape(m, gf::tile_get(m, 1), &nt, &rb, &k) != 0) return 0;
+    return (long)nwork * k <= gf::sm_count() ? 1 : 0;
+}
+
 /* Enqueue one batch on the context stream: clear the status, launch. */
 int enqueue_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int maux, double dt,
-                  double* d_cfl, DevStatus* d_status)
+                  double* d_cfl, DevStatus* d_status, int goal = 0)
 {
     GF_CK(c, cudaMemsetAsync(d_status, 0, sizeof(DevStatus), c->stream));
     if (c->exact)
@@ -181,7 +191,7 @@ int enqueue_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int 
                                                d_cfl, &d_status->gmax, &d_status->err, c->stream));
     else
         GF_CK(c, gf::launch_patch_update(m, d_work, nwork, c->d_phys, dt, nullptr, nullptr, maux, d_cfl,
-                                         &d_status->gmax, &d_status->err, c->stream));
+                                         &d_status->gmax, &d_status->err, c->stream, 0, goal));
     return GF_OK;
 }
 
@@ -199,9 +209,9 @@ int finish_batch(gf_ctx* c, DevStatus* d_status, double* maxcfl)
 }
 
 int run_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int maux, double dt,
-              double* d_cfl, DevStatus* d_status, double* maxcfl)
+              double* d_cfl, DevStatus* d_status, double* maxcfl, int goal = 0)
 {
-    int rc = enqueue_batch(c, m, d_work, nwork, maux, dt, d_cfl, d_status);
+    int rc = enqueue_batch(c, m, d_work, nwork, maux, dt, d_cfl, d_status, goal);
     if (rc) return rc;
     return finish_batch(c, d_status, maxcfl);
 }
@@ -383,7 +393,8 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
     GF_CK(c, gf::launch_aos_to_soa(c->aux_aos.p, c->aux_soa.p, npatch, (int)S, maux, maux * S,
                                    maux * S, c->stream));
     double mc = 0.0;
-    rc = run_batch(c, mx, c->work.p, npatch, maux, dt, c->cfl.p, c->d_status, &mc);
+    rc = run_batch(c, mx, c->work.p, npatch, maux, dt, c->cfl.p, c->d_status, &mc,
+                   small_batch_goal(mx, npatch));
     if (rc) return rc;
     GF_CK(c, gf::launch_soa_to_aos(c->q_soa.p, c->q_aos.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
     GF_CK(c, cudaMemcpyAsync(hq, c->q_aos.p, sizeof(double) * qn, cudaMemcpyDeviceToHost, c->stream));
@@ -1214,6 +1225,12 @@ int ctx_cuda_fail(gf_ctx* c, cudaError_t e, const char* what) { return cuda_fail
 } // namespace gf
 
 /* ------------------------------------------------------------ tiling */
+extern "C" int gf_tile_count(int mx)
+{
+    if (!(mx == 8 || mx == 16 || mx == 32)) return GF_ERR_ARG;
+    return gf::tile_count(mx);
+}
+
 extern "C" int gf_tile_get(int mx, int goal)
 {
     if (!(mx == 8 || mx == 16 || mx == 32)) return GF_ERR_ARG;
@@ -1276,7 +1293,7 @@ extern "C" int gf_autotune(gf_ctx* c, int reps, gf_tile_result* out)
         if (e == cudaSuccess) e = cudaMemcpy(dw, w.data(), w.size() * sizeof(gf_patch_work), cudaMemcpyHostToDevice);
         double best_t = -1.0, best_l = 1e300;
         for (int v = 0; v < R.nvariant && e == cudaSuccess; ++v) {
-            gf::tile_shape(m, v, &R.threads[v], &R.band[v]);
+            gf::tile_shape(m, v, &R.threads[v], &R.band[v], &R.cluster[v]);
             for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
                 const int n = pass == 0 ? np : nsmall;
                 /* a set error flag makes the kernel skip its items */

@@ -89,6 +89,22 @@ __global__ void __launch_bounds__(128) ghost_fill_kernel(const gf_ghost_block* _
 #pragma unroll
     for (int s = 0; s < 8; ++s) nb[s] = nbr[8 * p + s];
 
+    /* dry-patch culling: the patch's last update was an identity, no
+     * neighbour holds water and no side takes inflow, so this step's update
+     * would be the identity again; mark it skipped and leave its ghosts */
+    if (blk.fl) {
+        bool skip = blk.fl[p].ident != 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (nb[s] >= 0) skip = skip && blk.fl[nb[s]].wet == 0;
+            else if (nb[s] != -1) skip = false;               /* filled by another route */
+            else if (s < 4 && bc.mthbc[s] == 0) skip = false; /* hydrograph side */
+        }
+        __syncthreads(); /* every thread has read the flags before thread 0 writes */
+        if (threadIdx.x == 0) blk.fl[p].skip = skip ? 1 : 0;
+        if (skip) return;
+    }
+
     /* ---- step 1: same-level face and corner copies ---- */
     for (int k = threadIdx.x; k < S; k += blockDim.x) {
         const int i = k % N - 1, j = k / N - 1; /* Fortran indices 1-mbc..M+mbc */

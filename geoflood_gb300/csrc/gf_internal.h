@@ -57,7 +57,7 @@ int patch_update_occupancy(int m); /* resident CTAs per SM (throughput tile) */
 /* Tile shapes of the production patch kernel: variants per patch size, the
  * selection per goal (0 throughput, 1 latency) used by launch_patch_update. */
 int tile_count(int m);
-int tile_shape(int m, int v, int* nt, int* rb);
+int tile_shape(int m, int v, int* nt, int* rb, int* k = nullptr);
 int tile_get(int m, int goal);
 int tile_set(int m, int goal, int v);
 cudaError_t launch_patch_update_tile(int m, int v, const gf_patch_work* work, int nwork,

@@ -31,6 +31,37 @@ static cudaError_t launch_update(const gf_patch_work* work, int nwork, const gf_
     return cudaGetLastError();
 }
 
+/* The latency form: each work item on a cluster of K CTAs (one window of
+ * rows each); not persistent, so max_ctas does not apply. */
+template <int M, int NT, int RB, int K>
+static cudaError_t launch_window(const gf_patch_work* work, int nwork, const gf_phys* phys,
+                                 double dt, const double* gdt, const int* gpar, int maux, double* cfl,
+                                 unsigned long long* gmax, int* err, int max_ctas, cudaStream_t st)
+{
+    (void)max_ctas;
+    using L = Smem<M, RB, false>;
+    auto kern = patch_update_window_kernel<M, NT, RB, K, false>;
+    static std::atomic<unsigned long long> attr_done{0};
+    cudaError_t ae = smem_attr_per_device(kern, (int)L::BYTES, attr_done);
+    if (ae != cudaSuccess) return ae;
+    if (nwork <= 0) return cudaSuccess;
+    kern<<<nwork * K, NT, L::BYTES, st>>>(work, nwork, phys, dt, gdt, gpar, maux, cfl, gmax, err);
+    return cudaGetLastError();
+}
+
+template <int M, int NT, int RB, int K>
+static int window_occupancy()
+{
+    using L = Smem<M, RB, false>;
+    auto kern = patch_update_window_kernel<M, NT, RB, K, false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES) !=
+        cudaSuccess)
+        return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, NT, L::BYTES) != cudaSuccess) return 0;
+    return n;
+}
+
 /* ---- tile shapes (threads per patch x slices per band) per patch size ----
  * Variant 0 of each size is the default; gf_autotune measures them all and
  * installs the fastest for throughput (whole levels) and for latency (a
@@ -53,17 +84,23 @@ static int occupancy_of()
 }
 
 struct Tile {
-    int nt, rb;
+    int nt, rb, k; /* k > 1: the patch split over a cluster of k CTAs */
     UpdateFn fn;
     OccFn occ;
 };
 
-#define GF_TILE(M, NT, RB) {NT, RB, &launch_update<M, NT, RB, 1>, &occupancy_of<M, NT, RB>}
-static const Tile kTiles8[] = {GF_TILE(8, 64, 5), GF_TILE(8, 128, 10), GF_TILE(8, 128, 5)};
-static const Tile kTiles16[] = {GF_TILE(16, 128, 6), GF_TILE(16, 256, 13), GF_TILE(16, 256, 9)};
+#define GF_TILE(M, NT, RB) {NT, RB, 1, &launch_update<M, NT, RB, 1>, &occupancy_of<M, NT, RB>}
+#define GF_WTILE(M, NT, RB, K) {NT, RB, K, &launch_window<M, NT, RB, K>, &window_occupancy<M, NT, RB, K>}
+static const Tile kTiles8[] = {GF_TILE(8, 64, 5), GF_TILE(8, 128, 10), GF_TILE(8, 128, 5),
+                               GF_WTILE(8, 64, 5, 2), GF_WTILE(8, 64, 5, 4)};
+static const Tile kTiles16[] = {GF_TILE(16, 128, 6), GF_TILE(16, 256, 13), GF_TILE(16, 256, 9),
+                                GF_WTILE(16, 128, 6, 2), GF_WTILE(16, 128, 6, 4),
+                                GF_WTILE(16, 256, 9, 4)};
 static const Tile kTiles32[] = {GF_TILE(32, 256, 7), GF_TILE(32, 256, 5), GF_TILE(32, 384, 7),
-                                GF_TILE(32, 384, 9), GF_TILE(32, 512, 8), GF_TILE(32, 512, 9)};
+                                GF_TILE(32, 384, 9), GF_TILE(32, 512, 8), GF_TILE(32, 512, 9),
+                                GF_WTILE(32, 256, 7, 4), GF_WTILE(32, 256, 7, 8)};
 #undef GF_TILE
+#undef GF_WTILE
 
 static const Tile* tiles_of(int m, int* n)
 {
@@ -86,13 +123,14 @@ int tile_count(int m)
     return n;
 }
 
-int tile_shape(int m, int v, int* nt, int* rb)
+int tile_shape(int m, int v, int* nt, int* rb, int* k)
 {
     int n = 0;
     const Tile* t = tiles_of(m, &n);
     if (!t || v < 0 || v >= n) return -1;
     *nt = t[v].nt;
     *rb = t[v].rb;
+    if (k) *k = t[v].k;
     return 0;
 }
 

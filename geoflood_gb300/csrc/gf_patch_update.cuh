@@ -38,6 +38,7 @@
 #ifndef GF_PATCH_UPDATE_CUH
 #define GF_PATCH_UPDATE_CUH
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -181,6 +182,37 @@ __device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned ch
     return c;
 }
 
+/* The faces one sweep computes when a work item updates only the interior
+ * rows rlo..rhi of its patch (the whole patch: rlo = 1, rhi = M). The x
+ * sweep takes the slices (rows) rlo-1..rhi+1 with all their faces; the y
+ * sweep takes every slice (column) with the normal-solve faces rlo-1..rhi+2
+ * and the limited faces rlo..rhi+1, which are exactly the faces whose
+ * records the update of rows rlo..rhi reads. Records of a band are packed
+ * by the window's faces per slice (fa, fb), so a band holds rb slices
+ * within the same shared-memory records as a whole-patch band of RB. For
+ * rlo = 1, rhi = M every field is the whole-patch constant. */
+template <int M, int RB, int DIR>
+struct SweepWin {
+    int ts_lo, nsl; /* slices ts_lo .. ts_lo + nsl - 1                  */
+    int na_lo, fa;  /* normal-solve faces na_lo .. na_lo + fa - 1        */
+    int nb_lo, fb;  /* limited faces nb_lo .. nb_lo + fb - 1             */
+    int rb;         /* slices per band                                   */
+    __device__ __forceinline__ SweepWin(int rlo, int rhi)
+    {
+        if (DIR == 0) {
+            ts_lo = rlo - 1; nsl = rhi - rlo + 3;
+            na_lo = 0; fa = M + 3;
+            nb_lo = 1; fb = M + 1;
+            rb = RB;
+        } else {
+            ts_lo = 0; nsl = M + 2;
+            na_lo = rlo - 1; fa = rhi - rlo + 4;
+            nb_lo = rlo; fb = rhi - rlo + 2;
+            rb = min(RB * (M + 3) / fa, RB * (M + 1) / fb);
+        }
+    }
+};
+
 /* Build, for every band of one sweep direction, the normal-solve faces
  * (list A) and the limited faces (list B) ordered by class, so that a warp
  * runs one code path. Classes: 0..2 both cells wet, by the wave structure
@@ -194,7 +226,7 @@ __device__ __forceinline__ gf_cell load_cell(const double* sm, const unsigned ch
  * passes (count, then place) over all faces. */
 template <int M, int NT, int RB, int DIR, bool EXACT>
 __device__ __forceinline__ void build_lists(const double* sm, const unsigned char* wet, int* cnt, uint16_t* la,
-                                            uint16_t* lb, double g)
+                                            uint16_t* lb, double g, const SweepWin<M, RB, DIR>& w)
 {
     using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
@@ -205,13 +237,14 @@ __device__ __forceinline__ void build_lists(const double* sm, const unsigned cha
         return DIR == 0 ? (t + 1) * N + (n + 1) : (n + 1) * N + (t + 1);
     };
     /* cnt layout: [band][list 0|1][class 0..4][0 = count, 1 = position] */
-    auto C = [&](int band, int list, int cls, int w) -> int& {
-        return cnt[((band * 2 + list) * NC + cls) * 2 + w];
+    auto C = [&](int band, int list, int cls, int w2) -> int& {
+        return cnt[((band * 2 + list) * NC + cls) * 2 + w2];
     };
     for (int k = threadIdx.x; k < L::CNT_INTS; k += NT) cnt[k] = 0;
     __syncthreads();
-    for (int f = threadIdx.x; f < G::NSLICE * G::FA; f += NT) {
-        const int t = f / G::FA, n = f % G::FA;
+    for (int f = threadIdx.x; f < w.nsl * w.fa; f += NT) {
+        const int ts = f / w.fa, n = w.na_lo + f % w.fa;
+        const int t = w.ts_lo + ts;
         const int kl = cidx(n - 1, t), kr = cidx(n, t);
         const int nw = wet[kl] + wet[kr];
         int cls = nw == 0 ? 4 : nw == 1 ? 3 : 0;
@@ -230,12 +263,13 @@ __device__ __forceinline__ void build_lists(const double* sm, const unsigned cha
             else cls = 2;
         }
         fcls[f] = (unsigned char)cls;
-        atomicAdd(&C(t / RB, 0, cls, 0), 1);
+        atomicAdd(&C(ts / w.rb, 0, cls, 0), 1);
     }
-    for (int f = threadIdx.x; f < G::NSLICE * G::FB; f += NT) {
-        const int t = f / G::FB, n = 1 + f % G::FB;
+    for (int f = threadIdx.x; f < w.nsl * w.fb; f += NT) {
+        const int ts = f / w.fb, n = w.nb_lo + f % w.fb;
+        const int t = w.ts_lo + ts;
         const int nw = wet[cidx(n - 1, t)] + wet[cidx(n, t)];
-        atomicAdd(&C(t / RB, 1, nw == 0 ? 4 : nw == 1 ? 3 : 0, 0), 1);
+        atomicAdd(&C(ts / w.rb, 1, nw == 0 ? 4 : nw == 1 ? 3 : 0, 0), 1);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < L::NBAND * 2; e += NT) {
@@ -247,18 +281,18 @@ __device__ __forceinline__ void build_lists(const double* sm, const unsigned cha
         }
     }
     __syncthreads();
-    for (int f = threadIdx.x; f < G::NSLICE * G::FA; f += NT) {
-        const int t = f / G::FA;
-        const int band = t / RB;
+    for (int f = threadIdx.x; f < w.nsl * w.fa; f += NT) {
+        const int band = (f / w.fa) / w.rb;
         const int pos = atomicAdd(&C(band, 0, fcls[f], 1), 1);
-        la[band * RB * G::FA + pos] = (uint16_t)(f - band * RB * G::FA);
+        la[band * w.rb * w.fa + pos] = (uint16_t)(f - band * w.rb * w.fa);
     }
-    for (int f = threadIdx.x; f < G::NSLICE * G::FB; f += NT) {
-        const int t = f / G::FB, n = 1 + f % G::FB;
+    for (int f = threadIdx.x; f < w.nsl * w.fb; f += NT) {
+        const int ts = f / w.fb, n = w.nb_lo + f % w.fb;
+        const int t = w.ts_lo + ts;
         const int nw = wet[cidx(n - 1, t)] + wet[cidx(n, t)];
-        const int band = t / RB;
+        const int band = ts / w.rb;
         const int pos = atomicAdd(&C(band, 1, nw == 0 ? 4 : nw == 1 ? 3 : 0, 1), 1);
-        lb[band * RB * G::FB + pos] = (uint16_t)(f - band * RB * G::FB);
+        lb[band * w.rb * w.fb + pos] = (uint16_t)(f - band * w.rb * w.fb);
     }
     __syncthreads();
 }
@@ -268,7 +302,8 @@ __device__ __forceinline__ void build_lists(const double* sm, const unsigned cha
 template <int M, int NT, int RB, int DIR, bool EXACT>
 __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, int* cnt,
                                         uint16_t* la, uint16_t* lb, const gf_phys& P, double dtdn,
-                                        double c16g, double rsg, double crit, double crit2)
+                                        double c16g, double rsg, double crit, double crit2,
+                                        int rlo, int rhi)
 {
     using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
@@ -294,7 +329,17 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
         return cnt[((band * 2 + list) * L::NCLS + cls) * 2 + 0];
     };
 
-    build_lists<M, NT, RB, DIR, EXACT>(sm, wet, cnt, la, lb, g);
+    const SweepWin<M, RB, DIR> win(rlo, rhi);
+    const int fa = win.fa, fb = win.fb;
+    build_lists<M, NT, RB, DIR, EXACT>(sm, wet, cnt, la, lb, g, win);
+    /* cells the gather writes: slice-direction t clamped to the window's rows
+     * in the x sweep, cell-direction n clamped to them in the y sweep */
+    const int gt_lo = DIR == 0 ? rlo : 1, gt_hi = DIR == 0 ? rhi : M;
+    const int gn_lo = DIR == 0 ? 1 : rlo, gn_hi = DIR == 0 ? M : rhi;
+    /* record of limited face `face` (nb_lo..) of band slice ts */
+    auto orec = [&](int ts, int face) -> const double* {
+        return O + (ts * fb + (face - win.nb_lo)) * L::O_STRIDE;
+    };
 
     /* Contracted build: DX, DY. Exact build: fm(i+1,j), fp(i,j), gm(i,j+1),
      * gp(i,j) of the reference, in sweep coordinates N_M, N_P (normal) and
@@ -308,23 +353,25 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
     double* TP = TM + 3 * MM;
 
     auto gather = [&](int t0, int t1) {
-        /* slices t0..t1 feed cells n in [1, M], t in [t0-1, t1+1] (interior) */
-        const int ta = max(1, t0 - 1), tb = min(M, t1 + 1);
-        const int cnt_c = (tb - ta + 1) * M;
+        /* slices t0..t1 feed cells n in [1, M], t in [t0-1, t1+1] (interior),
+         * within the window */
+        const int ta = max(gt_lo, t0 - 1), tb = min(gt_hi, t1 + 1);
+        const int nn = gn_hi - gn_lo + 1;
+        const int cnt_c = (tb - ta + 1) * nn;
         for (int e = threadIdx.x; e < cnt_c; e += NT) {
-            const int t = ta + e / M;
-            const int n = 1 + e % M;
+            const int t = ta + e / nn;
+            const int n = gn_lo + e % nn;
             const int a = aidx(n, t);
             if (EXACT) {
                 if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
-                    const double* fr = O + ((t - 1 - t0) * G::FB + n) * L::O_STRIDE;
-                    const double* fl = O + ((t - 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    const double* fr = orec(t - 1 - t0, n + 1);
+                    const double* fl = orec(t - 1 - t0, n);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) TP[a + c * MM] += (0.0 - fr[9 + c]) - fl[15 + c];
                 }
                 if (t >= t0 && t <= t1) {
-                    const double* fr = O + ((t - t0) * G::FB + n) * L::O_STRIDE;
-                    const double* fl = O + ((t - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    const double* fr = orec(t - t0, n + 1);
+                    const double* fl = orec(t - t0, n);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         NM[a + c * MM] += fr[c];
@@ -334,8 +381,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                     }
                 }
                 if (t + 1 >= t0 && t + 1 <= t1) { /* slice above: down-going parts */
-                    const double* fr = O + ((t + 1 - t0) * G::FB + n) * L::O_STRIDE;
-                    const double* fl = O + ((t + 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    const double* fr = orec(t + 1 - t0, n + 1);
+                    const double* fl = orec(t + 1 - t0, n);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) TM[a + c * MM] += (0.0 - fr[6 + c]) - fl[12 + c];
                 }
@@ -344,15 +391,15 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                  * increasing order, so the sums do not depend on where the band
                  * boundaries fall: every tile shape gives the same bits */
                 if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
-                    const double* fr = O + ((t - 1 - t0) * G::FB + n) * L::O_STRIDE;
-                    const double* fl = O + ((t - 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    const double* fr = orec(t - 1 - t0, n + 1);
+                    const double* fl = orec(t - 1 - t0, n);
                     ACCT[a] += half_dtdn * (fr[9] + fl[15]);
                     ACCT[a + MM] += half_dtdn * (fr[10] + fl[16]);
                     ACCT[a + 2 * MM] += half_dtdn * (fr[11] + fl[17]);
                 }
                 if (t >= t0 && t <= t1) {
-                    const double* fr = O + ((t - t0) * G::FB + n) * L::O_STRIDE;       /* face n+1 */
-                    const double* fl = O + ((t - t0) * G::FB + (n - 1)) * L::O_STRIDE; /* face n   */
+                    const double* fr = orec(t - t0, n + 1);       /* face n+1 */
+                    const double* fl = orec(t - t0, n); /* face n   */
                     ACCN[a] += fr[0] - fl[3];
                     ACCN[a + MM] += fr[1] - fl[4];
                     ACCN[a + 2 * MM] += fr[2] - fl[5];
@@ -361,8 +408,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                     ACCT[a + 2 * MM] += half_dtdn * ((fr[8] - fr[11]) + (fl[14] - fl[17]));
                 }
                 if (t + 1 >= t0 && t + 1 <= t1) { /* slice above: down-going parts */
-                    const double* fr = O + ((t + 1 - t0) * G::FB + n) * L::O_STRIDE;
-                    const double* fl = O + ((t + 1 - t0) * G::FB + (n - 1)) * L::O_STRIDE;
+                    const double* fr = orec(t + 1 - t0, n + 1);
+                    const double* fl = orec(t + 1 - t0, n);
                     ACCT[a] -= half_dtdn * (fr[6] + fl[12]);
                     ACCT[a + MM] -= half_dtdn * (fr[7] + fl[13]);
                     ACCT[a + 2 * MM] -= half_dtdn * (fr[8] + fl[14]);
@@ -372,10 +419,11 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
     };
 
     int prev_t0 = -1, prev_t1 = -1;
-    for (int t0 = 0, band = 0; t0 < G::NSLICE; t0 += RB, ++band) {
-        const int t1 = min(t0 + RB, G::NSLICE) - 1; /* last slice of band */
-        const uint16_t* lA = la + band * RB * G::FA;
-        const uint16_t* lB = lb + band * RB * G::FB;
+    const int ts_end = win.ts_lo + win.nsl;
+    for (int t0 = win.ts_lo, band = 0; t0 < ts_end; t0 += win.rb, ++band) {
+        const int t1 = min(t0 + win.rb, ts_end) - 1; /* last slice of band */
+        const uint16_t* lA = la + band * win.rb * fa;
+        const uint16_t* lB = lb + band * win.rb * fb;
         /* a2 / b2 both cells wet (list A by wave structure), a1 / b1 one
          * wet, a0 / b0 both dry */
         const int a2 = C(band, 0, 0) + C(band, 0, 1) + C(band, 0, 2), a1 = C(band, 0, 3), a0 = C(band, 0, 4);
@@ -390,8 +438,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 for (int q = 0; q < L::W_STRIDE; ++q) w[q] = 0.0;
                 continue;
             }
-            const int t = t0 + f / G::FA;
-            const int n = f % G::FA;
+            const int t = t0 + f / fa;
+            const int n = win.na_lo + f % fa;
             const gf_cell cl = load_cell<DIR, EXACT, L>(sm, wet, cidx(n - 1, t));
             const gf_cell cr = load_cell<DIR, EXACT, L>(sm, wet, cidx(n, t));
             double s[3], fw[3][3];
@@ -417,10 +465,10 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 for (int q = 0; q < L::O_STRIDE; ++q) o[q] = 0.0;
                 continue;
             }
-            const int t = t0 + f / G::FB;
-            const int n = 1 + f % G::FB;
+            const int t = t0 + f / fb;
+            const int n = win.nb_lo + f % fb;
             const int kl = cidx(n - 1, t), kr = cidx(n, t);
-            const double* wc = W + ((t - t0) * G::FA + n) * L::W_STRIDE;
+            const double* wc = W + ((t - t0) * fa + (n - win.na_lo)) * L::W_STRIDE;
             double s[3], fw[3][3];
 #pragma unroll
             for (int mw = 0; mw < 3; ++mw) {
@@ -614,7 +662,8 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
                                            double dt_uniform, const double* __restrict__ group_dt,
                                            const int* __restrict__ group_par, int maux,
                                            double* __restrict__ cfl_out,
-                                           unsigned long long* __restrict__ group_max, int* __restrict__ err)
+                                           unsigned long long* __restrict__ group_max, int* __restrict__ err,
+                                           int rlo = 1, int rhi = M, double* part = nullptr)
 {
     using G = Geo<M>;
     using L = Smem<M, RB, EXACT>;
@@ -636,6 +685,8 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
         wk.q = wk.qout;
         wk.qout = t;
     }
+    /* culled: this update would be an exact identity (the ghost fill decided) */
+    if (wk.fl && wk.fl->skip) return true;
     const gf_phys P = phys_table[wk.phys];
     const double g = P.grav, drytol = P.dry_tolerance;
 
@@ -658,10 +709,13 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
     }
 
     /* ---- b4step2 on all cells + per-cell quotients ---- */
-    int any_wet = 0;
+    int any_wet = 0, changed = 0;
     for (int k = threadIdx.x; k < S; k += NT) {
         double h = sm[L::OFF_H + k];
         if (d_lt<FAST>(h, drytol)) {
+            /* b4step2 changes this cell's bits unless h >= 0 and both momenta are +0 */
+            changed |= (__double_as_longlong(h) < 0) | (__double_as_longlong(sm[L::OFF_HU + k]) != 0) |
+                       (__double_as_longlong(sm[L::OFF_HV + k]) != 0);
             h = d_max<FAST>(h, 0.0);
             sm[L::OFF_H + k] = h;
             sm[L::OFF_HU + k] = 0.0;
@@ -697,6 +751,7 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
     }
     for (int k = threadIdx.x; k < L::NACC * 3 * L::PLANE; k += NT) sm[L::OFF_ACC + k] = 0.0;
     any_wet = __syncthreads_or(any_wet);
+    if (wk.fl) changed = __syncthreads_or(changed);
 
     const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
     double smax_x = 0.0, smax_y = 0.0;
@@ -705,16 +760,16 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
         const double rsg = rsqrt(g);
         const double crit = fmax(drytol * g, 1e-6);
         const double crit2 = sqrt(crit);
-        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2);
-        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2);
+        smax_x = sweep<M, NT, RB, 0, EXACT>(sm, wet, cnt, la, lb, P, dtdx, c16g, rsg, crit, crit2, rlo, rhi);
+        smax_y = sweep<M, NT, RB, 1, EXACT>(sm, wet, cnt, la, lb, P, dtdy, c16g, rsg, crit, crit2, rlo, rhi);
     }
 
     /* ---- flux-difference update, src2, write interior ---- */
     double* gq = wk.qout ? wk.qout : wk.q;
     const double* gaux = wk.aux;
     const int fidx = P.friction_index - 1;
-    for (int e = threadIdx.x; e < M * M; e += NT) {
-        const int i = 1 + e % M, j = 1 + e / M;
+    for (int e = threadIdx.x; e < (rhi - rlo + 1) * M; e += NT) {
+        const int i = 1 + e % M, j = rlo + e / M;
         const int k = (j + 1) * N + (i + 1);
         double h = sm[L::OFF_H + k], hu = sm[L::OFF_HU + k], hv = sm[L::OFF_HV + k];
         constexpr int PL = L::PLANE;
@@ -746,6 +801,11 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
         gq[2 * S + k] = hv;
     }
 
+    if (wk.fl && threadIdx.x == 0) {
+        wk.fl->ident = (!any_wet && !changed) ? 1 : 0;
+        wk.fl->wet = any_wet ? 1 : 0;
+    }
+
     /* ---- CFL: warp-shuffle max, then across warps ---- */
     double cx = smax_x, cy = smax_y;
 #pragma unroll
@@ -759,6 +819,22 @@ __device__ __forceinline__ bool patch_item(double* sm, uint64_t* bar, uint32_t& 
         red[32 + warp] = cy;
     }
     __syncthreads();
+    if (threadIdx.x == 0) {
+        double mx = 0.0, my = 0.0;
+        for (int w2 = 0; w2 < NT / 32; ++w2) {
+            mx = fmax(mx, red[w2]);
+            my = fmax(my, red[32 + w2]);
+        }
+        if (part) { /* a window of a split item: the cluster forms the patch CFL */
+            part[0] = mx;
+            part[1] = my;
+        }
+    }
+    if (part) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        return true;
+    }
     if (threadIdx.x == 0) {
         double mx = 0.0, my = 0.0;
         for (int w2 = 0; w2 < NT / 32; ++w2) {
@@ -797,6 +873,66 @@ __global__ void __launch_bounds__(NT, MINB)
         if (!patch_item<M, NT, RB, EXACT>(sm, bar, phase, work[wi], wi, phys_table, dt_uniform, group_dt,
                                           group_par, maux, cfl_out, group_max, err))
             return;
+}
+
+/* Latency form: one patch split over a thread-block cluster of K CTAs on
+ * K SMs. CTA r of a cluster updates interior rows r*M/K+1 .. (r+1)*M/K of
+ * the cluster's work item; each stages the whole patch and computes exactly
+ * the faces those rows read (SweepWin), so the interior values are the same
+ * bits as the one-CTA kernel's (the same operations, summed per cell in the
+ * same slice order). The patch CFL is the maximum of the CTAs' partial wave
+ * speed maxima, read by rank 0 through distributed shared memory after a
+ * cluster barrier; a second barrier keeps every CTA resident until it has
+ * been read. A lone patch then runs on K SMs instead of one. */
+template <int M, int NT, int RB, int K, bool EXACT>
+__global__ void __cluster_dims__(K, 1, 1) __launch_bounds__(NT, 1)
+    patch_update_window_kernel(const gf_patch_work* __restrict__ work, int nwork,
+                               const gf_phys* __restrict__ phys_table, double dt_uniform,
+                               const double* __restrict__ group_dt, const int* __restrict__ group_par,
+                               int maux, double* __restrict__ cfl_out,
+                               unsigned long long* __restrict__ group_max, int* __restrict__ err)
+{
+    static_assert(M % K == 0, "the rows split evenly over the cluster");
+    namespace cg = cooperative_groups;
+    using L = Smem<M, RB, EXACT>;
+    constexpr int R = M / K;
+    extern __shared__ __align__(128) double sm[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int r = (int)cluster.block_rank();
+    const int wi = blockIdx.x / K;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::OFF_BAR);
+    double* part = sm + L::OFF_RED + 62; /* past the warp slots of the CFL reduction */
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        part[0] = 0.0;
+        part[1] = 0.0;
+    }
+    __syncthreads();
+    /* both tests are the same on every CTA of the cluster: it leaves whole */
+    if (wi >= nwork) return;
+    const gf_patch_work wk = work[wi];
+    if (group_dt && !(group_dt[wk.group] > 0.0)) return;
+    if (wk.fl && wk.fl->skip) return;
+    uint32_t phase = 0;
+    patch_item<M, NT, RB, EXACT>(sm, bar, phase, wk, wi, phys_table, dt_uniform, group_dt, group_par,
+                                 maux, cfl_out, group_max, err, 1 + r * R, (r + 1) * R, part);
+    cluster.sync();
+    if (r == 0 && threadIdx.x == 0) {
+        double mx = 0.0, my = 0.0;
+        for (int q = 0; q < K; ++q) {
+            const double* p = cluster.map_shared_rank(part, q);
+            mx = fmax(mx, p[0]);
+            my = fmax(my, p[1]);
+        }
+        const gf_phys& P = phys_table[wk.phys];
+        const double dt = group_dt ? group_dt[wk.group] : dt_uniform;
+        const double dtdx = dt / wk.dx, dtdy = dt / wk.dy;
+        double cfl = fmax(dtdx * mx, dtdy * my);
+        if (cfl > P.maxcfl_cap) cfl = 0.0;
+        if (cfl_out) cfl_out[wi] = cfl;
+        if (group_max) atomicMax(group_max + wk.group, dkey(cfl));
+    }
+    cluster.sync();
 }
 
 /* Shared-memory bytes of the mixed kernel: the largest class layout, then

@@ -75,6 +75,7 @@ struct Scen {
     double* aux = nullptr;
     int* nbr = nullptr;
     gf_patch_geom* geom = nullptr;
+    gf_patch_flags* fl = nullptr; /* dry-patch culling flags, zero at admission */
     bool cancel_req = false;
     bool failed = false;
     cudaEvent_t ev_fin = nullptr;
@@ -163,7 +164,8 @@ size_t footprint_of(const gf_scenario& sc)
     const long S = (long)(sc.mx + 2 * GF_MBC) * (sc.mx + 2 * GF_MBC);
     const size_t np = (size_t)sc.npx * sc.npy;
     return 2 * align256(np * 3 * S * sizeof(double)) + align256(np * sc.maux * S * sizeof(double)) +
-           align256(np * 8 * sizeof(int)) + align256(np * sizeof(gf_patch_geom));
+           align256(np * 8 * sizeof(int)) + align256(np * sizeof(gf_patch_geom)) +
+           align256(np * sizeof(gf_patch_flags));
 }
 
 const char* validate(const gf_scenario& sc)
@@ -253,6 +255,10 @@ int admit(gf_server* srv, Scen* s)
     s->nbr = reinterpret_cast<int*>(p);
     p += align256((size_t)np * 8 * sizeof(int));
     s->geom = reinterpret_cast<gf_patch_geom*>(p);
+    p += align256((size_t)np * sizeof(gf_patch_geom));
+    s->fl = reinterpret_cast<gf_patch_flags*>(p);
+    /* no update has run: no patch is known to be idle */
+    SV_CK(srv, cudaMemsetAsync(s->fl, 0, (size_t)np * sizeof(gf_patch_flags), L.st));
     srv->stats.bytes_in_use += s->bytes;
     srv->stats.bytes_peak = std::max(srv->stats.bytes_peak, srv->stats.bytes_in_use);
 
@@ -472,6 +478,7 @@ int rebuild_epoch(gf_server* srv, Lane& L)
         blk.nbr = s->nbr;
         blk.geom = s->geom;
         blk.phys_of = nullptr;
+        blk.fl = srv->o.cull_dry ? s->fl : nullptr;
         for (int k = 0; k < 4; ++k) {
             blk.bc.mthbc[k] = s->sc.mthbc[k];
             blk.bc.hydro_side[k] = s->sc.nhydro > 0 ? (s->sc.hydro_side[k] != 0) : 0;
@@ -500,6 +507,7 @@ int rebuild_epoch(gf_server* srv, Lane& L)
             w.dy = s->sc.dy;
             w.phys = s->slot;
             w.group = g;
+            w.fl = srv->o.cull_dry ? s->fl + p : nullptr;
             hwork[c][fill[c]] = w;
             ++fill[c];
         }
@@ -724,6 +732,7 @@ void gf_server_opts_default(gf_server_opts* o)
     o->backfill = 1;
     o->reserve_sms = 0; /* one CTA per patch: priority hands freed SMs to smaller lanes */
     o->mixed_update = 0; /* per-size launches: measured faster for served scenarios */
+    o->cull_dry = 1;
 }
 
 int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)

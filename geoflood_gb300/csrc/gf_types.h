@@ -17,11 +17,27 @@
 #define GF_MBC 2
 #define GF_MEQN 3
 
+/* Activity of one patch (dry-patch culling of the served form). The update
+ * kernel records, for the state it read (the patch and its two-cell halo):
+ * `wet` = some cell deeper than the dry tolerance, and `ident` = no cell
+ * wet and b4step2 changed nothing, so that update was an exact identity
+ * and left the same interior in both state buffers. Before the next
+ * update the ghost fill sets `skip` for a patch whose update would again be
+ * the identity: ident set, no neighbour (faces and corners) wet, no
+ * hydrograph side. Ghost fill and update then leave the patch alone. */
+typedef struct gf_patch_flags {
+    unsigned char skip;
+    unsigned char ident;
+    unsigned char wet;
+    unsigned char pad;
+} gf_patch_flags;
+
 /* One unit of work for the patch-update kernel: a patch of any forest. */
 typedef struct gf_patch_work {
     double* q;          /* device: 3 planes of (mx+4)*(my+4) doubles   */
     double* qout;       /* interior cells of the result; null = q      */
     const double* aux;  /* device: maux planes of (mx+4)*(my+4) doubles */
+    gf_patch_flags* fl; /* activity flags, or null: always updated     */
     double dx, dy;
     int phys;           /* index into the gf_phys table                */
     int group;          /* time-step group: dt slot and CFL max slot   */
@@ -51,6 +67,7 @@ typedef struct gf_ghost_block {
     const int* nbr;
     const gf_patch_geom* geom;
     const int* phys_of;         /* per-patch physics slot, or null = phys      */
+    gf_patch_flags* fl;         /* per-patch activity (culling), or null       */
     gf_bc_spec bc;
     int phys, maux;
     int skip;                   /* non-zero: leave this block alone this round */

@@ -105,7 +105,8 @@ class Server:
 
     def __init__(self, device: int = 0, hbm_budget: int | None = None, max_active: int = 256,
                  lanes: tuple = (100_000, 1_000_000), priority: bool = True,
-                 backfill: bool = True, reserve_sms: int | None = None, mixed_update: bool = False):
+                 backfill: bool = True, reserve_sms: int | None = None, mixed_update: bool = False,
+                 cull_dry: bool = True):
         self._lib = _lib.load()
         o = _lib.gf_server_opts()
         self._lib.gf_server_opts_default(C.byref(o))
@@ -120,6 +121,7 @@ class Server:
         if reserve_sms is not None:
             o.reserve_sms = int(reserve_sms)
         o.mixed_update = int(bool(mixed_update))
+        o.cull_dry = int(bool(cull_dry))
         h = C.c_void_p()
         rc = self._lib.gf_server_create(int(device), C.byref(o), C.byref(h))
         if rc != 0:

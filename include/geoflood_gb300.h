@@ -348,7 +348,7 @@ int gf_level_qad(gf_level* coarse, gf_level* fine, int ntask,
  * another. */
 #define GF_NOALLOC_MAX_PATCHES 16
 #define GF_NOALLOC_MAX_MAUX 4
-#define GF_NOALLOC_SCRATCH_BYTES 1162752
+#define GF_NOALLOC_SCRATCH_BYTES 1163008
 int gf_patch_update_noalloc(int device, const gf_phys* phys, int npatch,
                             int mx, int my, int mbc, int meqn, int maux,
                             const double* dx, const double* dy, double dt,
@@ -638,6 +638,12 @@ typedef struct gf_server_opts {
     int mixed_update;       /* 1: lanes after the first update every patch size in one
                                persistent launch (same results); 0 (default): one launch
                                per size, which keeps the small sizes' occupancy */
+    int cull_dry;           /* 1 (default): skip the ghost fill and update of a patch
+                               whose update would be an exact identity (it and its
+                               halo dry and unchanged by b4step2 at its last update,
+                               no neighbour wet, no hydrograph side); interior results
+                               are the same bits; a skipped patch's ghost cells keep
+                               their last values. 0: every patch every step */
 } gf_server_opts;
 
 typedef struct gf_scenario_info {
@@ -792,17 +798,25 @@ double gf_fserver_clock(const gf_fserver* s);
  * latency choice, everything else the throughput choice. Synthetic
  * all-wet patches, physics slot 0 of the context, `reps` timed launches
  * per variant. No reference counterpart (tuning support). */
-#define GF_MAX_TILES 4
+#define GF_MAX_TILES 12
 typedef struct gf_tile_result {
     int mx;
     int nvariant;
     int threads[GF_MAX_TILES], band[GF_MAX_TILES];
+    int cluster[GF_MAX_TILES];       /* > 1: one patch split over a cluster of
+                                        that many CTAs (the latency form)   */
     double throughput[GF_MAX_TILES]; /* cell-updates/s, ~4M-cell level     */
     double latency_us[GF_MAX_TILES]; /* one launch over 8 patches           */
     int best_throughput, best_latency;
 } gf_tile_result;
 int gf_autotune(gf_ctx* ctx, int reps, gf_tile_result* out /* [3]: mx 8, 16, 32 */);
-/* Current choice (goal 0 throughput, 1 latency) or a manual one. */
+/* Number of tile variants of patch size mx. */
+int gf_tile_count(int mx);
+/* Current choice (goal 0 throughput, 1 latency) or a manual one. Levels,
+ * forests and batched rounds take the throughput choice; a batch through
+ * gf_patch_update / gf_patch_update_batch / gf_step_buffer_update takes the
+ * latency choice when its patches times that tile's cluster size fit on
+ * the GPU's SMs, and the served form's smallest lane takes it always. */
 int gf_tile_get(int mx, int goal);
 int gf_tile_set(int mx, int goal, int variant);
 

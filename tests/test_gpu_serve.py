@@ -154,3 +154,19 @@ def test_submit_rejects_bad_scenarios():
             kw.update(bad)
             with pytest.raises((gf.GeoFloodError, ValueError)):
                 srv.submit(gf.Scenario(**kw))
+
+
+@pytest.mark.parametrize("mx", [8, 16, 32])
+def test_dry_patch_culling_gives_the_same_interior(mx):
+    """A valley mostly dry at the start, its channel fed by the hydrograph:
+    with the dry-patch culling on (the default) the run takes the same steps
+    and ends in the same interior bits as with every patch updated every
+    step."""
+    sc = scen(77 + mx, 40000, mx, ts=1.0 / 100.0)
+    on, info_on = serve_alone(sc)
+    off, info_off = serve_alone(sc, cull_dry=False)
+    assert (info_on["steps"], info_on["rejects"]) == (info_off["steps"], info_off["rejects"])
+    assert info_on["t"] == info_off["t"]
+    assert np.array_equal(interior(on), interior(off))
+    wet = interior(on)[..., 0] > sc.phys.dry_tolerance
+    assert 0.0 < wet.mean() < 0.5  # water arrived, and most of the valley stayed dry

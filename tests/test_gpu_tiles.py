@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 
 def variants(m):
-    return range({8: 3, 16: 3, 32: 2}[m])
+    return range(gf.Context.tile_count(m))
 
 
 @pytest.mark.parametrize("m", [8, 16, 32])
@@ -34,8 +34,9 @@ def test_every_tile_meets_the_parity_bar(ctx, m):
 
 @pytest.mark.parametrize("m", [8, 16, 32])
 def test_tile_shapes_give_the_same_bits(ctx, m):
-    """Threads per patch and slices per band change the work split, not the
-    sums: every variant's step equals variant 0's bit for bit."""
+    """Threads per patch, slices per band and the split of one patch over a
+    thread-block cluster change the work split, not the sums: every
+    variant's step equals variant 0's bit for bit."""
     keep = gf.Context.tile(m, 0)
     outs = []
     try:
@@ -64,3 +65,25 @@ def test_autotune_measures_and_selects(ctx):
         assert gf.Context.tile(r["mx"], 1) == r["best_latency"]
     with pytest.raises(gf.GeoFloodError):
         gf.Context.set_tile(8, 0, 9)
+
+
+@pytest.mark.parametrize("m", [8, 16, 32])
+def test_small_host_batches_take_the_latency_tile_with_the_same_bits(ctx, m):
+    """gf_patch_update_batch on a handful of patches runs the latency
+    choice (a patch split over a cluster for the window tiles): every
+    variant installed there gives the bits of the one-CTA kernel."""
+    keep = gf.Context.tile(m, 1)
+    q, aux, _, _ = synth.uniform_dam_break_level(2, 2, m, 1.0, seed=5, x_dam=1.0 * m)
+    outs = []
+    try:
+        for v in variants(m):
+            gf.Context.set_tile(m, 1, v)
+            qs = [np.array(q[k]) for k in range(4)]
+            cfl, mc = ctx.patch_update_batch(qs, [np.ascontiguousarray(aux[k]) for k in range(4)],
+                                             1.0, 1.0, 0.0, 0.05)
+            outs.append((np.stack(qs), cfl, mc))
+    finally:
+        gf.Context.set_tile(m, 1, keep)
+    for out, cfl, mc in outs[1:]:
+        assert np.array_equal(out, outs[0][0])
+        assert np.array_equal(cfl, outs[0][1]) and mc == outs[0][2]
