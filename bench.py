@@ -267,7 +267,8 @@ def served_stream(args):
     synth.flood_scenario(2, 3e6, mx=32, time_scale=ts)
 
     lanes = tuple(int(float(v)) for v in args.served_lanes.split(",") if v.strip())
-    srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms, lanes=lanes)
+    srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms, lanes=lanes,
+                    cull_dry=not args.served_no_cull)
     srv.start()
 
     # -- calibration: a saturated batch; throughput over a bounded window
@@ -1372,6 +1373,8 @@ def main():
     ap.add_argument("--served-cal-seconds", type=float, default=8.0)
     ap.add_argument("--served-sample", type=int, default=8,
                     help="scenarios re-run alone for the slowdown (size-stratified)")
+    ap.add_argument("--served-no-cull", action="store_true",
+                    help="update every patch of every served scenario every step")
     ap.add_argument("--served-low-load", action="store_true",
                     help="also run the first half of the stream at 50 %% load")
     ap.add_argument("--detail", default=None,

@@ -9,7 +9,7 @@ import oracle
 from geoflood_gb300 import _lib, synth
 
 
-def test_footprint_counts_two_state_buffers_aux_and_layout():
+def test_footprint_counts_two_state_buffers_aux_layout_and_flags():
     sc = synth.flood_scenario(5, 2048, mx=16)
     s, _ = sc.to_c(None)
     lib = _lib.load()
@@ -18,7 +18,8 @@ def test_footprint_counts_two_state_buffers_aux_and_layout():
 
     def a256(b):
         return (b + 255) // 256 * 256
-    want = 2 * a256(n * 3 * S * 8) + a256(n * 1 * S * 8) + a256(n * 32) + a256(n * 32)
+    # two state buffers, aux, neighbour table, geometry, dry-patch flags
+    want = 2 * a256(n * 3 * S * 8) + a256(n * 1 * S * 8) + a256(n * 32) + a256(n * 32) + a256(n * 4)
     assert lib.gf_scenario_footprint(C.byref(s)) == want
     s.mx = 12
     assert lib.gf_scenario_footprint(C.byref(s)) == 0
