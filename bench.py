@@ -589,7 +589,11 @@ def run_gpu(args):
     ncell = NPX * NPY * M * M
     ctx = gf.Context(local, gf.Phys())
     # tile shapes per patch size, measured on this device (process-wide choice)
-    tiles = ctx.autotune(reps=3) if not args.no_autotune else None
+    tiles = ctx.autotune(reps=3) if not (args.no_autotune or args.tiles) else None
+    for spec in filter(None, args.tiles.split(",")):
+        mx_s, thr, lat = (int(v) for v in spec.split(":"))
+        gf.Context.set_tile(mx_s, 0, thr)
+        gf.Context.set_tile(mx_s, 1, lat)
     lev = gf.Level(ctx, q.shape[0], M, 1)
     lev.set_geometry(DX, DX)
     lev.upload(q, aux)
@@ -1363,15 +1367,18 @@ def main():
                     help="forest arrivals per second (default: 80 %% of the calibrated capacity)")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tiles", default="",
+                    help="pin tile variants instead of autotuning: mx:throughput:latency,... "
+                         "(e.g. 32:3:7)")
     ap.add_argument("--large-only", action="store_true")
     ap.add_argument("--large-steps", type=int, default=24)
     ap.add_argument("--no-dem", action="store_true")
     ap.add_argument("--dem-only", action="store_true")
-    ap.add_argument("--served-scenarios", type=int, default=32)
+    ap.add_argument("--served-scenarios", type=int, default=16)
     ap.add_argument("--served-time-scale", type=float, default=1.0,
                     help="multiplies every scenario time (horizon, hydrograph rise)")
     ap.add_argument("--served-cal-seconds", type=float, default=8.0)
-    ap.add_argument("--served-sample", type=int, default=8,
+    ap.add_argument("--served-sample", type=int, default=6,
                     help="scenarios re-run alone for the slowdown (size-stratified)")
     ap.add_argument("--served-no-cull", action="store_true",
                     help="update every patch of every served scenario every step")

@@ -174,12 +174,7 @@ int check_phys_slot(gf_ctx* c, int slot, int maux = 0)
 /* Tile goal of a batch of nwork patches: the latency tile (goal 1) when
  * even split over its cluster the batch leaves SMs idle, so that a lone patch
  * or a handful of them spread over more SMs; the throughput tile otherwise. */
-int small_batch_goal(int m, int nwork)
-{
-    int nt = 0, rb = 0, k = 1;
-    if (gf::tile_shape(m, gf::tile_get(m, 1), &nt, &rb, &k) != 0) return 0;
-    return (long)nwork * k <= gf::sm_count() ? 1 : 0;
-}
+int small_batch_goal(int m, int nwork) { return gf::latency_goal_fits(m, nwork); }
 
 /* Enqueue one batch on the context stream: clear the status, launch. */
 int enqueue_batch(gf_ctx* c, int m, const gf_patch_work* d_work, int nwork, int maux, double dt,

@@ -136,6 +136,15 @@ int tile_shape(int m, int v, int* nt, int* rb, int* k)
 
 int tile_get(int m, int goal) { return g_tile[goal != 0][mcls(m)]; }
 
+int latency_goal_fits(int m, long npatch)
+{
+    int n = 0;
+    const Tile* t = tiles_of(m, &n);
+    if (!t) return 0;
+    const int k = t[g_tile[1][mcls(m)]].k;
+    return npatch * k <= (long)sm_count() ? 1 : 0;
+}
+
 int tile_set(int m, int goal, int v)
 {
     int n = 0;

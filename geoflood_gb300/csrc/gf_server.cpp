@@ -554,8 +554,11 @@ int enqueue_round(gf_server* srv, Lane& L)
     } else {
         for (int c = 0; c < 3; ++c)
             if (L.npm[c]) {
-                /* the smallest lane's step time is one patch's critical path: latency tiles */
-                const int goal = (L.idx == 0 && srv->o.nlanes > 1) ? 1 : 0;
+                /* the smallest lane's step time is one patch's critical path: the
+                 * latency tile, while its patches (split over their clusters)
+                 * fit on the SMs at once */
+                const int goal =
+                    (L.idx == 0 && srv->o.nlanes > 1 && gf::latency_goal_fits(ms[c], L.npm[c])) ? 1 : 0;
                 SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
                                                    L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux, nullptr,
                                                    rb + 1, err, L.st, srv->cta_cap[L.idx][c], goal));
