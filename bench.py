@@ -40,13 +40,14 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
-# DRAM traffic of one patch-update launch of this workload (one ncu capture:
-# dram__bytes_read.sum + dram__bytes_write.sum), against 234.9 MB algorithmic
-DRAM_BYTES_PER_LAUNCH = 170.340864e6 + 62.683392e6
-# FP64 pipe issue slots per cell-update of this workload: 37.46 M FP64 warp
-# instructions (ncu sm__inst_executed_pipe_fp64.sum) x 32 lanes / 4 194 304
-# cell-updates
-FP64_LANE_OPS_PER_CELL_UPDATE = 37.356532e6 * 32 / 4194304.0
+# Per tile shape of the mx = 32 update (threads, slices per band), from one ncu
+# capture of one launch on this workload each: DRAM traffic
+# (dram__bytes_read.sum + dram__bytes_write.sum, against 234.9 MB
+# algorithmic) and FP64 warp instructions (sm__inst_executed_pipe_fp64.sum;
+# x 32 lanes / 4 194 304 cell-updates = FP64 issue slots per cell-update)
+NCU_COUNTS = {(256, 7): (170.340864e6 + 62.683392e6, 37.356532e6),
+              (384, 9): (170.288896e6 + 66.034688e6, 37.118633e6)}
+NCU_DEFAULT_TILE = (384, 9)
 M = 32
 NPX = NPY = 64
 DX = 1.0
@@ -692,6 +693,16 @@ def run_gpu(args):
     lone_us = lone_patch_latency_us(ctx, q, aux)
 
     hbm_peak, peak_kind = load_peaks()
+    tile32 = (384, 9)
+    tsel = next((t for t in (tiles or []) if t["mx"] == M), None)
+    if tsel is not None:
+        tile32 = tuple(tsel["tiles"][tsel["best_throughput"]][:2])
+    elif args.tiles:
+        for spec in filter(None, args.tiles.split(",")):
+            mx_s, thr, _ = (int(v) for v in spec.split(":"))
+            if mx_s == M:
+                tile32 = {0: (256, 7), 1: (256, 5), 2: (384, 7), 3: (384, 9)}.get(thr, tile32)
+    traffic, fp64_warp_inst = NCU_COUNTS.get(tile32, NCU_COUNTS[NCU_DEFAULT_TILE])
     algo = BYTES_PER_CELL_UPDATE * ncell
     achieved = algo / (kernel_ms * 1e-3) / 1e9
     rates = fp64_rates()
@@ -705,7 +716,7 @@ def run_gpu(args):
         # FP64 issue slots (warp instructions x 32 lanes) per cell-update of
         # this workload, from the ncu capture of the same kernel: the achieved
         # FP64 issue rate follows from the live kernel time
-        ops = FP64_LANE_OPS_PER_CELL_UPDATE
+        ops = fp64_warp_inst * 32 / float(ncell)
         ach = ops * ncell / (kernel_ms * 1e-3) / 1e9
         fp64.update({"lane_ops_per_cell_update": ops, "achieved_gops": ach,
                      "frac_of_measured_dfma": ach / (rates["dfma"] / 1e9),
@@ -723,7 +734,7 @@ def run_gpu(args):
                 "h2d_bytes_per_step": qbytes, "d2h_bytes_per_step": qbytes + 16},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": DRAM_BYTES_PER_LAUNCH,
+                     "frac": achieved / hbm_peak, "traffic": traffic, "tile": list(tile32),
                      "traffic_unit": "bytes per launch",
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum "
                                        "of one launch (one capture)",
