@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <memory>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -159,6 +160,8 @@ struct gf_forest {
     int ss_copy_n[3] = {0, 0, 0};
     DArr<gf_slot_task> d_ss;
     DArr<int> d_par01;
+    std::vector<gf_xfer_task> h_sx;              /* host copies of d_sx, d_ss */
+    std::vector<gf_slot_task> h_ss;
     /* a subcycled step as a CUDA graph: a host-only plan pass writes the
      * step's level dts and ghost blocks (their boundary times) to pinned
      * staging; the graph's first node copies them to the device */
@@ -173,6 +176,7 @@ struct gf_forest {
     int sub_graph_par = -1, sub_graph_nblk = -1;
     bool sub_graph_exact = false;
     long long sub_updates = 0; /* cell-updates of the step in flight */
+    unsigned long long sub_epoch = 0; /* counts rebuilds of the subcycling tables */
     /* a subcycled run driven step by step among others (concurrent runner):
      * the outstyle-1 state between steps, the step in flight on `sst` */
     struct SubRun {
@@ -1138,7 +1142,10 @@ int build_sub_tables(gf_forest* f)
     FK(f, f->d_par01.reserve(2));
     const int p01[2] = {0, 1};
     FK(f, cudaMemcpyAsync(f->d_par01.p, p01, sizeof p01, cudaMemcpyHostToDevice, st));
+    f->h_sx.swap(x);
+    f->h_ss.swap(sl);
     f->sub_dirty = false;
+    ++f->sub_epoch;
     return GF_OK;
 }
 
@@ -2572,6 +2579,491 @@ int sub_run_pass(SubRunner& R, int wait, int* live, int* progress)
     return GF_OK;
 }
 
+
+/* ---- subcycled forests in shared launches ----
+ * Forests whose leaves span the same levels and that share the patch size,
+ * the aux count, the state buffer parity and the update build step
+ * together: every launch of the subcycled schedule (the order of
+ * sub_fill_level / sub_level above) carries the tasks of every member, with
+ * each member's own level dts (group = member in the update's work items),
+ * boundary times (one ghost block per member and call), buffers and CFL
+ * slot. Each member's arithmetic is the same as in its own step, so its run
+ * is the same bits; the launches per coarse step no longer grow with the
+ * number of forests. The merged lists are the concatenation of the members'
+ * own lists (build_sub_tables), rebuilt when a member's tables change
+ * (regrid) or the membership does. */
+struct SubGroup {
+    gf_ctx* ctx = nullptr;
+    int M = 0, lo = 0, hi = 0, par = 0, maux = 0;
+    bool exact = false;
+    std::vector<gf_forest*> mem;
+    std::vector<unsigned long long> epochs; /* the members' table epochs merged */
+    bool built = false;
+    DArr<gf_patch_work> d_work;
+    std::vector<int> w_off, w_n;             /* per level */
+    DArr<gf_ghost_ref> d_refs;
+    std::vector<int> ra_off, ra_n, rr_off, rr_n;
+    DArr<gf_xfer_task> d_x;
+    std::vector<int> xa_off, xi_off;         /* [l * 6 + bc * 2 + bf] */
+    std::vector<int> xa_n, xi_n;             /* per level */
+    DArr<gf_slot_task> d_s;
+    std::vector<int> ti_off, ti_n;           /* [l * 2 + po], per level */
+    int save_off = 0, save_n = 0;
+    DArr<int> d_par;                         /* K zeros, then K ones */
+    DArr<unsigned long long> d_rb;           /* [err][gmax of member k] */
+    unsigned long long* h_rb = nullptr;      /* pinned, 1 + K */
+    size_t h_rb_cap = 0;
+    DArr<char> d_stage;                      /* level dts [nlev * K], then the blocks */
+    char* h_stage = nullptr;
+    size_t h_stage_cap = 0;
+    std::vector<gf_ghost_block> blocks;      /* the step's ghost blocks, K per call */
+    std::vector<double> tl, dtl;             /* per member during the plan pass */
+    bool plan = false;
+    int ncall = 0;
+    size_t blk_off = 0;                      /* byte offset of the blocks in the staging */
+    ~SubGroup()
+    {
+        d_work.release();
+        d_refs.release();
+        d_x.release();
+        d_s.release();
+        d_par.release();
+        d_rb.release();
+        d_stage.release();
+        if (h_rb) cudaFreeHost(h_rb);
+        if (h_stage) cudaFreeHost(h_stage);
+    }
+};
+
+int sg_fail(SubGroup& G, cudaError_t e, const char* what) { return gf::ctx_cuda_fail(G.ctx, e, what); }
+#define GK(G, call)                                      \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return sg_fail((G), e_, #call); \
+    } while (0)
+
+/* merged tables of the group's members (their sub tables are current) */
+int sg_build(SubGroup& G)
+{
+    const int K = (int)G.mem.size();
+    const int nlev = G.hi + 1;
+    std::vector<gf_patch_work> work;
+    std::vector<gf_ghost_ref> refs;
+    std::vector<gf_xfer_task> x;
+    std::vector<gf_slot_task> sl;
+    G.w_off.assign(nlev, 0);
+    G.w_n.assign(nlev, 0);
+    G.ra_off.assign(nlev, 0);
+    G.ra_n.assign(nlev, 0);
+    G.rr_off.assign(nlev, 0);
+    G.rr_n.assign(nlev, 0);
+    G.xa_off.assign((size_t)nlev * 6, 0);
+    G.xi_off.assign((size_t)nlev * 6, 0);
+    G.xa_n.assign(nlev, 0);
+    G.xi_n.assign(nlev, 0);
+    G.ti_off.assign((size_t)nlev * 2, 0);
+    G.ti_n.assign(nlev, 0);
+    for (int l = G.lo; l <= G.hi; ++l) {
+        G.w_off[l] = (int)work.size();
+        G.ra_off[l] = (int)refs.size();
+        for (int k = 0; k < K; ++k) {
+            const gf_forest* f = G.mem[k];
+            for (int i = 0; i < f->lev_n[l]; ++i) {
+                gf_patch_work w = f->h_work[f->lev_off[l] + i];
+                w.group = k;
+                work.push_back(w);
+                refs.push_back(gf_ghost_ref{k, f->leaves[f->lev_off[l] + i].slot});
+            }
+        }
+        G.w_n[l] = (int)work.size() - G.w_off[l];
+        G.ra_n[l] = (int)refs.size() - G.ra_off[l];
+    }
+    for (int l = G.lo; l <= G.hi; ++l) {
+        G.rr_off[l] = (int)refs.size();
+        for (int k = 0; k < K; ++k)
+            for (int s : G.mem[k]->h_refresh[l]) refs.push_back(gf_ghost_ref{k, s});
+        G.rr_n[l] = (int)refs.size() - G.rr_off[l];
+    }
+    for (int l = G.lo; l <= G.hi; ++l)
+        for (int c = 0; c < 6; ++c) {
+            G.xa_off[(size_t)l * 6 + c] = (int)x.size();
+            for (int k = 0; k < K; ++k) {
+                const gf_forest* f = G.mem[k];
+                const int o = f->sx_avg_off[(size_t)l * 6 + c];
+                x.insert(x.end(), f->h_sx.begin() + o, f->h_sx.begin() + o + f->sx_avg_n[l]);
+            }
+            G.xa_n[l] = (int)x.size() - G.xa_off[(size_t)l * 6 + c];
+            G.xi_off[(size_t)l * 6 + c] = (int)x.size();
+            for (int k = 0; k < K; ++k) {
+                const gf_forest* f = G.mem[k];
+                const int o = f->sx_itp_off[(size_t)l * 6 + c];
+                x.insert(x.end(), f->h_sx.begin() + o, f->h_sx.begin() + o + f->itp_n[l]);
+            }
+            G.xi_n[l] = (int)x.size() - G.xi_off[(size_t)l * 6 + c];
+        }
+    for (int l = G.lo; l <= G.hi; ++l)
+        for (int po = 0; po < 2; ++po) {
+            G.ti_off[(size_t)l * 2 + po] = (int)sl.size();
+            for (int k = 0; k < K; ++k) {
+                const gf_forest* f = G.mem[k];
+                const int o = f->ss_ti_off[(size_t)l * 2 + po];
+                sl.insert(sl.end(), f->h_ss.begin() + o, f->h_ss.begin() + o + f->lev_n[l]);
+            }
+            G.ti_n[l] = (int)sl.size() - G.ti_off[(size_t)l * 2 + po];
+        }
+    G.save_off = (int)sl.size();
+    for (int k = 0; k < K; ++k) {
+        const gf_forest* f = G.mem[k];
+        const int o = f->ss_copy_off[0][G.par];
+        sl.insert(sl.end(), f->h_ss.begin() + o, f->h_ss.begin() + o + f->ss_copy_n[0]);
+    }
+    G.save_n = (int)sl.size() - G.save_off;
+    cudaStream_t st = gf::ctx_stream(G.ctx);
+    GK(G, G.d_work.reserve(work.size() + 1));
+    GK(G, G.d_refs.reserve(refs.size() + 1));
+    GK(G, G.d_x.reserve(x.size() + 1));
+    GK(G, G.d_s.reserve(sl.size() + 1));
+    if (!work.empty())
+        GK(G, cudaMemcpyAsync(G.d_work.p, work.data(), work.size() * sizeof(gf_patch_work), cudaMemcpyHostToDevice, st));
+    if (!refs.empty())
+        GK(G, cudaMemcpyAsync(G.d_refs.p, refs.data(), refs.size() * sizeof(gf_ghost_ref), cudaMemcpyHostToDevice, st));
+    if (!x.empty())
+        GK(G, cudaMemcpyAsync(G.d_x.p, x.data(), x.size() * sizeof(gf_xfer_task), cudaMemcpyHostToDevice, st));
+    if (!sl.empty())
+        GK(G, cudaMemcpyAsync(G.d_s.p, sl.data(), sl.size() * sizeof(gf_slot_task), cudaMemcpyHostToDevice, st));
+    std::vector<int> pars((size_t)2 * K, 0);
+    for (int k = 0; k < K; ++k) pars[(size_t)K + k] = 1;
+    GK(G, G.d_par.reserve(pars.size()));
+    GK(G, cudaMemcpyAsync(G.d_par.p, pars.data(), pars.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    GK(G, G.d_rb.reserve((size_t)K + 1));
+    if (G.h_rb_cap < (size_t)K + 1) {
+        if (G.h_rb) cudaFreeHost(G.h_rb);
+        G.h_rb = nullptr;
+        G.h_rb_cap = 0;
+        GK(G, cudaMallocHost(reinterpret_cast<void**>(&G.h_rb), ((size_t)K + 1) * 2 * sizeof(unsigned long long)));
+        G.h_rb_cap = ((size_t)K + 1) * 2;
+    }
+    G.epochs.clear();
+    for (gf_forest* f : G.mem) G.epochs.push_back(f->sub_epoch);
+    G.built = true;
+    return GF_OK;
+}
+
+/* one ghost fill of level l's leaves (refs at roff, n) in buffer b of every
+ * member, at each member's time tt[k] */
+int sg_ghost(SubGroup& G, int b, const std::vector<double>& tt, int roff, int n)
+{
+    const int K = (int)G.mem.size();
+    if (n <= 0) return GF_OK;
+    const int i = G.ncall++;
+    if (G.plan) {
+        if ((int)G.blocks.size() < (i + 1) * K) G.blocks.resize((size_t)(i + 1) * K);
+        for (int k = 0; k < K; ++k) {
+            gf_forest* f = G.mem[k];
+            gf_ghost_block blk{};
+            blk.q = b < 2 ? f->qbuf[b] : f->qi;
+            blk.aux = f->aux;
+            blk.nbr = f->d_nbr.p;
+            blk.geom = f->d_geom.p;
+            blk.phys_of = nullptr;
+            blk.bc = f->bc;
+            blk.bc.q0hu = hydro_at(f, tt[k]);
+            blk.phys = f->o.phys_slot;
+            blk.maux = f->o.maux;
+            blk.skip = 0;
+            G.blocks[(size_t)i * K + k] = blk;
+        }
+        return GF_OK;
+    }
+    const gf_ghost_block* d_blk =
+        reinterpret_cast<const gf_ghost_block*>(G.d_stage.p + G.blk_off) + (size_t)i * K;
+    GK(G, gf::launch_ghost_fill(G.M, d_blk, G.d_refs.p + roff, n, gf::ctx_device_phys(G.ctx),
+                                gf::ctx_stream(G.ctx)));
+    return GF_OK;
+}
+
+/* sub_fill_level for the group */
+int sg_fill_level(SubGroup& G, int l, const std::vector<double>& tt, const int* p, int cbuf)
+{
+    cudaStream_t st = gf::ctx_stream(G.ctx);
+    const gf_phys* phys = gf::ctx_device_phys(G.ctx);
+    const bool go = !G.plan;
+    int rc;
+    if (go && l < G.hi && G.xa_n[l])
+        GK(G, gf::launch_transfer(G.M, G.d_x.p + G.xa_off[(size_t)l * 6 + p[l] * 2 + p[l + 1]], G.xa_n[l],
+                                  phys, st));
+    if ((rc = sg_ghost(G, p[l], tt, G.ra_off[l], G.ra_n[l]))) return rc;
+    if (cbuf >= 0 && G.xi_n[l]) {
+        if (go)
+            GK(G, gf::launch_transfer(G.M, G.d_x.p + G.xi_off[(size_t)l * 6 + cbuf * 2 + p[l]], G.xi_n[l],
+                                      phys, st));
+        if ((rc = sg_ghost(G, p[l], tt, G.rr_off[l], G.rr_n[l]))) return rc;
+    }
+    return GF_OK;
+}
+
+int sg_update(SubGroup& G, int l, int* p)
+{
+    const int K = (int)G.mem.size();
+    if (!G.plan && G.w_n[l]) {
+        cudaStream_t st = gf::ctx_stream(G.ctx);
+        const gf_phys* phys = gf::ctx_device_phys(G.ctx);
+        int* err = reinterpret_cast<int*>(G.d_rb.p);
+        const double* dts = reinterpret_cast<const double*>(G.d_stage.p) + (size_t)l * K;
+        const gf_patch_work* w = G.d_work.p + G.w_off[l];
+        const int* gpar = G.d_par.p + (size_t)p[l] * K;
+        if (G.exact)
+            GK(G, gf::launch_patch_update_exact(G.M, w, G.w_n[l], phys, 0.0, dts, gpar, G.maux, nullptr,
+                                                G.d_rb.p + 1, err, st));
+        else
+            GK(G, gf::launch_patch_update(G.M, w, G.w_n[l], phys, 0.0, dts, gpar, G.maux, nullptr,
+                                          G.d_rb.p + 1, err, st));
+    }
+    p[l] ^= 1;
+    return GF_OK;
+}
+
+/* sub_level for the group: tl / dtl per member as in the member's own step */
+int sg_level(SubGroup& G, int l, const std::vector<double>& tl, const std::vector<double>& dtl, int* p)
+{
+    int rc;
+    if ((rc = sg_update(G, l, p))) return rc;
+    if (l >= G.hi) return GF_OK;
+    const int K = (int)G.mem.size();
+    const int po = p[l] ^ 1;
+    cudaStream_t st = gf::ctx_stream(G.ctx);
+    const gf_phys* phys = gf::ctx_device_phys(G.ctx);
+    std::vector<double> tf(K), dth(K);
+    for (int k = 0; k < K; ++k) dth[k] = dtl[k] * 0.5;
+    for (int s = 0; s < 2; ++s) {
+        for (int k = 0; k < K; ++k) tf[k] = s ? tl[k] + dtl[k] * 0.5 : tl[k];
+        int cbuf = po;
+        if (s == 1) {
+            if (!G.plan) {
+                if (G.ti_n[l])
+                    GK(G, gf::launch_tinterp_strip(G.M, G.d_s.p + G.ti_off[(size_t)l * 2 + po], G.ti_n[l], 0.5, st));
+                if (G.xa_n[l])
+                    GK(G, gf::launch_transfer(G.M, G.d_x.p + G.xa_off[(size_t)l * 6 + 2 * 2 + p[l + 1]],
+                                              G.xa_n[l], phys, st));
+            }
+            if ((rc = sg_ghost(G, 2, tf, G.ra_off[l], G.ra_n[l]))) return rc;
+            cbuf = 2;
+        }
+        if ((rc = sg_fill_level(G, l + 1, tf, p, cbuf))) return rc;
+        if ((rc = sg_level(G, l + 1, tf, dth, p))) return rc;
+    }
+    return GF_OK;
+}
+
+/* one coarse step of every member (t[k], dt[k]), launched on the context's
+ * stream with the per-member CFL readback into G.h_rb */
+int sg_launch(SubGroup& G, const std::vector<double>& t, const std::vector<double>& dt)
+{
+    const int K = (int)G.mem.size();
+    const int nlev = G.hi + 1;
+    cudaStream_t st = gf::ctx_stream(G.ctx);
+    std::vector<int> p(nlev + 1, G.par);
+    /* plan: the step's ghost blocks */
+    G.plan = true;
+    G.ncall = 0;
+    int rc = sg_fill_level(G, G.lo, t, p.data(), -1);
+    if (!rc) rc = sg_level(G, G.lo, t, dt, p.data());
+    G.plan = false;
+    if (rc) return rc;
+    const int ncall = G.ncall;
+    G.blk_off = ((size_t)nlev * K * sizeof(double) + 255) / 256 * 256;
+    const size_t bytes = G.blk_off + (size_t)ncall * K * sizeof(gf_ghost_block);
+    if (bytes > G.h_stage_cap) {
+        if (G.h_stage) cudaFreeHost(G.h_stage);
+        G.h_stage = nullptr;
+        G.h_stage_cap = 0;
+        GK(G, cudaMallocHost(reinterpret_cast<void**>(&G.h_stage), bytes + bytes / 2));
+        G.h_stage_cap = bytes + bytes / 2;
+    }
+    double* hdt = reinterpret_cast<double*>(G.h_stage);
+    for (size_t e = 0; e < (size_t)nlev * K; ++e) hdt[e] = 0.0;
+    for (int k = 0; k < K; ++k) {
+        double d = dt[k];
+        for (int l = G.lo; l <= G.hi; ++l, d *= 0.5) hdt[(size_t)l * K + k] = d;
+    }
+    std::memcpy(G.h_stage + G.blk_off, G.blocks.data(), (size_t)ncall * K * sizeof(gf_ghost_block));
+    GK(G, G.d_stage.reserve(bytes));
+    GK(G, cudaMemcpyAsync(G.d_stage.p, G.h_stage, bytes, cudaMemcpyHostToDevice, st));
+    GK(G, cudaMemsetAsync(G.d_rb.p, 0, ((size_t)K + 1) * sizeof(unsigned long long), st));
+    if (G.save_n) GK(G, gf::launch_slot_copy(G.M, G.d_s.p + G.save_off, G.save_n, st));
+    std::vector<int> q(nlev + 1, G.par);
+    G.ncall = 0;
+    if ((rc = sg_fill_level(G, G.lo, t, q.data(), -1))) return rc;
+    if ((rc = sg_level(G, G.lo, t, dt, q.data()))) return rc;
+    GK(G, cudaMemcpyAsync(G.h_rb, G.d_rb.p, ((size_t)K + 1) * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, st));
+    return GF_OK;
+}
+
+/* Subcycled forests in shared launches, each with its own outstyle-1
+ * control (as sub_run_launch / sub_run_complete); forests that match
+ * (same level range, patch size, aux count, parity, build) share a group. */
+struct SubBatch {
+    gf_ctx* ctx = nullptr;
+    std::vector<gf_forest*> fs;
+    std::vector<std::unique_ptr<SubGroup>> groups;
+    long long regrids = 0, cell_updates = 0, steps_launched = 0;
+};
+
+int sb_add(SubBatch& B, gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
+           double max_cfl)
+{
+    if (!f || f->ctx != B.ctx) return GF_ERR_ARG;
+    if (f->leaves.empty()) return ffail(f, GF_ERR_STATE, "forest not initialised");
+    if (!f->o.subcycle) return ffail(f, GF_ERR_ARG, "not a subcycled forest");
+    gf_forest::SubRun& r = f->sr;
+    r = gf_forest::SubRun{};
+    r.t_curr = f->st.t;
+    r.dt_minlevel = initial_dt;
+    r.dt_outer = t_final / nout;
+    r.tend = r.t_curr + r.dt_outer;
+    r.nout = nout;
+    r.desired_cfl = desired_cfl;
+    r.max_cfl = max_cfl;
+    r.active = true;
+    B.fs.push_back(f);
+    return GF_OK;
+}
+
+/* the outstyle-1 clipping of the member's next step; false when its run is over */
+bool sb_next(gf_forest* f)
+{
+    gf_forest::SubRun& r = f->sr;
+    while (!(r.t_curr < r.tend)) {
+        if (++r.nint >= r.nout) {
+            r.active = false;
+            f->st.t = r.t_curr;
+            f->st.dt = r.dt_minlevel;
+            f->st.npatch = (int)f->leaves.size();
+            f->st.npatch_max = std::max(f->st.npatch_max, f->st.npatch);
+            return false;
+        }
+        r.tend = r.t_curr + r.dt_outer;
+    }
+    double dt_step = r.dt_minlevel;
+    const double tol = 1e-2 * dt_step;
+    r.took_small = false;
+    const double small_step = r.tend - (r.t_curr + dt_step);
+    if (small_step < tol) {
+        dt_step = r.tend - r.t_curr;
+        if (small_step < 0) r.took_small = true;
+    }
+    r.dt_step = dt_step;
+    return true;
+}
+
+/* One iteration: every running forest takes one coarse step (accepted or
+ * retaken), group by group; *live = forests still running. */
+int sb_iterate(SubBatch& B, int* live)
+{
+    std::vector<gf_forest*> run;
+    for (gf_forest* f : B.fs)
+        if (f->sr.active && !f->sr.cancel && sb_next(f)) run.push_back(f);
+    for (gf_forest* f : run) {
+        int rc = build_sub_tables(f);
+        if (rc) return rc;
+    }
+    /* regroup: key (patch size, levels present, aux count, parity, build) */
+    const bool exact = gf::ctx_exact(B.ctx);
+    std::vector<std::unique_ptr<SubGroup>> next;
+    for (gf_forest* f : run) {
+        SubGroup* g = nullptr;
+        for (auto& h : next)
+            if (h->M == f->M && h->lo == f->sub_lo && h->hi == f->sub_hi && h->maux == f->o.maux &&
+                h->par == f->par)
+                g = h.get();
+        if (!g) {
+            next.emplace_back(new SubGroup());
+            g = next.back().get();
+            g->ctx = B.ctx;
+            g->M = f->M;
+            g->lo = f->sub_lo;
+            g->hi = f->sub_hi;
+            g->maux = f->o.maux;
+            g->par = f->par;
+            g->exact = exact;
+        }
+        g->mem.push_back(f);
+    }
+    /* keep the built tables of groups whose members and epochs are unchanged */
+    for (auto& g : next)
+        for (auto& old : B.groups)
+            if (old && old->M == g->M && old->lo == g->lo && old->hi == g->hi && old->maux == g->maux &&
+                old->par == g->par && old->exact == g->exact && old->mem == g->mem) {
+                bool same = old->built;
+                for (size_t k = 0; same && k < g->mem.size(); ++k)
+                    same = old->epochs[k] == g->mem[k]->sub_epoch;
+                if (same) std::swap(g, old);
+                break;
+            }
+    B.groups.swap(next);
+    for (auto& g : B.groups) {
+        if (!g->built) {
+            int rc = sg_build(*g);
+            if (rc) return rc;
+        }
+        const int K = (int)g->mem.size();
+        std::vector<double> t(K), dt(K);
+        for (int k = 0; k < K; ++k) {
+            t[k] = g->mem[k]->sr.t_curr;
+            dt[k] = g->mem[k]->sr.dt_step;
+        }
+        int rc = sg_launch(*g, t, dt);
+        if (rc) return rc;
+        B.steps_launched += K;
+    }
+    cudaStream_t st = gf::ctx_stream(B.ctx);
+    const cudaError_t se = cudaStreamSynchronize(st);
+    if (se != cudaSuccess) return gf::ctx_cuda_fail(B.ctx, se, "subcycled group step");
+    /* take in each member's step: accept or retake, next dt, regrid when due */
+    for (auto& g : B.groups) {
+        const int K = (int)g->mem.size();
+        if ((int)g->h_rb[0]) return gf::ctx_fail(B.ctx, GF_ERR_DEVICE, "a patch-update copy wait timed out");
+        for (int k = 0; k < K; ++k) {
+            gf_forest* f = g->mem[k];
+            gf_forest::SubRun& r = f->sr;
+            double cfl;
+            std::memcpy(&cfl, &g->h_rb[1 + k], sizeof cfl);
+            long long cu = 0;
+            for (int l = f->sub_lo; l <= f->sub_hi; ++l)
+                cu += (long long)f->lev_n[l] * f->M * f->M << (l - f->sub_lo);
+            f->st.max_cfl_seen = std::max(f->st.max_cfl_seen, cfl);
+            int rc;
+            if (cfl > r.max_cfl) {
+                if ((rc = sub_finish(f, false))) return rc;
+                r.dt_minlevel = r.dt_minlevel * r.desired_cfl / cfl;
+                f->st.rejects++;
+                continue;
+            }
+            if ((rc = sub_finish(f, true))) return rc;
+            f->st.steps++;
+            f->st.cell_updates += cu;
+            B.cell_updates += cu;
+            r.t_curr += r.dt_step;
+            const double dt_new = r.dt_minlevel * r.desired_cfl / cfl;
+            if (!r.took_small) r.dt_minlevel = dt_new;
+            f->st.t = r.t_curr;
+            f->st.dt = r.dt_minlevel;
+            if (f->o.regrid_interval > 0 && f->st.steps % f->o.regrid_interval == 0) {
+                bool changed = false;
+                if ((rc = regrid(f, r.t_curr, &changed))) return rc;
+                B.regrids++;
+                f->st.npatch_max = std::max(f->st.npatch_max, (int)f->leaves.size());
+            }
+        }
+    }
+    int n = 0;
+    for (gf_forest* f : B.fs) n += f->sr.active && !f->sr.cancel;
+    *live = n;
+    return GF_OK;
+}
+#undef GK
+
 } // namespace
 
 extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, int nout,
@@ -2593,16 +3085,17 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
             if (forests[j] == forests[k]) return ffail(forests[k], GF_ERR_ARG, "a forest appears twice");
     }
     /* forests that take every level's step together share rounds;
-     * subcycled forests run side by side on their own streams */
+     * subcycled forests share the launches of their coarse steps, grouped
+     * by the levels they span */
     BatchRun R;
-    SubRunner U;
+    SubBatch U;
     U.ctx = ctx;
     int rc = batch_begin(R, ctx);
     if (rc) return rc;
     int nb = 0, ns = 0;
     for (int k = 0; k < n; ++k) {
         if (forests[k]->o.subcycle) {
-            if ((rc = sub_run_add(U, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl))) return rc;
+            if ((rc = sb_add(U, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl))) return rc;
             ++ns;
         } else {
             batch_add(R, forests[k], t_final, nout, initial_dt, desired_cfl, max_cfl);
@@ -2611,7 +3104,7 @@ extern "C" int gf_forest_batch_run(gf_forest** forests, int n, double t_final, i
     }
     int live_b = nb, live_s = ns;
     while (live_b || live_s) {
-        if (live_s && (rc = sub_run_pass(U, live_b == 0, &live_s, nullptr))) return rc;
+        if (live_s && (rc = sb_iterate(U, &live_s))) return rc;
         if (live_b && (rc = batch_iterate(R, &live_b))) return rc;
     }
     if (bst) {

@@ -122,9 +122,9 @@ def forest(ctx, m=M, seed=3, regrid=2, subcycle=True, mthbc=(3, 3, 3, 3), hydro=
 
 
 def test_subcycled_forests_in_a_batch_equal_their_own_runs(ctx):
-    """Subcycled forests run side by side in gf_forest_batch_run (each
-    coarse step its own graph on one of the runner's streams), beside
-    forests that share rounds: every forest ends as its own gf_forest_run."""
+    """Subcycled forests of different patch sizes in gf_forest_batch_run
+    (each in a launch group of its own), beside forests that share rounds:
+    every forest ends as its own gf_forest_run."""
     from geoflood_gb300.forest import batch_run
 
     ctx.set_phys(SLOT, gf.Phys(manning_coefficient=(0.035,), manning_break=(1e10,)))
@@ -147,3 +147,38 @@ def test_subcycled_forests_in_a_batch_equal_their_own_runs(ctx):
     assert bst["regrids"] == sum(F.stats()["regrids"] for F in fs)
     for F in fs:
         F.close()
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_subcycled_forests_share_launches_and_equal_their_own_runs(ctx, exact):
+    """Six subcycled forests of one patch size (different beds, regrid
+    cadences, one with hydrograph inflow) in gf_forest_batch_run: forests
+    whose leaves span the same levels step in shared launches, and the groups
+    change as regrids add and remove levels; every forest ends as its own
+    gf_forest_run, bit for bit, in both builds."""
+    from geoflood_gb300.forest import batch_run
+
+    ctx.set_phys(SLOT, gf.Phys(manning_coefficient=(0.035,), manning_break=(1e10,)))
+    ctx.set_fp_contract(not exact)
+    try:
+        specs = [dict(m=16, seed=3 + k, regrid=2 + k % 2) for k in range(5)]
+        specs.append(dict(m=16, seed=11, regrid=2, mthbc=(0, 3, 3, 3), hydro=HYDRO))
+        alone = []
+        for sp in specs:
+            F = forest(ctx, **sp)
+            st = F.run(30.0, 2, 5.0, 0.9, 1.0)
+            alone.append((F.patches(), F.download(), st))
+            F.close()
+        fs = [forest(ctx, **sp) for sp in specs]
+        bst = batch_run(fs, 30.0, 2, 5.0, 0.9, 1.0)
+        for F, (P, q, st) in zip(fs, alone):
+            got = F.stats()
+            assert np.array_equal(F.patches(), P)
+            assert np.array_equal(F.download()[S], q[S])
+            for k in ("steps", "rejects", "regrids", "cell_updates", "t"):
+                assert got[k] == st[k], k
+        assert bst["regrids"] == sum(F.stats()["regrids"] for F in fs)
+        for F in fs:
+            F.close()
+    finally:
+        ctx.set_fp_contract(True)
