@@ -2621,8 +2621,15 @@ struct SubGroup {
     bool plan = false;
     int ncall = 0;
     size_t blk_off = 0;                      /* byte offset of the blocks in the staging */
+    /* the step's launches as a CUDA graph, captured after a rebuild and
+     * replayed while the tables stand; the plan pass rewrites the staging
+     * (level dts, ghost blocks) that the graph's first node copies */
+    cudaGraphExec_t exec = nullptr;
+    bool graph_ok = false;
+    size_t graph_bytes = 0;
     ~SubGroup()
     {
+        if (exec) cudaGraphExecDestroy(exec);
         d_work.release();
         d_refs.release();
         d_x.release();
@@ -2746,6 +2753,7 @@ int sg_build(SubGroup& G)
     G.epochs.clear();
     for (gf_forest* f : G.mem) G.epochs.push_back(f->sub_epoch);
     G.built = true;
+    G.graph_ok = false;
     return GF_OK;
 }
 
@@ -2879,6 +2887,7 @@ int sg_launch(SubGroup& G, const std::vector<double>& t, const std::vector<doubl
         G.h_stage_cap = 0;
         GK(G, cudaMallocHost(reinterpret_cast<void**>(&G.h_stage), bytes + bytes / 2));
         G.h_stage_cap = bytes + bytes / 2;
+        G.graph_ok = false; /* the graph's first node reads the old staging */
     }
     double* hdt = reinterpret_cast<double*>(G.h_stage);
     for (size_t e = 0; e < (size_t)nlev * K; ++e) hdt[e] = 0.0;
@@ -2887,16 +2896,49 @@ int sg_launch(SubGroup& G, const std::vector<double>& t, const std::vector<doubl
         for (int l = G.lo; l <= G.hi; ++l, d *= 0.5) hdt[(size_t)l * K + k] = d;
     }
     std::memcpy(G.h_stage + G.blk_off, G.blocks.data(), (size_t)ncall * K * sizeof(gf_ghost_block));
-    GK(G, G.d_stage.reserve(bytes));
-    GK(G, cudaMemcpyAsync(G.d_stage.p, G.h_stage, bytes, cudaMemcpyHostToDevice, st));
-    GK(G, cudaMemsetAsync(G.d_rb.p, 0, ((size_t)K + 1) * sizeof(unsigned long long), st));
-    if (G.save_n) GK(G, gf::launch_slot_copy(G.M, G.d_s.p + G.save_off, G.save_n, st));
-    std::vector<int> q(nlev + 1, G.par);
-    G.ncall = 0;
-    if ((rc = sg_fill_level(G, G.lo, t, q.data(), -1))) return rc;
-    if ((rc = sg_level(G, G.lo, t, dt, q.data()))) return rc;
-    GK(G, cudaMemcpyAsync(G.h_rb, G.d_rb.p, ((size_t)K + 1) * sizeof(unsigned long long),
-                          cudaMemcpyDeviceToHost, st));
+    if (!G.graph_ok || G.graph_bytes != bytes) {
+        G.graph_ok = false;
+        GK(G, G.d_stage.reserve(bytes));
+        GK(G, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int crc = GF_OK;
+        auto cap = [&](cudaError_t e) {
+            if (e != cudaSuccess && crc == GF_OK) crc = sg_fail(G, e, "subcycled group step capture");
+        };
+        cap(cudaMemcpyAsync(G.d_stage.p, G.h_stage, bytes, cudaMemcpyHostToDevice, st));
+        cap(cudaMemsetAsync(G.d_rb.p, 0, ((size_t)K + 1) * sizeof(unsigned long long), st));
+        if (G.save_n) cap(gf::launch_slot_copy(G.M, G.d_s.p + G.save_off, G.save_n, st));
+        std::vector<int> q(nlev + 1, G.par);
+        G.ncall = 0;
+        if (crc == GF_OK) crc = sg_fill_level(G, G.lo, t, q.data(), -1);
+        if (crc == GF_OK) crc = sg_level(G, G.lo, t, dt, q.data());
+        cap(cudaMemcpyAsync(G.h_rb, G.d_rb.p, ((size_t)K + 1) * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, st));
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+        if (crc) {
+            if (graph) cudaGraphDestroy(graph);
+            return crc;
+        }
+        GK(G, ee);
+        /* the same launch sequence as the last capture: update in place */
+        bool updated = false;
+        if (G.exec) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(G.exec, graph, &info) == cudaSuccess;
+            if (!updated) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(G.exec);
+                G.exec = nullptr;
+            }
+        }
+        cudaError_t ei = cudaSuccess;
+        if (!updated) ei = cudaGraphInstantiate(&G.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        GK(G, ei);
+        G.graph_ok = true;
+        G.graph_bytes = bytes;
+    }
+    GK(G, cudaGraphLaunch(G.exec, st));
     return GF_OK;
 }
 
@@ -2908,6 +2950,16 @@ struct SubBatch {
     std::vector<gf_forest*> fs;
     std::vector<std::unique_ptr<SubGroup>> groups;
     long long regrids = 0, cell_updates = 0, steps_launched = 0;
+    /* the step's end for every member in one launch: restore copies of
+     * retaken steps, unify copies of accepted ones */
+    DArr<gf_slot_task> d_fin;
+    gf_slot_task* h_fin = nullptr; /* pinned */
+    size_t h_fin_cap = 0;
+    ~SubBatch()
+    {
+        d_fin.release();
+        if (h_fin) cudaFreeHost(h_fin);
+    }
 };
 
 int sb_add(SubBatch& B, gf_forest* f, double t_final, int nout, double initial_dt, double desired_cfl,
@@ -3001,6 +3053,17 @@ int sb_iterate(SubBatch& B, int* live)
                 if (same) std::swap(g, old);
                 break;
             }
+    /* a rebuilt group takes over the graph of the group it replaces, which
+     * is updated in place when the launch sequence is unchanged */
+    for (auto& g : next)
+        if (!g->built && !g->exec)
+            for (auto& old : B.groups)
+                if (old && old->exec && old->M == g->M && old->lo == g->lo && old->hi == g->hi &&
+                    old->maux == g->maux && old->par == g->par && old->exact == g->exact) {
+                    g->exec = old->exec;
+                    old->exec = nullptr;
+                    break;
+                }
     B.groups.swap(next);
     for (auto& g : B.groups) {
         if (!g->built) {
@@ -3020,7 +3083,12 @@ int sb_iterate(SubBatch& B, int* live)
     cudaStream_t st = gf::ctx_stream(B.ctx);
     const cudaError_t se = cudaStreamSynchronize(st);
     if (se != cudaSuccess) return gf::ctx_cuda_fail(B.ctx, se, "subcycled group step");
-    /* take in each member's step: accept or retake, next dt, regrid when due */
+    /* take in each member's step: accept or retake, next dt; the restore /
+     * unify copies of all members in one launch, then the due regrids
+     * together (one tag launch and one transfer launch per patch size) */
+    std::vector<gf_slot_task> fin[3]; /* per patch size 8, 16, 32 */
+    std::vector<gf_forest*> due;
+    std::vector<double> due_t;
     for (auto& g : B.groups) {
         const int K = (int)g->mem.size();
         if ((int)g->h_rb[0]) return gf::ctx_fail(B.ctx, GF_ERR_DEVICE, "a patch-update copy wait timed out");
@@ -3033,14 +3101,16 @@ int sb_iterate(SubBatch& B, int* live)
             for (int l = f->sub_lo; l <= f->sub_hi; ++l)
                 cu += (long long)f->lev_n[l] * f->M * f->M << (l - f->sub_lo);
             f->st.max_cfl_seen = std::max(f->st.max_cfl_seen, cfl);
-            int rc;
-            if (cfl > r.max_cfl) {
-                if ((rc = sub_finish(f, false))) return rc;
+            const bool accept = !(cfl > r.max_cfl);
+            const int kind = accept ? 2 : 1; /* sub_finish's copy lists */
+            std::vector<gf_slot_task>& fl = fin[f->M == 8 ? 0 : f->M == 16 ? 1 : 2];
+            const int o = f->ss_copy_off[kind][f->par];
+            fl.insert(fl.end(), f->h_ss.begin() + o, f->h_ss.begin() + o + f->ss_copy_n[kind]);
+            if (!accept) {
                 r.dt_minlevel = r.dt_minlevel * r.desired_cfl / cfl;
                 f->st.rejects++;
                 continue;
             }
-            if ((rc = sub_finish(f, true))) return rc;
             f->st.steps++;
             f->st.cell_updates += cu;
             B.cell_updates += cu;
@@ -3050,12 +3120,44 @@ int sb_iterate(SubBatch& B, int* live)
             f->st.t = r.t_curr;
             f->st.dt = r.dt_minlevel;
             if (f->o.regrid_interval > 0 && f->st.steps % f->o.regrid_interval == 0) {
-                bool changed = false;
-                if ((rc = regrid(f, r.t_curr, &changed))) return rc;
-                B.regrids++;
-                f->st.npatch_max = std::max(f->st.npatch_max, (int)f->leaves.size());
+                due.push_back(f);
+                due_t.push_back(r.t_curr);
             }
         }
+    }
+    const size_t nfin = fin[0].size() + fin[1].size() + fin[2].size();
+    if (nfin) {
+        if (B.h_fin_cap < nfin) {
+            if (B.h_fin) cudaFreeHost(B.h_fin);
+            B.h_fin = nullptr;
+            B.h_fin_cap = 0;
+            const cudaError_t e =
+                cudaMallocHost(reinterpret_cast<void**>(&B.h_fin), (nfin + nfin / 2) * sizeof(gf_slot_task));
+            if (e != cudaSuccess) return gf::ctx_cuda_fail(B.ctx, e, "subcycled step end");
+            B.h_fin_cap = nfin + nfin / 2;
+        }
+        size_t off[3], o = 0;
+        for (int c = 0; c < 3; ++c) {
+            off[c] = o;
+            if (!fin[c].empty()) std::memcpy(B.h_fin + o, fin[c].data(), fin[c].size() * sizeof(gf_slot_task));
+            o += fin[c].size();
+        }
+        cudaError_t e = B.d_fin.reserve(nfin);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(B.d_fin.p, B.h_fin, nfin * sizeof(gf_slot_task), cudaMemcpyHostToDevice, st);
+        static const int ms[3] = {8, 16, 32};
+        for (int c = 0; c < 3 && e == cudaSuccess; ++c)
+            if (!fin[c].empty()) e = gf::launch_slot_copy(ms[c], B.d_fin.p + off[c], (int)fin[c].size(), st);
+        if (e != cudaSuccess) return gf::ctx_cuda_fail(B.ctx, e, "subcycled step end");
+        /* the pinned list is reused next iteration: its copy must have landed */
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return gf::ctx_cuda_fail(B.ctx, e, "subcycled step end");
+    }
+    if (!due.empty()) {
+        int rc = regrid_many(B.ctx, due, due_t);
+        if (rc) return rc;
+        B.regrids += (long long)due.size();
+        for (gf_forest* f : due) f->st.npatch_max = std::max(f->st.npatch_max, (int)f->leaves.size());
     }
     int n = 0;
     for (gf_forest* f : B.fs) n += f->sr.active && !f->sr.cancel;
