@@ -943,8 +943,8 @@ def forest_leg(args, dev=0):
         "forests": nsub, "value": work / bat_s, "unit": METRIC, "seconds": bat_s,
         "one_by_one": {"value": work / seq_s, "seconds": seq_s},
         "speedup_vs_one_by_one": seq_s / bat_s, "batch_equals_one_by_one": bool(same),
-        "note": "gf_forest_batch_run of subcycled forests: each coarse step the forest's own graph "
-                "on a stream of a pool, the host loop waiting on no forest"}
+        "note": "gf_forest_batch_run of subcycled forests: forests spanning the same levels step "
+                "in shared launches, each group's coarse step a CUDA graph"}
     rp = regrid_parity(ctx, c, steps, resync=True)
     fr = regrid_parity(ctx, c, steps, resync=False, exact=True)
     ctx.close()

@@ -446,11 +446,13 @@ int gf_forest_upload(gf_forest* f, const double* q);
  * every forest, CFL reduction) is captured as a CUDA graph per epoch and
  * replayed; a forest whose regrid is due waits on the device until the
  * host regrids it, after which the epoch is rebuilt and captured again.
- * Subcycled forests (subcycle = 1) run side by side instead: each coarse
- * step is that forest's captured graph, launched on one of a pool of
- * streams, and the host drives every forest's loop without waiting on the
- * device, so many forests' steps overlap on the GPU. Each forest's result
- * equals its own gf_forest_run. */
+ * Subcycled forests (subcycle = 1) share launches in groups instead: the
+ * forests whose leaves span the same levels take their coarse steps
+ * together, each launch of the subcycled schedule carrying every member's
+ * tasks (each member its own level dts, boundary times and CFL), one CUDA
+ * graph per group step, each member under its own outstyle-1 control
+ * (fclaw2d_advance_all_levels' schedule, fc2d_geoclaw_run.c:229-395). Each
+ * forest's result equals its own gf_forest_run. */
 typedef struct gf_forest_batch_stats {
     long long rounds;        /* graph replays                               */
     long long epochs;        /* captures (membership or tables changed)     */
@@ -706,9 +708,9 @@ double gf_server_clock(const gf_server* s);
  * the budget, until gf_fserver_release; read it meanwhile through
  * gf_fserver_forest (or gf_fserver_download while the loop thread runs).
  * The caller keeps fields and topo alive until the request leaves QUEUED.
- * Subcycled forests (opts.subcycle = 1) run in lane 3, side by side as in
- * gf_forest_batch_run (each coarse step the forest's own graph on a stream
- * of a pool). */
+ * Subcycled forests (opts.subcycle = 1) run in lane 3, side by side: each
+ * coarse step the forest's own graph on a stream of a pool, so the loop
+ * never waits on the device. */
 typedef struct gf_fserver gf_fserver;
 
 typedef struct gf_forest_request {
