@@ -387,16 +387,21 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
     GF_CK(c, gf::launch_aos_to_soa(c->q_aos.p, c->q_soa.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
     GF_CK(c, gf::launch_aos_to_soa(c->aux_aos.p, c->aux_soa.p, npatch, (int)S, maux, maux * S,
                                    maux * S, c->stream));
-    double mc = 0.0;
-    rc = run_batch(c, mx, c->work.p, npatch, maux, dt, c->cfl.p, c->d_status, &mc,
-                   small_batch_goal(mx, npatch));
+    /* update, layout back, results and status out: one wait at the end */
+    rc = enqueue_batch(c, mx, c->work.p, npatch, maux, dt, c->cfl.p, c->d_status,
+                       small_batch_goal(mx, npatch));
     if (rc) return rc;
     GF_CK(c, gf::launch_soa_to_aos(c->q_soa.p, c->q_aos.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
     GF_CK(c, cudaMemcpyAsync(hq, c->q_aos.p, sizeof(double) * qn, cudaMemcpyDeviceToHost, c->stream));
     if (cfl)
         GF_CK(c, cudaMemcpyAsync(c->h_cfl.p, c->cfl.p, sizeof(double) * npatch,
                                  cudaMemcpyDeviceToHost, c->stream));
+    GF_CK(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                             c->stream));
     GF_CK(c, cudaStreamSynchronize(c->stream));
+    if (c->h_status->err) return fail(c, GF_ERR_DEVICE, "patch kernel: bounded wait expired");
+    double mc;
+    std::memcpy(&mc, &c->h_status->gmax, sizeof mc);
     gf::host_parallel_for(npatch, (long)(qn * sizeof(double)), [&](long lo, long hi) {
         for (long k = lo; k < hi; ++k)
             std::memcpy(q[k], hq + (size_t)k * 3 * S, sizeof(double) * 3 * S);
