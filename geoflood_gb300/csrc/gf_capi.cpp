@@ -89,10 +89,11 @@ struct gf_ctx {
     bool exact = false; /* run the contraction-free build */
     bool mixed = true;  /* batched forms: one persistent launch for all patch sizes */
     /* scratch for the host-buffer drop-in paths */
-    DevBuf<double> q_aos, q_soa, aux_aos, aux_soa, cfl;
-    DevBuf<gf_patch_work> work;
-    HostBuf<double> h_stage, h_cfl;
-    HostBuf<gf_patch_work> h_work;
+    DevBuf<double> q_soa, aux_soa, cfl;
+    HostBuf<double> h_cfl;
+    /* a host batch's traffic in one block each side (io_layout) */
+    DevBuf<char> io_dev;
+    HostBuf<char> io_host;
     /* coarse/fine transfers and tags */
     DevBuf<gf_xfer_task> xfer;
     DevBuf<gf_tinterp_task> tint;
@@ -276,15 +277,12 @@ void gf_ctx_destroy(gf_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    c->q_aos.release();
     c->q_soa.release();
-    c->aux_aos.release();
     c->aux_soa.release();
     c->cfl.release();
-    c->work.release();
-    c->h_stage.release();
     c->h_cfl.release();
-    c->h_work.release();
+    c->io_dev.release();
+    c->io_host.release();
     c->xfer.release();
     c->tint.release();
     c->tagt.release();
@@ -348,20 +346,31 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
     GF_CK(c, cudaSetDevice(c->device));
     const long S = cells_of(mx, my);
     const size_t qn = (size_t)npatch * 3 * S, an = (size_t)npatch * maux * S;
-    GF_CK(c, c->q_aos.reserve(qn));
     GF_CK(c, c->q_soa.reserve(qn));
-    GF_CK(c, c->aux_aos.reserve(an));
     GF_CK(c, c->aux_soa.reserve(an));
     GF_CK(c, c->cfl.reserve(npatch));
-    GF_CK(c, c->work.reserve(npatch));
-    GF_CK(c, c->h_stage.reserve(qn + an));
-    GF_CK(c, c->h_work.reserve(npatch));
     GF_CK(c, c->h_cfl.reserve(npatch));
+    /* One block each side, [aux | work | status | q]: one copy carries the
+     * batch in (the status zeroed on the host) and one brings the status and
+     * q back. */
+    auto a256 = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t o_work = a256(an * sizeof(double));
+    const size_t o_status = o_work + a256((size_t)npatch * sizeof(gf_patch_work));
+    const size_t o_q = o_status + a256(sizeof(DevStatus));
+    const size_t io_bytes = o_q + qn * sizeof(double);
+    GF_CK(c, c->io_dev.reserve(io_bytes));
+    GF_CK(c, c->io_host.reserve(io_bytes));
+    char* hio = c->io_host.p;
+    char* dio = c->io_dev.p;
+    double* hq = reinterpret_cast<double*>(hio + o_q);
+    double* ha = reinterpret_cast<double*>(hio);
+    gf_patch_work* hw = reinterpret_cast<gf_patch_work*>(hio + o_work);
+    DevStatus* hs = reinterpret_cast<DevStatus*>(hio + o_status);
+    DevStatus* d_status = reinterpret_cast<DevStatus*>(dio + o_status);
+    const gf_patch_work* d_work = reinterpret_cast<const gf_patch_work*>(dio + o_work);
 
-    /* Gather the patches into one pinned block, one copy in each direction;
-     * large batches gather on several host threads. */
-    double* hq = c->h_stage.p;
-    double* ha = c->h_stage.p + qn;
+    /* Gather the patches into the pinned block; large batches gather on
+     * several host threads. */
     for (int k = 0; k < npatch; ++k)
         if (!q[k] || !aux[k]) return fail(c, GF_ERR_ARG, "null patch pointer");
     gf::host_parallel_for(npatch, (long)((qn + an) * sizeof(double)), [&](long lo, long hi) {
@@ -378,30 +387,32 @@ int gf_patch_update_batch(gf_ctx* c, int npatch, int mx, int my, int mbc, int me
         w.dy = dy[k];
         w.phys = 0;
         w.group = 0;
-        c->h_work.p[k] = w;
+        hw[k] = w;
     }
-    GF_CK(c, cudaMemcpyAsync(c->q_aos.p, hq, sizeof(double) * qn, cudaMemcpyHostToDevice, c->stream));
-    GF_CK(c, cudaMemcpyAsync(c->aux_aos.p, ha, sizeof(double) * an, cudaMemcpyHostToDevice, c->stream));
-    GF_CK(c, cudaMemcpyAsync(c->work.p, c->h_work.p, sizeof(gf_patch_work) * npatch,
-                             cudaMemcpyHostToDevice, c->stream));
-    GF_CK(c, gf::launch_aos_to_soa(c->q_aos.p, c->q_soa.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
-    GF_CK(c, gf::launch_aos_to_soa(c->aux_aos.p, c->aux_soa.p, npatch, (int)S, maux, maux * S,
-                                   maux * S, c->stream));
+    std::memset(hs, 0, sizeof(DevStatus));
+    GF_CK(c, cudaMemcpyAsync(dio, hio, io_bytes, cudaMemcpyHostToDevice, c->stream));
+    GF_CK(c, gf::launch_aos_to_soa_pair(reinterpret_cast<const double*>(dio + o_q), c->q_soa.p, 3,
+                                        reinterpret_cast<const double*>(dio), c->aux_soa.p, maux, npatch,
+                                        (int)S, c->stream));
     /* update, layout back, results and status out: one wait at the end */
-    rc = enqueue_batch(c, mx, c->work.p, npatch, maux, dt, c->cfl.p, c->d_status,
-                       small_batch_goal(mx, npatch));
-    if (rc) return rc;
-    GF_CK(c, gf::launch_soa_to_aos(c->q_soa.p, c->q_aos.p, npatch, (int)S, 3, 3 * S, 3 * S, c->stream));
-    GF_CK(c, cudaMemcpyAsync(hq, c->q_aos.p, sizeof(double) * qn, cudaMemcpyDeviceToHost, c->stream));
+    if (c->exact)
+        GF_CK(c, gf::launch_patch_update_exact(mx, d_work, npatch, c->d_phys, dt, nullptr, nullptr, maux,
+                                               c->cfl.p, &d_status->gmax, &d_status->err, c->stream));
+    else
+        GF_CK(c, gf::launch_patch_update(mx, d_work, npatch, c->d_phys, dt, nullptr, nullptr, maux,
+                                         c->cfl.p, &d_status->gmax, &d_status->err, c->stream, 0,
+                                         small_batch_goal(mx, npatch)));
+    GF_CK(c, gf::launch_soa_to_aos(c->q_soa.p, reinterpret_cast<double*>(dio + o_q), npatch, (int)S, 3,
+                                   3 * S, 3 * S, c->stream));
+    GF_CK(c, cudaMemcpyAsync(hio + o_status, dio + o_status, io_bytes - o_status, cudaMemcpyDeviceToHost,
+                             c->stream));
     if (cfl)
         GF_CK(c, cudaMemcpyAsync(c->h_cfl.p, c->cfl.p, sizeof(double) * npatch,
                                  cudaMemcpyDeviceToHost, c->stream));
-    GF_CK(c, cudaMemcpyAsync(c->h_status, c->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
-                             c->stream));
     GF_CK(c, cudaStreamSynchronize(c->stream));
-    if (c->h_status->err) return fail(c, GF_ERR_DEVICE, "patch kernel: bounded wait expired");
+    if (hs->err) return fail(c, GF_ERR_DEVICE, "patch kernel: bounded wait expired");
     double mc;
-    std::memcpy(&mc, &c->h_status->gmax, sizeof mc);
+    std::memcpy(&mc, &hs->gmax, sizeof mc);
     gf::host_parallel_for(npatch, (long)(qn * sizeof(double)), [&](long lo, long hi) {
         for (long k = lo; k < hi; ++k)
             std::memcpy(q[k], hq + (size_t)k * 3 * S, sizeof(double) * 3 * S);

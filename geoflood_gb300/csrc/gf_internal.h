@@ -93,6 +93,10 @@ cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int n
                               long src_stride, long dst_stride, cudaStream_t st);
 cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int ncell, int nf,
                               long src_stride, long dst_stride, cudaStream_t st);
+/* both of a host batch's layouts (q with nfa fields, aux with nfb) in one
+ * launch; each set is npatch contiguous blocks of nf * ncell doubles */
+cudaError_t launch_aos_to_soa_pair(const double* sa, double* da, int nfa, const double* sb, double* db,
+                                   int nfb, long npatch, int ncell, cudaStream_t st);
 
 /* Served scenarios: device-side time-step control around a round. */
 cudaError_t launch_served_prepare(gf_group_state* gs, gf_ghost_block* blocks, double* gdt, int* gpar,

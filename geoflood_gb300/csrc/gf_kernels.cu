@@ -279,6 +279,35 @@ cudaError_t launch_aos_to_soa(const double* src, double* dst, long npatch, int n
     return cudaGetLastError();
 }
 
+/* Two layouts in one launch (a host batch's q and aux): element e of the
+ * first npatch * ncell is a cell of set a, the rest cells of set b. */
+__global__ void aos_to_soa_pair_kernel(const double* __restrict__ sa, double* __restrict__ da, int nfa,
+                                       const double* __restrict__ sb, double* __restrict__ db, int nfb,
+                                       long npatch, int ncell)
+{
+    const long per = npatch * (long)ncell;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < 2 * per;
+         e += (long)gridDim.x * blockDim.x) {
+        const bool second = e >= per;
+        const long ee = second ? e - per : e;
+        const int nf = second ? nfb : nfa;
+        const long p = ee / ncell;
+        const int k = (int)(ee % ncell);
+        const double* s = (second ? sb : sa) + p * nf * (long)ncell + (long)k * nf;
+        double* d = (second ? db : da) + p * nf * (long)ncell + k;
+        for (int f = 0; f < nf; ++f) d[(long)f * ncell] = s[f];
+    }
+}
+
+cudaError_t launch_aos_to_soa_pair(const double* sa, double* da, int nfa, const double* sb, double* db,
+                                   int nfb, long npatch, int ncell, cudaStream_t st)
+{
+    const long total = 2 * npatch * (long)ncell;
+    if (total == 0) return cudaSuccess;
+    aos_to_soa_pair_kernel<<<conv_grid(total), 256, 0, st>>>(sa, da, nfa, sb, db, nfb, npatch, ncell);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_soa_to_aos(const double* src, double* dst, long npatch, int ncell, int nf,
                               long src_stride, long dst_stride, cudaStream_t st)
 {
