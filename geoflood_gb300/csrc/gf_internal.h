@@ -60,7 +60,7 @@ int tile_count(int m);
 int tile_shape(int m, int v, int* nt, int* rb, int* k = nullptr);
 int tile_get(int m, int goal);
 /* 1 when npatch patches of size m on the latency tile (each over its
- * cluster of CTAs) fit on the device's SMs at once, else 0 */
+ * cluster of CTAs) are all resident at once on the device, else 0 */
 int latency_goal_fits(int m, long npatch);
 int tile_set(int m, int goal, int v);
 cudaError_t launch_patch_update_tile(int m, int v, const gf_patch_work* work, int nwork,

@@ -10,6 +10,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "gf_internal.h"
 #include "gf_patch_update.cuh"
 
@@ -49,6 +51,25 @@ static cudaError_t launch_window(const gf_patch_work* work, int nwork, const gf_
     return cudaGetLastError();
 }
 
+/* Patches one launch of the window kernel runs at once: the clusters of K
+ * CTAs the device holds resident together (placement inside a GPC counted). */
+template <int M, int NT, int RB, int K>
+static int window_slots()
+{
+    using L = Smem<M, RB, false>;
+    auto kern = patch_update_window_kernel<M, NT, RB, K, false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES) !=
+        cudaSuccess)
+        return 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(K * sm_count());
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = L::BYTES;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) return 0;
+    return n;
+}
+
 template <int M, int NT, int RB, int K>
 static int window_occupancy()
 {
@@ -83,14 +104,21 @@ static int occupancy_of()
     return n;
 }
 
+template <int M, int NT, int RB>
+static int tile_slots() { return occupancy_of<M, NT, RB>() * sm_count(); }
+
 struct Tile {
     int nt, rb, k; /* k > 1: the patch split over a cluster of k CTAs */
     UpdateFn fn;
     OccFn occ;
+    OccFn slots; /* patches resident at once in one launch */
 };
 
-#define GF_TILE(M, NT, RB) {NT, RB, 1, &launch_update<M, NT, RB, 1>, &occupancy_of<M, NT, RB>}
-#define GF_WTILE(M, NT, RB, K) {NT, RB, K, &launch_window<M, NT, RB, K>, &window_occupancy<M, NT, RB, K>}
+#define GF_TILE(M, NT, RB) \
+    {NT, RB, 1, &launch_update<M, NT, RB, 1>, &occupancy_of<M, NT, RB>, &tile_slots<M, NT, RB>}
+#define GF_WTILE(M, NT, RB, K)                                                                \
+    {NT, RB, K, &launch_window<M, NT, RB, K>, &window_occupancy<M, NT, RB, K>,                \
+     &window_slots<M, NT, RB, K>}
 static const Tile kTiles8[] = {GF_TILE(8, 64, 5), GF_TILE(8, 128, 10), GF_TILE(8, 128, 5),
                                GF_WTILE(8, 64, 5, 2), GF_WTILE(8, 64, 5, 4)};
 static const Tile kTiles16[] = {GF_TILE(16, 128, 6), GF_TILE(16, 256, 13), GF_TILE(16, 256, 9),
@@ -136,13 +164,27 @@ int tile_shape(int m, int v, int* nt, int* rb, int* k)
 
 int tile_get(int m, int goal) { return g_tile[goal != 0][mcls(m)]; }
 
+/* The latency tile pays for its split only while every patch of the launch
+ * is resident at once; past one wave the throughput tile finishes sooner. */
 int latency_goal_fits(int m, long npatch)
 {
     int n = 0;
     const Tile* t = tiles_of(m, &n);
     if (!t) return 0;
-    const int k = t[g_tile[1][mcls(m)]].k;
-    return npatch * k <= (long)sm_count() ? 1 : 0;
+    const int v = g_tile[1][mcls(m)];
+    static std::atomic<int> cache[64][3][GF_MAX_TILES] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || v >= GF_MAX_TILES)
+        return npatch * t[v].k <= (long)sm_count() ? 1 : 0;
+    std::atomic<int>& c = cache[dev][mcls(m)][v];
+    int slots = c.load(std::memory_order_relaxed);
+    if (!slots) {
+        slots = t[v].slots();
+        if (slots <= 0) slots = sm_count() / t[v].k;
+        if (slots <= 0) slots = 1;
+        c.store(slots, std::memory_order_relaxed);
+    }
+    return npatch <= (long)slots ? 1 : 0;
 }
 
 int tile_set(int m, int goal, int v)

@@ -89,6 +89,12 @@ struct Chunk {
 struct Lane {
     int idx = 0;
     cudaStream_t st = nullptr;
+    /* two more streams of the lane's priority: a round's patch sizes run as
+     * parallel branches of its graph (fork after the controllers' prepare,
+     * join before their finish) */
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+    int goal[3] = {0, 0, 0}; /* update tile goal per patch size of the epoch */
     std::vector<Scen*> members; /* group g of the epoch = members[g] */
     std::vector<Scen*> joining; /* admitted, enter at the next epoch */
     std::vector<Scen*> fin;     /* final download in flight */
@@ -513,6 +519,12 @@ int rebuild_epoch(gf_server* srv, Lane& L)
         }
     }
     SV_CK(srv, cudaMemcpyAsync(L.d_ep, L.h_ep, need, cudaMemcpyHostToDevice, L.st));
+    /* the smallest lane's step time is one patch's critical path: the
+     * latency tile, while its patches (split over their clusters) all run in
+     * one wave; decided here, outside the capture */
+    static const int ms[3] = {8, 16, 32};
+    for (int c = 0; c < 3; ++c)
+        L.goal[c] = (L.idx == 0 && srv->o.nlanes > 1 && npm[c] && gf::latency_goal_fits(ms[c], npm[c])) ? 1 : 0;
     return capture_round(srv, L);
 }
 
@@ -534,13 +546,13 @@ int enqueue_round(gf_server* srv, Lane& L)
     int n = 0;
     SV_CK(srv, gf::launch_served_prepare(gs, blk, gdt, gpar, rb + 1, hyt, hyu, nm, L.st));
     ++n;
-    for (int c = 0; c < 3; ++c)
-        if (L.npm[c]) {
-            SV_CK(srv, gf::launch_ghost_fill(ms[c], blk, reinterpret_cast<const gf_ghost_ref*>(d + L.off_ref[c]),
-                                             L.npm[c], srv->d_phys, L.st));
-            ++n;
-        }
     if (srv->o.mixed_update && L.idx > 0) {
+        for (int c = 0; c < 3; ++c)
+            if (L.npm[c]) {
+                SV_CK(srv, gf::launch_ghost_fill(ms[c], blk, reinterpret_cast<const gf_ghost_ref*>(d + L.off_ref[c]),
+                                                 L.npm[c], srv->d_phys, L.st));
+                ++n;
+            }
         /* later lanes: every size in one persistent launch (a device cursor
          * over the contiguous work list), on the lane's capped grid */
         const int nw[3] = {L.npm[2], L.npm[1], L.npm[0]};
@@ -552,18 +564,35 @@ int enqueue_round(gf_server* srv, Lane& L)
             ++n;
         }
     } else {
-        for (int c = 0; c < 3; ++c)
+        /* Each patch size's ghost fill and update form one branch; the sizes
+         * touch disjoint patches and meet only in the atomic maxima, so the
+         * branches run concurrently with the same results. */
+        int nb = 0;
+        cudaStream_t bst[3];
+        for (int c = 2; c >= 0; --c)
             if (L.npm[c]) {
-                /* the smallest lane's step time is one patch's critical path: the
-                 * latency tile, while its patches (split over their clusters)
-                 * fit on the SMs at once */
-                const int goal =
-                    (L.idx == 0 && srv->o.nlanes > 1 && gf::latency_goal_fits(ms[c], L.npm[c])) ? 1 : 0;
+                bst[nb] = nb == 0 ? L.st : L.side[nb - 1];
+                ++nb;
+            }
+        if (nb > 1) {
+            SV_CK(srv, cudaEventRecord(L.ev_fork, L.st));
+            for (int b = 1; b < nb; ++b) SV_CK(srv, cudaStreamWaitEvent(bst[b], L.ev_fork, 0));
+        }
+        int b = 0;
+        for (int c = 2; c >= 0; --c)
+            if (L.npm[c]) {
+                cudaStream_t st = bst[b++];
+                SV_CK(srv, gf::launch_ghost_fill(ms[c], blk, reinterpret_cast<const gf_ghost_ref*>(d + L.off_ref[c]),
+                                                 L.npm[c], srv->d_phys, st));
                 SV_CK(srv, gf::launch_patch_update(ms[c], reinterpret_cast<const gf_patch_work*>(d + L.off_work[c]),
                                                    L.npm[c], srv->d_phys, 0.0, gdt, gpar, kLaneMaux, nullptr,
-                                                   rb + 1, err, L.st, srv->cta_cap[L.idx][c], goal));
-                ++n;
+                                                   rb + 1, err, st, srv->cta_cap[L.idx][c], L.goal[c]));
+                n += 2;
             }
+        for (int j = 1; j < nb; ++j) {
+            SV_CK(srv, cudaEventRecord(L.ev_join[j - 1], bst[j]));
+            SV_CK(srv, cudaStreamWaitEvent(L.st, L.ev_join[j - 1], 0));
+        }
     }
     SV_CK(srv, gf::launch_served_finish(gs, gdt, rb + 1, err, nm, L.st));
     ++n;
@@ -768,7 +797,10 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
         for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
             e = cudaEventCreate(&L.ev_start[j]);
             if (e == cudaSuccess) e = cudaEventCreate(&L.ev_end[j]);
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&L.side[j], cudaStreamNonBlocking, prio);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.ev_join[j], cudaEventDisableTiming);
         }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.ev_fork, cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->d_phys, kMaxSlots * sizeof(gf_phys));
     if (e == cudaSuccess) {
@@ -834,7 +866,10 @@ void gf_server_destroy(gf_server* s)
             if (L.h_rb[j]) cudaFreeHost(L.h_rb[j]);
             if (L.ev_start[j]) cudaEventDestroy(L.ev_start[j]);
             if (L.ev_end[j]) cudaEventDestroy(L.ev_end[j]);
+            if (L.ev_join[j]) cudaEventDestroy(L.ev_join[j]);
+            if (L.side[j]) cudaStreamDestroy(L.side[j]);
         }
+        if (L.ev_fork) cudaEventDestroy(L.ev_fork);
         drop_graph(L);
         if (L.st) cudaStreamDestroy(L.st);
     }

@@ -816,9 +816,10 @@ int gf_autotune(gf_ctx* ctx, int reps, gf_tile_result* out /* [3]: mx 8, 16, 32 
 int gf_tile_count(int mx);
 /* Current choice (goal 0 throughput, 1 latency) or a manual one. Levels,
  * forests and batched rounds take the throughput choice; a batch through
- * gf_patch_update / gf_patch_update_batch / gf_step_buffer_update takes the
- * latency choice when its patches times that tile's cluster size fit on
- * the GPU's SMs, and the served form's smallest lane takes it always. */
+ * gf_patch_update / gf_patch_update_batch / gf_step_buffer_update, and a
+ * step of the served form's smallest lane, take the latency choice when
+ * all their patches run in one wave of it (no more patches than the
+ * clusters of that tile the GPU holds resident at once). */
 int gf_tile_get(int mx, int goal);
 int gf_tile_set(int mx, int goal, int variant);
 
