@@ -289,7 +289,7 @@ def served_stream(args):
 
     lanes = tuple(int(float(v)) for v in args.served_lanes.split(",") if v.strip())
     srv = gf.Server(device=dev, reserve_sms=args.served_reserve_sms, lanes=lanes,
-                    cull_dry=not args.served_no_cull)
+                    cull_dry=not args.served_no_cull, split_sizes=not args.served_no_split)
     srv.start()
 
     # -- calibration: a saturated batch; throughput over a bounded window
@@ -319,7 +319,8 @@ def served_stream(args):
     steps_per_sim_s = (sum(i["steps"] for i in cal_info) /
                        max(sum(i["t"] for i in cal_info), 1e-9))
     est_work = float(np.mean([cells[k] * params[k]["horizon"] * steps_per_sim_s for k in range(n)]))
-    rate = 0.8 * cap / est_work
+    rate = 0.8 * cap / est_work if args.served_rate is None else float(args.served_rate)
+    load = rate * est_work / cap
     gaps = np.random.default_rng(SERVED_SEED + 7).exponential(1.0 / rate, n)
     arrivals = np.cumsum(gaps) - gaps[0]
     # size-stratified sample for the isolated re-runs
@@ -466,7 +467,7 @@ def served_stream(args):
         "capacity": {"value": cap, "unit": METRIC, "scenarios": ncal, "window_s": t_now - t0,
                      "note": "saturated batch, until half of it had finished or the window "
                              "closed"},
-        "arrival_rate_per_s": rate, "offered_load": 0.8, "late_submissions": late,
+        "arrival_rate_per_s": rate, "offered_load": load, "late_submissions": late,
         "stream_seconds": t_end - t_start, "cell_updates": work,
         "launches": st1["launches"] - st0["launches"], "rounds": st1["rounds"] - st0["rounds"],
         "peak_device_bytes": st1["bytes_peak"],
@@ -1414,6 +1415,10 @@ def main():
     ap.add_argument("--served-cal-seconds", type=float, default=8.0)
     ap.add_argument("--served-sample", type=int, default=6,
                     help="scenarios re-run alone for the slowdown (size-stratified)")
+    ap.add_argument("--served-rate", type=float, default=None,
+                    help="served stream: arrivals per second (default: 80 %% of the measured capacity)")
+    ap.add_argument("--served-no-split", action="store_true",
+                    help="served stream: one round queue per lane (patch sizes as graph branches)")
     ap.add_argument("--served-no-cull", action="store_true",
                     help="update every patch of every served scenario every step")
     ap.add_argument("--served-low-load", action="store_true",

@@ -90,7 +90,7 @@ class gf_server_opts(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("nlanes", C.c_int),
                 ("lane_cells", C.c_longlong * GF_SERVER_MAX_LANES), ("priority", C.c_int),
                 ("backfill", C.c_int), ("reserve_sms", C.c_int), ("mixed_update", C.c_int),
-                ("cull_dry", C.c_int)]
+                ("cull_dry", C.c_int), ("split_sizes", C.c_int)]
 
 
 class gf_scenario_info(C.Structure):

@@ -66,6 +66,7 @@ struct Scen {
     gf_scenario_info info{};
     gf_group_state gst{}; /* host copy of the device controller */
     int lane = -1, slot = -1;
+    int queue = -1; /* the round queue: lane x patch size */
     int np = 0;
     long S = 0;          /* cells per patch incl. halo */
     long long cells = 0; /* interior cells */
@@ -86,8 +87,12 @@ struct Chunk {
     int rounds = 0;
 };
 
+/* One queue of shared rounds: the scenarios of one size lane and one patch
+ * size (all sizes of a lane when its update is the one-launch form). Queues
+ * step independently, so a small scenario's round never waits for a larger
+ * patch size's update in the same lane. */
 struct Lane {
-    int idx = 0;
+    int idx = 0; /* the size lane: stream priority, tile goal, grid caps */
     cudaStream_t st = nullptr;
     /* two more streams of the lane's priority: a round's patch sizes run as
      * parallel branches of its graph (fork after the controllers' prepare,
@@ -131,7 +136,8 @@ struct gf_server {
     long long next_id = 1;
     std::map<long long, Scen*> all;
     std::deque<Scen*> queue;
-    Lane lanes[GF_SERVER_MAX_LANES];
+    Lane lanes[GF_SERVER_MAX_LANES * 3]; /* queue lane * 3 + size class */
+    int nqueues() const { return o.nlanes * 3; }
     gf_phys* d_phys = nullptr;
     std::vector<gf_phys> h_phys;
     std::vector<int> free_slots;
@@ -208,6 +214,12 @@ int lane_of(const gf_server* s, long long cells)
     return s->o.nlanes - 1;
 }
 
+int queue_of(const gf_server* s, int lane, int mx)
+{
+    const bool one_queue = !s->o.split_sizes || (s->o.mixed_update && lane > 0);
+    return lane * 3 + (one_queue ? 0 : mclass(mx));
+}
+
 void sync_info(Scen* s)
 {
     s->info.t = s->gst.t_curr;
@@ -246,7 +258,7 @@ void end_scenario(gf_server* srv, Scen* s, int state)
 
 int admit(gf_server* srv, Scen* s)
 {
-    Lane& L = srv->lanes[s->lane];
+    Lane& L = srv->lanes[s->queue];
     const gf_scenario& sc = s->sc;
     const int np = s->np;
     const long S = s->S;
@@ -682,7 +694,7 @@ int pump_locked(gf_server* srv, int* busy)
 {
     if (srv->broken) return GF_ERR_STATE;
     SV_CK(srv, cudaSetDevice(srv->device));
-    for (int k = 0; k < srv->o.nlanes; ++k) {
+    for (int k = 0; k < srv->nqueues(); ++k) {
         Lane& L = srv->lanes[k];
         for (size_t i = 0; i < L.fin.size();) {
             Scen* s = L.fin[i];
@@ -704,7 +716,7 @@ int pump_locked(gf_server* srv, int* busy)
     }
     int rc = admit_queued(srv);
     if (rc) return rc;
-    for (int k = 0; k < srv->o.nlanes; ++k) {
+    for (int k = 0; k < srv->nqueues(); ++k) {
         Lane& L = srv->lanes[k];
         if (lane_needs_epoch(L)) {
             if (!L.inflight.empty()) continue; /* drain first */
@@ -718,7 +730,7 @@ int pump_locked(gf_server* srv, int* busy)
         }
     }
     int b = !srv->queue.empty();
-    for (int k = 0; k < srv->o.nlanes; ++k) {
+    for (int k = 0; k < srv->nqueues(); ++k) {
         const Lane& L = srv->lanes[k];
         b |= !L.inflight.empty() || !L.members.empty() || !L.joining.empty() || !L.fin.empty();
     }
@@ -765,6 +777,7 @@ void gf_server_opts_default(gf_server_opts* o)
     o->reserve_sms = 0; /* one CTA per patch: priority hands freed SMs to smaller lanes */
     o->mixed_update = 0; /* per-size launches: measured faster for served scenarios */
     o->cull_dry = 1;
+    o->split_sizes = 1;
 }
 
 int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
@@ -788,11 +801,11 @@ int gf_server_create(int device, const gf_server_opts* opts, gf_server** out)
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi); /* hi is the numerically lowest (greatest) */
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < o.nlanes && e == cudaSuccess; ++k) {
+    for (int k = 0; k < s->nqueues() && e == cudaSuccess; ++k) {
         Lane& L = s->lanes[k];
-        L.idx = k;
+        L.idx = k / 3;
         int prio = lo;
-        if (o.priority && o.nlanes > 1) prio = hi + (lo - hi) * k / (o.nlanes - 1);
+        if (o.priority && o.nlanes > 1) prio = hi + (lo - hi) * L.idx / (o.nlanes - 1);
         e = cudaStreamCreateWithPriority(&L.st, cudaStreamNonBlocking, prio);
         for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
             e = cudaEventCreate(&L.ev_start[j]);
@@ -848,7 +861,7 @@ void gf_server_destroy(gf_server* s)
     if (!s) return;
     gf_server_stop(s);
     cudaSetDevice(s->device);
-    for (int k = 0; k < GF_SERVER_MAX_LANES; ++k) {
+    for (int k = 0; k < GF_SERVER_MAX_LANES * 3; ++k) {
         Lane& L = s->lanes[k];
         if (L.st) cudaStreamSynchronize(L.st);
     }
@@ -858,7 +871,7 @@ void gf_server_destroy(gf_server* s)
         if (sc->ev_fin) cudaEventDestroy(sc->ev_fin);
         delete sc;
     }
-    for (int k = 0; k < GF_SERVER_MAX_LANES; ++k) {
+    for (int k = 0; k < GF_SERVER_MAX_LANES * 3; ++k) {
         Lane& L = s->lanes[k];
         if (L.d_ep) cudaFree(L.d_ep);
         if (L.h_ep) cudaFreeHost(L.h_ep);
@@ -904,6 +917,7 @@ int gf_server_submit(gf_server* s, const gf_scenario* sc, long long* id)
     x->cells = (long long)x->np * sc->mx * sc->mx;
     x->bytes = bytes;
     x->lane = lane_of(s, x->cells);
+    x->queue = queue_of(s, x->lane, sc->mx);
     x->info.state = GF_SCEN_QUEUED;
     x->info.lane = x->lane;
     x->info.t_submit = s->now();

@@ -106,7 +106,7 @@ class Server:
     def __init__(self, device: int = 0, hbm_budget: int | None = None, max_active: int = 256,
                  lanes: tuple = (100_000, 1_000_000), priority: bool = True,
                  backfill: bool = True, reserve_sms: int | None = None, mixed_update: bool = False,
-                 cull_dry: bool = True):
+                 cull_dry: bool = True, split_sizes: bool = True):
         self._lib = _lib.load()
         o = _lib.gf_server_opts()
         self._lib.gf_server_opts_default(C.byref(o))
@@ -122,6 +122,7 @@ class Server:
             o.reserve_sms = int(reserve_sms)
         o.mixed_update = int(bool(mixed_update))
         o.cull_dry = int(bool(cull_dry))
+        o.split_sizes = int(bool(split_sizes))
         h = C.c_void_p()
         rc = self._lib.gf_server_create(int(device), C.byref(o), C.byref(h))
         if rc != 0:

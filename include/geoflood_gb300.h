@@ -581,9 +581,10 @@ int gf_forest_flush_gauges(gf_forest* f);
 /* ------------------------------------------------- served scenarios */
 /* A request loop over flood scenarios (continuous batching). Each admitted
  * scenario keeps its state resident on the device; every batching round
- * steps all active scenarios of a size lane with shared launches (one ghost
- * fill and one patch update per mx present), each scenario with its own dt
- * and CFL slot. Time stepping per scenario follows ForestClaw's outstyle 1
+ * steps all active scenarios of one size lane and one patch size with
+ * shared launches (one ghost fill and one patch update), each scenario with
+ * its own dt and CFL slot; the queues of different patch sizes step
+ * independently, on streams of their lane's priority. Time stepping per scenario follows ForestClaw's outstyle 1
  * loop (src/fc2d_geoclaw/fc2d_geoclaw_run.c:190-395): dt clipped to hit each
  * output time with the 1% tolerance, a step whose CFL exceeds max_cfl is
  * retaken with dt * desired_cfl / cfl, otherwise the next dt is
@@ -646,6 +647,10 @@ typedef struct gf_server_opts {
                                no neighbour wet, no hydrograph side); interior results
                                are the same bits; a skipped patch's ghost cells keep
                                their last values. 0: every patch every step */
+    int split_sizes;        /* 1 (default): each lane keeps one round queue per patch
+                               size, stepping independently; 0: one queue per lane,
+                               its sizes as parallel branches of every round (same
+                               results either way) */
 } gf_server_opts;
 
 typedef struct gf_scenario_info {

@@ -60,14 +60,16 @@ def test_served_scenario_matches_oracle_run(mx, cells):
     assert abs(mass_g - mass_r) <= 1e-11 * mass_r
 
 
-@pytest.mark.parametrize("lanes", [(100_000, 1_000_000), ()])
-def test_result_is_the_same_alone_and_in_the_mix(lanes):
-    """Bitwise: a scenario's result does not depend on what shares its launches."""
+@pytest.mark.parametrize("lanes,split", [((100_000, 1_000_000), True), ((), True), ((), False)])
+def test_result_is_the_same_alone_and_in_the_mix(lanes, split):
+    """Bitwise: a scenario's result does not depend on what shares its launches,
+    with one round queue per patch size or the sizes as branches of one
+    queue's rounds."""
     a = scen(21, 1200, 8)
     b = scen(22, 4096, 16)
     c = scen(23, 9000, 32)
     alone, info_a = serve_alone(a, lanes=lanes)
-    with gf.Server(lanes=lanes) as srv:
+    with gf.Server(lanes=lanes, split_sizes=split) as srv:
         outs = {k: np.zeros_like(s.q) for k, s in (("a", a), ("b", b), ("c", c))}
         ids = {"b": srv.submit(b, outs["b"]), "a": srv.submit(a, outs["a"]),
                "c": srv.submit(c, outs["c"])}
