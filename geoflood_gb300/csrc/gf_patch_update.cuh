@@ -125,7 +125,12 @@ struct Smem {
     /* Odd strides (in doubles) spread a warp's accesses to face records and
      * accumulator rows over the shared-memory banks. */
     static constexpr int W_STRIDE = 13; /* s[3] + fw[3][3], 1 pad            */
-    static constexpr int O_STRIDE = 19; /* faddm faddp A B C D, 3 comps each, 1 pad */
+    /* limited-face records: exact build faddm faddp A B C D (3 comps each, 1
+     * pad); contracted build amdq apdq cq (local order) */
+    static constexpr int O_STRIDE = EXACT ? 19 : 9;
+    /* per-cell records of the contracted build: N (flux difference), U (up-going
+     * and Dn (down-going transverse parts), global order, one slot per face slot */
+    static constexpr int C_STRIDE = 9;
     static constexpr int MS = M + 1;    /* accumulator row stride            */
     static constexpr int PLANE = M * MS; /* one accumulator component        */
     static constexpr int OFF_H = 0;
@@ -140,7 +145,8 @@ struct Smem {
     static constexpr int OFF_ACC = OFF_RC + (EXACT ? 0 : G::S);     /* NACC x [3][M*M] */
     static constexpr int OFF_W = OFF_ACC + NACC * 3 * PLANE;
     static constexpr int OFF_O = OFF_W + RB * G::FA * W_STRIDE;
-    static constexpr int OFF_RED = OFF_O + RB * G::FB * O_STRIDE; /* 2*32 doubles */
+    static constexpr int OFF_C2 = OFF_O + RB * G::FB * O_STRIDE;   /* contracted only */
+    static constexpr int OFF_RED = OFF_C2 + (EXACT ? 0 : RB * G::FB * C_STRIDE); /* 2*32 doubles */
     static constexpr int OFF_BAR = OFF_RED + 64;                    /* 1 x u64     */
     /* integer region: class counts per band and face lists (u16) */
     static constexpr int OFF_INT = OFF_BAR + 2;
@@ -340,6 +346,11 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
     auto orec = [&](int ts, int face) -> const double* {
         return O + (ts * fb + (face - win.nb_lo)) * L::O_STRIDE;
     };
+    /* per-cell record of cell `cell` of band slice ts (contracted build) */
+    double* C2 = sm + L::OFF_C2;
+    auto crec = [&](int ts, int cell) -> double* {
+        return C2 + (ts * fb + (cell - win.nb_lo)) * L::C_STRIDE;
+    };
 
     /* Contracted build: DX, DY. Exact build: fm(i+1,j), fp(i,j), gm(i,j+1),
      * gp(i,j) of the reference, in sweep coordinates N_M, N_P (normal) and
@@ -389,47 +400,52 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
             } else {
                 /* each slice's part enters the accumulators on its own, slices in
                  * increasing order, so the sums do not depend on where the band
-                 * boundaries fall: every tile shape gives the same bits */
+                 * boundaries fall: every tile shape gives the same bits. A
+                 * slice's per-cell record holds its flux difference N and the
+                 * up-going (U) and down-going (Dn) transverse parts. */
                 if (t - 1 >= t0 && t - 1 <= t1) { /* slice below: up-going parts */
-                    const double* fr = orec(t - 1 - t0, n + 1);
-                    const double* fl = orec(t - 1 - t0, n);
-                    ACCT[a] += half_dtdn * (fr[9] + fl[15]);
-                    ACCT[a + MM] += half_dtdn * (fr[10] + fl[16]);
-                    ACCT[a + 2 * MM] += half_dtdn * (fr[11] + fl[17]);
+                    const double* r = crec(t - 1 - t0, n);
+                    ACCT[a] += half_dtdn * r[3];
+                    ACCT[a + MM] += half_dtdn * r[4];
+                    ACCT[a + 2 * MM] += half_dtdn * r[5];
                 }
                 if (t >= t0 && t <= t1) {
-                    const double* fr = orec(t - t0, n + 1);       /* face n+1 */
-                    const double* fl = orec(t - t0, n); /* face n   */
-                    ACCN[a] += fr[0] - fl[3];
-                    ACCN[a + MM] += fr[1] - fl[4];
-                    ACCN[a + 2 * MM] += fr[2] - fl[5];
-                    ACCT[a] += half_dtdn * ((fr[6] - fr[9]) + (fl[12] - fl[15]));
-                    ACCT[a + MM] += half_dtdn * ((fr[7] - fr[10]) + (fl[13] - fl[16]));
-                    ACCT[a + 2 * MM] += half_dtdn * ((fr[8] - fr[11]) + (fl[14] - fl[17]));
+                    const double* r = crec(t - t0, n);
+                    ACCN[a] += r[0];
+                    ACCN[a + MM] += r[1];
+                    ACCN[a + 2 * MM] += r[2];
+                    ACCT[a] += half_dtdn * (r[6] - r[3]);
+                    ACCT[a + MM] += half_dtdn * (r[7] - r[4]);
+                    ACCT[a + 2 * MM] += half_dtdn * (r[8] - r[5]);
                 }
                 if (t + 1 >= t0 && t + 1 <= t1) { /* slice above: down-going parts */
-                    const double* fr = orec(t + 1 - t0, n + 1);
-                    const double* fl = orec(t + 1 - t0, n);
-                    ACCT[a] -= half_dtdn * (fr[6] + fl[12]);
-                    ACCT[a + MM] -= half_dtdn * (fr[7] + fl[13]);
-                    ACCT[a + 2 * MM] -= half_dtdn * (fr[8] + fl[14]);
+                    const double* r = crec(t + 1 - t0, n);
+                    ACCT[a] -= half_dtdn * r[6];
+                    ACCT[a + MM] -= half_dtdn * r[7];
+                    ACCT[a + 2 * MM] -= half_dtdn * r[8];
                 }
             }
         }
     };
 
-    int prev_t0 = -1, prev_t1 = -1;
-    const int ts_end = win.ts_lo + win.nsl;
-    for (int t0 = win.ts_lo, band = 0; t0 < ts_end; t0 += win.rb, ++band) {
-        const int t1 = min(t0 + win.rb, ts_end) - 1; /* last slice of band */
-        const uint16_t* lA = la + band * win.rb * fa;
-        const uint16_t* lB = lb + band * win.rb * fb;
-        /* a2 / b2 both cells wet (list A by wave structure), a1 / b1 one
-         * wet, a0 / b0 both dry */
-        const int a2 = C(band, 0, 0) + C(band, 0, 1) + C(band, 0, 2), a1 = C(band, 0, 3), a0 = C(band, 0, 4);
-        const int b2 = C(band, 1, 0), b1 = C(band, 1, 3), b0 = C(band, 1, 4);
+    /* a2 / b2 both cells wet (list A by wave structure), a1 / b1 one wet,
+     * a0 / b0 both dry */
+    auto counts_a = [&](int band, int& a2, int& a1, int& a0) {
+        a2 = C(band, 0, 0) + C(band, 0, 1) + C(band, 0, 2);
+        a1 = C(band, 0, 3);
+        a0 = C(band, 0, 4);
+    };
+    auto counts_b = [&](int band, int& b2, int& b1, int& b0) {
+        b2 = C(band, 1, 0);
+        b1 = C(band, 1, 3);
+        b0 = C(band, 1, 4);
+    };
 
-        /* ---- stage A: normal Riemann solves, faces 0..M+2, by class ---- */
+    /* ---- stage A: normal Riemann solves, faces 0..M+2, by class ---- */
+    auto stage_a = [&](int t0, int band) {
+        const uint16_t* lA = la + band * win.rb * fa;
+        int a2, a1, a0;
+        counts_a(band, a2, a1, a0);
         for (int idx = threadIdx.x; idx < a2 + a1 + a0; idx += NT) {
             const int f = lA[idx];
             double* w = W + f * L::W_STRIDE;
@@ -453,10 +469,106 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 smax = d_max_nn<FAST>(smax, fabs(s[mw]));
             }
         }
-        if (prev_t0 >= 0) gather(prev_t0, prev_t1);
-        __syncthreads();
+    };
 
-        /* ---- stage B: limiter, 2nd-order terms, transverse split ---- */
+    /* Fluctuations from the unlimited f-waves (rpn2_geoclaw.f:359-376) and
+     * the limited second-order term cqxx of one face (flux2: limiter.f /
+     * philim.f and the correction loop). The middle f-wave is (0, beta2, 0) in
+     * local order: the contracted build skips its two zero components (adding
+     * +0.0 to a sum that starts at +0.0 changes no bits). */
+    auto face_terms = [&](const double* wc, double amdq[3], double apdq[3], double cq[3]) {
+        double s[3], fw[3][3];
+#pragma unroll
+        for (int mw = 0; mw < 3; ++mw) {
+            s[mw] = wc[mw];
+            fw[mw][0] = wc[3 + 3 * mw]; fw[mw][1] = wc[4 + 3 * mw]; fw[mw][2] = wc[5 + 3 * mw];
+        }
+        amdq[0] = amdq[1] = amdq[2] = 0.0;
+        apdq[0] = apdq[1] = apdq[2] = 0.0;
+        cq[0] = cq[1] = cq[2] = 0.0;
+#pragma unroll
+        for (int mw = 0; mw < 3; ++mw) {
+            if (FAST && mw == 1) {
+                if (d_ltz<FAST>(s[1])) {
+                    amdq[1] += fw[1][1];
+                } else if (d_gtz<FAST>(s[1])) {
+                    apdq[1] += fw[1][1];
+                } else {
+                    amdq[1] += 0.5 * fw[1][1];
+                    apdq[1] += 0.5 * fw[1][1];
+                }
+                continue;
+            }
+            if (d_ltz<FAST>(s[mw])) {
+                amdq[0] += fw[mw][0]; amdq[1] += fw[mw][1]; amdq[2] += fw[mw][2];
+            } else if (d_gtz<FAST>(s[mw])) {
+                apdq[0] += fw[mw][0]; apdq[1] += fw[mw][1]; apdq[2] += fw[mw][2];
+            } else {
+                amdq[0] += 0.5 * fw[mw][0]; amdq[1] += 0.5 * fw[mw][1]; amdq[2] += 0.5 * fw[mw][2];
+                apdq[0] += 0.5 * fw[mw][0]; apdq[1] += 0.5 * fw[mw][1]; apdq[2] += 0.5 * fw[mw][2];
+            }
+        }
+        if (P.order == 1) return;
+        const double* wl = wc - L::W_STRIDE; /* face n-1 */
+        const double* wr = wc + L::W_STRIDE; /* face n+1 */
+#pragma unroll
+        for (int mw = 0; mw < 3; ++mw) {
+            const double* fa = fw[mw];
+            if (FAST && mw == 1) {
+                /* the middle wave has one non-zero component: its norm and
+                 * projections are single products */
+                double lim = 1.0;
+                const double a = fa[1];
+                if (P.mthlim[1] != 0) {
+                    const double wnorm2 = a * a;
+                    if (!d_eqz<FAST>(wnorm2)) {
+                        const double dotl = (wl + 3 + 3)[1] * a;
+                        const double dotr = a * (wr + 3 + 3)[1];
+                        lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[1]) ? dotl : dotr, P.mthlim[1]);
+                    }
+                }
+                const double fac = copysign(1.0, s[1]) * (1.0 - fabs(s[1]) * dtdn);
+                cq[1] += (fac * lim) * a;
+                continue;
+            }
+            double lim = 1.0;
+            if (P.mthlim[mw] != 0) {
+                /* dot products in the global (h, hu, hv) order */
+                const double a0 = fa[0], a1 = (DIR == 0) ? fa[1] : fa[2], a2 = (DIR == 0) ? fa[2] : fa[1];
+                const double* ql = wl + 3 + 3 * mw;
+                const double* qr = wr + 3 + 3 * mw;
+                const double l0 = ql[0], l1 = (DIR == 0) ? ql[1] : ql[2], l2 = (DIR == 0) ? ql[2] : ql[1];
+                const double r0 = qr[0], r1 = (DIR == 0) ? qr[1] : qr[2], r2 = (DIR == 0) ? qr[2] : qr[1];
+                const double wnorm2 = a0 * a0 + a1 * a1 + a2 * a2;
+                if (!d_eqz<FAST>(wnorm2)) {
+                    /* the upwind neighbour's projection only (the same
+                     * products in the same order) */
+                    const bool up = d_gtz<FAST>(s[mw]);
+                    const double p0 = up ? l0 : r0, p1 = up ? l1 : r1, p2 = up ? l2 : r2;
+                    const double dot = p0 * a0 + p1 * a1 + p2 * a2;
+                    lim = gf_philim<FAST>(wnorm2, dot, P.mthlim[mw]);
+                }
+            }
+            const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
+            if (FAST) {
+                const double fl = fac * lim;
+                cq[0] += fl * fa[0];
+                cq[1] += fl * fa[1];
+                cq[2] += fl * fa[2];
+            } else {
+                cq[0] += fac * (lim * fa[0]);
+                cq[1] += fac * (lim * fa[1]);
+                cq[2] += fac * (lim * fa[2]);
+            }
+        }
+    };
+
+    /* ---- exact build, stage B: limiter, 2nd-order terms, both transverse
+     * splits of every face (flux2's per-face order) ---- */
+    auto stage_b_exact = [&](int t0, int band) {
+        const uint16_t* lB = lb + band * win.rb * fb;
+        int b2, b1, b0;
+        counts_b(band, b2, b1, b0);
         for (int idx = threadIdx.x; idx < b2 + b1 + b0; idx += NT) {
             const int f = lB[idx];
             double* o = O + f * L::O_STRIDE;
@@ -469,98 +581,11 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
             const int n = win.nb_lo + f % fb;
             const int kl = cidx(n - 1, t), kr = cidx(n, t);
             const double* wc = W + ((t - t0) * fa + (n - win.na_lo)) * L::W_STRIDE;
-            double s[3], fw[3][3];
-#pragma unroll
-            for (int mw = 0; mw < 3; ++mw) {
-                s[mw] = wc[mw];
-                fw[mw][0] = wc[3 + 3 * mw]; fw[mw][1] = wc[4 + 3 * mw]; fw[mw][2] = wc[5 + 3 * mw];
-            }
-            /* fluctuations from the unlimited f-waves (rpn2_geoclaw.f:359-376).
-             * The middle f-wave is (0, beta2, 0) in local order: the contracted
-             * build skips its two zero components (adding +0.0 to a sum that
-             * starts at +0.0 changes no bits). */
-            double amdq[3] = {0.0, 0.0, 0.0}, apdq[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-            for (int mw = 0; mw < 3; ++mw) {
-                if (FAST && mw == 1) {
-                    if (d_ltz<FAST>(s[1])) {
-                        amdq[1] += fw[1][1];
-                    } else if (d_gtz<FAST>(s[1])) {
-                        apdq[1] += fw[1][1];
-                    } else {
-                        amdq[1] += 0.5 * fw[1][1];
-                        apdq[1] += 0.5 * fw[1][1];
-                    }
-                    continue;
-                }
-                if (d_ltz<FAST>(s[mw])) {
-                    amdq[0] += fw[mw][0]; amdq[1] += fw[mw][1]; amdq[2] += fw[mw][2];
-                } else if (d_gtz<FAST>(s[mw])) {
-                    apdq[0] += fw[mw][0]; apdq[1] += fw[mw][1]; apdq[2] += fw[mw][2];
-                } else {
-                    amdq[0] += 0.5 * fw[mw][0]; amdq[1] += 0.5 * fw[mw][1]; amdq[2] += 0.5 * fw[mw][2];
-                    apdq[0] += 0.5 * fw[mw][0]; apdq[1] += 0.5 * fw[mw][1]; apdq[2] += 0.5 * fw[mw][2];
-                }
-            }
+            double amdq[3], apdq[3], cq[3];
+            face_terms(wc, amdq, apdq, cq);
             double faddm[3] = {amdq[0], amdq[1], amdq[2]};
             double faddp[3] = {-apdq[0], -apdq[1], -apdq[2]};
             if (P.order != 1) {
-                const double* wl = wc - L::W_STRIDE; /* face n-1 */
-                const double* wr = wc + L::W_STRIDE; /* face n+1 */
-                double cq[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-                for (int mw = 0; mw < 3; ++mw) {
-                    const double* fa = fw[mw];
-                    if (FAST && mw == 1) {
-                        /* the middle wave has one non-zero component: its norm
-                         * and projections are single products */
-                        double lim = 1.0;
-                        const double a = fa[1];
-                        if (P.mthlim[1] != 0) {
-                            const double wnorm2 = a * a;
-                            if (!d_eqz<FAST>(wnorm2)) {
-                                const double dotl = (wl + 3 + 3)[1] * a;
-                                const double dotr = a * (wr + 3 + 3)[1];
-                                lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[1]) ? dotl : dotr, P.mthlim[1]);
-                            }
-                        }
-                        const double fac = copysign(1.0, s[1]) * (1.0 - fabs(s[1]) * dtdn);
-                        cq[1] += (fac * lim) * a;
-                        continue;
-                    }
-                    double lim = 1.0;
-                    if (P.mthlim[mw] != 0) {
-                        /* dot products in the global (h, hu, hv) order */
-                        const double a0 = fa[0], a1 = (DIR == 0) ? fa[1] : fa[2],
-                                     a2 = (DIR == 0) ? fa[2] : fa[1];
-                        const double* ql = wl + 3 + 3 * mw;
-                        const double* qr = wr + 3 + 3 * mw;
-                        const double l0 = ql[0], l1 = (DIR == 0) ? ql[1] : ql[2],
-                                     l2 = (DIR == 0) ? ql[2] : ql[1];
-                        const double r0 = qr[0], r1 = (DIR == 0) ? qr[1] : qr[2],
-                                     r2 = (DIR == 0) ? qr[2] : qr[1];
-                        const double wnorm2 = a0 * a0 + a1 * a1 + a2 * a2;
-                        if (!d_eqz<FAST>(wnorm2)) {
-                            /* the upwind neighbour's projection only (the
-                             * same products in the same order) */
-                            const bool up = d_gtz<FAST>(s[mw]);
-                            const double p0 = up ? l0 : r0, p1 = up ? l1 : r1, p2 = up ? l2 : r2;
-                            const double dot = p0 * a0 + p1 * a1 + p2 * a2;
-                            lim = gf_philim<FAST>(wnorm2, dot, P.mthlim[mw]);
-                        }
-                    }
-                    const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
-                    if (FAST) {
-                        const double fl = fac * lim;
-                        cq[0] += fl * fa[0];
-                        cq[1] += fl * fa[1];
-                        cq[2] += fl * fa[2];
-                    } else {
-                        cq[0] += fac * (lim * fa[0]);
-                        cq[1] += fac * (lim * fa[1]);
-                        cq[2] += fac * (lim * fa[2]);
-                    }
-                }
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     faddm[c] += 0.5 * cq[c];
@@ -583,9 +608,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                                        sm[L::OFF_B + cidx(n - 1, t + 1)], drytol, amdq, bm, bp);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        /* the contracted build scales the transverse sums once per cell */
-                        A[c] = FAST ? bm[c] : half_dtdn * bm[c];
-                        B[c] = FAST ? bp[c] : half_dtdn * bp[c];
+                        A[c] = half_dtdn * bm[c];
+                        B[c] = half_dtdn * bp[c];
                     }
                 }
                 if (wet[kr]) { /* rpt2 imp=2: right-going part into cell n */
@@ -594,8 +618,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                                        sm[L::OFF_B + cidx(n, t + 1)], drytol, apdq, bm, bp);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        Cc[c] = FAST ? bm[c] : half_dtdn * bm[c];
-                        D[c] = FAST ? bp[c] : half_dtdn * bp[c];
+                        Cc[c] = half_dtdn * bm[c];
+                        D[c] = half_dtdn * bp[c];
                     }
                 }
             }
@@ -607,12 +631,119 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
             o[12] = Cc[0]; o[12 + G1] = Cc[1]; o[12 + G2] = Cc[2];
             o[15] = D[0]; o[15 + G1] = D[1]; o[15 + G2] = D[2];
         }
+    };
+
+    /* ---- contracted build, stage B1: per limited face, the fluctuations
+     * amdq, apdq and the limited second-order term cq (local order) ---- */
+    auto stage_b1 = [&](int t0, int band) {
+        const uint16_t* lB = lb + band * win.rb * fb;
+        int b2, b1, b0;
+        counts_b(band, b2, b1, b0);
+        for (int idx = threadIdx.x; idx < b2 + b1 + b0; idx += NT) {
+            const int f = lB[idx];
+            double* o = O + f * L::O_STRIDE;
+            if (idx >= b2 + b1) {
+#pragma unroll
+                for (int q = 0; q < L::O_STRIDE; ++q) o[q] = 0.0;
+                continue;
+            }
+            const int t = t0 + f / fb;
+            const int n = win.nb_lo + f % fb;
+            const double* wc = W + ((t - t0) * fa + (n - win.na_lo)) * L::W_STRIDE;
+            double amdq[3], apdq[3], cq[3];
+            face_terms(wc, amdq, apdq, cq);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                o[c] = amdq[c];
+                o[3 + c] = apdq[c];
+                o[6 + c] = cq[c];
+            }
+        }
+    };
+
+    /* ---- contracted build, stage B2: per cell n of each band slice, from
+     * its faces n (apdq, cq) and n+1 (amdq, cq): the flux difference
+     * N = faddm(n+1) - faddp(n) = P + Q/2 with P = amdq(n+1) + apdq(n),
+     * Q = cq(n+1) - cq(n), and the transverse split of the fluctuations that
+     * enter the cell. rpt2 is linear in its input and the cell alone decides
+     * its branches, so the splits of amdq(n+1) and apdq(n) (with the
+     * second-order terms for transverse = 2) are one split of their sum
+     * P + Q (P for transverse = 1): bm is the down-going part Dn, bp the
+     * up-going part U, equal to the sum of the reference's two splits up to
+     * rounding. ---- */
+    auto stage_b2 = [&](int t0, int t1) {
+        const int ncell = fb - 1;
+        const int cnt_c = (t1 - t0 + 1) * ncell;
+        for (int e = threadIdx.x; e < cnt_c; e += NT) {
+            const int ts = e / ncell;
+            const int n = win.nb_lo + e % ncell;
+            const int t = t0 + ts;
+            const int k = cidx(n, t);
+            double* r = crec(ts, n);
+            if (!(wet[cidx(n - 1, t)] | wet[k] | wet[cidx(n + 1, t)])) {
+                /* faces n and n+1 both between dry cells: no waves */
+#pragma unroll
+                for (int q = 0; q < L::C_STRIDE; ++q) r[q] = 0.0;
+                continue;
+            }
+            const double* orr = O + (ts * fb + (n + 1 - win.nb_lo)) * L::O_STRIDE; /* face n+1 */
+            const double* orl = O + (ts * fb + (n - win.nb_lo)) * L::O_STRIDE;     /* face n   */
+            double Pv[3], Qv[3], Nv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                Pv[c] = orr[c] + orl[3 + c];
+                Qv[c] = orr[6 + c] - orl[6 + c];
+                Nv[c] = Pv[c] + 0.5 * Qv[c];
+            }
+            double bm[3] = {0.0, 0.0, 0.0}, bp[3] = {0.0, 0.0, 0.0};
+            if (P.transverse != 0 && wet[k]) {
+                double x[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) x[c] = P.transverse == 2 ? Pv[c] + Qv[c] : Pv[c];
+                const gf_cell cc = load_cell<DIR, EXACT, L>(sm, wet, k);
+                gf_rpt2_face<FAST>(cc, sm[L::OFF_B + cidx(n, t - 1)], sm[L::OFF_B + cidx(n, t + 1)], drytol, x,
+                                   bm, bp);
+            }
+            /* global component order (h, hu, hv) */
+            r[0] = Nv[0]; r[G1] = Nv[1]; r[G2] = Nv[2];
+            r[3] = bp[0]; r[3 + G1] = bp[1]; r[3 + G2] = bp[2];
+            r[6] = bm[0]; r[6 + G1] = bm[1]; r[6 + G2] = bm[2];
+        }
+    };
+
+    const int ts_end = win.ts_lo + win.nsl;
+    int prev_t0 = -1, prev_t1 = -1;
+    if (EXACT) {
+        for (int t0 = win.ts_lo, band = 0; t0 < ts_end; t0 += win.rb, ++band) {
+            const int t1 = min(t0 + win.rb, ts_end) - 1; /* last slice of band */
+            stage_a(t0, band);
+            if (prev_t0 >= 0) gather(prev_t0, prev_t1);
+            __syncthreads();
+            stage_b_exact(t0, band);
+            __syncthreads();
+            prev_t0 = t0;
+            prev_t1 = t1;
+        }
+        gather(prev_t0, prev_t1);
         __syncthreads();
+        return smax;
+    }
+    /* Contracted build, pipelined over bands with two barriers per band:
+     * [stage A of band b | B2 of band b-1], [B1 of band b | gather of band
+     * b-1]. Each stage reads what the phase before the last barrier wrote. */
+    for (int t0 = win.ts_lo, band = 0;; t0 += win.rb, ++band) {
+        const bool have = t0 < ts_end;
+        const int t1 = have ? min(t0 + win.rb, ts_end) - 1 : -1;
+        if (have) stage_a(t0, band);
+        if (prev_t0 >= 0) stage_b2(prev_t0, prev_t1);
+        __syncthreads();
+        if (have) stage_b1(t0, band);
+        if (prev_t0 >= 0) gather(prev_t0, prev_t1);
+        __syncthreads();
+        if (!have) break;
         prev_t0 = t0;
         prev_t1 = t1;
     }
-    gather(prev_t0, prev_t1);
-    __syncthreads();
     return smax;
 }
 
