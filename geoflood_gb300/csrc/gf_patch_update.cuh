@@ -748,8 +748,12 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
 }
 
 /* Manning friction source term on one interior cell (geoclaw_src2_fort.f90:41-71).
- * The contracted build forms h^(-7/3) = (1/h)^2 rcbrt(h) and one reciprocal
- * of 1 + dt gamma instead of pow and three divisions. */
+ * The contracted build forms h^(-7/3) = y^7 from y = h^(-1/3) and one
+ * reciprocal of 1 + dt gamma instead of pow and three divisions: y by
+ * Newton's iteration for the inverse cube root, y <- y + y (1 - h y^3) / 3,
+ * two steps from the single-precision value (each step doubles the correct
+ * bits, 23 -> 46 -> the FP64 rounding), so no FP64 division or cube root
+ * is taken. */
 template <bool FAST>
 __device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double bathy, double nvar,
                                           double& h, double& hu, double& hv)
@@ -767,10 +771,17 @@ __device__ __forceinline__ void src2_cell(const gf_phys& P, double dt, double ba
             coeff = nvar;
         }
         if (FAST) {
-            const double rh = 1.0 / h;
-            const double gamma =
-                d_sqrt<FAST>(hu * hu + hv * hv) * P.grav * (coeff * coeff) * ((rh * rh) * rcbrt(h));
-            const double rdg = 1.0 / (1.0 + dt * gamma);
+            /* 1e-30 <= h here: a normal single-precision number */
+            double y = (double)rcbrtf((float)h);
+#pragma unroll
+            for (int it = 0; it < 2; ++it) {
+                const double e = fma(-h, (y * y) * y, 1.0);
+                y = fma(y * (1.0 / 3.0), e, y);
+            }
+            const double y2 = y * y;
+            const double hm73 = ((y2 * y2) * y2) * y; /* h^(-7/3) */
+            const double gamma = d_sqrt<FAST>(hu * hu + hv * hv) * P.grav * (coeff * coeff) * hm73;
+            const double rdg = gf_rcp(1.0 + dt * gamma);
             hu = hu * rdg;
             hv = hv * rdg;
         } else {
