@@ -45,8 +45,8 @@ BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
 # (dram__bytes_read.sum + dram__bytes_write.sum, against 234.9 MB
 # algorithmic) and FP64 warp instructions (sm__inst_executed_pipe_fp64.sum;
 # x 32 lanes / 4 194 304 cell-updates = FP64 issue slots per cell-update)
-NCU_COUNTS = {(256, 7): (170.340864e6 + 62.683392e6, 37.356532e6),
-              (384, 9): (170.288896e6 + 66.034688e6, 37.118633e6)}
+NCU_COUNTS = {(256, 7): (170.305792e6 + 62.232064e6, 32.727916e6),
+              (384, 9): (170.806784e6 + 65.378304e6, 32.645566e6)}
 NCU_DEFAULT_TILE = (384, 9)
 M = 32
 NPX = NPY = 64
