@@ -41,12 +41,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
 # Per tile shape of the mx = 32 update (threads, slices per band), from one ncu
-# capture of one launch on this workload each: DRAM traffic
-# (dram__bytes_read.sum + dram__bytes_write.sum, against 234.9 MB
+# capture each of the launch this bench times first in its kernel-only loop
+# (update launch 24 of `--steps 20 --warmup 3`, the same state): DRAM
+# traffic (dram__bytes_read.sum + dram__bytes_write.sum, against 234.9 MB
 # algorithmic) and FP64 warp instructions (sm__inst_executed_pipe_fp64.sum;
 # x 32 lanes / 4 194 304 cell-updates = FP64 issue slots per cell-update)
-NCU_COUNTS = {(256, 7): (170.305792e6 + 62.232064e6, 32.727916e6),
-              (384, 9): (170.806784e6 + 65.378304e6, 32.645566e6)}
+NCU_COUNTS = {(256, 7): (170.296576e6 + 62.487040e6, 33.253064e6),
+              (384, 9): (170.447872e6 + 65.717760e6, 33.201380e6)}
 NCU_DEFAULT_TILE = (384, 9)
 M = 32
 NPX = NPY = 64
