@@ -50,6 +50,15 @@ __device__ __forceinline__ double d_sqrt(double a)
     return sqrt(a);
 }
 
+/* a * b < 0 for nonzero finite factors, from the sign bits on the integer
+ * pipe (a product that underflows to zero aside) */
+__device__ __forceinline__ bool opposite_signs(double a, double b)
+{
+    const unsigned long long ia = static_cast<unsigned long long>(__double_as_longlong(a));
+    const unsigned long long ib = static_cast<unsigned long long>(__double_as_longlong(b));
+    return ((ia ^ ib) >> 63) != 0 && (ia << 1) != 0 && (ib << 1) != 0;
+}
+
 /* riemanntype (geoclaw_riemann_utils.f:566-677), maxiter = 1.
  * cL = sqrt(g hL), cR = sqrt(g hR) are supplied by the caller (they equal
  * the Fortran's sqrt(g*hL), sqrt(g*hR) bit for bit). Returns hm, s1m, s2m. */
@@ -244,12 +253,16 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     else if (d_lt<FAST>(d_min<FAST>(fabs(sE1), fabs(sE2)), crit2)) sonic = true;
     else if (d_lt<FAST>(sE1, crit2) && d_gt<FAST>(s1m, -crit2)) sonic = true;
     else if (d_gt<FAST>(sE2, -crit2) && d_lt<FAST>(s2m, crit2)) sonic = true;
-    else if (d_ltz<FAST>((uL + cL) * (uR + cR))) sonic = true;
-    else if (d_ltz<FAST>((uL - cL) * (uR - cR))) sonic = true;
+    else if (FAST ? opposite_signs(uL + cL, uR + cR) : d_ltz<FAST>((uL + cL) * (uR + cR))) sonic = true;
+    else if (FAST ? opposite_signs(uL - cL, uR - cR) : d_ltz<FAST>((uL - cL) * (uR - cR))) sonic = true;
     else sonic = false;
 
     const double rs12 = (FAST && !sonic) ? gf_rcp(s1s2bar) : 0.0;
-    double deldelh = sonic ? -delb : (FAST ? delb * g * hbar * rs12 : delb * g * hbar / s1s2bar);
+    /* contracted build: g hbar delb once; deldelphi below is -(g hbar delb /
+     * s1s2bar) s1s2tilde, i.e. the unclamped deldelh times -s1s2tilde */
+    const double ghd = FAST ? (g * hbar) * delb : 0.0;
+    double deldelh = sonic ? -delb : (FAST ? ghd * rs12 : delb * g * hbar / s1s2bar);
+    const double deldelh0 = deldelh;
     const double hsd = hstarHLL * (sE2 - sE1);
     if (FAST) {
         /* The bounds hsd / sE clamp rarely: compare hsd with deldelh * sE (the
@@ -274,11 +287,21 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
         deldelh = d_min<FAST>(deldelh, hR);
         deldelh = d_max<FAST>(deldelh, d_div<FAST>(hsd, sE2));
     }
-    double deldelphi = sonic ? -g * hbar * delb
-                             : (FAST ? -delb * g * hbar * s1s2tilde * rs12
-                                     : -delb * g * hbar * s1s2tilde / s1s2bar);
-    deldelphi = d_min<FAST>(deldelphi, g * d_max<FAST>(-hL * delb, -hR * delb));
-    deldelphi = d_max<FAST>(deldelphi, g * d_min<FAST>(-hL * delb, -hR * delb));
+    double deldelphi;
+    if (FAST) {
+        deldelphi = sonic ? -ghd : -deldelh0 * s1s2tilde;
+        /* g max(-hL delb, -hR delb) = -g delb h_lo and g min(..) = -g delb h_hi,
+         * with h_lo the smaller depth when delb > 0 (the larger otherwise) */
+        const double mgd = -g * delb;
+        const bool pos = d_gtz<FAST>(delb);
+        const double hmn = d_min<FAST>(hL, hR), hmx = d_max<FAST>(hL, hR);
+        deldelphi = d_min<FAST>(deldelphi, mgd * (pos ? hmn : hmx));
+        deldelphi = d_max<FAST>(deldelphi, mgd * (pos ? hmx : hmn));
+    } else {
+        deldelphi = sonic ? -g * hbar * delb : -delb * g * hbar * s1s2tilde / s1s2bar;
+        deldelphi = d_min<FAST>(deldelphi, g * d_max<FAST>(-hL * delb, -hR * delb));
+        deldelphi = d_max<FAST>(deldelphi, g * d_min<FAST>(-hL * delb, -hR * delb));
+    }
 
     const double d1 = delh - deldelh;
     const double d2 = delhu;
@@ -288,15 +311,23 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
      * r(:,3) = (1,l3,l3^2): determinant = l1 - l3. */
     const double A2 = l1 * l1, C2 = l3 * l3;
     const double det = l1 - l3;
-    const double n2 = (d2 * C2 - l3 * d3) - d1 * (l1 * C2 - l3 * A2) + (l1 * d3 - d2 * A2);
+    /* n2 = (l1 - l3) (d3 + d1 l1 l3 - d2 (l1 + l3)): the contracted build
+     * takes beta2 = n2 / det as that bracket, without the division */
     const double beta1 = FAST ? (d2 - d1 * l3) * rdet : (d2 - d1 * l3) / det;
-    const double beta2 = FAST ? n2 * rdet : n2 / det;
+    double beta2;
+    if (FAST) {
+        beta2 = fma(-d2, l1 + l3, fma(d1, l1 * l3, d3));
+    } else {
+        const double n2 = (d2 * C2 - l3 * d3) - d1 * (l1 * C2 - l3 * A2) + (l1 * d3 - d2 * A2);
+        beta2 = n2 / det;
+    }
     const double beta3 = FAST ? (d1 * l1 - d2) * rdet : (d1 * l1 - d2) / det;
 
     /* f-waves (geoclaw_riemann_utils.f:289-306). */
     double f11 = beta1 * l1, f21 = beta1 * A2, f31 = beta1 * l1 * vL;
     double f13 = beta3 * l3, f23 = beta3 * C2, f33 = beta3 * l3 * vR;
-    const double corr = hR * uR * vR - hL * uL * vL - f31 - f33;
+    /* h u v: the contracted build takes hu v (hu = h u up to rounding) */
+    const double corr = FAST ? (huR * vR - huL * vL - f31 - f33) : (hR * uR * vR - hL * uL * vL - f31 - f33);
     if (d_lez<FAST>(huL + f11)) f31 = f31 + corr;
     else f33 = f33 + corr;
 
