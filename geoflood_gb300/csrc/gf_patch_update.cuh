@@ -98,6 +98,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     return false;
 }
 
+/* sign(s) * x for the limiter's factor: x with its sign bit flipped when s
+ * is negative (-0 included), on the integer pipe instead of a product */
+__device__ __forceinline__ double with_sign_of(double x, double s)
+{
+    const unsigned long long ux = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned long long us = static_cast<unsigned long long>(__double_as_longlong(s));
+    return __longlong_as_double(static_cast<long long>(ux ^ (us & 0x8000000000000000ull)));
+}
+
 /* Order-preserving key of a non-negative double (for atomicMax). */
 __device__ __forceinline__ unsigned long long dkey(double v)
 {
@@ -499,6 +508,17 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 }
                 continue;
             }
+            if (FAST && mw == 0) { /* into zero sums: assigned (a zero's sign aside) */
+                if (d_ltz<FAST>(s[0])) {
+                    amdq[0] = fw[0][0]; amdq[1] = fw[0][1]; amdq[2] = fw[0][2];
+                } else if (d_gtz<FAST>(s[0])) {
+                    apdq[0] = fw[0][0]; apdq[1] = fw[0][1]; apdq[2] = fw[0][2];
+                } else {
+                    amdq[0] = 0.5 * fw[0][0]; amdq[1] = 0.5 * fw[0][1]; amdq[2] = 0.5 * fw[0][2];
+                    apdq[0] = amdq[0]; apdq[1] = amdq[1]; apdq[2] = amdq[2];
+                }
+                continue;
+            }
             if (d_ltz<FAST>(s[mw])) {
                 amdq[0] += fw[mw][0]; amdq[1] += fw[mw][1]; amdq[2] += fw[mw][2];
             } else if (d_gtz<FAST>(s[mw])) {
@@ -527,7 +547,7 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                         lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[1]) ? dotl : dotr, P.mthlim[1]);
                     }
                 }
-                const double fac = copysign(1.0, s[1]) * (1.0 - fabs(s[1]) * dtdn);
+                const double fac = with_sign_of(1.0 - fabs(s[1]) * dtdn, s[1]);
                 cq[1] += (fac * lim) * a;
                 continue;
             }
@@ -549,7 +569,8 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                     lim = gf_philim<FAST>(wnorm2, dot, P.mthlim[mw]);
                 }
             }
-            const double fac = copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
+            const double fac = FAST ? with_sign_of(1.0 - fabs(s[mw]) * dtdn, s[mw])
+                                    : copysign(1.0, s[mw]) * (1.0 - fabs(s[mw]) * dtdn);
             if (FAST) {
                 const double fl = fac * lim;
                 cq[0] += fl * fa[0];

@@ -85,16 +85,19 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
     const double F_min = delu + 2.0 * (c_min - c_max);
     /* (h_max + h_min)/(h_max h_min) = 1/h_min + 1/h_max: the contracted
      * build uses the per-cell reciprocals instead of a division. */
-    double F_max, q_fm = 0.0, s_fm = 0.0;
-    if (FAST) {
-        /* the root through rsqrt, whose value the two-shock step reuses */
-        const double a_fm = 0.5 * g * (d_max<FAST>(rhL, rhR) + d_min<FAST>(rhL, rhR));
-        q_fm = rsqrt(a_fm);
-        s_fm = a_fm * q_fm;
-        F_max = delu + (h_max - h_min) * s_fm;
-    } else {
-        F_max = delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
-    }
+    double F_max = 0.0, q_fm = 0.0, s_fm = 0.0;
+    if (!FAST) F_max = delu + (h_max - h_min) * sqrt(0.5 * g * (h_max + h_min) / (h_max * h_min));
+    /* the contracted build forms F_max only where it is read (not for two
+     * rarefactions), its root through rsqrt, whose value the two-shock step
+     * reuses */
+    auto f_max = [&]() {
+        if (FAST) {
+            const double a_fm = 0.5 * g * (d_max<FAST>(rhL, rhR) + d_min<FAST>(rhL, rhR));
+            q_fm = rsqrt(a_fm);
+            s_fm = a_fm * q_fm;
+            F_max = delu + (h_max - h_min) * s_fm;
+        }
+    };
     if (d_gtz<FAST>(F_min)) { /* 2-rarefactions */
         const double t = d_max<FAST>(0.0, -delu + 2.0 * (cL + cR));
         hm = c16g * (t * t);
@@ -102,7 +105,7 @@ __device__ __forceinline__ void gf_riemanntype(double hL, double hR, double uL,
         const double cm = FAST ? 0.25 * t : sqrt(g * hm);
         s1m = uL + 2.0 * cL - 3.0 * cm;
         s2m = uR - 2.0 * cR + 3.0 * cm;
-    } else if (d_lez<FAST>(F_max)) { /* 2 shocks, one Newton step on sqrt(h) */
+    } else if ((f_max(), d_lez<FAST>(F_max))) { /* 2 shocks, one Newton step on sqrt(h) */
         const double h0 = h_max;
         double gL, gR, dfdh, sh0, rL, rR;
         if (FAST) {
