@@ -219,7 +219,10 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double sL = uL - cL;
     const double sR = uR + cR;
     const double uhat = d_div<FAST>(cL * uL + cR * uR, cR + cL);
-    const double chat = d_sqrt<FAST>(g * 0.5 * (hR + hL));
+    /* hbar of the steady-state wave below; g (hL + hR) / 2 = g hbar for the
+     * non-negative depths here, so the contracted build shares the product */
+    const double hbar = d_max<FAST>(0.5 * (hL + hR), 0.0);
+    const double chat = FAST ? d_sqrt<FAST>(g * hbar) : d_sqrt<FAST>(g * 0.5 * (hR + hL));
     double sE1 = d_min<FAST>(sL, uhat - chat);
     double sE2 = d_max<FAST>(sR, uhat + chat);
 
@@ -240,12 +243,13 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     /* One reciprocal serves h*_HLL and Cramer's rule in the contracted
      * build: sE2 - sE1 = l3 - l1 = -(l1 - l3). */
     const double rdet = FAST ? gf_rcp(l1 - l3) : 0.0;
-    const double hstarHLL = FAST ? d_max<FAST>((huL - huR + sE2 * hR - sE1 * hL) * -rdet, 0.0)
-                                 : fmax((huL - huR + sE2 * hR - sE1 * hL) / (sE2 - sE1), 0.0);
+    /* h*_HLL (sE2 - sE1) enters only as hsd: the contracted build takes it as
+     * max(numerator, 0) (sE2 - sE1 = l3 - l1 > 0 for a wet face) */
+    const double hll_num = huL - huR + sE2 * hR - sE1 * hL;
+    const double hstarHLL = FAST ? 0.0 : fmax(hll_num / (sE2 - sE1), 0.0);
     const double l2 = 0.5 * (l1 + l3);
 
     /* steady-state wave, first (only) iteration: hLstar = hL etc. */
-    const double hbar = d_max<FAST>(0.5 * (hL + hR), 0.0);
     const double s1s2bar = 0.25 * ((uL + uR) * (uL + uR)) - g * hbar;
     const double s1s2tilde = d_max<FAST>(0.0, uL * uR) - g * hbar;
     const double crit_sq = crit * crit;
@@ -266,7 +270,7 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double ghd = FAST ? (g * hbar) * delb : 0.0;
     double deldelh = sonic ? -delb : (FAST ? ghd * rs12 : delb * g * hbar / s1s2bar);
     const double deldelh0 = deldelh;
-    const double hsd = hstarHLL * (sE2 - sE1);
+    const double hsd = FAST ? d_max<FAST>(hll_num, 0.0) : hstarHLL * (sE2 - sE1);
     if (FAST) {
         /* The bounds hsd / sE clamp rarely: compare hsd with deldelh * sE (the
          * sign of sE is known in each branch) and divide only to clamp. */
