@@ -542,9 +542,9 @@ __device__ __forceinline__ double sweep(double* sm, const unsigned char* wet, in
                 if (P.mthlim[1] != 0) {
                     const double wnorm2 = a * a;
                     if (!d_eqz<FAST>(wnorm2)) {
-                        const double dotl = (wl + 3 + 3)[1] * a;
-                        const double dotr = a * (wr + 3 + 3)[1];
-                        lim = gf_philim<FAST>(wnorm2, d_gtz<FAST>(s[1]) ? dotl : dotr, P.mthlim[1]);
+                        /* the upwind neighbour's projection only */
+                        const double up = d_gtz<FAST>(s[1]) ? (wl + 3 + 3)[1] : (wr + 3 + 3)[1];
+                        lim = gf_philim<FAST>(wnorm2, up * a, P.mthlim[1]);
                     }
                 }
                 const double fac = with_sign_of(1.0 - fabs(s[1]) * dtdn, s[1]);

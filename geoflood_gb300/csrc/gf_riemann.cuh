@@ -416,7 +416,9 @@ __device__ __forceinline__ double gf_philim(double a, double b, int meth)
     case 2: return d_max<FAST>(d_max<FAST>(0.0, d_min<FAST>(1.0, 2.0 * r)), d_min<FAST>(2.0, r));
     case 3: return (r + fabs(r)) / (1.0 + fabs(r));
     case 4: {
-        const double c = (1.0 + r) * 0.5;
+        /* (1 + r) / 2: halving is exact, so the single rounding of the fused
+         * form gives the same value */
+        const double c = FAST ? fma(r, 0.5, 0.5) : (1.0 + r) * 0.5;
         return d_max<FAST>(0.0, d_min<FAST>(d_min<FAST>(c, 2.0), 2.0 * r));
     }
     case 5: return r;
