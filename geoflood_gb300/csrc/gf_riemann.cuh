@@ -179,13 +179,13 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     if (Rc.wet) {
         hR = Rc.h; huR = Rc.hun; hvR = Rc.hut; uR = Rc.un; vR = Rc.ut; cR = Rc.c; rhR = Rc.rh;
         /* hu^2/h = hu u: the contracted build reuses the cell quotient */
-        phiR = FAST ? 0.5 * g * (hR * hR) + huR * uR : 0.5 * g * (hR * hR) + (huR * huR) / hR;
+        phiR = FAST ? 0.0 : 0.5 * g * (hR * hR) + (huR * huR) / hR; /* contracted: delphi below */
     } else {
         hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0; phiR = 0.0; cR = 0.0;
     }
     if (Lc.wet) {
         hL = Lc.h; huL = Lc.hun; hvL = Lc.hut; uL = Lc.un; vL = Lc.ut; cL = Lc.c; rhL = Lc.rh;
-        phiL = FAST ? 0.5 * g * (hL * hL) + huL * uL : 0.5 * g * (hL * hL) + (huL * huL) / hL;
+        phiL = FAST ? 0.0 : 0.5 * g * (hL * hL) + (huL * huL) / hL;
     } else {
         hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0; phiL = 0.0; cL = 0.0;
     }
@@ -229,7 +229,11 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     /* ---- riemann_aug_JCP (geoclaw_riemann_utils.f:57-306) ---- */
     const double delh = hR - hL;
     const double delhu = huR - huL;
-    const double delphi = phiR - phiL;
+    /* phi = g h^2 / 2 + hu^2 / h: the contracted build forms the jump as
+     * (g / 2) (hR - hL) (hR + hL) + (huR uR - huL uL), with hu^2 / h = hu u;
+     * both products rounded, so a mirrored wall state gives exactly zero */
+    const double delphi = FAST ? fma((0.5 * g) * delh, hR + hL, __dmul_rn(huR, uR) - __dmul_rn(huL, uL))
+                               : phiR - phiL;
     const double delb = bR - bL;
 
     double hm, s1m, s2m;
@@ -250,7 +254,8 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double l2 = 0.5 * (l1 + l3);
 
     /* steady-state wave, first (only) iteration: hLstar = hL etc. */
-    const double s1s2bar = 0.25 * ((uL + uR) * (uL + uR)) - g * hbar;
+    const double s1s2bar = FAST ? fma(0.25 * (uL + uR), uL + uR, -(g * hbar))
+                                : 0.25 * ((uL + uR) * (uL + uR)) - g * hbar;
     const double s1s2tilde = d_max<FAST>(0.0, uL * uR) - g * hbar;
     const double crit_sq = crit * crit;
     bool sonic;
@@ -331,8 +336,9 @@ __device__ __forceinline__ void gf_rpn2_face(const gf_cell& Lc, const gf_cell& R
     const double beta3 = FAST ? (d1 * l1 - d2) * rdet : (d1 * l1 - d2) / det;
 
     /* f-waves (geoclaw_riemann_utils.f:289-306). */
-    double f11 = beta1 * l1, f21 = beta1 * A2, f31 = beta1 * l1 * vL;
-    double f13 = beta3 * l3, f23 = beta3 * C2, f33 = beta3 * l3 * vR;
+    /* contracted build: l^2 beta = (beta l) l, no squares */
+    double f11 = beta1 * l1, f21 = FAST ? f11 * l1 : beta1 * A2, f31 = beta1 * l1 * vL;
+    double f13 = beta3 * l3, f23 = FAST ? f13 * l3 : beta3 * C2, f33 = beta3 * l3 * vR;
     /* h u v: the contracted build takes hu v (hu = h u up to rounding) */
     const double corr = FAST ? (huR * vR - huL * vL - f31 - f33) : (hR * uR * vR - hL * uL * vL - f31 - f33);
     if (d_lez<FAST>(huL + f11)) f31 = f31 + corr;
