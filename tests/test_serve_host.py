@@ -58,3 +58,17 @@ def test_oracle_outstyle1_lands_on_output_times_and_keeps_a_lake():
     eta = qt[s][..., 0] + at[s][..., 0]
     wet = qt[s][..., 0] > 1e-3
     assert np.allclose(eta[wet], 3.0, rtol=0, atol=1e-12)
+
+
+def test_server_option_defaults():
+    """Defaults of gf_server_opts_default as the C ABI fills them: three size
+    lanes, priority streams, per-size round queues, dry-patch culling, one
+    CTA per patch (no reserved SMs), the per-size updates."""
+    lib = _lib.load()
+    o = _lib.gf_server_opts()
+    lib.gf_server_opts_default(C.byref(o))
+    assert o.nlanes == 3 and list(o.lane_cells)[:2] == [100000, 1000000]
+    assert o.priority == 1 and o.backfill == 1
+    assert o.split_sizes == 1 and o.cull_dry == 1
+    assert o.reserve_sms == 0 and o.mixed_update == 0
+    assert 1 <= o.max_active <= 1024 and o.hbm_budget > 0
