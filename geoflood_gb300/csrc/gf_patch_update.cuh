@@ -263,17 +263,33 @@ __device__ __forceinline__ void build_lists(const double* sm, const unsigned cha
         const int kl = cidx(n - 1, t), kr = cidx(n, t);
         const int nw = wet[kl] + wet[kr];
         int cls = nw == 0 ? 4 : nw == 1 ? 3 : 0;
-        if (nw == 2) {
+        if (nw == 2 && EXACT) {
             const double hL = sm[L::OFF_H + kl], hR = sm[L::OFF_H + kr];
             const double uL = sm[(DIR == 0 ? L::OFF_U : L::OFF_V) + kl];
             const double uR = sm[(DIR == 0 ? L::OFF_U : L::OFF_V) + kr];
             const double cL = sm[L::OFF_C + kl], cR = sm[L::OFF_C + kr];
-            constexpr bool F = !EXACT; /* comparisons on the integer pipe */
+            constexpr bool F = false;
             const double delu = uR - uL;
             const double hmin = d_min<F>(hL, hR), hmax = d_max<F>(hL, hR);
             const double dh = hmax - hmin;
             if (d_gtz<F>(delu + 2.0 * (d_min<F>(cL, cR) - d_max<F>(cL, cR)))) cls = 1;
             else if (d_lez<F>(delu) && d_ge<F>(delu * delu * (hmin * hmax), dh * dh * (0.5 * g) * (hmin + hmax)))
+                cls = 0;
+            else cls = 2;
+        } else if (nw == 2) {
+            /* The class only orders the list (a face in the neighbouring
+             * class costs divergence, not bits), so the contracted build
+             * estimates it in single precision off the FP64 pipe. */
+            const float hL = __double2float_rn(sm[L::OFF_H + kl]), hR = __double2float_rn(sm[L::OFF_H + kr]);
+            const float uL = __double2float_rn(sm[(DIR == 0 ? L::OFF_U : L::OFF_V) + kl]);
+            const float uR = __double2float_rn(sm[(DIR == 0 ? L::OFF_U : L::OFF_V) + kr]);
+            const float cL = __double2float_rn(sm[L::OFF_C + kl]), cR = __double2float_rn(sm[L::OFF_C + kr]);
+            const float delu = uR - uL;
+            const float hmin = fminf(hL, hR), hmax = fmaxf(hL, hR);
+            const float dh = hmax - hmin;
+            if (delu + 2.0f * (fminf(cL, cR) - fmaxf(cL, cR)) > 0.0f) cls = 1;
+            else if (delu <= 0.0f &&
+                     delu * delu * (hmin * hmax) >= dh * dh * (0.5f * (float)g) * (hmin + hmax))
                 cls = 0;
             else cls = 2;
         }
