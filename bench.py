@@ -46,8 +46,8 @@ BYTES_PER_CELL_UPDATE = 56  # read h, hu, hv, b; write h, hu, hv (FP64)
 # traffic (dram__bytes_read.sum + dram__bytes_write.sum, against 234.9 MB
 # algorithmic) and FP64 warp instructions (sm__inst_executed_pipe_fp64.sum;
 # x 32 lanes / 4 194 304 cell-updates = FP64 issue slots per cell-update)
-NCU_COUNTS = {(256, 7): (170.292480e6 + 62.866176e6, 30.352613e6),
-              (384, 9): (170.423040e6 + 65.750272e6, 30.358232e6)}
+NCU_COUNTS = {(256, 7): (170.886912e6 + 62.938880e6, 29.892596e6),
+              (384, 9): (170.445312e6 + 66.367744e6, 29.903210e6)}
 NCU_DEFAULT_TILE = (384, 9)
 M = 32
 NPX = NPY = 64
