@@ -389,13 +389,17 @@ __device__ __forceinline__ void gf_rpt2_face(const gf_cell& cl, double topo_lo,
     const double beta1 = FAST ? (s3 * delf1 - delf3) * rden : (s3 * delf1 - delf3) / den;
     const double beta2 = -u * delf1 + delf2;
     const double beta3 = FAST ? (delf3 - s1 * delf1) * rden : (delf3 - s1 * delf1) / den;
-    /* r(:,1) = (1, u, s1); r(:,2) = (0, 1, 0); r(:,3) = (1, u, s3) */
+    /* r(:,1) = (1, u, s1); r(:,2) = (0, 1, 0); r(:,3) = (1, u, s3). The first
+     * wave enters zero sums: the contracted build assigns (a zero's sign
+     * aside). */
     if (d_ltz<FAST>(s1) && up_lo) {
         const double a = s1 * beta1;
-        bm[0] += a; bm[1] += a * u; bm[2] += a * s1;
+        if (FAST) { bm[0] = a; bm[1] = a * u; bm[2] = a * s1; }
+        else { bm[0] += a; bm[1] += a * u; bm[2] += a * s1; }
     } else if (d_gtz<FAST>(s1) && up_hi) {
         const double a = s1 * beta1;
-        bp[0] += a; bp[1] += a * u; bp[2] += a * s1;
+        if (FAST) { bp[0] = a; bp[1] = a * u; bp[2] = a * s1; }
+        else { bp[0] += a; bp[1] += a * u; bp[2] += a * s1; }
     }
     if (d_ltz<FAST>(s2) && up_lo) {
         bm[1] += s2 * beta2;
@@ -417,6 +421,9 @@ template <bool FAST>
 __device__ __forceinline__ double gf_philim(double a, double b, int meth)
 {
     if (d_eqz<FAST>(a)) return 0.0;
+    /* MC with b <= 0: r <= 0 and the limiter is zero; the contracted build
+     * skips the division (a zero's sign aside) */
+    if (FAST && meth == 4 && d_lez<FAST>(b)) return 0.0;
     const double r = d_div<FAST>(b, a);
     switch (meth) {
     case 2: return d_max<FAST>(d_max<FAST>(0.0, d_min<FAST>(1.0, 2.0 * r)), d_min<FAST>(2.0, r));
